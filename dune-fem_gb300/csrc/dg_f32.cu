@@ -1,0 +1,10 @@
+// FP32 instantiations of the DG apply kernel (the inner-solve precision of
+// the mixed-precision path).
+#include "dg_launch.cuh"
+
+namespace gbfem {
+int dg_launch_f32(const DgArgsT<float>& a, const DgTablesT<float>& t, int n, int q, bool kappa,
+                  cudaStream_t s) {
+  return dg_launch<float>(a, t, n, q, kappa, s);
+}
+}  // namespace gbfem

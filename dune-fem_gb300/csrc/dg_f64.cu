@@ -1,0 +1,9 @@
+// FP64 instantiations of the DG apply kernel.
+#include "dg_launch.cuh"
+
+namespace gbfem {
+int dg_launch_f64(const DgArgsT<double>& a, const DgTablesT<double>& t, int n, int q, bool kappa,
+                  cudaStream_t s) {
+  return dg_launch<double>(a, t, n, q, kappa, s);
+}
+}  // namespace gbfem

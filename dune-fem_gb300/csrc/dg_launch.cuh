@@ -1,0 +1,47 @@
+// Instantiation and launch of dg_apply_kernel for the supported (n, q)
+// pairs: n = p+1 in 2..5, q in {p+1, p+2}.
+#pragma once
+#include "dg_kernel.cuh"
+#include "gbfem_internal.cuh"
+
+namespace gbfem {
+
+template <typename T, int N, int Q, bool KAPPA>
+int dg_launch_one(const DgArgsT<T>& args, const DgTablesT<T>& tabs, cudaStream_t stream) {
+  // Cells per CTA: as many as fit ~100 KB of shared memory, at most 8.
+  constexpr int PER_CELL = DgSmem<N, Q, KAPPA, 1>::PER_CELL;
+  constexpr int CPB0 = (100 * 1024) / (PER_CELL * int(sizeof(T)));
+  constexpr int CPB = CPB0 >= 8 ? 8 : (CPB0 >= 4 ? 4 : (CPB0 >= 2 ? 2 : 1));
+  constexpr int THREADS = 256;
+  const size_t smem = size_t(DgSmem<N, Q, KAPPA, CPB>::TOTAL) * sizeof(T);
+  auto kern = dg_apply_kernel<T, N, Q, KAPPA, CPB>;
+  GBFEM_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  constexpr int N3 = N * N * N;
+  const long long nvirt = args.unit_mode ? args.ncells * N3 : args.ncells;
+  const long long blocks = (nvirt + CPB - 1) / CPB;
+  if (blocks <= 0) return GBFEM_OK;
+  if (blocks > 2147483647LL) return set_error(GBFEM_ERR_INVALID, "dg apply: grid too large");
+  kern<<<unsigned(blocks), THREADS, smem, stream>>>(args, tabs);
+  GBFEM_CUDA_TRY(cudaGetLastError());
+  return GBFEM_OK;
+}
+
+template <typename T>
+int dg_launch(const DgArgsT<T>& args, const DgTablesT<T>& tabs, int n, int q, bool kappa, cudaStream_t stream) {
+#define GBFEM_DG_CASE(NN, QQ)                                                    \
+  if (n == NN && q == QQ)                                                        \
+    return kappa ? dg_launch_one<T, NN, QQ, true>(args, tabs, stream)            \
+                 : dg_launch_one<T, NN, QQ, false>(args, tabs, stream);
+  GBFEM_DG_CASE(2, 2)
+  GBFEM_DG_CASE(2, 3)
+  GBFEM_DG_CASE(3, 3)
+  GBFEM_DG_CASE(3, 4)
+  GBFEM_DG_CASE(4, 4)
+  GBFEM_DG_CASE(4, 5)
+  GBFEM_DG_CASE(5, 5)
+  GBFEM_DG_CASE(5, 6)
+#undef GBFEM_DG_CASE
+  return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "dg apply: unsupported (p, q)");
+}
+
+}  // namespace gbfem

@@ -1,0 +1,294 @@
+// Host side of the operator handles: creation from the descriptor, the
+// 1-D tables, dispatch of apply / diagonal / block-diagonal, and the
+// continuous Lagrange Q1 operator of the 2-D Poisson-type problem.
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "dg_kernel.cuh"
+#include "gbfem_internal.cuh"
+#include "operator_impl.hpp"
+#include "tables.hpp"
+
+namespace gbfem {
+
+int dg_launch_f64(const DgArgsT<double>&, const DgTablesT<double>&, int, int, bool, cudaStream_t);
+int dg_launch_f32(const DgArgsT<float>&, const DgTablesT<float>&, int, int, bool, cudaStream_t);
+
+template <typename T>
+static void fill_dg_tables(const Tables1D& t, DgTablesT<T>* out) {
+  std::memset(out, 0, sizeof(*out));
+  for (int a = 0; a < t.q; ++a)
+    for (int i = 0; i < t.n; ++i) out->B[a * t.n + i] = T(t.B[a][i]);
+  for (int a = 0; a < t.q; ++a)
+    for (int b = 0; b < t.q; ++b) out->Dc[a * t.q + b] = T(t.Dc[a][b]);
+  for (int a = 0; a < t.q; ++a) out->w[a] = T(t.wts[a]);
+  for (int s = 0; s < 2; ++s)
+    for (int i = 0; i < t.n; ++i) {
+      out->tr[s * t.n + i] = T(t.tr[s][i]);
+      out->dtr[s * t.n + i] = T(t.dtr[s][i]);
+    }
+}
+
+template <typename T>
+static void fill_dg_args(const gbfem_operator_s* op, DgArgsT<T>* a) {
+  std::memset(a, 0, sizeof(*a));
+  const gbfem_dg_desc& d = op->dg;
+  double h[3], vol = 1.0;
+  for (int k = 0; k < 3; ++k) {
+    a->nc[k] = d.grid.cells[k];
+    a->periodic[k] = d.grid.periodic[k];
+    h[k] = (d.grid.upper[k] - d.grid.lower[k]) / d.grid.cells[k];
+    vol *= h[k];
+  }
+  a->ncells = op->ncells;
+  a->detK = T(vol);
+  for (int k = 0; k < 3; ++k) {
+    a->invh[k] = T(1.0 / h[k]);
+    const double area = vol / h[k];
+    a->faceA[k] = T(area);
+    a->sigma[k] = T(d.penalty / (vol / area));  // h_F = avg|K| / |F|
+  }
+  a->eps = T(d.diffusion);
+  a->mass = T(d.mass);
+  for (int k = 0; k < 3; ++k) a->b[k] = T(d.velocity[k]);
+  a->advect = (d.velocity[0] != 0.0 || d.velocity[1] != 0.0 || d.velocity[2] != 0.0) ? 1 : 0;
+  a->weak_dirichlet = d.weak_dirichlet;
+  a->kappa = static_cast<const T*>(d.kappa);
+}
+
+int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
+             void* blocks) {
+  if (op->precision == GBFEM_F64) {
+    DgArgsT<double> a;
+    fill_dg_args(op, &a);
+    a.u = static_cast<const double*>(u);
+    a.w = static_cast<double*>(w);
+    a.unit_mode = unit_mode;
+    a.blocks = static_cast<double*>(blocks);
+    return dg_launch_f64(a, op->tab64, op->n, op->q, op->dg.kappa != nullptr, s);
+  } else {
+    DgArgsT<float> a;
+    fill_dg_args(op, &a);
+    a.u = static_cast<const float*>(u);
+    a.w = static_cast<float*>(w);
+    a.unit_mode = unit_mode;
+    a.blocks = static_cast<float*>(blocks);
+    return dg_launch_f32(a, op->tab32, op->n, op->q, op->dg.kappa != nullptr, s);
+  }
+}
+
+// ---- continuous Q1 (2-D) ---------------------------------------------------
+// Vertex-owner gather: each thread owns one vertex and sums the rows of the
+// element matrices of the (up to) four cells around it.  Dirichlet rows are
+// w_D = u_D (g = 0), as DirichletWrapperOperator::operator() produces
+// (schemes/dirichletwrapper.hh:101-105, dirichletconstraints.hh:396-430).
+template <typename T>
+__global__ void q1_apply_kernel(const T* __restrict__ u, T* __restrict__ w, int nx, int ny, Q1Element e,
+                                int diag_only) {
+  const int vx_n = nx + 1, vy_n = ny + 1;
+  const long long nv = (long long)vx_n * vy_n;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv;
+       v += (long long)gridDim.x * blockDim.x) {
+    const int vx = int(v % vx_n), vy = int(v / vx_n);
+    if (vx == 0 || vy == 0 || vx == nx || vy == ny) {
+      w[v] = diag_only ? T(1) : u[v];
+      continue;
+    }
+    double acc = 0.0;
+    // cells (vx-1+cx, vy-1+cy), cx,cy in {0,1}; local index of v in that cell = (1-cx) + 2*(1-cy)
+#pragma unroll
+    for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+      for (int cx = 0; cx < 2; ++cx) {
+        const int ex = vx - 1 + cx, ey = vy - 1 + cy;
+        const int a = (1 - cx) + 2 * (1 - cy);
+        if (diag_only) {
+          acc += e.K[a * 4 + a];
+          continue;
+        }
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const int bx = ex + (b & 1), by = ey + (b >> 1);
+          acc += e.K[a * 4 + b] * double(u[(long long)by * vx_n + bx]);
+        }
+      }
+    w[v] = T(acc);
+  }
+}
+
+int q1_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int diag_only) {
+  const long long nv = op->ndofs;
+  const int threads = 256;
+  const int blocks = int((nv + threads - 1) / threads);
+  if (op->precision == GBFEM_F64)
+    q1_apply_kernel<double><<<blocks, threads, 0, s>>>(static_cast<const double*>(u), static_cast<double*>(w),
+                                                        op->grid.cells[0], op->grid.cells[1], op->q1, diag_only);
+  else
+    q1_apply_kernel<float><<<blocks, threads, 0, s>>>(static_cast<const float*>(u), static_cast<float*>(w),
+                                                       op->grid.cells[0], op->grid.cells[1], op->q1, diag_only);
+  GBFEM_CUDA_TRY(cudaGetLastError());
+  return GBFEM_OK;
+}
+
+// Element matrix of eps*grad.grad + c*mass for bilinear Q1 on an hx x hy
+// rectangle, 2x2 Gauss (the reference's default interior order 2p = 2,
+// schemes/galerkin.hh:131).
+static Q1Element make_q1_element(double hx, double hy, double eps, double c) {
+  Q1Element e;
+  long double p[2], wq[2];
+  gauss01(2, p, wq);
+  for (int a = 0; a < 4; ++a)
+    for (int b = 0; b < 4; ++b) {
+      long double s = 0.0L;
+      for (int qy = 0; qy < 2; ++qy)
+        for (int qx = 0; qx < 2; ++qx) {
+          auto phi = [&](int k, long double x, long double y, long double* v, long double* dx, long double* dy) {
+            const int kx = k & 1, ky = k >> 1;
+            long double fx = kx ? x : 1.0L - x, fy = ky ? y : 1.0L - y;
+            long double gx = kx ? 1.0L : -1.0L, gy = ky ? 1.0L : -1.0L;
+            *v = fx * fy;
+            *dx = gx * fy / hx;
+            *dy = fx * gy / hy;
+          };
+          long double va, dxa, dya, vb, dxb, dyb;
+          phi(a, p[qx], p[qy], &va, &dxa, &dya);
+          phi(b, p[qx], p[qy], &vb, &dxb, &dyb);
+          s += wq[qx] * wq[qy] * hx * hy * (eps * (dxa * dxb + dya * dyb) + c * va * vb);
+        }
+      e.K[a * 4 + b] = double(s);
+    }
+  return e;
+}
+
+}  // namespace gbfem
+
+using namespace gbfem;
+
+static int check_grid(const gbfem_grid_desc* g, int want_dim) {
+  if (!g) return set_error(GBFEM_ERR_INVALID, "grid descriptor is null");
+  if (g->dim != want_dim) return set_error(GBFEM_ERR_INVALID, "grid dim " + std::to_string(g->dim) +
+                                                                  " not supported here (want " +
+                                                                  std::to_string(want_dim) + ")");
+  for (int k = 0; k < want_dim; ++k) {
+    if (g->cells[k] <= 0) return set_error(GBFEM_ERR_INVALID, "grid: cells must be positive");
+    if (!(g->upper[k] > g->lower[k])) return set_error(GBFEM_ERR_INVALID, "grid: upper must exceed lower");
+  }
+  return GBFEM_OK;
+}
+
+extern "C" {
+
+int gbfem_dg_operator_create(const gbfem_dg_desc* desc, gbfem_operator* out) {
+  if (!desc || !out) return set_error(GBFEM_ERR_INVALID, "gbfem_dg_operator_create: null argument");
+  *out = nullptr;
+  GBFEM_TRY(check_grid(&desc->grid, 3));
+  const int p = desc->order;
+  if (p < 1 || p > 4) return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "DG order must be 1..4");
+  int q = desc->quad_points == 0 ? p + 2 : desc->quad_points;
+  if (q != p + 1 && q != p + 2)
+    return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "quad_points must be p+1 or p+2 (or 0 for p+2)");
+  if (desc->precision != GBFEM_F64 && desc->precision != GBFEM_F32)
+    return set_error(GBFEM_ERR_INVALID, "precision must be GBFEM_F64 or GBFEM_F32");
+  auto* op = new (std::nothrow) gbfem_operator_s();
+  if (!op) return set_error(GBFEM_ERR_INVALID, "out of host memory");
+  op->kind = OpKind::DG;
+  op->precision = desc->precision;
+  op->dg = *desc;
+  op->dg.quad_points = q;
+  op->grid = desc->grid;
+  op->n = p + 1;
+  op->q = q;
+  op->nloc = op->n * op->n * op->n;
+  op->ncells = (long long)desc->grid.cells[0] * desc->grid.cells[1] * desc->grid.cells[2];
+  op->ndofs = op->ncells * op->nloc;
+  Tables1D t = make_tables(op->n, q);
+  fill_dg_tables(t, &op->tab64);
+  fill_dg_tables(t, &op->tab32);
+  *out = op;
+  return GBFEM_OK;
+}
+
+int gbfem_q1_operator_create(const gbfem_grid_desc* grid, int precision, double diffusion, double mass,
+                             gbfem_operator* out) {
+  if (!out) return set_error(GBFEM_ERR_INVALID, "gbfem_q1_operator_create: null out");
+  *out = nullptr;
+  GBFEM_TRY(check_grid(grid, 2));
+  if (precision != GBFEM_F64 && precision != GBFEM_F32)
+    return set_error(GBFEM_ERR_INVALID, "precision must be GBFEM_F64 or GBFEM_F32");
+  auto* op = new (std::nothrow) gbfem_operator_s();
+  if (!op) return set_error(GBFEM_ERR_INVALID, "out of host memory");
+  op->kind = OpKind::Q1;
+  op->precision = precision;
+  op->grid = *grid;
+  op->n = 2;
+  op->q = 2;
+  op->nloc = 1;
+  op->ncells = (long long)grid->cells[0] * grid->cells[1];
+  op->ndofs = (long long)(grid->cells[0] + 1) * (grid->cells[1] + 1);
+  const double hx = (grid->upper[0] - grid->lower[0]) / grid->cells[0];
+  const double hy = (grid->upper[1] - grid->lower[1]) / grid->cells[1];
+  op->q1 = make_q1_element(hx, hy, diffusion, mass);
+  *out = op;
+  return GBFEM_OK;
+}
+
+int gbfem_operator_destroy(gbfem_operator op) {
+  if (!op) return GBFEM_OK;
+  if (op->host_u) cudaFree(op->host_u);
+  if (op->host_w) cudaFree(op->host_w);
+  delete op;
+  return GBFEM_OK;
+}
+
+int gbfem_operator_size(gbfem_operator op, int64_t* ndofs) {
+  if (!op || !ndofs) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_size: null argument");
+  *ndofs = op->ndofs;
+  return GBFEM_OK;
+}
+
+int gbfem_operator_precision(gbfem_operator op, int* precision) {
+  if (!op || !precision) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_precision: null argument");
+  *precision = op->precision;
+  return GBFEM_OK;
+}
+
+int gbfem_operator_apply(gbfem_operator op, const void* u, void* w, void* stream) {
+  if (!op || !u || !w) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_apply: null argument");
+  if (u == w) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_apply: u and w must not alias");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (op->kind == OpKind::DG) return dg_apply(op, u, w, s, 0, nullptr);
+  return q1_apply(op, u, w, s, 0);
+}
+
+int gbfem_operator_apply_host(gbfem_operator op, const void* u_host, void* w_host) {
+  if (!op || !u_host || !w_host) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_apply_host: null argument");
+  const size_t bytes = size_t(op->ndofs) * (op->precision == GBFEM_F64 ? 8 : 4);
+  if (!op->host_u) {
+    GBFEM_CUDA_TRY(cudaMalloc(&op->host_u, bytes));
+    GBFEM_CUDA_TRY(cudaMalloc(&op->host_w, bytes));
+  }
+  GBFEM_CUDA_TRY(cudaMemcpyAsync(op->host_u, u_host, bytes, cudaMemcpyHostToDevice, 0));
+  GBFEM_TRY(gbfem_operator_apply(op, op->host_u, op->host_w, nullptr));
+  GBFEM_CUDA_TRY(cudaMemcpyAsync(w_host, op->host_w, bytes, cudaMemcpyDeviceToHost, 0));
+  GBFEM_CUDA_TRY(cudaStreamSynchronize(0));
+  return GBFEM_OK;
+}
+
+int gbfem_operator_block_diagonal(gbfem_operator op, void* blocks, void* stream) {
+  if (!op || !blocks) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_block_diagonal: null argument");
+  if (op->kind != OpKind::DG)
+    return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "block diagonal is defined for DG operators only");
+  return dg_apply(op, nullptr, nullptr, static_cast<cudaStream_t>(stream), 1, blocks);
+}
+
+}  // extern "C"
+
+extern "C" int gbfem_operator_diagonal(gbfem_operator op, void* diag, void* stream) {
+  if (!op || !diag) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_diagonal: null argument");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (op->kind == OpKind::DG) return dg_apply(op, nullptr, nullptr, s, 2, diag);
+  return q1_apply(op, nullptr, diag, s, 1);
+}

@@ -1,0 +1,35 @@
+// Definition of the opaque operator handle.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "../../include/gbfem.h"
+#include "dg_kernel.cuh"
+
+namespace gbfem {
+
+enum class OpKind { DG = 1, Q1 = 2 };
+
+// Element matrix of the continuous Q1 operator; local vertex k = kx + 2*ky.
+struct Q1Element {
+  double K[16];
+};
+
+int dg_apply(const struct ::gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
+             void* blocks);
+int q1_apply(const struct ::gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int diag_only);
+
+}  // namespace gbfem
+
+struct gbfem_operator_s {
+  gbfem::OpKind kind = gbfem::OpKind::DG;
+  int precision = GBFEM_F64;
+  gbfem_dg_desc dg{};
+  gbfem_grid_desc grid{};
+  int n = 0, q = 0, nloc = 0;
+  long long ncells = 0, ndofs = 0;
+  gbfem::DgTablesT<double> tab64{};
+  gbfem::DgTablesT<float> tab32{};
+  gbfem::Q1Element q1{};
+  void* host_u = nullptr;  // device staging of gbfem_operator_apply_host
+  void* host_w = nullptr;
+};

@@ -1,0 +1,218 @@
+"""Python binding of libgbfem's C-ABI (include/gbfem.h) through ctypes.
+
+It mirrors the reference's Python surface for this path: an operator object
+called as ``op(u, w)`` (dune/fempy/py/operator.hh:49,215), solvers called as
+``solver(f, u)`` (InverseOperator::operator(), solver/inverseoperatorinterface.hh:81-84).
+Dof vectors are DeviceArray objects resident in GPU memory.
+
+There is no CPU fallback: if libgbfem.so is missing, loading raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libgbfem.so")
+
+F64, F32 = 0, 1
+_DTYPES = {F64: np.float64, F32: np.float32}
+
+
+class GbfemError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("gbfem error %d: %s" % (code, msg))
+        self.code = code
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("dim", C.c_int), ("cells", C.c_int * 3), ("lower", C.c_double * 3),
+                ("upper", C.c_double * 3), ("periodic", C.c_int * 3)]
+
+
+class DgDesc(C.Structure):
+    _fields_ = [("grid", GridDesc), ("order", C.c_int), ("quad_points", C.c_int), ("precision", C.c_int),
+                ("diffusion", C.c_double), ("penalty", C.c_double), ("mass", C.c_double),
+                ("velocity", C.c_double * 3), ("weak_dirichlet", C.c_int), ("kappa", C.c_void_p)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libgbfem.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libgbfem.so not built: run __graft_entry__.build() (%s)" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        L.gbfem_last_error.restype = C.c_char_p
+        L.gbfem_dot.argtypes = [C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]
+        L.gbfem_axpy.argtypes = [C.c_int, C.c_int64, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.gbfem_scal.argtypes = [C.c_int, C.c_int64, C.c_double, C.c_void_p, C.c_void_p]
+        L.gbfem_copy.argtypes = [C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.gbfem_convert.argtypes = [C.c_int64, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        L.gbfem_malloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+        L.gbfem_free.argtypes = [C.c_void_p]
+        L.gbfem_memcpy_h2d.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+        L.gbfem_memcpy_d2h.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+        L.gbfem_memset.argtypes = [C.c_void_p, C.c_int, C.c_size_t]
+        L.gbfem_operator_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.gbfem_operator_apply_host.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.gbfem_operator_diagonal.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.gbfem_operator_block_diagonal.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.gbfem_operator_destroy.argtypes = [C.c_void_p]
+        L.gbfem_operator_size.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+        L.gbfem_dg_operator_create.argtypes = [C.POINTER(DgDesc), C.POINTER(C.c_void_p)]
+        L.gbfem_q1_operator_create.argtypes = [C.POINTER(GridDesc), C.c_int, C.c_double, C.c_double,
+                                               C.POINTER(C.c_void_p)]
+        L.gbfem_measure_fma_peaks.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != 0:
+        raise GbfemError(rc, lib().gbfem_last_error().decode())
+    return rc
+
+
+class DeviceArray:
+    """A dof vector in GPU memory (the storage of an AdaptiveDiscreteFunction)."""
+
+    def __init__(self, n, precision=F64):
+        self.n = int(n)
+        self.precision = precision
+        self.itemsize = 8 if precision == F64 else 4
+        self.ptr = C.c_void_p()
+        check(lib().gbfem_malloc(C.byref(self.ptr), self.n * self.itemsize))
+
+    @classmethod
+    def from_numpy(cls, a, precision=None):
+        a = np.ascontiguousarray(a)
+        if precision is None:
+            precision = F32 if a.dtype == np.float32 else F64
+        a = np.ascontiguousarray(a, dtype=_DTYPES[precision])
+        d = cls(a.size, precision)
+        check(lib().gbfem_memcpy_h2d(d.ptr, a.ctypes.data, a.nbytes))
+        return d
+
+    def numpy(self):
+        out = np.empty(self.n, dtype=_DTYPES[self.precision])
+        check(lib().gbfem_memcpy_d2h(out.ctypes.data, self.ptr, out.nbytes))
+        return out
+
+    def clear(self):
+        check(lib().gbfem_memset(self.ptr, 0, self.n * self.itemsize))
+
+    def free(self):
+        if self.ptr:
+            lib().gbfem_free(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def grid_desc(cells, lower=None, upper=None, periodic=None):
+    dim = len(cells)
+    g = GridDesc()
+    g.dim = dim
+    for k in range(3):
+        g.cells[k] = int(cells[k]) if k < dim else 1
+        g.lower[k] = (lower[k] if lower is not None else 0.0) if k < dim else 0.0
+        g.upper[k] = (upper[k] if upper is not None else 1.0) if k < dim else 1.0
+        g.periodic[k] = int(periodic[k]) if (periodic is not None and k < dim) else 0
+    return g
+
+
+class Operator:
+    """w = op(u): dune-fem's Operator::operator()(u, w) (operator/common/operator.hh:55)."""
+
+    def __init__(self, handle, precision):
+        self.handle = handle
+        self.precision = precision
+        n = C.c_int64()
+        check(lib().gbfem_operator_size(self.handle, C.byref(n)))
+        self.size = n.value
+
+    def __call__(self, u, w, stream=None):
+        check(lib().gbfem_operator_apply(self.handle, u.ptr, w.ptr, stream))
+
+    def apply_host(self, u, w):
+        """Host-buffer apply: copies u in, applies, copies w out (synchronous)."""
+        check(lib().gbfem_operator_apply_host(self.handle, u.ctypes.data, w.ctypes.data))
+
+    def diagonal(self):
+        d = DeviceArray(self.size, self.precision)
+        check(lib().gbfem_operator_diagonal(self.handle, d.ptr, None))
+        return d
+
+    def block_diagonal(self, nloc):
+        b = DeviceArray(self.size * nloc, self.precision)
+        check(lib().gbfem_operator_block_diagonal(self.handle, b.ptr, None))
+        return b
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().gbfem_operator_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+
+class DGOperator(Operator):
+    """SIPG / upwind / mass DG operator on a structured hexahedral grid."""
+
+    def __init__(self, cells, order, quad_points=0, precision=F64, diffusion=1.0, penalty=None, mass=0.0,
+                 velocity=(0.0, 0.0, 0.0), weak_dirichlet=True, periodic=(0, 0, 0), lower=(0.0, 0.0, 0.0),
+                 upper=(1.0, 1.0, 1.0), kappa=None):
+        d = DgDesc()
+        d.grid = grid_desc(cells, lower, upper, periodic)
+        d.order = order
+        d.quad_points = quad_points
+        d.precision = precision
+        d.diffusion = diffusion
+        d.penalty = 10.0 * (order + 1) ** 2 if penalty is None else penalty
+        d.mass = mass
+        for k in range(3):
+            d.velocity[k] = velocity[k]
+        d.weak_dirichlet = 1 if weak_dirichlet else 0
+        self.kappa = kappa  # keep the device array alive
+        d.kappa = kappa.ptr if kappa is not None else None
+        h = C.c_void_p()
+        check(lib().gbfem_dg_operator_create(C.byref(d), C.byref(h)))
+        self.desc = d
+        self.order = order
+        self.nloc = (order + 1) ** 3
+        super().__init__(h, precision)
+
+
+class Q1Operator(Operator):
+    """Continuous Lagrange Q1 on a 2-D grid with strong homogeneous Dirichlet rows."""
+
+    def __init__(self, cells, precision=F64, diffusion=1.0, mass=0.0, lower=(0.0, 0.0), upper=(1.0, 1.0)):
+        g = grid_desc(cells, lower, upper)
+        h = C.c_void_p()
+        check(lib().gbfem_q1_operator_create(C.byref(g), precision, diffusion, mass, C.byref(h)))
+        super().__init__(h, precision)
+
+
+def dot(x, y, stream=None):
+    r = C.c_double()
+    check(lib().gbfem_dot(x.precision, x.n, x.ptr, y.ptr, C.byref(r), stream))
+    return r.value
+
+
+def axpy(alpha, x, y, stream=None):
+    check(lib().gbfem_axpy(x.precision, x.n, alpha, x.ptr, y.ptr, stream))
+
+
+def measure_fma_peaks():
+    a, b = C.c_double(), C.c_double()
+    check(lib().gbfem_measure_fma_peaks(C.byref(a), C.byref(b)))
+    return a.value, b.value

@@ -1,0 +1,136 @@
+/*
+ * gbfem.h -- C-ABI of the GB300-native matrix-free operator apply and Krylov
+ * solve of dune-fem.
+ *
+ * Every entry point is `extern "C"`, takes opaque handles, plain pointers and
+ * sizes, and returns an int status (GBFEM_OK = 0, negative on error; the
+ * message is in gbfem_last_error()).  Dof vectors are device pointers unless
+ * a function name ends in `_host`.  A `stream` argument is a cudaStream_t
+ * passed as void* (NULL = the legacy default stream).
+ *
+ * Each declaration names the dune-fem interface it replaces (paths are
+ * relative to the dune-fem source tree).
+ */
+#ifndef GBFEM_H
+#define GBFEM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define GBFEM_OK 0
+#define GBFEM_ERR_INVALID (-1)         /* bad argument: DUNE_THROW(InvalidStateException/RangeError) */
+#define GBFEM_ERR_NOT_IMPLEMENTED (-2) /* DUNE_THROW(NotImplemented) */
+#define GBFEM_ERR_CUDA (-3)            /* CUDA runtime error (message holds cudaGetErrorString) */
+#define GBFEM_ERR_NO_DEVICE (-4)       /* no CUDA device visible */
+#define GBFEM_ERR_NONFINITE (-5)       /* NaN/Inf met in a solver (the reference asserts) */
+
+/* precisions of dof vectors and of the arithmetic of an operator */
+#define GBFEM_F64 0
+#define GBFEM_F32 1
+
+/* Returns the calling thread's last error message ("" if none). */
+const char* gbfem_last_error(void);
+/* Library version, major*10000 + minor*100 + patch. */
+int gbfem_version(void);
+
+/* ---- device memory (stands in for the DofManager-owned storage of
+ *      AdaptiveDiscreteFunction, function/adaptivefunction/adaptivefunction.hh:45-203)
+ * ----------------------------------------------------------------------- */
+int gbfem_malloc(void** ptr, size_t bytes);
+int gbfem_free(void* ptr);
+int gbfem_memcpy_h2d(void* dst, const void* src, size_t bytes);
+int gbfem_memcpy_d2h(void* dst, const void* src, size_t bytes);
+int gbfem_memset(void* ptr, int value, size_t bytes);
+int gbfem_synchronize(void);
+
+/* ---- structured Cartesian grid (replaces the YaspGrid leaf grid part the
+ *      reference tests build, e.g. solver/test/inverseoperatortest.cc:74) -- */
+typedef struct {
+  int dim;            /* 2 or 3 */
+  int cells[3];       /* cells per direction; cell index = ix + Nx*(iy + Ny*iz) */
+  double lower[3];    /* lower-left corner */
+  double upper[3];    /* upper-right corner */
+  int periodic[3];    /* 1 = periodic in that direction */
+} gbfem_grid_desc;
+
+/* ---- DG operator on a Q_p tensor Legendre space --------------------------
+ * Replaces GalerkinOperator<DGConservationLawModelIntegrands> for the SIPG
+ * diffusion + upwind advection + mass form (schemes/galerkin.hh:1383-1504,
+ * schemes/integrands.hh:748-967, UFL form pydemo/advectiondiffusion.py:33-55).
+ * Dof layout = the reference's DG block layout (space/discontinuousgalerkin/
+ * generic.hh:51-124): dof = cell*(p+1)^d + local, local = i0*(p+1)^2 + i1*(p+1)
+ * + i2 with i0 the x-degree (space/shapefunctionset/legendre.hh:168-193).
+ * ----------------------------------------------------------------------- */
+typedef struct {
+  gbfem_grid_desc grid;
+  int order;            /* p, 1..4 */
+  int quad_points;      /* Gauss points per direction q (volume and faces), p+1..p+3; 0 = p+2 */
+  int precision;        /* GBFEM_F64 or GBFEM_F32: dof vectors and arithmetic */
+  double diffusion;     /* eps in eps*kappa*grad u.grad v (0 = no diffusion) */
+  double penalty;       /* SIPG beta; face weight beta*avg(kappa)/h_F, h_F = avg|K|/|F| */
+  double mass;          /* c in c*u*v */
+  double velocity[3];   /* constant advection b, upwind flux; all zero = no advection */
+  int weak_dirichlet;   /* 1 = Nitsche weak u=0 on non-periodic boundary faces, 0 = do-nothing */
+  const void* kappa;    /* device DG coefficients of kappa (same layout/precision) or NULL = 1 */
+} gbfem_dg_desc;
+
+typedef struct gbfem_operator_s* gbfem_operator;
+
+/* Creates the SIPG/upwind DG operator.  ≙ constructing GalerkinOperator +
+ * DGConservationLawModelIntegrands (schemes/galerkin.hh:1383-1430). */
+int gbfem_dg_operator_create(const gbfem_dg_desc* desc, gbfem_operator* op);
+/* Continuous Lagrange Q1 operator for -div(eps grad u) + c u on a 2-D grid
+ * with strong Dirichlet rows on the whole boundary: w = A u, w_D = u_D.
+ * ≙ DirichletWrapperOperator over GalerkinOperator (schemes/dirichletwrapper.hh:
+ * 101-105, schemes/dirichletconstraints.hh:396-430).  Vertex dof numbering
+ * = ix + (Nx+1)*iy. */
+int gbfem_q1_operator_create(const gbfem_grid_desc* grid, int precision, double diffusion,
+                             double mass, gbfem_operator* op);
+int gbfem_operator_destroy(gbfem_operator op);
+/* Number of dofs of the domain/range space. */
+int gbfem_operator_size(gbfem_operator op, int64_t* ndofs);
+int gbfem_operator_precision(gbfem_operator op, int* precision);
+
+/* w = op(u).  ≙ Operator<D,R>::operator()(const D& u, R& w) const
+ * (operator/common/operator.hh:55); the reference clears w and rebuilds it
+ * (schemes/galerkin.hh:1459-1496), as this does.  u and w: device arrays of
+ * gbfem_operator_size elements of the operator's precision; must not alias. */
+int gbfem_operator_apply(gbfem_operator op, const void* u, void* w, void* stream);
+/* Same as gbfem_operator_apply with host arrays: copies u to the device,
+ * applies, copies w back, synchronously.  Device buffers are cached in op. */
+int gbfem_operator_apply_host(gbfem_operator op, const void* u_host, void* w_host);
+
+/* Diagonal of the operator's matrix.  ≙ DifferentiableOperator::jacobian
+ * (operator/common/differentiableoperator.hh:54) followed by
+ * SparseRowMatrix::extractDiagonal / DiagonalPreconditioner's setup
+ * (solver/diagonalpreconditioner.hh:60-99), without assembling the matrix. */
+int gbfem_operator_diagonal(gbfem_operator op, void* diag, void* stream);
+/* Dense element-diagonal blocks, row-major nloc x nloc per cell
+ * (nloc = (p+1)^d).  ≙ jacobian into BlockDiagonalLinearOperator
+ * (operator/linear/blockdiagonal.hh:24-135). */
+int gbfem_operator_block_diagonal(gbfem_operator op, void* blocks, void* stream);
+
+/* ---- BLAS-1 on dof vectors (function/common/discretefunction.hh:781-901,
+ *      function/common/scalarproducts.hh:101-127).  Reductions are
+ *      deterministic: fixed-order two-pass, independent of launch shape. -- */
+int gbfem_dot(int precision, int64_t n, const void* x, const void* y, double* result, void* stream);
+int gbfem_axpy(int precision, int64_t n, double alpha, const void* x, void* y, void* stream);
+int gbfem_scal(int precision, int64_t n, double alpha, void* x, void* stream);
+int gbfem_copy(int precision, int64_t n, const void* x, void* y, void* stream);
+/* y = (precision_y) x : precision conversion between FP64 and FP32 vectors. */
+int gbfem_convert(int64_t n, int precision_x, const void* x, int precision_y, void* y, void* stream);
+
+/* ---- microbenchmarks ---------------------------------------------------- */
+/* FP64 and FP32 FMA-pipe peaks of the current device in TFLOP/s. */
+int gbfem_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBFEM_H */

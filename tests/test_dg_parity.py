@@ -1,0 +1,142 @@
+"""Parity of the GPU DG operator apply (through the C-ABI) with the CPU oracle.
+
+The bar: FP64 within 1e-12 relative in the max norm; FP32 within 2e-5.
+"""
+import numpy as np
+import pytest
+
+from conftest import relmax
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 2e-5
+
+
+def _pair(gb, orc, cells, order, q=0, precision=0, kappa=None, **kw):
+    op = gb.DGOperator(cells, order, quad_points=q, precision=precision,
+                       kappa=None if kappa is None else gb.DeviceArray.from_numpy(kappa, precision), **kw)
+    prob = orc.DGProblem(cells, order, quad_points=q, **kw)
+    return op, prob
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+@pytest.mark.parametrize("qoff", [1, 2])
+def test_sipg_apply_fp64(gb, orc, order, qoff):
+    cells = (3, 4, 2)
+    rng = np.random.default_rng(100 + order)
+    op, prob = _pair(gb, orc, cells, order, q=order + qoff)
+    u = rng.uniform(-1, 1, prob.ndofs)
+    w = gb.DeviceArray(prob.ndofs)
+    op(gb.DeviceArray.from_numpy(u), w)
+    assert relmax(w.numpy(), prob.apply(u)) < TOL64
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_full_form_fp64(gb, orc, order):
+    """Diffusion + variable kappa + upwind advection + mass, periodic in y,
+    anisotropic cells."""
+    cells = (3, 2, 4)
+    kw = dict(diffusion=0.7, mass=1.3, velocity=(1.0, -0.5, 0.25), periodic=(0, 1, 0),
+              lower=(0.0, -1.0, 0.5), upper=(1.0, 0.5, 1.5))
+    rng = np.random.default_rng(7 + order)
+    nloc = (order + 1) ** 3
+    ncell = int(np.prod(cells))
+    kappa = np.zeros(ncell * nloc)
+    kappa[::nloc] = rng.uniform(0.5, 2.0, ncell)  # positive mean per cell
+    kappa += 0.05 * rng.uniform(-1, 1, ncell * nloc)
+    op, prob = _pair(gb, orc, cells, order, kappa=kappa, **kw)
+    u = rng.uniform(-1, 1, prob.ndofs)
+    w = gb.DeviceArray(prob.ndofs)
+    op(gb.DeviceArray.from_numpy(u), w)
+    assert relmax(w.numpy(), prob.apply(u, kappa=kappa)) < TOL64
+
+
+def test_periodic_advection_only(gb, orc):
+    cells = (4, 3, 2)
+    kw = dict(diffusion=0.0, velocity=(1.0, 0.5, 0.25), periodic=(1, 1, 1), weak_dirichlet=False)
+    op, prob = _pair(gb, orc, cells, 2, **kw)
+    u = np.random.default_rng(3).uniform(-1, 1, prob.ndofs)
+    w = gb.DeviceArray(prob.ndofs)
+    op(gb.DeviceArray.from_numpy(u), w)
+    assert relmax(w.numpy(), prob.apply(u)) < TOL64
+
+
+@pytest.mark.parametrize("order", [2, 3])
+def test_sipg_apply_fp32(gb, orc, order):
+    cells = (3, 3, 3)
+    op, prob = _pair(gb, orc, cells, order, precision=gb.F32)
+    u = np.random.default_rng(5).uniform(-1, 1, prob.ndofs).astype(np.float32)
+    w = gb.DeviceArray(prob.ndofs, gb.F32)
+    op(gb.DeviceArray.from_numpy(u), w)
+    assert relmax(w.numpy(), prob.apply(u.astype(np.float64))) < TOL32
+
+
+def test_apply_is_deterministic_and_host_path_matches(gb, orc):
+    cells = (5, 4, 3)
+    op, prob = _pair(gb, orc, cells, 3)
+    u = np.random.default_rng(11).uniform(-1, 1, prob.ndofs)
+    du = gb.DeviceArray.from_numpy(u)
+    w1 = gb.DeviceArray(prob.ndofs)
+    w2 = gb.DeviceArray(prob.ndofs)
+    op(du, w1)
+    op(du, w2)
+    a, b = w1.numpy(), w2.numpy()
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+    wh = np.empty(prob.ndofs)
+    op.apply_host(u, wh)
+    assert np.array_equal(wh.view(np.uint64), a.view(np.uint64))
+
+
+def test_linearity_and_symmetry_at_size(gb):
+    """Size-independent properties at a larger grid: A(au+bv) = aAu + bAv and
+    <Au, v> = <u, Av> (SIPG is symmetric)."""
+    cells = (16, 16, 16)
+    op = gb.DGOperator(cells, 3)
+    n = op.size
+    rng = np.random.default_rng(1)
+    u, v = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    Au, Av, Auv = (gb.DeviceArray(n) for _ in range(3))
+    op(gb.DeviceArray.from_numpy(u), Au)
+    op(gb.DeviceArray.from_numpy(v), Av)
+    op(gb.DeviceArray.from_numpy(2.0 * u - 0.5 * v), Auv)
+    au, av = Au.numpy(), Av.numpy()
+    assert relmax(Auv.numpy(), 2.0 * au - 0.5 * av) < 1e-13
+    s1, s2 = float(au @ v), float(u @ av)
+    assert abs(s1 - s2) <= 1e-12 * (abs(s1) + abs(s2))
+
+
+@pytest.mark.parametrize("order", [1, 3])
+def test_block_diagonal_and_diagonal(gb, orc, order):
+    cells = (3, 2, 2)
+    kw = dict(mass=0.5, velocity=(0.3, 0.0, -0.2))
+    op, prob = _pair(gb, orc, cells, order, **kw)
+    nloc = prob.nloc
+    blocks = op.block_diagonal(nloc).numpy().reshape(prob.ncells, nloc, nloc)
+    ref = prob.block_diagonal()
+    assert relmax(blocks, ref) < TOL64
+    diag = op.diagonal().numpy()
+    assert relmax(diag, np.einsum("cii->ci", ref).ravel()) < TOL64
+
+
+def test_q1_apply_and_diagonal(gb, orc):
+    cells = (9, 7)
+    op = gb.Q1Operator(cells, diffusion=1.0, mass=1.0)
+    u = np.random.default_rng(2).uniform(-1, 1, op.size)
+    w = gb.DeviceArray(op.size)
+    op(gb.DeviceArray.from_numpy(u), w)
+    assert relmax(w.numpy(), orc.q1_apply(cells, u, 1.0, 1.0)) < 1e-14
+    assert relmax(op.diagonal().numpy(), orc.q1_apply(cells, None, 1.0, 1.0, diag_only=True)) < 1e-14
+
+
+def test_dot_is_deterministic_fp64_and_fp32(gb):
+    n = 3_000_001
+    rng = np.random.default_rng(9)
+    x, y = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    dx, dy = gb.DeviceArray.from_numpy(x), gb.DeviceArray.from_numpy(y)
+    d1, d2 = gb.dot(dx, dy), gb.dot(dx, dy)
+    assert d1 == d2
+    assert abs(d1 - float(x @ y)) < 1e-10
+    fx, fy = gb.DeviceArray.from_numpy(x.astype(np.float32)), gb.DeviceArray.from_numpy(y.astype(np.float32))
+    ref = float(x.astype(np.float32).astype(np.float64) @ y.astype(np.float32).astype(np.float64))
+    assert abs(gb.dot(fx, fy) - ref) < 1e-9

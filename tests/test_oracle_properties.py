@@ -1,0 +1,57 @@
+"""Properties of the CPU oracle itself (no GPU): the invariants the reference's
+tests rely on (SURVEY of dune-fem tests: apply = assembled Jacobian . vector,
+symmetry of SIPG, thread-count invariance)."""
+import numpy as np
+import pytest
+
+from conftest import relmax
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_sipg_is_symmetric(orc, order):
+    prob = orc.DGProblem((3, 2, 2), order, mass=0.3)
+    rng = np.random.default_rng(order)
+    u, v = rng.uniform(-1, 1, prob.ndofs), rng.uniform(-1, 1, prob.ndofs)
+    a, b = prob.apply(u) @ v, u @ prob.apply(v)
+    assert abs(a - b) < 1e-12 * (abs(a) + abs(b))
+
+
+def test_sipg_is_positive_definite_on_random_vectors(orc):
+    prob = orc.DGProblem((2, 2, 2), 2)
+    rng = np.random.default_rng(0)
+    for _ in range(5):
+        u = rng.uniform(-1, 1, prob.ndofs)
+        assert u @ prob.apply(u) > 0
+
+
+def test_apply_equals_assembled_matrix_times_vector(orc):
+    """Matrix-free apply == (dense matrix assembled column by column) . u
+    (the self-consistency check of dune/fempy/test/testoperator.py:33-71)."""
+    prob = orc.DGProblem((2, 2, 1), 1, velocity=(0.4, -0.2, 0.1), mass=1.0, periodic=(1, 0, 0))
+    n = prob.ndofs
+    A = np.zeros((n, n))
+    for j in range(n):
+        e = np.zeros(n)
+        e[j] = 1.0
+        A[:, j] = prob.apply(e)
+    u = np.random.default_rng(1).uniform(-1, 1, n)
+    assert relmax(A @ u, prob.apply(u)) < 1e-14
+    # the diagonal blocks of that matrix are the oracle's block diagonal
+    B = prob.block_diagonal()
+    for c in range(prob.ncells):
+        s = slice(c * prob.nloc, (c + 1) * prob.nloc)
+        assert relmax(B[c], A[s, s]) < 1e-14
+
+
+def test_threaded_apply_matches_serial(orc):
+    prob = orc.DGProblem((4, 4, 4), 2, velocity=(1, 0.5, 0.25))
+    u = np.random.default_rng(2).uniform(-1, 1, prob.ndofs)
+    assert relmax(prob.apply(u, nthreads=4), prob.apply(u, nthreads=1)) < 1e-14
+
+
+def test_constant_is_in_kernel_of_periodic_diffusion(orc):
+    """On a fully periodic grid the SIPG Laplacian annihilates constants."""
+    prob = orc.DGProblem((3, 3, 3), 2, periodic=(1, 1, 1), weak_dirichlet=False)
+    u = np.zeros(prob.ndofs)
+    u[::prob.nloc] = 1.0  # L_0 = 1 in every cell
+    assert np.max(np.abs(prob.apply(u))) < 1e-12
