@@ -191,3 +191,24 @@ int gbfem_convert(int64_t n, int px, const void* x, int py, void* y, void* strea
 }
 
 }  // extern "C"
+
+namespace gbfem {
+
+// Dot product over fixed chunks of `chunk` elements (one partial each),
+// launched on caller-provided scratch.  Used by the allocation-free entry
+// point; gbfem_dot keeps its own partition above.
+int dot_device_fixed_chunks(int precision, long long n, long long chunk, const void* x, const void* y,
+                            double* d_out, double* d_partial, cudaStream_t s) {
+  const long long np = (n + chunk - 1) / chunk;
+  if (precision == GBFEM_F64)
+    dot_partial_kernel<double><<<unsigned(np), kRedThreads, 0, s>>>(static_cast<const double*>(x),
+                                                                   static_cast<const double*>(y), n, chunk, d_partial);
+  else
+    dot_partial_kernel<float><<<unsigned(np), kRedThreads, 0, s>>>(static_cast<const float*>(x),
+                                                                  static_cast<const float*>(y), n, chunk, d_partial);
+  dot_final_kernel<<<1, kRedThreads, 0, s>>>(d_partial, int(np), d_out);
+  GBFEM_CUDA_TRY(cudaGetLastError());
+  return GBFEM_OK;
+}
+
+}  // namespace gbfem

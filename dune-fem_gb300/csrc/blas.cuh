@@ -10,6 +10,10 @@ int dot_num_partials(long long n);
 // d_partial must hold dot_num_partials(n) doubles.
 int dot_device(int precision, long long n, const void* x, const void* y, double* d_out, double* d_partial,
                cudaStream_t s);
+// Dot product over fixed chunks of `chunk` elements on caller-provided
+// scratch (ceil(n/chunk) partials).
+int dot_device_fixed_chunks(int precision, long long n, long long chunk, const void* x, const void* y,
+                            double* d_out, double* d_partial, cudaStream_t s);
 // The library's per-device scratch (allocated on first use).
 int library_scratch(double** partial, double** result);
 // Grid size of the grid-stride streaming kernels.
