@@ -65,7 +65,9 @@ struct DgArgsT {
   int advect;         // b != 0
   int weak_dirichlet; // Nitsche u = 0 on non-periodic boundary faces
   int unit_mode;      // 1: block-diagonal assembly (own dofs = e_j, neighbour u = 0); 2: diagonal only
-  T* blocks;          // unit_mode 1 output blocks[cell][i][j]; unit_mode 2 output diag[cell][j]
+  T* blocks;          // unit_mode 1 output blocks[cell - cell_begin][i][j]; unit_mode 2 output diag[cell][j]
+  long long cell_begin;  // unit_mode 1: first cell of the batch
+  long long cell_count;  // unit_mode 1: cells in the batch (0 = all)
 };
 
 // out = contraction of `in` along axis AX with matrix M.
@@ -140,9 +142,11 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args, co
   for (int i = tid; i < 2 * N; i += blockDim.x) { str[i] = tabs.tr[i]; sdtr[i] = tabs.dtr[i]; }
 
   const long long ncells = args.ncells;
-  // In unit mode the "virtual cells" are (cell, j) pairs: vcell = cell*N3 + j.
-  const long long nvirt = args.unit_mode ? ncells * N3 : ncells;
-  const long long v0 = (long long)blockIdx.x * CPB;
+  // In unit mode the "virtual cells" are (cell, j) pairs: vcell = cell*N3 + j,
+  // for cells in [cell_begin, cell_begin + cell_count).
+  const long long ucount = args.cell_count > 0 ? args.cell_count : ncells;
+  const long long nvirt = args.unit_mode ? (args.cell_begin + ucount) * N3 : ncells;
+  const long long v0 = (long long)blockIdx.x * CPB + (args.unit_mode ? args.cell_begin * N3 : 0);
   if (v0 >= nvirt) return;
 
   // ---- load own dofs (and kappa) ------------------------------------------
@@ -395,7 +399,7 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args, co
     if (args.unit_mode) {
       const long long cell = v / N3;
       const int j = int(v - cell * N3);
-      if (args.unit_mode == 1) args.blocks[(cell * N3 + i) * N3 + j] = sr[e];
+      if (args.unit_mode == 1) args.blocks[((cell - args.cell_begin) * N3 + i) * N3 + j] = sr[e];
       else if (i == j) args.blocks[cell * N3 + j] = sr[e];  // diagonal only
     } else {
       __stcs(args.w + v * N3 + i, sr[e]);

@@ -60,10 +60,12 @@ static void fill_dg_args(const gbfem_operator_s* op, DgArgsT<T>* a) {
 }
 
 int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
-             void* blocks) {
+             void* blocks, long long cell_begin, long long cell_count) {
   if (op->precision == GBFEM_F64) {
     DgArgsT<double> a;
     fill_dg_args(op, &a);
+    a.cell_begin = cell_begin;
+    a.cell_count = cell_count;
     a.u = static_cast<const double*>(u);
     a.w = static_cast<double*>(w);
     a.unit_mode = unit_mode;
@@ -72,6 +74,8 @@ int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s,
   } else {
     DgArgsT<float> a;
     fill_dg_args(op, &a);
+    a.cell_begin = cell_begin;
+    a.cell_count = cell_count;
     a.u = static_cast<const float*>(u);
     a.w = static_cast<float*>(w);
     a.unit_mode = unit_mode;

@@ -14,8 +14,10 @@ struct Q1Element {
   double K[16];
 };
 
+// unit_mode 0: w = A u; 1: diagonal blocks of cells [cell_begin, cell_begin+cell_count)
+// (cell_count 0 = all) into blocks; 2: the diagonal into blocks.
 int dg_apply(const struct ::gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
-             void* blocks);
+             void* blocks, long long cell_begin = 0, long long cell_count = 0);
 int q1_apply(const struct ::gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int diag_only);
 
 }  // namespace gbfem

@@ -1,0 +1,767 @@
+// Krylov inverse operators and preconditioners on device-resident dof
+// vectors.
+//
+// The loops follow dune-fem's LinearSolver templates statement by statement
+// (solver/linear/cg.hh:18-117, gmres.hh:116-299, bicgstab.hh:63-222) so the
+// iteration counts and iterates match the reference's.  Only vector
+// operations and scalar products run on the device; the Krylov scalars
+// (alpha, beta, Givens rotations) are FP64 host values, as in the
+// reference.  Each dot product is the deterministic two-pass FP64 reduction
+// of blas.cu, read back with one stream synchronisation.  FCG and FGMRES
+// (flexible variants for a preconditioner that changes between iterations,
+// e.g. the learned one) follow Notay (2000) and Saad (1993).
+#include <cuda_runtime.h>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "blas.cuh"
+#include "gbfem_internal.cuh"
+#include "operator_impl.hpp"
+#include "solver_impl.hpp"
+
+namespace gbfem {
+
+// ---------------------------------------------------------------- kernels --
+template <typename T>
+__global__ void k_axpby(long long n, double a, const T* __restrict__ x, double b, T* __restrict__ y) {
+  // y = a*x + b*y
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = T(a) * x[i] + T(b) * y[i];
+}
+template <typename T>
+__global__ void k_axpbypcz(long long n, double a, const T* __restrict__ x, double b, const T* __restrict__ y,
+                           double c, T* __restrict__ z) {
+  // z = a*x + b*y + c*z
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    z[i] = T(a) * x[i] + T(b) * y[i] + T(c) * z[i];
+}
+template <typename T>
+__global__ void k_diag_apply(long long n, const T* __restrict__ dinv, const T* __restrict__ r, T* __restrict__ z) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    z[i] = r[i] * dinv[i];
+}
+template <typename T>
+__global__ void k_diag_invert(long long n, T* __restrict__ d) {
+  // DiagonalPreconditionerBase: near-zero entries become 1 (diagonalpreconditioner.hh:94-99)
+  const T eps = T(16) * (sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-07));
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const T v = d[i];
+    d[i] = (v < eps && v > -eps) ? T(1) : T(1) / v;
+  }
+}
+
+// In-place Gauss-Jordan inversion with partial pivoting of one nb x nb block
+// per CTA, in FP64 shared memory; result stored in TO.
+template <typename TI, typename TO>
+__global__ void k_block_invert(const TI* __restrict__ blocks, TO* __restrict__ inv, int nb, long long nblocks,
+                               int* __restrict__ singular) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  double* a = reinterpret_cast<double*>(smraw);  // nb*nb
+  int* perm = reinterpret_cast<int*>(a + nb * nb);  // nb
+  __shared__ int s_piv;
+  const long long b = blockIdx.x;
+  if (b >= nblocks) return;
+  const TI* src = blocks + b * nb * nb;
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) a[e] = double(src[e]);
+  __syncthreads();
+  for (int k = 0; k < nb; ++k) {
+    if (threadIdx.x == 0) {
+      int p = k;
+      double best = fabs(a[k * nb + k]);
+      for (int i = k + 1; i < nb; ++i) {
+        const double v = fabs(a[i * nb + k]);
+        if (v > best) { best = v; p = i; }
+      }
+      s_piv = p;
+      perm[k] = p;
+      if (best == 0.0) atomicExch(singular, 1);
+    }
+    __syncthreads();
+    const int p = s_piv;
+    if (p != k)
+      for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+        const double t = a[k * nb + j];
+        a[k * nb + j] = a[p * nb + j];
+        a[p * nb + j] = t;
+      }
+    __syncthreads();
+    const double piv = a[k * nb + k];
+    const double ipiv = piv != 0.0 ? 1.0 / piv : 0.0;
+    __syncthreads();
+    // scale pivot row; a[k][k] becomes 1/piv
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) a[k * nb + j] = (j == k) ? ipiv : a[k * nb + j] * ipiv;
+    __syncthreads();
+    // eliminate column k from all other rows
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+      const int i = e / nb, j = e - i * nb;
+      if (i == k) continue;
+      const double f = a[i * nb + k];
+      if (j == k) continue;
+      a[e] -= f * a[k * nb + j];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb; i += blockDim.x)
+      if (i != k) a[i * nb + k] = -a[i * nb + k] * ipiv;
+    __syncthreads();
+  }
+  // undo the row interchanges as column interchanges, last first
+  for (int k = nb - 1; k >= 0; --k) {
+    const int p = perm[k];
+    if (p != k)
+      for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        const double t = a[i * nb + k];
+        a[i * nb + k] = a[i * nb + p];
+        a[i * nb + p] = t;
+      }
+    __syncthreads();
+  }
+  TO* dst = inv + b * nb * nb;
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) dst[e] = TO(a[e]);
+}
+
+// z_K = Binv_K r_K: one warp per row group, CPB cells per CTA, r_K in smem.
+template <typename T>
+__global__ void k_block_apply(const T* __restrict__ binv, const T* __restrict__ r, T* __restrict__ z, int nb,
+                              long long ncells) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* rs = reinterpret_cast<T*>(smraw);
+  const long long c = blockIdx.x;
+  if (c >= ncells) return;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) rs[i] = r[c * nb + i];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const T* B = binv + c * (long long)nb * nb;
+  for (int row = warp; row < nb; row += nw) {
+    double s = 0.0;
+    for (int j = lane; j < nb; j += 32) s += double(B[(long long)row * nb + j]) * double(rs[j]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) z[c * nb + row] = T(s);
+  }
+}
+
+// ------------------------------------------------------------ vector ops --
+struct Ctx {
+  int prec;
+  long long n;
+  cudaStream_t s;
+  double* d_partial = nullptr;
+  double* d_res = nullptr;
+  double* h_res = nullptr;  // pinned
+  int op_applies = 0, pc_applies = 0;
+  int setup(int precision, long long nn, cudaStream_t st) {
+    prec = precision;
+    n = nn;
+    s = st;
+    GBFEM_CUDA_TRY(cudaMalloc(&d_partial, sizeof(double) * (dot_num_partials(n) + 8)));
+    GBFEM_CUDA_TRY(cudaMalloc(&d_res, sizeof(double) * 8));
+    GBFEM_CUDA_TRY(cudaMallocHost(&h_res, sizeof(double) * 8));
+    return GBFEM_OK;
+  }
+  ~Ctx() {
+    if (d_partial) cudaFree(d_partial);
+    if (d_res) cudaFree(d_res);
+    if (h_res) cudaFreeHost(h_res);
+  }
+  size_t bytes() const { return size_t(n) * (prec == GBFEM_F64 ? 8 : 4); }
+  int dot(const void* x, const void* y, double* out) {
+    GBFEM_TRY(dot_device(prec, n, x, y, d_res, d_partial, s));
+    GBFEM_CUDA_TRY(cudaMemcpyAsync(h_res, d_res, sizeof(double), cudaMemcpyDeviceToHost, s));
+    GBFEM_CUDA_TRY(cudaStreamSynchronize(s));
+    *out = h_res[0];
+    return GBFEM_OK;
+  }
+  // y = a*x + b*y
+  int axpby(double a, const void* x, double b, void* y) {
+    if (prec == GBFEM_F64)
+      k_axpby<double><<<stream_grid(n), 256, 0, s>>>(n, a, (const double*)x, b, (double*)y);
+    else
+      k_axpby<float><<<stream_grid(n), 256, 0, s>>>(n, a, (const float*)x, b, (float*)y);
+    GBFEM_CUDA_TRY(cudaGetLastError());
+    return GBFEM_OK;
+  }
+  // z = a*x + b*y + c*z
+  int axpbypcz(double a, const void* x, double b, const void* y, double c, void* z) {
+    if (prec == GBFEM_F64)
+      k_axpbypcz<double><<<stream_grid(n), 256, 0, s>>>(n, a, (const double*)x, b, (const double*)y, c, (double*)z);
+    else
+      k_axpbypcz<float><<<stream_grid(n), 256, 0, s>>>(n, a, (const float*)x, b, (const float*)y, c, (float*)z);
+    GBFEM_CUDA_TRY(cudaGetLastError());
+    return GBFEM_OK;
+  }
+  int copy(const void* x, void* y) {
+    GBFEM_CUDA_TRY(cudaMemcpyAsync(y, x, bytes(), cudaMemcpyDeviceToDevice, s));
+    return GBFEM_OK;
+  }
+  int clear(void* x) {
+    GBFEM_CUDA_TRY(cudaMemsetAsync(x, 0, bytes(), s));
+    return GBFEM_OK;
+  }
+};
+
+struct Vecs {
+  std::vector<void*> v;
+  ~Vecs() {
+    for (void* p : v) cudaFree(p);
+  }
+  int alloc(int k, size_t bytes) {
+    for (int i = 0; i < k; ++i) {
+      void* p = nullptr;
+      GBFEM_CUDA_TRY(cudaMalloc(&p, bytes));
+      v.push_back(p);
+    }
+    return GBFEM_OK;
+  }
+  void* operator[](int i) const { return v[i]; }
+};
+
+static bool finite(double x) { return std::isfinite(x); }
+
+int precond_apply(const gbfem_preconditioner_s* pc, const void* r, void* z, cudaStream_t s) {
+  const long long n = pc->n;
+  switch (pc->kind) {
+    case PcKind::Diagonal:
+      if (pc->precision == GBFEM_F64)
+        k_diag_apply<double><<<stream_grid(n), 256, 0, s>>>(n, (const double*)pc->data, (const double*)r, (double*)z);
+      else
+        k_diag_apply<float><<<stream_grid(n), 256, 0, s>>>(n, (const float*)pc->data, (const float*)r, (float*)z);
+      break;
+    case PcKind::BlockJacobi: {
+      const int nb = pc->nloc;
+      const long long nc = n / nb;
+      const size_t sm = size_t(nb) * (pc->precision == GBFEM_F64 ? 8 : 4);
+      if (pc->precision == GBFEM_F64)
+        k_block_apply<double><<<unsigned(nc), 128, sm, s>>>((const double*)pc->data, (const double*)r, (double*)z, nb, nc);
+      else
+        k_block_apply<float><<<unsigned(nc), 128, sm, s>>>((const float*)pc->data, (const float*)r, (float*)z, nb, nc);
+      break;
+    }
+    case PcKind::External:
+      return pc->ext_apply(pc->ext_ctx, r, z, s);
+  }
+  GBFEM_CUDA_TRY(cudaGetLastError());
+  return GBFEM_OK;
+}
+
+static int op_apply(gbfem_operator op, const void* u, void* w, Ctx& c) {
+  ++c.op_applies;
+  return gbfem_operator_apply(op, u, w, c.s);
+}
+static int pc_apply(gbfem_preconditioner pc, const void* r, void* z, Ctx& c) {
+  ++c.pc_applies;
+  return precond_apply(pc, r, z, c.s);
+}
+
+// ------------------------------------------------------------------- CG ----
+// LinearSolver::cg (solver/linear/cg.hh:18-117), same statements in order.
+static int cg(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_params& prm, const void* b, void* x,
+              Ctx& c, gbfem_solver_info* info) {
+  Vecs tmp;
+  GBFEM_TRY(tmp.alloc(pc ? 5 : 3, c.bytes()));
+  void* h = tmp[0];
+  void* r = tmp[1];
+  void* p = tmp[2];
+  void* s = pc ? tmp[3] : p;
+  void* q = pc ? tmp[4] : p;
+  GBFEM_TRY(op_apply(op, x, h, c));
+  GBFEM_TRY(c.copy(h, r));
+  GBFEM_TRY(c.axpby(-1.0, b, 1.0, r));   // r = h - b
+  GBFEM_TRY(c.copy(b, p));
+  GBFEM_TRY(c.axpby(-1.0, h, 1.0, p));   // p = b - h
+  if (pc) {
+    GBFEM_TRY(pc_apply(pc, p, q, c));
+    GBFEM_TRY(c.copy(q, s));
+  }
+  double prev = 0.0, residual = 0.0;
+  GBFEM_TRY(c.dot(p, q, &residual));
+  double bb = 1.0;
+  if (prm.error_measure == GBFEM_TOL_RELATIVE) GBFEM_TRY(c.dot(b, b, &bb));
+  const double tolerance = prm.tolerance * prm.tolerance *
+                           (prm.error_measure == GBFEM_TOL_RELATIVE ? bb
+                            : prm.error_measure == GBFEM_TOL_RESIDUAL_REDUCTION ? residual : 1.0);
+  int it = 0;
+  if (!finite(residual) || !finite(tolerance)) info->status = GBFEM_ERR_NONFINITE;
+  for (it = 0; info->status == GBFEM_OK && residual > tolerance && it < prm.max_iterations; ++it) {
+    if (it > 0) {
+      const double beta = residual / prev;
+      if (pc) GBFEM_TRY(c.axpby(1.0, s, beta, q));   // q = beta q + s
+      else GBFEM_TRY(c.axpby(-1.0, r, beta, p));     // p = beta p - r
+    }
+    GBFEM_TRY(op_apply(op, q, h, c));
+    double qdoth = 0.0;
+    GBFEM_TRY(c.dot(q, h, &qdoth));
+    const double alpha = residual / qdoth;
+    if (!finite(alpha)) { info->status = GBFEM_ERR_NONFINITE; break; }
+    GBFEM_TRY(c.axpby(alpha, q, 1.0, x));
+    if (pc) {
+      GBFEM_TRY(c.axpby(-alpha, h, 1.0, p));
+      GBFEM_TRY(pc_apply(pc, p, s, c));
+      prev = residual;
+      GBFEM_TRY(c.dot(p, s, &residual));
+    } else {
+      GBFEM_TRY(c.axpby(alpha, h, 1.0, r));
+      prev = residual;
+      GBFEM_TRY(c.dot(r, r, &residual));
+    }
+    if (prm.verbose) std::printf("gbfem CG it: %d : residual %.6e\n", it, std::sqrt(std::fabs(residual)));
+  }
+  info->residual = std::sqrt(std::fabs(residual));
+  info->iterations = it < prm.max_iterations ? it : -it;
+  info->converged = (it < prm.max_iterations && info->status == GBFEM_OK) ? 1 : 0;
+  return GBFEM_OK;
+}
+
+// ----------------------------------------------------------------- GMRES ---
+static void rotate(double* x, double* y, double cc, double ss) {
+  const double a = *x, b = *y;
+  *x = cc * a + ss * b;
+  *y = cc * b - ss * a;
+}
+
+// LinearSolver::gmres (solver/linear/gmres.hh:116-299), right-preconditioned
+// restarted GMRES(m) with Givens rotations.  flexible = true keeps every
+// preconditioned direction z_j = M_j^{-1} v_j and updates u += Z y (FGMRES,
+// Saad 1993), so the preconditioner may change between iterations.
+static int gmres(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_params& prm, const void* b,
+                 void* u, Ctx& c, gbfem_solver_info* info, bool flexible) {
+  const int m = prm.restart > 0 ? prm.restart : 20;
+  Vecs v, zf;
+  GBFEM_TRY(v.alloc(m + 2, c.bytes()));
+  if (flexible && pc) GBFEM_TRY(zf.alloc(m, c.bytes()));
+  std::vector<double> H((m + 1) * m, 0.0), g(m + 1, 0.0), sn(m, 0.0), cs(m, 0.0), y(m, 0.0), gd(m + 1, 0.0);
+  auto Hm = [&](int i, int j) -> double& { return H[i * m + j]; };
+  double tol = prm.tolerance;
+  if (prm.error_measure == GBFEM_TOL_RELATIVE) {
+    double bb;
+    GBFEM_TRY(c.dot(b, b, &bb));
+    tol *= std::sqrt(bb);
+  }
+  int iterations = 0;
+  double res = 0.0;
+  while (true) {
+    GBFEM_TRY(op_apply(op, u, v[0], c));
+    GBFEM_TRY(c.axpby(-1.0, b, 1.0, v[0]));  // v0 = A u - b
+    double d0;
+    GBFEM_TRY(c.dot(v[0], v[0], &d0));
+    res = std::sqrt(d0);
+    if (prm.error_measure == GBFEM_TOL_RESIDUAL_REDUCTION && iterations == 0) tol *= res;
+    if (!finite(res)) { info->status = GBFEM_ERR_NONFINITE; break; }
+    if (prm.verbose) std::printf("gbfem GMRES outer iteration : %.6e\n", res);
+    if (res <= tol * (1 + 1e-15)) break;
+    g[0] = -res;
+    for (int i = 1; i <= m; ++i) g[i] = 0.0;
+    GBFEM_TRY(c.axpby(0.0, v[0], 1.0 / res, v[0]));
+    int jlast = 0;
+    for (int j = 0; j < m; ++j) {
+      void* vj = v[j];
+      void* vjp = v[j + 1];
+      if (pc) {
+        void* z = flexible ? zf[j] : v[m + 1];
+        GBFEM_TRY(pc_apply(pc, vj, z, c));
+        GBFEM_TRY(op_apply(op, z, vjp, c));
+      } else {
+        GBFEM_TRY(op_apply(op, vj, vjp, c));
+      }
+      for (int l = 0; l <= j; ++l) GBFEM_TRY(c.dot(vjp, v[l], &gd[l]));
+      for (int i = 0; i <= j; ++i) Hm(i, j) = gd[i];
+      for (int l = 0; l <= j; ++l) GBFEM_TRY(c.axpby(-gd[l], v[l], 1.0, vjp));
+      double nn;
+      GBFEM_TRY(c.dot(vjp, vjp, &nn));
+      Hm(j + 1, j) = std::sqrt(nn);
+      GBFEM_TRY(c.axpby(0.0, vjp, 1.0 / Hm(j + 1, j), vjp));
+      for (int i = 0; i < j; ++i) rotate(&Hm(i + 1, j), &Hm(i, j), cs[i], sn[i]);
+      const double hjj = Hm(j, j), hjpj = Hm(j + 1, j);
+      const double nrm = std::sqrt(hjj * hjj + hjpj * hjpj);
+      cs[j] = hjj / nrm;
+      sn[j] = -hjpj / nrm;
+      rotate(&Hm(j + 1, j), &Hm(j, j), cs[j], sn[j]);
+      rotate(&g[j + 1], &g[j], cs[j], sn[j]);
+      ++iterations;
+      jlast = j;
+      if (prm.verbose) std::printf("gbfem GMRES it: %d : %.6e\n", iterations, std::fabs(g[j + 1]));
+      if (!finite(g[j + 1])) { info->status = GBFEM_ERR_NONFINITE; break; }
+      if (std::fabs(g[j + 1]) < tol || iterations >= prm.max_iterations) break;
+    }
+    if (info->status != GBFEM_OK) break;
+    int last = iterations % m;
+    if (last == 0) last = m;
+    if (flexible) last = jlast + 1;
+    for (int i = last - 1; i >= 0; --i) {
+      double dt = 0.0;
+      for (int k = 0; k < last - (i + 1); ++k) dt += Hm(i, i + 1 + k) * y[i + 1 + k];
+      y[i] = (g[i] - dt) / Hm(i, i);
+    }
+    if (pc && !flexible) {
+      void* ut = v[m];
+      void* z = v[m + 1];
+      GBFEM_TRY(c.clear(ut));
+      for (int i = 0; i < last; ++i) GBFEM_TRY(c.axpby(y[i], v[i], 1.0, ut));
+      GBFEM_TRY(pc_apply(pc, ut, z, c));
+      GBFEM_TRY(c.axpby(1.0, z, 1.0, u));
+    } else if (pc && flexible) {
+      for (int i = 0; i < last; ++i) GBFEM_TRY(c.axpby(y[i], zf[i], 1.0, u));
+    } else {
+      for (int i = 0; i < last; ++i) GBFEM_TRY(c.axpby(y[i], v[i], 1.0, u));
+    }
+    res = std::fabs(g[last]);
+    if (std::fabs(g[last]) < tol) break;
+    // The reference loops on here even past maxIterations (gmres.hh:150-286);
+    // stop instead.
+    if (iterations >= prm.max_iterations) break;
+  }
+  info->residual = res;
+  info->iterations = iterations < prm.max_iterations ? iterations : -iterations;
+  info->converged = (iterations < prm.max_iterations && info->status == GBFEM_OK) ? 1 : 0;
+  return GBFEM_OK;
+}
+
+// -------------------------------------------------------------- BiCGstab ---
+// LinearSolver::bicgstab (solver/linear/bicgstab.hh:63-222), right
+// preconditioning with x the preconditioned variable, as the reference.
+static int bicgstab(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_params& prm, const void* b,
+                    void* x, Ctx& c, gbfem_solver_info* info) {
+  Vecs t;
+  GBFEM_TRY(t.alloc(pc ? 6 : 5, c.bytes()));
+  void *r = t[0], *rs = t[1], *p = t[2], *s = t[3], *tmp = t[4];
+  void* z = pc ? t[5] : r;
+  double tol = prm.tolerance, gdot[5];
+  if (prm.error_measure == GBFEM_TOL_RELATIVE) {
+    GBFEM_TRY(c.dot(b, b, &gdot[0]));
+    tol *= std::sqrt(gdot[0]);
+  }
+  if (pc) {
+    GBFEM_TRY(pc_apply(pc, x, z, c));
+    GBFEM_TRY(op_apply(op, z, r, c));
+  } else {
+    GBFEM_TRY(op_apply(op, x, r, c));
+  }
+  GBFEM_TRY(c.axpby(1.0, b, -1.0, r));  // r = b - r
+  GBFEM_TRY(c.copy(r, p));
+  GBFEM_TRY(c.copy(r, rs));
+  GBFEM_TRY(c.dot(r, rs, &gdot[0]));
+  double nu = gdot[0];
+  if (prm.error_measure == GBFEM_TOL_RESIDUAL_REDUCTION) tol *= std::sqrt(nu);
+  int iterations = 0;
+  double res = 0.0;
+  while (true) {
+    if (pc) {
+      GBFEM_TRY(pc_apply(pc, p, z, c));
+      GBFEM_TRY(op_apply(op, z, tmp, c));
+    } else {
+      GBFEM_TRY(op_apply(op, p, tmp, c));
+    }
+    GBFEM_TRY(c.dot(tmp, rs, &gdot[0]));
+    const double alpha = nu / gdot[0];
+    GBFEM_TRY(c.copy(r, s));
+    GBFEM_TRY(c.axpby(-alpha, tmp, 1.0, s));
+    if (pc) {
+      GBFEM_TRY(pc_apply(pc, s, z, c));
+      GBFEM_TRY(op_apply(op, z, r, c));
+    } else {
+      GBFEM_TRY(op_apply(op, s, r, c));
+    }
+    GBFEM_TRY(c.dot(r, s, &gdot[0]));
+    GBFEM_TRY(c.dot(r, r, &gdot[1]));
+    GBFEM_TRY(c.dot(s, s, &gdot[2]));
+    GBFEM_TRY(c.dot(s, rs, &gdot[3]));
+    GBFEM_TRY(c.dot(r, rs, &gdot[4]));
+    const double omega = gdot[0] / gdot[1];
+    res = std::sqrt(gdot[2] - omega * (2.0 * gdot[0] - omega * gdot[1]));
+    const double beta = (gdot[3] - omega * gdot[4]) * alpha / (omega * nu);
+    nu = gdot[3] - omega * gdot[4];
+    GBFEM_TRY(c.axpbypcz(alpha, p, omega, s, 1.0, x));
+    ++iterations;
+    if (!finite(res) || !finite(beta)) { info->status = GBFEM_ERR_NONFINITE; break; }
+    if (res < tol || iterations >= prm.max_iterations) break;
+    GBFEM_TRY(c.axpby(1.0, s, -omega, r));                       // r = s - omega r
+    GBFEM_TRY(c.axpbypcz(1.0, r, -omega * beta, tmp, beta, p));  // p = r + beta (p - omega tmp)
+    if (prm.verbose) std::printf("gbfem BiCGstab it: %d : %.6e\n", iterations, res);
+  }
+  if (pc) {
+    GBFEM_TRY(pc_apply(pc, x, z, c));
+    GBFEM_TRY(c.copy(z, x));
+  }
+  info->residual = res;
+  info->iterations = iterations >= prm.max_iterations ? -iterations : iterations;
+  info->converged = (iterations < prm.max_iterations && info->status == GBFEM_OK) ? 1 : 0;
+  return GBFEM_OK;
+}
+
+// ------------------------------------------------------------------- FCG ---
+// Flexible CG with truncated A-orthogonalisation against the last mmax
+// directions (Notay, SIAM J. Sci. Comput. 22(4), 2000):
+//   z_k = M_k^{-1} r_k,  d_k = z_k - sum_i (z_k . w_i)/(d_i . w_i) d_i,  w_i = A d_i,
+//   alpha = (d_k . r_k)/(d_k . w_k),  x += alpha d_k,  r -= alpha w_k.
+// Residual r = b - A x; stopping as in cg.hh (||r||^2 against eps^2 ||b||^2).
+static int fcg(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_params& prm, const void* b, void* x,
+               Ctx& c, gbfem_solver_info* info) {
+  const int mmax = prm.restart > 0 ? prm.restart : 1;
+  Vecs t, dirs, ws;
+  GBFEM_TRY(t.alloc(2, c.bytes()));
+  GBFEM_TRY(dirs.alloc(mmax + 1, c.bytes()));
+  GBFEM_TRY(ws.alloc(mmax + 1, c.bytes()));
+  void *r = t[0], *z = t[1];
+  std::vector<double> dw(mmax + 1, 1.0);
+  GBFEM_TRY(op_apply(op, x, r, c));
+  GBFEM_TRY(c.axpby(1.0, b, -1.0, r));  // r = b - A x
+  double rr, bb = 1.0;
+  GBFEM_TRY(c.dot(r, r, &rr));
+  if (prm.error_measure == GBFEM_TOL_RELATIVE) GBFEM_TRY(c.dot(b, b, &bb));
+  const double tolerance = prm.tolerance * prm.tolerance *
+                           (prm.error_measure == GBFEM_TOL_RELATIVE ? bb
+                            : prm.error_measure == GBFEM_TOL_RESIDUAL_REDUCTION ? rr : 1.0);
+  int it = 0;
+  if (!finite(rr) || !finite(tolerance)) info->status = GBFEM_ERR_NONFINITE;
+  for (it = 0; info->status == GBFEM_OK && rr > tolerance && it < prm.max_iterations; ++it) {
+    const int slot = it % (mmax + 1);
+    void* d = dirs[slot];
+    void* w = ws[slot];
+    if (pc) GBFEM_TRY(pc_apply(pc, r, z, c));
+    else GBFEM_TRY(c.copy(r, z));
+    GBFEM_TRY(c.copy(z, d));
+    const int kept = it < mmax ? it : mmax;
+    for (int k = 1; k <= kept; ++k) {
+      const int sl = (it - k) % (mmax + 1);
+      double zw;
+      GBFEM_TRY(c.dot(z, ws[sl], &zw));
+      GBFEM_TRY(c.axpby(-zw / dw[sl], dirs[sl], 1.0, d));
+    }
+    GBFEM_TRY(op_apply(op, d, w, c));
+    double dwk, dr;
+    GBFEM_TRY(c.dot(d, w, &dwk));
+    GBFEM_TRY(c.dot(d, r, &dr));
+    dw[slot] = dwk;
+    const double alpha = dr / dwk;
+    if (!finite(alpha)) { info->status = GBFEM_ERR_NONFINITE; break; }
+    GBFEM_TRY(c.axpby(alpha, d, 1.0, x));
+    GBFEM_TRY(c.axpby(-alpha, w, 1.0, r));
+    GBFEM_TRY(c.dot(r, r, &rr));
+    if (prm.verbose) std::printf("gbfem FCG it: %d : residual %.6e\n", it, std::sqrt(rr));
+  }
+  info->residual = std::sqrt(rr);
+  info->iterations = it < prm.max_iterations ? it : -it;
+  info->converged = (it < prm.max_iterations && info->status == GBFEM_OK) ? 1 : 0;
+  return GBFEM_OK;
+}
+
+int solve_impl(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_params& prm, const void* f, void* u,
+               gbfem_solver_info* info, cudaStream_t s) {
+  Ctx c;
+  GBFEM_TRY(c.setup(op->precision, op->ndofs, s));
+  *info = gbfem_solver_info{};
+  const auto t0 = std::chrono::steady_clock::now();
+  int rc;
+  switch (prm.method) {
+    case GBFEM_SOLVER_CG: rc = cg(op, pc, prm, f, u, c, info); break;
+    case GBFEM_SOLVER_GMRES: rc = gmres(op, pc, prm, f, u, c, info, false); break;
+    case GBFEM_SOLVER_FGMRES: rc = gmres(op, pc, prm, f, u, c, info, true); break;
+    case GBFEM_SOLVER_BICGSTAB: rc = bicgstab(op, pc, prm, f, u, c, info); break;
+    case GBFEM_SOLVER_FCG: rc = fcg(op, pc, prm, f, u, c, info); break;
+    default: return set_error(GBFEM_ERR_INVALID, "gbfem_solve: unknown method " + std::to_string(prm.method));
+  }
+  GBFEM_CUDA_TRY(cudaStreamSynchronize(s));
+  info->time_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  info->operator_applies = c.op_applies;
+  info->preconditioner_applies = c.pc_applies;
+  return rc;
+}
+
+}  // namespace gbfem
+
+using namespace gbfem;
+
+extern "C" {
+
+int gbfem_solver_params_default(gbfem_solver_params* prm) {
+  if (!prm) return set_error(GBFEM_ERR_INVALID, "null params");
+  prm->method = GBFEM_SOLVER_CG;
+  prm->tolerance = 1e-8;
+  prm->error_measure = GBFEM_TOL_ABSOLUTE;
+  prm->max_iterations = INT_MAX;
+  prm->restart = 20;
+  prm->verbose = 0;
+  return GBFEM_OK;
+}
+
+int gbfem_preconditioner_diagonal_create(gbfem_operator op, gbfem_preconditioner* out) {
+  if (!op || !out) return set_error(GBFEM_ERR_INVALID, "gbfem_preconditioner_diagonal_create: null argument");
+  *out = nullptr;
+  auto* pc = new (std::nothrow) gbfem_preconditioner_s();
+  if (!pc) return set_error(GBFEM_ERR_INVALID, "out of host memory");
+  pc->kind = PcKind::Diagonal;
+  pc->precision = op->precision;
+  pc->n = op->ndofs;
+  pc->nloc = 1;
+  const size_t bytes = size_t(pc->n) * (pc->precision == GBFEM_F64 ? 8 : 4);
+  cudaError_t e = cudaMalloc(&pc->data, bytes);
+  if (e != cudaSuccess) { delete pc; return set_cuda_error(e, "diagonal preconditioner"); }
+  int rc = gbfem_operator_diagonal(op, pc->data, nullptr);
+  if (rc) { gbfem_preconditioner_destroy(pc); return rc; }
+  if (pc->precision == GBFEM_F64) k_diag_invert<double><<<stream_grid(pc->n), 256>>>(pc->n, (double*)pc->data);
+  else k_diag_invert<float><<<stream_grid(pc->n), 256>>>(pc->n, (float*)pc->data);
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) { gbfem_preconditioner_destroy(pc); return set_cuda_error(e, "diagonal invert"); }
+  *out = pc;
+  return GBFEM_OK;
+}
+
+int gbfem_preconditioner_block_jacobi_create(gbfem_operator op, int precision, gbfem_preconditioner* out) {
+  if (!op || !out) return set_error(GBFEM_ERR_INVALID, "gbfem_preconditioner_block_jacobi_create: null argument");
+  *out = nullptr;
+  if (op->kind != OpKind::DG) return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "block Jacobi needs a DG operator");
+  if (precision != GBFEM_F64 && precision != GBFEM_F32) return set_error(GBFEM_ERR_INVALID, "bad precision");
+  auto* pc = new (std::nothrow) gbfem_preconditioner_s();
+  if (!pc) return set_error(GBFEM_ERR_INVALID, "out of host memory");
+  pc->kind = PcKind::BlockJacobi;
+  pc->precision = precision;
+  pc->n = op->ndofs;
+  pc->nloc = op->nloc;
+  const int nb = op->nloc;
+  const size_t isz = precision == GBFEM_F64 ? 8 : 4;
+  const size_t osz = op->precision == GBFEM_F64 ? 8 : 4;
+  cudaError_t e = cudaMalloc(&pc->data, size_t(op->ncells) * nb * nb * isz);
+  if (e != cudaSuccess) { delete pc; return set_cuda_error(e, "block Jacobi storage"); }
+  // blocks in batches of cells (bounded temporary: <= ~1 GB)
+  long long batch = (1LL << 30) / ((long long)nb * nb * (long long)osz);
+  if (batch < 1) batch = 1;
+  if (batch > op->ncells) batch = op->ncells;
+  void* tmp = nullptr;
+  int* d_sing = nullptr;
+  e = cudaMalloc(&tmp, size_t(batch) * nb * nb * osz);
+  if (e == cudaSuccess) e = cudaMalloc(&d_sing, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(d_sing, 0, sizeof(int));
+  if (e != cudaSuccess) {
+    if (tmp) cudaFree(tmp);
+    gbfem_preconditioner_destroy(pc);
+    return set_cuda_error(e, "block Jacobi temporary");
+  }
+  int rc = GBFEM_OK;
+  const size_t sm = size_t(nb) * nb * 8 + size_t(nb) * 4;
+  for (long long c0 = 0; c0 < op->ncells && rc == GBFEM_OK; c0 += batch) {
+    const long long cnt = (c0 + batch <= op->ncells) ? batch : op->ncells - c0;
+    rc = dg_apply(op, nullptr, nullptr, nullptr, 1, tmp, c0, cnt);
+    if (rc) break;
+    if (op->precision == GBFEM_F64 && precision == GBFEM_F64) {
+      cudaFuncSetAttribute(k_block_invert<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+      k_block_invert<double, double><<<unsigned(cnt), 256, sm>>>((const double*)tmp,
+                                                                ((double*)pc->data) + c0 * nb * nb, nb, cnt, d_sing);
+    } else if (op->precision == GBFEM_F64) {
+      cudaFuncSetAttribute(k_block_invert<double, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+      k_block_invert<double, float><<<unsigned(cnt), 256, sm>>>((const double*)tmp,
+                                                               ((float*)pc->data) + c0 * nb * nb, nb, cnt, d_sing);
+    } else if (precision == GBFEM_F64) {
+      cudaFuncSetAttribute(k_block_invert<float, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+      k_block_invert<float, double><<<unsigned(cnt), 256, sm>>>((const float*)tmp,
+                                                               ((double*)pc->data) + c0 * nb * nb, nb, cnt, d_sing);
+    } else {
+      cudaFuncSetAttribute(k_block_invert<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+      k_block_invert<float, float><<<unsigned(cnt), 256, sm>>>((const float*)tmp,
+                                                              ((float*)pc->data) + c0 * nb * nb, nb, cnt, d_sing);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) rc = set_cuda_error(e, "block invert launch");
+  }
+  int sing = 0;
+  if (rc == GBFEM_OK) {
+    e = cudaMemcpy(&sing, d_sing, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = set_cuda_error(e, "block invert");
+  }
+  cudaFree(tmp);
+  cudaFree(d_sing);
+  if (rc == GBFEM_OK && sing) rc = set_error(GBFEM_ERR_INVALID, "block Jacobi: a diagonal block is singular");
+  if (rc) { gbfem_preconditioner_destroy(pc); return rc; }
+  *out = pc;
+  return GBFEM_OK;
+}
+
+int gbfem_preconditioner_apply(gbfem_preconditioner pc, const void* r, void* z, void* stream) {
+  if (!pc || !r || !z) return set_error(GBFEM_ERR_INVALID, "gbfem_preconditioner_apply: null argument");
+  return precond_apply(pc, r, z, static_cast<cudaStream_t>(stream));
+}
+
+int gbfem_preconditioner_precision(gbfem_preconditioner pc, int* precision) {
+  if (!pc || !precision) return set_error(GBFEM_ERR_INVALID, "null argument");
+  *precision = pc->precision;
+  return GBFEM_OK;
+}
+
+int gbfem_preconditioner_destroy(gbfem_preconditioner pc) {
+  if (!pc) return GBFEM_OK;
+  if (pc->data && pc->owns_data) cudaFree(pc->data);
+  if (pc->ext_destroy) pc->ext_destroy(pc->ext_ctx);
+  delete pc;
+  return GBFEM_OK;
+}
+
+int gbfem_solve(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_params* prm, const void* f, void* u,
+                gbfem_solver_info* info) {
+  if (!op || !prm || !f || !u || !info) return set_error(GBFEM_ERR_INVALID, "gbfem_solve: null argument");
+  if (pc && pc->precision != op->precision)
+    return set_error(GBFEM_ERR_INVALID, "gbfem_solve: preconditioner and operator precisions differ");
+  if (pc && pc->n != op->ndofs) return set_error(GBFEM_ERR_INVALID, "gbfem_solve: preconditioner size mismatch");
+  return solve_impl(op, pc, *prm, f, u, info, nullptr);
+}
+
+// FP64 iterative refinement around an FP32 inner solve.
+//   r = f - A64 u;  while ||r|| > tol ||f||:  solve A32 d = r/||r|| (FP32),  u += ||r|| d
+int gbfem_solve_mixed(gbfem_operator op64, gbfem_operator op32, gbfem_preconditioner pc32, const gbfem_ir_params* prm,
+                      const void* f, void* u, gbfem_solver_info* info) {
+  if (!op64 || !op32 || !prm || !f || !u || !info) return set_error(GBFEM_ERR_INVALID, "gbfem_solve_mixed: null argument");
+  if (op64->precision != GBFEM_F64 || op32->precision != GBFEM_F32)
+    return set_error(GBFEM_ERR_INVALID, "gbfem_solve_mixed: needs an FP64 and an FP32 operator");
+  if (op64->ndofs != op32->ndofs) return set_error(GBFEM_ERR_INVALID, "gbfem_solve_mixed: operator sizes differ");
+  if (pc32 && pc32->precision != GBFEM_F32) return set_error(GBFEM_ERR_INVALID, "gbfem_solve_mixed: pc must be FP32");
+  *info = gbfem_solver_info{};
+  const auto t0 = std::chrono::steady_clock::now();
+  const long long n = op64->ndofs;
+  Ctx c64, c32;
+  GBFEM_TRY(c64.setup(GBFEM_F64, n, nullptr));
+  GBFEM_TRY(c32.setup(GBFEM_F32, n, nullptr));
+  Vecs v64, v32;
+  GBFEM_TRY(v64.alloc(2, size_t(n) * 8));
+  GBFEM_TRY(v32.alloc(2, size_t(n) * 4));
+  void *r = v64[0], *d64 = v64[1], *r32 = v32[0], *d32 = v32[1];
+  double ff;
+  GBFEM_TRY(c64.dot(f, f, &ff));
+  const double fnorm = std::sqrt(ff);
+  int inner_total = 0, outer = 0;
+  double rel = 0.0;
+  gbfem_solver_params ip = prm->inner;
+  ip.error_measure = GBFEM_TOL_RELATIVE;
+  for (outer = 0; outer <= prm->max_outer; ++outer) {
+    GBFEM_TRY(op_apply(op64, u, r, c64));
+    GBFEM_TRY(c64.axpby(1.0, f, -1.0, r));  // r = f - A u
+    double rr;
+    GBFEM_TRY(c64.dot(r, r, &rr));
+    const double rn = std::sqrt(rr);
+    rel = fnorm > 0 ? rn / fnorm : rn;
+    if (prm->inner.verbose) std::printf("gbfem IR outer %d : relative residual %.6e\n", outer, rel);
+    if (!std::isfinite(rel)) { info->status = GBFEM_ERR_NONFINITE; break; }
+    if (rel <= prm->tolerance || outer == prm->max_outer) break;
+    GBFEM_TRY(gbfem_convert(n, GBFEM_F64, r, GBFEM_F32, r32, nullptr));
+    GBFEM_TRY(c32.axpby(0.0, r32, 1.0 / rn, r32));
+    GBFEM_TRY(c32.clear(d32));
+    gbfem_solver_info ii{};
+    GBFEM_TRY(solve_impl(op32, pc32, ip, r32, d32, &ii, nullptr));
+    inner_total += ii.iterations >= 0 ? ii.iterations : -ii.iterations;
+    c64.op_applies += ii.operator_applies;
+    c64.pc_applies += ii.preconditioner_applies;
+    GBFEM_TRY(gbfem_convert(n, GBFEM_F32, d32, GBFEM_F64, d64, nullptr));
+    GBFEM_TRY(c64.axpby(rn, d64, 1.0, u));
+  }
+  GBFEM_CUDA_TRY(cudaDeviceSynchronize());
+  info->time_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  info->residual = rel;
+  info->converged = (rel <= prm->tolerance && info->status == GBFEM_OK) ? 1 : 0;
+  info->iterations = info->converged ? inner_total : -inner_total;
+  info->operator_applies = c64.op_applies;
+  info->preconditioner_applies = c64.pc_applies;
+  return GBFEM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,26 @@
+// Definition of the opaque preconditioner handle.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "../../include/gbfem.h"
+
+namespace gbfem {
+
+enum class PcKind { Diagonal = 1, BlockJacobi = 2, External = 3 };
+
+int precond_apply(const struct ::gbfem_preconditioner_s* pc, const void* r, void* z, cudaStream_t s);
+
+}  // namespace gbfem
+
+struct gbfem_preconditioner_s {
+  gbfem::PcKind kind = gbfem::PcKind::Diagonal;
+  int precision = GBFEM_F64;
+  long long n = 0;
+  int nloc = 1;
+  void* data = nullptr;  // diagonal inverse or block inverses
+  bool owns_data = true;
+  // External (e.g. the learned preconditioner): z = P(r)
+  int (*ext_apply)(void* ctx, const void* r, void* z, cudaStream_t s) = nullptr;
+  void (*ext_destroy)(void* ctx) = nullptr;
+  void* ext_ctx = nullptr;
+};

@@ -36,6 +36,25 @@ class DgDesc(C.Structure):
                 ("velocity", C.c_double * 3), ("weak_dirichlet", C.c_int), ("kappa", C.c_void_p)]
 
 
+class SolverParams(C.Structure):
+    _fields_ = [("method", C.c_int), ("tolerance", C.c_double), ("error_measure", C.c_int),
+                ("max_iterations", C.c_int), ("restart", C.c_int), ("verbose", C.c_int)]
+
+
+class SolverInfo(C.Structure):
+    _fields_ = [("converged", C.c_int), ("iterations", C.c_int), ("residual", C.c_double),
+                ("time_ms", C.c_double), ("operator_applies", C.c_int), ("preconditioner_applies", C.c_int),
+                ("status", C.c_int)]
+
+
+class IRParams(C.Structure):
+    _fields_ = [("tolerance", C.c_double), ("max_outer", C.c_int), ("inner", SolverParams)]
+
+
+CG, GMRES, BICGSTAB, FCG, FGMRES = 0, 1, 2, 3, 4
+ABSOLUTE, RELATIVE, RESIDUAL_REDUCTION = 0, 1, 2
+METHODS = {"cg": CG, "gmres": GMRES, "bicgstab": BICGSTAB, "fcg": FCG, "fgmres": FGMRES}
+
 _lib = None
 
 
@@ -67,6 +86,15 @@ def lib():
         L.gbfem_q1_operator_create.argtypes = [C.POINTER(GridDesc), C.c_int, C.c_double, C.c_double,
                                                C.POINTER(C.c_void_p)]
         L.gbfem_measure_fma_peaks.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.gbfem_preconditioner_diagonal_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+        L.gbfem_preconditioner_block_jacobi_create.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
+        L.gbfem_preconditioner_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.gbfem_preconditioner_destroy.argtypes = [C.c_void_p]
+        L.gbfem_solver_params_default.argtypes = [C.POINTER(SolverParams)]
+        L.gbfem_solve.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(SolverParams), C.c_void_p, C.c_void_p,
+                                  C.POINTER(SolverInfo)]
+        L.gbfem_solve_mixed.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(IRParams), C.c_void_p,
+                                        C.c_void_p, C.POINTER(SolverInfo)]
         _lib = L
     return _lib
 
@@ -216,3 +244,100 @@ def measure_fma_peaks():
     a, b = C.c_double(), C.c_double()
     check(lib().gbfem_measure_fma_peaks(C.byref(a), C.byref(b)))
     return a.value, b.value
+
+
+class Preconditioner:
+    """z = P(r) (any Operator<D,D> in the reference, krylovinverseoperators.hh:36)."""
+
+    def __init__(self, handle, precision, keep=None):
+        self.handle = handle
+        self.precision = precision
+        self._keep = keep
+
+    @classmethod
+    def diagonal(cls, op):
+        h = C.c_void_p()
+        check(lib().gbfem_preconditioner_diagonal_create(op.handle, C.byref(h)))
+        return cls(h, op.precision, op)
+
+    @classmethod
+    def block_jacobi(cls, op, precision=None):
+        precision = op.precision if precision is None else precision
+        h = C.c_void_p()
+        check(lib().gbfem_preconditioner_block_jacobi_create(op.handle, precision, C.byref(h)))
+        return cls(h, precision, op)
+
+    def __call__(self, r, z, stream=None):
+        check(lib().gbfem_preconditioner_apply(self.handle, r.ptr, z.ptr, stream))
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().gbfem_preconditioner_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+
+def solver_params(method="cg", tolerance=1e-8, error_measure=RELATIVE, max_iterations=None, restart=20,
+                  verbose=False):
+    p = SolverParams()
+    check(lib().gbfem_solver_params_default(C.byref(p)))
+    p.method = METHODS[method] if isinstance(method, str) else method
+    p.tolerance = tolerance
+    p.error_measure = error_measure
+    if max_iterations is not None:
+        p.max_iterations = max_iterations
+    p.restart = restart
+    p.verbose = 1 if verbose else 0
+    return p
+
+
+class KrylovInverseOperator:
+    """u = op^{-1}(f): the shape of dune-fem's KrylovInverseOperator
+    (solver/krylovinverseoperators.hh:46-274, inverseoperatorinterface.hh:81-146):
+    bind(op[, precond]), __call__(f, u), iterations(), info()."""
+
+    def __init__(self, method="cg", tolerance=1e-8, error_measure=RELATIVE, max_iterations=None, restart=20,
+                 verbose=False):
+        self.params = solver_params(method, tolerance, error_measure, max_iterations, restart, verbose)
+        self.op = None
+        self.precond = None
+        self._info = SolverInfo()
+
+    def bind(self, op, precond=None):
+        self.op = op
+        self.precond = precond
+
+    def unbind(self):
+        self.op = None
+        self.precond = None
+
+    def __call__(self, f, u):
+        if self.op is None:
+            raise GbfemError(-1, "KrylovInverseOperator: no operator bound")
+        pc = self.precond.handle if self.precond is not None else None
+        check(lib().gbfem_solve(self.op.handle, pc, C.byref(self.params), f.ptr, u.ptr, C.byref(self._info)))
+        return self._info
+
+    def iterations(self):
+        return self._info.iterations
+
+    def info(self):
+        i = self._info
+        return {"converged": bool(i.converged), "iterations": i.iterations, "residual": i.residual,
+                "time_ms": i.time_ms, "operator_applies": i.operator_applies,
+                "preconditioner_applies": i.preconditioner_applies, "status": i.status}
+
+
+def solve_mixed(op64, op32, pc32, f, u, tolerance=1e-10, max_outer=50, inner_method="cg", inner_tolerance=1e-4,
+                inner_max_iterations=100000, verbose=False):
+    """FP64 iterative refinement around an FP32 inner Krylov solve."""
+    p = IRParams()
+    p.tolerance = tolerance
+    p.max_outer = max_outer
+    p.inner = solver_params(inner_method, inner_tolerance, RELATIVE, inner_max_iterations, 20, verbose)
+    info = SolverInfo()
+    check(lib().gbfem_solve_mixed(op64.handle, op32.handle, pc32.handle if pc32 is not None else None,
+                                  C.byref(p), f.ptr, u.ptr, C.byref(info)))
+    return info

@@ -115,6 +115,80 @@ int gbfem_operator_diagonal(gbfem_operator op, void* diag, void* stream);
  * (operator/linear/blockdiagonal.hh:24-135). */
 int gbfem_operator_block_diagonal(gbfem_operator op, void* blocks, void* stream);
 
+/* ---- preconditioners ------------------------------------------------------
+ * A preconditioner is any map z = P(r) on dof vectors (the reference takes
+ * any Operator<D,D>, solver/krylovinverseoperators.hh:36).
+ * ----------------------------------------------------------------------- */
+typedef struct gbfem_preconditioner_s* gbfem_preconditioner;
+/* z = r / diag(A), entries with |diag| < 16 eps set to 1.
+ * ≙ DiagonalPreconditioner (solver/diagonalpreconditioner.hh:80-142). */
+int gbfem_preconditioner_diagonal_create(gbfem_operator op, gbfem_preconditioner* pc);
+/* z_K = (A_KK)^{-1} r_K with the exact element-diagonal blocks of op, inverted
+ * by Gauss-Jordan with partial pivoting, stored in `precision`.
+ * ≙ BlockDiagonalLinearOperator::invert + multiply
+ * (operator/linear/blockdiagonal.hh:102-135).  op must be a DG operator. */
+int gbfem_preconditioner_block_jacobi_create(gbfem_operator op, int precision, gbfem_preconditioner* pc);
+int gbfem_preconditioner_apply(gbfem_preconditioner pc, const void* r, void* z, void* stream);
+int gbfem_preconditioner_precision(gbfem_preconditioner pc, int* precision);
+int gbfem_preconditioner_destroy(gbfem_preconditioner pc);
+
+/* ---- Krylov inverse operators ---------------------------------------------
+ * ≙ KrylovInverseOperator::operator()(f,u) -> LinearSolver::cg/gmres/bicgstab
+ * (solver/krylovinverseoperators.hh:118-208, solver/linear/cg.hh:18-117,
+ * solver/linear/gmres.hh:116-299, solver/linear/bicgstab.hh), plus flexible
+ * CG (Notay, SIAM J. Sci. Comput. 22, 2000) and flexible GMRES (Saad, SIAM J.
+ * Sci. Comput. 14, 1993), which the reference only has through dune-istl
+ * (solver/istl.hh:688-696).  u is the initial guess on entry.
+ * ----------------------------------------------------------------------- */
+#define GBFEM_SOLVER_CG 0
+#define GBFEM_SOLVER_GMRES 1
+#define GBFEM_SOLVER_BICGSTAB 2
+#define GBFEM_SOLVER_FCG 3
+#define GBFEM_SOLVER_FGMRES 4
+
+/* LinearSolver::ToleranceCriteria (solver/parameter.hh:14-17) */
+#define GBFEM_TOL_ABSOLUTE 0
+#define GBFEM_TOL_RELATIVE 1
+#define GBFEM_TOL_RESIDUAL_REDUCTION 2
+
+typedef struct {
+  int method;          /* GBFEM_SOLVER_* (fem.solver.method) */
+  double tolerance;    /* fem.solver.tolerance */
+  int error_measure;   /* GBFEM_TOL_* (fem.solver.errormeasure) */
+  int max_iterations;  /* fem.solver.maxiterations */
+  int restart;         /* fem.solver.gmres.restart; FCG: directions kept */
+  int verbose;         /* print per-iteration residuals to stdout */
+} gbfem_solver_params;
+
+typedef struct {
+  int converged;
+  int iterations;        /* iterations; negative if not converged (as the reference) */
+  double residual;       /* final residual norm in the solver's measure */
+  double time_ms;
+  int operator_applies;
+  int preconditioner_applies;
+  int status;            /* GBFEM_OK, GBFEM_ERR_NONFINITE on NaN/Inf */
+} gbfem_solver_info;
+
+/* Fills the reference's defaults: cg, tolerance 1e-8, absolute, max
+ * iterations INT_MAX, restart 20 (solver/parameter.hh:91-201). */
+int gbfem_solver_params_default(gbfem_solver_params* prm);
+/* u = op^{-1}(f) with optional preconditioner pc (NULL = none).  All vectors
+ * in the operator's precision; dot products accumulate in FP64. */
+int gbfem_solve(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_params* prm, const void* f,
+                void* u, gbfem_solver_info* info);
+
+/* Mixed precision: FP64 iterative refinement (residual f - A u, update and
+ * convergence test in FP64 with op64) around an FP32 inner Krylov solve with
+ * op32 and pc32.  No counterpart in the reference (spec extension). */
+typedef struct {
+  double tolerance;          /* outer relative residual ||f - A u|| / ||f|| */
+  int max_outer;             /* refinement steps */
+  gbfem_solver_params inner; /* FP32 inner solve; its tolerance is relative */
+} gbfem_ir_params;
+int gbfem_solve_mixed(gbfem_operator op64, gbfem_operator op32, gbfem_preconditioner pc32,
+                      const gbfem_ir_params* prm, const void* f, void* u, gbfem_solver_info* info);
+
 /* ---- BLAS-1 on dof vectors (function/common/discretefunction.hh:781-901,
  *      function/common/scalarproducts.hh:101-127).  Reductions are
  *      deterministic: fixed-order two-pass, independent of launch shape. -- */

@@ -1,0 +1,151 @@
+"""GPU Krylov solvers (through the C-ABI) against the oracle's restatement of
+dune-fem's LinearSolver::cg / gmres, itself pinned to the reference's
+compiled templates (tests/test_oracle_pins.py)."""
+import numpy as np
+import pytest
+
+from conftest import relmax
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(gb, orc, cells=(3, 3, 3), order=2, **kw):
+    op = gb.DGOperator(cells, order, **kw)
+    prob = orc.DGProblem(cells, order, **kw)
+    f = np.random.default_rng(4).uniform(-1, 1, prob.ndofs)
+    return op, prob, f
+
+
+def _solve(gb, op, f, method="cg", pc=None, tol=1e-10, **kw):
+    inv = gb.KrylovInverseOperator(method, tolerance=tol, **kw)
+    inv.bind(op, pc)
+    u = gb.DeviceArray(op.size, op.precision)
+    u.clear()
+    inv(gb.DeviceArray.from_numpy(f, op.precision), u)
+    return inv.info(), u.numpy()
+
+
+def test_cg_matches_oracle_cg(gb, orc):
+    op, prob, f = _problem(gb, orc)
+    info, u = _solve(gb, op, f, "cg")
+    it, uo, _ = orc.cg(prob.apply, f, epsilon=1e-10, max_iter=10000)
+    assert info["converged"]
+    assert abs(info["iterations"] - it) <= 1
+    assert relmax(u, uo) < 1e-8
+    assert info["operator_applies"] == info["iterations"] + 1
+
+
+def test_pcg_diagonal_and_block_jacobi_match_oracle(gb, orc):
+    op, prob, f = _problem(gb, orc, mass=0.5)
+    blocks = prob.block_diagonal()
+    dinv = 1.0 / np.einsum("cii->ci", blocks).ravel()
+    binv = np.linalg.inv(blocks)
+    nl = prob.nloc
+    bj = lambda r: np.einsum("cij,cj->ci", binv, r.reshape(-1, nl)).ravel()
+    for pc, ref_pc in ((gb.Preconditioner.diagonal(op), lambda r: r * dinv),
+                       (gb.Preconditioner.block_jacobi(op), bj)):
+        info, u = _solve(gb, op, f, "cg", pc)
+        it, uo, _ = orc.cg(prob.apply, f, prec=ref_pc, epsilon=1e-10, max_iter=10000)
+        assert info["converged"]
+        assert abs(info["iterations"] - it) <= 1
+        assert relmax(u, uo) < 1e-8
+
+
+def test_block_jacobi_apply_matches_dense_inverse(gb, orc):
+    op, prob, f = _problem(gb, orc, cells=(2, 3, 2), order=3, velocity=(0.5, 0.1, 0.0))
+    pc = gb.Preconditioner.block_jacobi(op)
+    z = gb.DeviceArray(op.size)
+    pc(gb.DeviceArray.from_numpy(f), z)
+    binv = np.linalg.inv(prob.block_diagonal())
+    ref = np.einsum("cij,cj->ci", binv, f.reshape(-1, prob.nloc)).ravel()
+    assert relmax(z.numpy(), ref) < 1e-11
+
+
+def test_gmres_matches_oracle_gmres_nonsymmetric(gb, orc):
+    op, prob, f = _problem(gb, orc, velocity=(1.0, 0.5, -0.25), diffusion=0.1)
+    info, u = _solve(gb, op, f, "gmres", restart=10)
+    it, uo, _ = orc.gmres(prob.apply, f, 10, tolerance=1e-10, max_iter=10000)
+    assert info["converged"]
+    assert abs(info["iterations"] - it) <= 1
+    assert relmax(u, uo) < 1e-8
+
+
+@pytest.mark.parametrize("method", ["bicgstab", "fcg", "fgmres", "gmres"])
+def test_other_methods_reach_tolerance(gb, orc, method):
+    kw = dict(velocity=(0.3, 0.0, 0.2)) if method in ("bicgstab", "fgmres", "gmres") else {}
+    op, prob, f = _problem(gb, orc, **kw)
+    pc = gb.Preconditioner.block_jacobi(op)
+    info, u = _solve(gb, op, f, method, pc, restart=10 if "gmres" in method else 4)
+    assert info["converged"], info
+    res = f - prob.apply(u)
+    assert np.linalg.norm(res) <= 2e-10 * np.linalg.norm(f)
+
+
+def test_mixed_precision_refinement_reaches_fp64_tolerance(gb, orc):
+    cells, order = (4, 4, 4), 3
+    op64 = gb.DGOperator(cells, order)
+    op32 = gb.DGOperator(cells, order, precision=gb.F32)
+    pc32 = gb.Preconditioner.block_jacobi(op64, gb.F32)
+    prob = orc.DGProblem(cells, order)
+    f = np.random.default_rng(5).uniform(-1, 1, prob.ndofs)
+    u = gb.DeviceArray(op64.size)
+    u.clear()
+    info = gb.solve_mixed(op64, op32, pc32, gb.DeviceArray.from_numpy(f), u, tolerance=1e-10, inner_tolerance=1e-3)
+    assert info.converged and info.residual <= 1e-10
+    x = u.numpy()
+    assert np.linalg.norm(f - prob.apply(x)) <= 1.01e-10 * np.linalg.norm(f)
+    _, ref = _solve(gb, op64, f, "cg", tol=1e-12)
+    assert relmax(x, ref) < 1e-7
+
+
+def test_q1_diagonal_pcg_matches_oracle_and_converges_at_h2(gb, orc):
+    """Config-1 shape: -lap u + u = f, Q1, u = sin(pi x) sin(pi y), Dirichlet."""
+    errs = []
+    for N in (16, 32):
+        op = gb.Q1Operator((N, N), diffusion=1.0, mass=1.0)
+        f = q1_rhs(N)
+        pc = gb.Preconditioner.diagonal(op)
+        info, u = _solve(gb, op, f, "cg", pc)
+        dg = orc.q1_apply((N, N), None, 1.0, 1.0, diag_only=True)
+        it, uo, _ = orc.cg(lambda x: orc.q1_apply((N, N), x, 1.0, 1.0), f, prec=lambda r: r / dg, epsilon=1e-10)
+        assert info["converged"] and abs(info["iterations"] - it) <= 1
+        assert relmax(u, uo) < 1e-8
+        xs = np.linspace(0, 1, N + 1)
+        X, Y = np.meshgrid(xs, xs)
+        errs.append(np.max(np.abs(u - (np.sin(np.pi * X) * np.sin(np.pi * Y)).ravel())))
+    assert np.log2(errs[0] / errs[1]) > 1.8  # second order at the nodes
+
+
+def q1_rhs(N):
+    """b_i = int f phi_i with f = (2 pi^2 + 1) sin(pi x) sin(pi y), 3x3 Gauss per cell; b = 0 on the boundary."""
+    h = 1.0 / N
+    g, w = np.polynomial.legendre.leggauss(3)
+    g, w = 0.5 * (g + 1), 0.5 * w
+    b = np.zeros((N + 1) * (N + 1))
+    for ey in range(N):
+        for ex in range(N):
+            for qy in range(3):
+                for qx in range(3):
+                    x, y = (ex + g[qx]) * h, (ey + g[qy]) * h
+                    fv = (2 * np.pi ** 2 + 1) * np.sin(np.pi * x) * np.sin(np.pi * y) * w[qx] * w[qy] * h * h
+                    for k in range(4):
+                        kx, ky = k & 1, k >> 1
+                        phi = (g[qx] if kx else 1 - g[qx]) * (g[qy] if ky else 1 - g[qy])
+                        b[(ey + ky) * (N + 1) + ex + kx] += fv * phi
+    b2 = b.reshape(N + 1, N + 1)
+    b2[0, :] = b2[-1, :] = b2[:, 0] = b2[:, -1] = 0.0
+    return b
+
+
+def test_nonconvergence_is_a_negative_iteration_count(gb, orc):
+    op, prob, f = _problem(gb, orc)
+    info, _ = _solve(gb, op, f, "cg", max_iterations=3)
+    assert info["iterations"] == -3 and not info["converged"]
+
+
+def test_nan_input_reports_nonfinite(gb, orc):
+    op, prob, f = _problem(gb, orc)
+    f = f.copy()
+    f[7] = np.nan
+    info, _ = _solve(gb, op, f, "cg", max_iterations=50)
+    assert not info["converged"]
