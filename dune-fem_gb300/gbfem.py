@@ -86,6 +86,12 @@ def lib():
         L.gbfem_q1_operator_create.argtypes = [C.POINTER(GridDesc), C.c_int, C.c_double, C.c_double,
                                                C.POINTER(C.c_void_p)]
         L.gbfem_measure_fma_peaks.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.gbfem_fourier_modes.argtypes = [C.c_uint64, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double)]
+        L.gbfem_dg_project.argtypes = [C.POINTER(GridDesc), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        L.gbfem_rk3_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+        L.gbfem_rk3_step.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]
+        L.gbfem_rk3_destroy.argtypes = [C.c_void_p]
         L.gbfem_preconditioner_diagonal_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
         L.gbfem_preconditioner_block_jacobi_create.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
         L.gbfem_preconditioner_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -341,3 +347,48 @@ def solve_mixed(op64, op32, pc32, f, u, tolerance=1e-10, max_outer=50, inner_met
     check(lib().gbfem_solve_mixed(op64.handle, op32.handle, pc32.handle if pc32 is not None else None,
                                   C.byref(p), f.ptr, u.ptr, C.byref(info)))
     return info
+
+
+FN_EXP_FOURIER, FN_GAUSSIAN, FN_CONSTANT = 0, 1, 2
+
+
+def fourier_modes(seed, nmodes=256, corr_length=0.1, stddev=1.0):
+    """Seeded random Fourier modes of a log-Gaussian field: array [nmodes, 5]."""
+    m = np.zeros(5 * nmodes)
+    check(lib().gbfem_fourier_modes(seed, nmodes, corr_length, stddev, m.ctypes.data_as(C.POINTER(C.c_double))))
+    return m.reshape(nmodes, 5)
+
+
+def project(cells, order, kind, params=None, modes=None, quad_points=0, scale_by_volume=False, precision=F64,
+            lower=(0.0, 0.0, 0.0), upper=(1.0, 1.0, 1.0)):
+    """L2 projection of a closed-form function onto DG Q_order: a DeviceArray."""
+    g = grid_desc(cells, lower, upper)
+    n = int(np.prod(cells)) * (order + 1) ** 3
+    out = DeviceArray(n, precision)
+    pr = np.zeros(8) if params is None else np.array(params, dtype=np.float64)
+    md = np.ascontiguousarray(modes, dtype=np.float64).ravel() if modes is not None else None
+    check(lib().gbfem_dg_project(C.byref(g), order, quad_points, kind, pr.ctypes.data_as(C.POINTER(C.c_double)),
+                                 md.ctypes.data_as(C.POINTER(C.c_double)) if md is not None else None,
+                                 0 if md is None else md.size // 5, 1 if scale_by_volume else 0, precision,
+                                 out.ptr, None))
+    return out
+
+
+class RK3:
+    """Explicit SSP-RK3 for u' = -M^{-1} A(u) (ExplicitRungeKuttaSolver + TVD3)."""
+
+    def __init__(self, op):
+        self.op = op
+        self.handle = C.c_void_p()
+        check(lib().gbfem_rk3_create(op.handle, C.byref(self.handle)))
+
+    def step(self, u, dt, stream=None):
+        check(lib().gbfem_rk3_step(self.handle, u.ptr, dt, stream))
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().gbfem_rk3_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass

@@ -189,6 +189,36 @@ typedef struct {
 int gbfem_solve_mixed(gbfem_operator op64, gbfem_operator op32, gbfem_preconditioner pc32,
                       const gbfem_ir_params* prm, const void* f, void* u, gbfem_solver_info* info);
 
+/* ---- projection of closed-form functions (coefficient fields, data) ----- */
+#define GBFEM_FN_EXP_FOURIER 0 /* exp(sum_k a_k cos(2 pi w_k.x + phi_k)): log-Gaussian random field */
+#define GBFEM_FN_GAUSSIAN 1    /* exp(-|x-c|^2/width^2); params = cx, cy, cz, width */
+#define GBFEM_FN_CONSTANT 2    /* params[0] */
+/* Seeded random Fourier modes of a Gaussian field with squared-exponential
+ * correlation: modes[5m..5m+4] = (w_x, w_y, w_z, phi, a), w ~ N(0, (1/(2 pi
+ * corr_length))^2 I), phi ~ U[0, 2 pi), a = stddev sqrt(2/nmodes).  Host
+ * array.  No counterpart in the reference (benchmark input generator). */
+int gbfem_fourier_modes(uint64_t seed, int nmodes, double corr_length, double stddev, double* modes);
+/* L2 projection onto the DG Q_order space (same dof layout as the DG
+ * operator), q-point Gauss per direction (0 = order+2); scale_by_volume = 1
+ * gives the load vector int_K f phi_l instead.  ≙ interpolating / projecting a
+ * grid function into a DiscreteFunction (space.interpolate, function/
+ * localfunction and operator/projection/l2projection.hh). */
+int gbfem_dg_project(const gbfem_grid_desc* grid, int order, int quad_points, int kind, const double* params,
+                     const double* modes_host, int nmodes, int scale_by_volume, int precision, void* out,
+                     void* stream);
+
+/* ---- explicit SSP-RK3 of the method-of-lines DG operator --------------------
+ * u' = -M^{-1} A(u), M^{-1} = 1/|K| for the orthonormal basis on affine cells.
+ * ≙ ExplicitRungeKuttaSolver with tvd3ButcherTable (solver/rungekutta/
+ * explicit.hh:160-215, butchertable.cc:43-52) over MOLGalerkinOperator
+ * (schemes/molgalerkin.hh:100-196).
+ * ----------------------------------------------------------------------- */
+typedef struct gbfem_rk_solver_s* gbfem_rk_solver;
+int gbfem_rk3_create(gbfem_operator op, gbfem_rk_solver* rk);
+/* One step of size dt, in place on the device vector u (op's precision). */
+int gbfem_rk3_step(gbfem_rk_solver rk, void* u, double dt, void* stream);
+int gbfem_rk3_destroy(gbfem_rk_solver rk);
+
 /* ---- BLAS-1 on dof vectors (function/common/discretefunction.hh:781-901,
  *      function/common/scalarproducts.hh:101-127).  Reductions are
  *      deterministic: fixed-order two-pass, independent of launch shape. -- */

@@ -498,6 +498,84 @@ int oracle_q1_apply(const int* cells, const double* lower, const double* upper, 
   return 0;
 }
 
+// L2 projection of a closed-form function onto DG Q_p (kind 0: exp of a
+// Fourier sum with modes[m] = (wx, wy, wz, phi, a); 1: Gaussian bump with
+// params (cx, cy, cz, width); 2: constant params[0]); direct evaluation at
+// every quadrature point, dense basis (the interpolation/projection of a
+// grid function into a DiscreteFunction).
+int oracle_dg_project(const int* cells, const double* lower, const double* upper, int order, int quad, int kind,
+                      const double* params, const double* modes, int nmodes, int scale_by_volume, double* out) {
+  const int zero3[3] = {0, 0, 0};
+  const double zv[3] = {0, 0, 0};
+  Desc d = make_desc(cells, lower, upper, zero3, order, quad, 0, 0, 0, zv, 0);
+  Space S(d);
+  const double pi = 3.14159265358979323846;
+  const int nq = S.q * S.q * S.q;
+  for (long long c = 0; c < S.ncells; ++c) {
+    long long xc[3];
+    S.coords(c, xc);
+    for (int l = 0; l < S.nloc; ++l) out[c * S.nloc + l] = 0.0;
+    for (int iq = 0; iq < nq; ++iq) {
+      const int ix[3] = {iq % S.q, (iq / S.q) % S.q, iq / (S.q * S.q)};
+      double x[3];
+      for (int k = 0; k < 3; ++k) x[k] = d.lower[k] + (double(xc[k]) + S.gp[ix[k]]) * S.h[k];
+      double f;
+      if (kind == 0) {
+        double sum = 0.0;
+        for (int m = 0; m < nmodes; ++m) {
+          const double* md = modes + 5 * m;
+          sum += md[4] * std::cos(2.0 * pi * (md[0] * x[0] + md[1] * x[1] + md[2] * x[2]) + md[3]);
+        }
+        f = std::exp(sum);
+      } else if (kind == 1) {
+        double r2 = 0.0;
+        for (int k = 0; k < 3; ++k) r2 += (x[k] - params[k]) * (x[k] - params[k]);
+        f = std::exp(-r2 / (params[3] * params[3]));
+      } else {
+        f = params[0];
+      }
+      const double wf = S.vwt[iq] * f * (scale_by_volume ? S.vol : 1.0);
+      for (int l = 0; l < S.nloc; ++l) out[c * S.nloc + l] += wf * S.vphi[iq * S.nloc + l];
+    }
+  }
+  return 0;
+}
+
+// One step of SSP-RK3 (TVD3 Butcher table, solver/rungekutta/butchertable.cc:
+// 43-52) in the Butcher form of ExplicitRungeKuttaSolver::solve
+// (solver/rungekutta/explicit.hh:160-215) for u' = L(u) = -A(u)/|K|.
+int oracle_dg_rk3_step(const int* cells, const double* lower, const double* upper, const int* periodic, int order,
+                       int quad, double diffusion, double penalty, double mass, const double* velocity,
+                       int weak_dirichlet, const double* kappa, double* u, double dt, int nthreads) {
+  Desc d = make_desc(cells, lower, upper, periodic, order, quad, diffusion, penalty, mass, velocity, weak_dirichlet);
+  Space S(d);
+  const long long n = S.ncells * S.nloc;
+  static const double A[3][3] = {{0, 0, 0}, {1.0, 0, 0}, {0.25, 0.25, 0}};
+  static const double b[3] = {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0};
+  std::vector<std::vector<double>> k(3, std::vector<double>(n));
+  std::vector<double> y(n);
+  Lockset locks(4096);
+  auto L = [&](const double* in, double* out) {
+    std::memset(out, 0, sizeof(double) * n);
+    run_partitioned(S.ncells, nthreads, [&](long long bb, long long ee) {
+      dg_apply_range(S, in, kappa, out, bb, ee, locks, nthreads > 1);
+    });
+    for (long long i = 0; i < n; ++i) out[i] *= -1.0 / S.vol;  // applyInverseMass
+  };
+  L(u, k[0].data());
+  for (int i = 1; i < 3; ++i) {
+    for (long long t = 0; t < n; ++t) {
+      double v = u[t];
+      for (int j = 0; j < i; ++j) v += A[i][j] * dt * k[j][t];
+      y[t] = v;
+    }
+    L(y.data(), k[i].data());
+  }
+  for (int j = 0; j < 3; ++j)
+    for (long long t = 0; t < n; ++t) u[t] += b[j] * dt * k[j][t];
+  return 0;
+}
+
 // ---------------------------------------------------------------- Krylov --
 typedef void (*oracle_op_fn)(void* ctx, const double* x, double* y);
 

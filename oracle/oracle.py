@@ -39,6 +39,8 @@ def lib():
         L.oracle_dg_apply.argtypes = dg_args + [dp, dp, C.c_int]
         L.oracle_dg_block_diagonal.argtypes = dg_args + [dp, C.c_int]
         L.oracle_dg_apply_cells.argtypes = dg_args + [dp, dp, C.c_longlong, C.c_longlong, C.c_int]
+        L.oracle_dg_project.argtypes = [ip, dp, dp, C.c_int, C.c_int, C.c_int, dp, dp, C.c_int, C.c_int, dp]
+        L.oracle_dg_rk3_step.argtypes = dg_args + [dp, C.c_double, C.c_int]
         L.oracle_q1_apply.argtypes = [ip, dp, dp, C.c_double, C.c_double, dp, dp, C.c_int]
         L.oracle_cg.argtypes = [C.c_longlong, OPFN, C.c_void_p, OPFN, C.c_void_p, dp, dp, C.c_double, C.c_int,
                                 C.c_int, dp]
@@ -107,6 +109,24 @@ class DGProblem:
     def apply_cells(self, u, w, c0, c1, kappa=None, nthreads=1):
         """Adds the contributions of cells [c0, c1) to w (a bounded sample of an apply)."""
         lib().oracle_dg_apply_cells(*self._args(kappa), _dp(u), _dp(w), int(c0), int(c1), nthreads)
+
+    def rk3_step(self, u, dt, kappa=None, nthreads=1):
+        """One SSP-RK3 step of u' = -A(u)/|K| (in place on a copy; returns it)."""
+        u = np.array(u, dtype=np.float64)
+        if kappa is not None:
+            kappa = np.ascontiguousarray(kappa, dtype=np.float64)
+        lib().oracle_dg_rk3_step(*self._args(kappa), _dp(u), dt, nthreads)
+        return u
+
+    def project(self, kind, params=None, modes=None, scale_by_volume=False):
+        """L2 projection of a closed-form function (0 exp-Fourier, 1 Gaussian, 2 constant)."""
+        out = np.zeros(self.ndofs)
+        pr = np.zeros(8) if params is None else np.array(params, dtype=np.float64)
+        md = np.zeros(5) if modes is None else np.ascontiguousarray(modes, dtype=np.float64)
+        nm = 0 if modes is None else md.size // 5
+        lib().oracle_dg_project(_ip(self.cells), _dp(self.lower), _dp(self.upper), self.order, self.quad, kind,
+                                _dp(pr), _dp(md), nm, 1 if scale_by_volume else 0, _dp(out))
+        return out
 
     def block_diagonal(self, kappa=None, nthreads=1):
         b = np.zeros(self.ncells * self.nloc * self.nloc)
