@@ -252,13 +252,169 @@ def run_gpu(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------
+# Secondary workloads (the other problem configurations; one JSON line each).
+# ----------------------------------------------------------------------------
+def _timed(fn):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    return out, time.perf_counter() - t0
+
+
+def q1_rhs(N):
+    """Load vector of f = (2 pi^2 + 1) sin(pi x) sin(pi y) for Q1 (3x3 Gauss), zero Dirichlet rows."""
+    h = 1.0 / N
+    g, w = np.polynomial.legendre.leggauss(3)
+    g, w = 0.5 * (g + 1), 0.5 * w
+    b = np.zeros((N + 1, N + 1))
+    ex = np.arange(N)
+    for qy in range(3):
+        for qx in range(3):
+            X = (ex[None, :] + g[qx]) * h
+            Y = (ex[:, None] + g[qy]) * h
+            fv = (2 * np.pi ** 2 + 1) * np.sin(np.pi * X) * np.sin(np.pi * Y) * w[qx] * w[qy] * h * h
+            for ky in range(2):
+                for kx in range(2):
+                    phi = (g[qx] if kx else 1 - g[qx]) * (g[qy] if ky else 1 - g[qy])
+                    b[ky:ky + N, kx:kx + N] += fv * phi
+    b[0, :] = b[-1, :] = b[:, 0] = b[:, -1] = 0.0
+    return b.ravel()
+
+
+def workload_q1cg(args):
+    """2-D -lap u + u = f, 64x64 Q1, Dirichlet, diagonal-preconditioned CG to 1e-10 relative."""
+    import gbfem
+    import oracle
+    N = 64
+    op = gbfem.Q1Operator((N, N), diffusion=1.0, mass=1.0)
+    pc = gbfem.Preconditioner.diagonal(op)
+    b = q1_rhs(N)
+    inv = gbfem.KrylovInverseOperator("cg", tolerance=1e-10)
+    inv.bind(op, pc)
+    bd = gbfem.DeviceArray.from_numpy(b)
+    u = gbfem.DeviceArray(op.size)
+    times = []
+    for _ in range(args.warmup + args.steps):
+        u.clear()
+        _, t = _timed(lambda: inv(bd, u))
+        times.append(t)
+    t = float(np.median(times[args.warmup:]))
+    # e2e: host rhs in, host solution out
+    def e2e():
+        bd2 = gbfem.DeviceArray.from_numpy(b)
+        u2 = gbfem.DeviceArray(op.size)
+        u2.clear()
+        inv(bd2, u2)
+        return u2.numpy()
+    x, te = _timed(e2e)
+    xs = np.linspace(0, 1, N + 1)
+    X, Y = np.meshgrid(xs, xs)
+    err = float(np.max(np.abs(x - (np.sin(np.pi * X) * np.sin(np.pi * Y)).ravel())))
+    dg = oracle.q1_apply((N, N), None, 1.0, 1.0, diag_only=True)
+    t0 = time.perf_counter()
+    it_ref, x_ref, _ = oracle.cg(lambda v: oracle.q1_apply((N, N), v, 1.0, 1.0), b, prec=lambda r: r / dg,
+                                 epsilon=1e-10, max_iter=100000)
+    t_ref = time.perf_counter() - t0
+    return {"metric": "Q1 64x64 diag-PCG solve time to 1e-10", "value": 1e3 * t, "unit": "ms",
+            "higher_is_better": False, "iterations": inv.iterations(), "oracle_iterations": it_ref,
+            "max_nodal_error_vs_exact": err, "rel_diff_vs_oracle": float(np.max(np.abs(x - x_ref)) / np.max(np.abs(x_ref))),
+            "e2e": {"value": 1e3 * te, "unit": "ms", "h2d_bytes_per_step": 8 * b.size, "d2h_bytes_per_step": 8 * b.size},
+            "cpu_baseline": {"value": 1e3 * t_ref, "unit": "ms", "cores": 1, "kind": "port",
+                             "sample": "whole solve: oracle CG (cg.hh restated) + oracle Q1 apply"},
+            "dtype": "f64", "config": {"workload": "Q1 CG 64x64, -lap u + u = f, Dirichlet, diagonal preconditioner"}}
+
+
+def workload_rk3(args):
+    """3-D periodic advection-diffusion, 128^3 Q2, SSP-RK3 CFL 0.2, FP64 and FP32."""
+    import gbfem
+    N, p = 128, 2
+    steps = args.rk_steps
+    kw = dict(diffusion=1e-3, velocity=(1.0, 0.5, 0.25), periodic=(1, 1, 1), weak_dirichlet=False)
+    bnorm = float(np.sqrt(1 + 0.25 + 0.0625))
+    dt = 0.2 * (1.0 / N) / (bnorm * (2 * p + 1))
+    res = {}
+    for prec, name in ((gbfem.F64, "f64"), (gbfem.F32, "f32")):
+        op = gbfem.DGOperator((N, N, N), p, precision=prec, **kw)
+        u = gbfem.project((N, N, N), p, gbfem.FN_GAUSSIAN, params=(0.5, 0.5, 0.5, 0.1), precision=prec)
+        rk = gbfem.RK3(op)
+        rk.step(u, dt)  # warm-up step (then restart from the initial condition)
+        u = gbfem.project((N, N, N), p, gbfem.FN_GAUSSIAN, params=(0.5, 0.5, 0.5, 0.1), precision=prec)
+        _, t = _timed(lambda: [rk.step(u, dt) for _ in range(steps)])
+        res[name] = (t, u.numpy().astype(np.float64))
+        del rk, op
+    ndofs = N ** 3 * (p + 1) ** 3
+    err = float(np.max(np.abs(res["f32"][1] - res["f64"][1])) / np.max(np.abs(res["f64"][1])))
+    return {"metric": "SSP-RK3 128^3 Q2 advection-diffusion, time per step", "value": 1e3 * res["f64"][0] / steps,
+            "unit": "ms/step", "higher_is_better": False, "steps": steps, "dt": dt,
+            "f32_ms_per_step": 1e3 * res["f32"][0] / steps,
+            "f64_dof_stage_per_s": 3 * ndofs * steps / res["f64"][0],
+            "f32_dof_stage_per_s": 3 * ndofs * steps / res["f32"][0],
+            "f32_vs_f64_rel_max_error": err, "dtype": "f64 (and f32)",
+            "config": {"workload": "DG Q2 128^3 periodic, b=(1,0.5,0.25), eps=1e-3, Gaussian bump w=0.1, CFL 0.2"}}
+
+
+def workload_mixed(args):
+    """3-D SIPG -div(kappa grad u) = 1, 96^3 Q4 (or --cells), log-Gaussian kappa; mixed IR vs FP64 CG."""
+    import gbfem
+    N, p = args.cells, 4
+    cells = (N, N, N)
+    modes = gbfem.fourier_modes(args.seed, 256, 0.1, 1.0)
+    k64 = gbfem.project(cells, p, gbfem.FN_EXP_FOURIER, modes=modes)
+    k32 = gbfem.project(cells, p, gbfem.FN_EXP_FOURIER, modes=modes, precision=gbfem.F32)
+    f = gbfem.project(cells, p, gbfem.FN_CONSTANT, params=(1.0,), scale_by_volume=True)
+    op64 = gbfem.DGOperator(cells, p, kappa=k64)
+    op32 = gbfem.DGOperator(cells, p, precision=gbfem.F32, kappa=k32)
+    out = {"metric": "SIPG Q4 variable-kappa solve time to 1e-10 (mixed FP32-in-FP64 IR vs FP64 CG)",
+           "unit": "s", "higher_is_better": False, "dtype": "f64 outer / f32 inner",
+           "config": {"workload": "SIPG Q4 %d^3, -div(kappa grad u) = 1, u = 0 weak, log kappa ~ 256 Fourier modes "
+                                  "(std 1, corr 0.1), seed %d" % (N, args.seed), "dofs": op64.size}}
+    (pc32, t_setup32) = _timed(lambda: gbfem.Preconditioner.block_jacobi(op64, gbfem.F32))
+    u = gbfem.DeviceArray(op64.size)
+    u.clear()
+    info, t_mixed = _timed(lambda: gbfem.solve_mixed(op64, op32, pc32, f, u, tolerance=1e-10,
+                                                     inner_tolerance=args.inner_tol, max_outer=60))
+    out.update({"value": t_mixed, "mixed_setup_s": t_setup32, "mixed_converged": bool(info.converged),
+                "mixed_rel_residual": info.residual, "mixed_inner_iterations": info.iterations,
+                "mixed_operator_applies": info.operator_applies})
+    x_mixed = u.numpy()
+    del pc32
+    if not args.skip_fp64:
+        (pc64, t_setup64) = _timed(lambda: gbfem.Preconditioner.block_jacobi(op64))
+        inv = gbfem.KrylovInverseOperator("cg", tolerance=1e-10, max_iterations=args.fp64_max_iter)
+        inv.bind(op64, pc64)
+        u.clear()
+        _, t64 = _timed(lambda: inv(f, u))
+        i64 = inv.info()
+        x64 = u.numpy()
+        out.update({"fp64_cg_s": t64, "fp64_setup_s": t_setup64, "fp64_converged": i64["converged"],
+                    "fp64_iterations": i64["iterations"], "speedup_mixed_vs_fp64": t64 / t_mixed,
+                    "mixed_vs_fp64_rel_max_diff": float(np.max(np.abs(x_mixed - x64)) / np.max(np.abs(x64)))})
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbfem", choices=["gbfem", "reference"])
+    ap.add_argument("--workload", default="apply", choices=["apply", "q1cg", "rk3", "mixed"])
+    ap.add_argument("--rk-steps", type=int, default=100)
+    ap.add_argument("--cells", type=int, default=96)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--inner-tol", type=float, default=1e-3)
+    ap.add_argument("--fp64-max-iter", type=int, default=20000)
+    ap.add_argument("--skip-fp64", action="store_true")
     args = ap.parse_args()
+    if args.workload != "apply":
+        fn = {"q1cg": workload_q1cg, "rk3": workload_rk3, "mixed": workload_mixed}[args.workload]
+        line = fn(args)
+        line.update({"n_gpus": 1, "data": "synthetic"})
+        print(json.dumps(line), flush=True)
+        return
     world, rank, local = dist_init() if args.impl == "gbfem" else (
         int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0)
     if args.impl == "reference":

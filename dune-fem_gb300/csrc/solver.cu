@@ -498,9 +498,15 @@ static int bicgstab(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solv
 //   z_k = M_k^{-1} r_k,  d_k = z_k - sum_i (z_k . w_i)/(d_i . w_i) d_i,  w_i = A d_i,
 //   alpha = (d_k . r_k)/(d_k . w_k),  x += alpha d_k,  r -= alpha w_k.
 // Residual r = b - A x; stopping as in cg.hh (||r||^2 against eps^2 ||b||^2).
+// Fallback: when the preconditioner has one (the learned preconditioner's
+// block Jacobi) and the residual norm has not dropped by 10 % within
+// kStagnation iterations, or the step is not finite, the iteration switches
+// to the fallback and restarts its direction history.  The FP64 residual
+// decides convergence either way.
 static int fcg(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_params& prm, const void* b, void* x,
                Ctx& c, gbfem_solver_info* info) {
   const int mmax = prm.restart > 0 ? prm.restart : 1;
+  constexpr int kStagnation = 25;
   Vecs t, dirs, ws;
   GBFEM_TRY(t.alloc(2, c.bytes()));
   GBFEM_TRY(dirs.alloc(mmax + 1, c.bytes()));
@@ -515,18 +521,20 @@ static int fcg(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_pa
   const double tolerance = prm.tolerance * prm.tolerance *
                            (prm.error_measure == GBFEM_TOL_RELATIVE ? bb
                             : prm.error_measure == GBFEM_TOL_RESIDUAL_REDUCTION ? rr : 1.0);
-  int it = 0;
+  gbfem_preconditioner cur = pc;
+  int it = 0, hist = 0, mark_it = 0;
+  double mark_rr = rr;
   if (!finite(rr) || !finite(tolerance)) info->status = GBFEM_ERR_NONFINITE;
   for (it = 0; info->status == GBFEM_OK && rr > tolerance && it < prm.max_iterations; ++it) {
-    const int slot = it % (mmax + 1);
+    const int slot = hist % (mmax + 1);
     void* d = dirs[slot];
     void* w = ws[slot];
-    if (pc) GBFEM_TRY(pc_apply(pc, r, z, c));
+    if (cur) GBFEM_TRY(pc_apply(cur, r, z, c));
     else GBFEM_TRY(c.copy(r, z));
     GBFEM_TRY(c.copy(z, d));
-    const int kept = it < mmax ? it : mmax;
+    const int kept = hist < mmax ? hist : mmax;
     for (int k = 1; k <= kept; ++k) {
-      const int sl = (it - k) % (mmax + 1);
+      const int sl = (hist - k) % (mmax + 1);
       double zw;
       GBFEM_TRY(c.dot(z, ws[sl], &zw));
       GBFEM_TRY(c.axpby(-zw / dw[sl], dirs[sl], 1.0, d));
@@ -535,12 +543,34 @@ static int fcg(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_pa
     double dwk, dr;
     GBFEM_TRY(c.dot(d, w, &dwk));
     GBFEM_TRY(c.dot(d, r, &dr));
-    dw[slot] = dwk;
     const double alpha = dr / dwk;
-    if (!finite(alpha)) { info->status = GBFEM_ERR_NONFINITE; break; }
+    if (!finite(alpha) || !(dwk > 0.0)) {
+      if (cur && cur->fallback && cur != cur->fallback) {  // a bad direction from the variable preconditioner
+        cur = cur->fallback;
+        ++info->fallbacks;
+        hist = 0;
+        mark_it = it;
+        mark_rr = rr;
+        continue;
+      }
+      info->status = GBFEM_ERR_NONFINITE;
+      break;
+    }
+    dw[slot] = dwk;
+    ++hist;
     GBFEM_TRY(c.axpby(alpha, d, 1.0, x));
     GBFEM_TRY(c.axpby(-alpha, w, 1.0, r));
     GBFEM_TRY(c.dot(r, r, &rr));
+    if (rr < 0.81 * mark_rr) {
+      mark_rr = rr;
+      mark_it = it;
+    } else if (it - mark_it >= kStagnation && cur && cur->fallback && cur != cur->fallback) {
+      cur = cur->fallback;
+      ++info->fallbacks;
+      hist = 0;
+      mark_it = it;
+      mark_rr = rr;
+    }
     if (prm.verbose) std::printf("gbfem FCG it: %d : residual %.6e\n", it, std::sqrt(rr));
   }
   info->residual = std::sqrt(rr);

@@ -23,4 +23,7 @@ struct gbfem_preconditioner_s {
   int (*ext_apply)(void* ctx, const void* r, void* z, cudaStream_t s) = nullptr;
   void (*ext_destroy)(void* ctx) = nullptr;
   void* ext_ctx = nullptr;
+  // Flexible solvers switch to this preconditioner when the iteration with
+  // this one stagnates (the learned preconditioner's block-Jacobi fallback).
+  struct gbfem_preconditioner_s* fallback = nullptr;
 };

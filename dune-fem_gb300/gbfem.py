@@ -44,7 +44,7 @@ class SolverParams(C.Structure):
 class SolverInfo(C.Structure):
     _fields_ = [("converged", C.c_int), ("iterations", C.c_int), ("residual", C.c_double),
                 ("time_ms", C.c_double), ("operator_applies", C.c_int), ("preconditioner_applies", C.c_int),
-                ("status", C.c_int)]
+                ("status", C.c_int), ("fallbacks", C.c_int)]
 
 
 class IRParams(C.Structure):
@@ -92,6 +92,23 @@ def lib():
         L.gbfem_rk3_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
         L.gbfem_rk3_step.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]
         L.gbfem_rk3_destroy.argtypes = [C.c_void_p]
+        L.gbfem_cnn_create.argtypes = [C.c_int, C.c_int, C.c_uint64, C.POINTER(C.c_void_p)]
+        L.gbfem_cnn_destroy.argtypes = [C.c_void_p]
+        L.gbfem_cnn_set_kappa.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        L.gbfem_cnn_set_output_scale.argtypes = [C.c_void_p, C.c_double]
+        L.gbfem_cnn_get_output_scale.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.gbfem_cnn_forward.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+        L.gbfem_cnn_loss_grad.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_double),
+                                          C.c_void_p]
+        L.gbfem_cnn_train_step.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_double,
+                                           C.POINTER(C.c_double), C.c_void_p]
+        L.gbfem_cnn_num_params.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+        L.gbfem_cnn_get_params.argtypes = [C.c_void_p, C.c_void_p]
+        L.gbfem_cnn_set_params.argtypes = [C.c_void_p, C.c_void_p]
+        L.gbfem_cnn_get_grads.argtypes = [C.c_void_p, C.c_void_p]
+        L.gbfem_cnn_save.argtypes = [C.c_void_p, C.c_char_p]
+        L.gbfem_cnn_load.argtypes = [C.c_void_p, C.c_char_p]
+        L.gbfem_preconditioner_learned_create.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]
         L.gbfem_preconditioner_diagonal_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
         L.gbfem_preconditioner_block_jacobi_create.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
         L.gbfem_preconditioner_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -333,16 +350,17 @@ class KrylovInverseOperator:
         i = self._info
         return {"converged": bool(i.converged), "iterations": i.iterations, "residual": i.residual,
                 "time_ms": i.time_ms, "operator_applies": i.operator_applies,
-                "preconditioner_applies": i.preconditioner_applies, "status": i.status}
+                "preconditioner_applies": i.preconditioner_applies, "status": i.status,
+                "fallbacks": i.fallbacks}
 
 
 def solve_mixed(op64, op32, pc32, f, u, tolerance=1e-10, max_outer=50, inner_method="cg", inner_tolerance=1e-4,
-                inner_max_iterations=100000, verbose=False):
+                inner_max_iterations=100000, inner_restart=20, verbose=False):
     """FP64 iterative refinement around an FP32 inner Krylov solve."""
     p = IRParams()
     p.tolerance = tolerance
     p.max_outer = max_outer
-    p.inner = solver_params(inner_method, inner_tolerance, RELATIVE, inner_max_iterations, 20, verbose)
+    p.inner = solver_params(inner_method, inner_tolerance, RELATIVE, inner_max_iterations, inner_restart, verbose)
     info = SolverInfo()
     check(lib().gbfem_solve_mixed(op64.handle, op32.handle, pc32.handle if pc32 is not None else None,
                                   C.byref(p), f.ptr, u.ptr, C.byref(info)))
@@ -392,3 +410,92 @@ class RK3:
                 self.handle = None
         except Exception:
             pass
+
+
+class CNN:
+    """The learned preconditioner's network on a cells^3 grid of DG Q_order."""
+
+    def __init__(self, order, cells, seed=0):
+        self.order = order
+        self.cells = cells
+        self.nloc = (order + 1) ** 3
+        self.handle = C.c_void_p()
+        check(lib().gbfem_cnn_create(order, cells, seed, C.byref(self.handle)))
+        n = C.c_int64()
+        check(lib().gbfem_cnn_num_params(self.handle, C.byref(n)))
+        self.num_params = n.value
+
+    def set_kappa(self, kappa):
+        check(lib().gbfem_cnn_set_kappa(self.handle, kappa.precision if kappa is not None else F64,
+                                        kappa.ptr if kappa is not None else None, None))
+
+    @property
+    def scale(self):
+        v = C.c_double()
+        check(lib().gbfem_cnn_get_output_scale(self.handle, C.byref(v)))
+        return v.value
+
+    @scale.setter
+    def scale(self, v):
+        check(lib().gbfem_cnn_set_output_scale(self.handle, float(v)))
+
+    def forward(self, r, z, accumulate=False):
+        check(lib().gbfem_cnn_forward(self.handle, r.precision, r.ptr, z.ptr, 1 if accumulate else 0, None))
+
+    def loss_grad(self, r, target):
+        l = C.c_double()
+        check(lib().gbfem_cnn_loss_grad(self.handle, r.precision, r.ptr, target.ptr, C.byref(l), None))
+        return l.value
+
+    def train_step(self, r, target, lr=1e-3):
+        l = C.c_double()
+        check(lib().gbfem_cnn_train_step(self.handle, r.precision, r.ptr, target.ptr, lr, C.byref(l), None))
+        return l.value
+
+    def params(self):
+        a = np.zeros(self.num_params, dtype=np.float32)
+        check(lib().gbfem_cnn_get_params(self.handle, a.ctypes.data))
+        return a
+
+    def set_params(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        check(lib().gbfem_cnn_set_params(self.handle, a.ctypes.data))
+
+    def grads(self):
+        a = np.zeros(self.num_params, dtype=np.float32)
+        check(lib().gbfem_cnn_get_grads(self.handle, a.ctypes.data))
+        return a
+
+    def save(self, path):
+        check(lib().gbfem_cnn_save(self.handle, path.encode()))
+
+    def load(self, path):
+        check(lib().gbfem_cnn_load(self.handle, path.encode()))
+
+    def preconditioner(self, bj):
+        """z = bj(r) + NN(r), with bj as the fallback of flexible solvers."""
+        h = C.c_void_p()
+        check(lib().gbfem_preconditioner_learned_create(self.handle, bj.handle if bj is not None else None,
+                                                        C.byref(h)))
+        return Preconditioner(h, bj.precision if bj is not None else F64, (self, bj))
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().gbfem_cnn_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+
+def convert(x, precision):
+    """A copy of the dof vector x in the given precision."""
+    y = DeviceArray(x.n, precision)
+    check(lib().gbfem_convert(x.n, x.precision, x.ptr, precision, y.ptr, None))
+    return y
+
+
+def copy(x):
+    y = DeviceArray(x.n, x.precision)
+    check(lib().gbfem_copy(x.precision, x.n, x.ptr, y.ptr, None))
+    return y

@@ -1,0 +1,120 @@
+"""Training and evaluation driver of the learned preconditioner.
+
+Training pairs come from the solver itself, on seeded log-Gaussian kappa
+fields (256 Fourier modes, std 1, correlation length 0.1):
+  1. x* = the FP64-accurate solution of -div(kappa grad u) = 1 (SIPG, weak
+     u = 0), from the mixed FP32/FP64 iterative refinement to 1e-10;
+  2. iterates x_k of block-Jacobi PCG at k in `ks` give errors e_k = x* - x_k
+     and residuals r_k = A e_k (FP64 apply);
+  3. the network learns the part of e_k block Jacobi misses:
+     target_k = e_k - BJ(r_k).
+The network is then used as z = BJ(r) + NN(r) inside flexible CG, where the
+FP64 residual decides convergence and block Jacobi is the fallback.
+All compute runs in the library's CUDA kernels; this module only sequences
+calls through the C-ABI.
+"""
+import time
+
+import numpy as np
+
+import gbfem
+
+
+def sipg_problem(cells, order, seed, precision=gbfem.F64):
+    """(op64, op32, kappa64, f): the variable-kappa SIPG problem of `seed`."""
+    cl = (cells, cells, cells)
+    modes = gbfem.fourier_modes(seed, 256, 0.1, 1.0)
+    k64 = gbfem.project(cl, order, gbfem.FN_EXP_FOURIER, modes=modes)
+    k32 = gbfem.convert(k64, gbfem.F32)
+    op64 = gbfem.DGOperator(cl, order, kappa=k64)
+    op32 = gbfem.DGOperator(cl, order, precision=gbfem.F32, kappa=k32)
+    f = gbfem.project(cl, order, gbfem.FN_CONSTANT, params=(1.0,), scale_by_volume=True)
+    return op64, op32, k64, k32, f
+
+
+def _rms(x):
+    return np.sqrt(max(gbfem.dot(x, x), 0.0) / x.n)
+
+
+def make_pairs(cells, order, seed, ks=(10, 40, 120), inner_tol=1e-3):
+    """Training pairs (r_k, target_k) in FP32 for one kappa seed, plus the kappa field."""
+    op64, op32, k64, k32, f = sipg_problem(cells, order, seed)
+    bj32 = gbfem.Preconditioner.block_jacobi(op64, gbfem.F32)
+    xs = gbfem.DeviceArray(op64.size)
+    xs.clear()
+    info = gbfem.solve_mixed(op64, op32, bj32, f, xs, tolerance=1e-10, inner_tolerance=inner_tol)
+    if not info.converged:
+        raise RuntimeError("make_pairs: reference solve did not converge (seed %d)" % seed)
+    f32 = gbfem.convert(f, gbfem.F32)
+    pairs = []
+    for k in ks:
+        inv = gbfem.KrylovInverseOperator("cg", tolerance=1e-12, max_iterations=k)
+        inv.bind(op32, bj32)
+        xk = gbfem.DeviceArray(op32.size, gbfem.F32)
+        xk.clear()
+        inv(f32, xk)
+        e = gbfem.copy(xs)                      # e = x* - x_k (FP64)
+        gbfem.axpy(-1.0, gbfem.convert(xk, gbfem.F64), e)
+        r = gbfem.DeviceArray(op64.size)
+        op64(e, r)                              # r = A e
+        r32 = gbfem.convert(r, gbfem.F32)
+        z = gbfem.DeviceArray(op32.size, gbfem.F32)
+        bj32(r32, z)
+        t = gbfem.convert(e, gbfem.F32)         # target = e - BJ(r)
+        gbfem.axpy(-1.0, z, t)
+        pairs.append((r32, t))
+    return pairs, k32
+
+
+def train(cnn, cells, order, seeds, ks=(10, 40, 120), steps_per_pair=4, lr=1e-3, log=None):
+    """Online training over `seeds`; returns the per-step losses."""
+    losses = []
+    t0 = time.perf_counter()
+    for i, seed in enumerate(seeds):
+        pairs, k32 = make_pairs(cells, order, seed, ks)
+        cnn.set_kappa(k32)
+        if i == 0:
+            r, t = pairs[-1]
+            cnn.scale = _rms(t) / _rms(r)
+        for _ in range(steps_per_pair):
+            for r, t in pairs:
+                losses.append(cnn.train_step(r, t, lr))
+        if log:
+            log("seed %d (%d/%d): loss %.4e  (%.1f s)" % (seed, i + 1, len(seeds), losses[-1],
+                                                         time.perf_counter() - t0))
+    return losses
+
+
+def evaluate(cnn, cells, order, seed, tol=1e-10, max_iterations=20000, plain=True):
+    """Iterations and times on one held-out seed: FP64 flexible CG with the
+    learned preconditioner vs FP64 block-Jacobi PCG (and unpreconditioned CG),
+    plus the mixed FP32/FP64 solve with the learned preconditioner inside."""
+    op64, op32, k64, k32, f = sipg_problem(cells, order, seed)
+    out = {"seed": seed}
+    bj64 = gbfem.Preconditioner.block_jacobi(op64)
+    bj32 = gbfem.Preconditioner.block_jacobi(op64, gbfem.F32)
+    cnn.set_kappa(k64)
+    learned64 = cnn.preconditioner(bj64)
+    u = gbfem.DeviceArray(op64.size)
+    runs = [("bj_cg", "cg", bj64), ("learned_fcg", "fcg", learned64)]
+    if plain:
+        runs.insert(0, ("plain_cg", "cg", None))
+    for name, method, pc in runs:
+        inv = gbfem.KrylovInverseOperator(method, tolerance=tol, max_iterations=max_iterations, restart=4)
+        inv.bind(op64, pc)
+        u.clear()
+        t0 = time.perf_counter()
+        inv(f, u)
+        i = inv.info()
+        out[name] = {"iterations": i["iterations"], "time_s": time.perf_counter() - t0,
+                     "converged": i["converged"], "fallbacks": i["fallbacks"]}
+    # mixed precision + learned (FP32 inner flexible CG, FP64 refinement)
+    learned32 = cnn.preconditioner(bj32)
+    for name, pc, method in (("mixed_bj", bj32, "cg"), ("mixed_learned", learned32, "fcg")):
+        u.clear()
+        t0 = time.perf_counter()
+        info = gbfem.solve_mixed(op64, op32, pc, f, u, tolerance=tol, inner_method=method, inner_tolerance=1e-3,
+                                 inner_restart=4)
+        out[name] = {"iterations": info.iterations, "time_s": time.perf_counter() - t0,
+                     "converged": bool(info.converged), "rel_residual": info.residual}
+    return out

@@ -168,6 +168,7 @@ typedef struct {
   int operator_applies;
   int preconditioner_applies;
   int status;            /* GBFEM_OK, GBFEM_ERR_NONFINITE on NaN/Inf */
+  int fallbacks;         /* flexible solvers: switches to the fallback preconditioner */
 } gbfem_solver_info;
 
 /* Fills the reference's defaults: cg, tolerance 1e-8, absolute, max
@@ -218,6 +219,46 @@ int gbfem_rk3_create(gbfem_operator op, gbfem_rk_solver* rk);
 /* One step of size dt, in place on the device vector u (op's precision). */
 int gbfem_rk3_step(gbfem_rk_solver rk, void* u, double dt, void* stream);
 int gbfem_rk3_destroy(gbfem_rk_solver rk);
+
+/* ---- learned preconditioner ------------------------------------------------
+ * A 4-level convolutional network (32 channels, 3x3x3 convolutions, BF16
+ * weights/activations, FP32 accumulation) on the cells x cells x cells grid of
+ * a DG Q_order space: input the residual's per-cell coefficients (scaled by
+ * 1/rms) and log of the cell mean of kappa, output per-cell coefficients.
+ * Trained on the GPU by its own forward/backward kernels.  Used as
+ * z = BJ(r) + S rms(r) NN(r/rms(r)) inside flexible CG/GMRES, with block
+ * Jacobi as the fallback.  No counterpart in the reference (north-star
+ * extension); it plugs in where the reference takes a user preconditioner
+ * (solver/preconditionfunctionwrapper.hh:18-47, schemes/femscheme.hh:202-209).
+ * ----------------------------------------------------------------------- */
+typedef struct gbfem_cnn_s* gbfem_cnn;
+/* cells: per direction (cubic grid), a multiple of 8; seeded He initialisation. */
+int gbfem_cnn_create(int order, int cells, uint64_t seed, gbfem_cnn* cnn);
+int gbfem_cnn_destroy(gbfem_cnn cnn);
+/* Sets the log-kappa input channel from DG kappa coefficients (device; NULL = 1). */
+int gbfem_cnn_set_kappa(gbfem_cnn cnn, int precision, const void* kappa, void* stream);
+int gbfem_cnn_set_output_scale(gbfem_cnn cnn, double scale);
+int gbfem_cnn_get_output_scale(gbfem_cnn cnn, double* scale);
+/* z = S rms(r) NN(r/rms(r)) (accumulate = 1: z += ...). */
+int gbfem_cnn_forward(gbfem_cnn cnn, int precision, const void* r, void* z, int accumulate, void* stream);
+/* Loss = mean_l (NN(r/rms)_l - target_l/(S rms))^2 and all weight gradients
+ * (no update); loss may be NULL (then no synchronisation). */
+int gbfem_cnn_loss_grad(gbfem_cnn cnn, int precision, const void* r, const void* target, double* loss,
+                        void* stream);
+/* loss_grad followed by one Adam step (lr, beta = 0.9/0.999, eps 1e-8). */
+int gbfem_cnn_train_step(gbfem_cnn cnn, int precision, const void* r, const void* target, double lr,
+                         double* loss, void* stream);
+int gbfem_cnn_num_params(gbfem_cnn cnn, int64_t* n);
+/* Host FP32 copies of weights / gradients, layer by layer, [taps][cout][cin]. */
+int gbfem_cnn_get_params(gbfem_cnn cnn, float* host);
+int gbfem_cnn_set_params(gbfem_cnn cnn, const float* host);
+int gbfem_cnn_get_grads(gbfem_cnn cnn, float* host);
+/* Weight file (checkpoint/resume); load rejects files of another shape or
+ * with non-finite weights. */
+int gbfem_cnn_save(gbfem_cnn cnn, const char* path);
+int gbfem_cnn_load(gbfem_cnn cnn, const char* path);
+/* z = bj(r) + NN(r); bj is the fallback of flexible solvers (not owned). */
+int gbfem_preconditioner_learned_create(gbfem_cnn cnn, gbfem_preconditioner bj, gbfem_preconditioner* pc);
 
 /* ---- BLAS-1 on dof vectors (function/common/discretefunction.hh:781-901,
  *      function/common/scalarproducts.hh:101-127).  Reductions are

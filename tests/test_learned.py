@@ -1,0 +1,104 @@
+"""The learned preconditioner: GPU forward/backward kernels against the CPU
+oracle (oracle/cnn_oracle.py), training, checkpoint/resume, and its use in
+flexible CG with the block-Jacobi fallback."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.mark.parametrize("order", [1, 3])
+def test_forward_and_gradients_match_cpu_oracle(gb, order):
+    import cnn_oracle as co
+    N = 8
+    nloc = (order + 1) ** 3
+    net = gb.CNN(order, N, seed=3)
+    rng = np.random.default_rng(order)
+    n = N ** 3 * nloc
+    kappa = np.zeros(n)
+    kappa[::nloc] = np.exp(rng.normal(0, 1, N ** 3))
+    net.set_kappa(gb.DeviceArray.from_numpy(kappa))
+    net.scale = 0.7
+    r = rng.uniform(-1, 1, n)
+    t = rng.uniform(-1, 1, n)
+    dr, dt = gb.DeviceArray.from_numpy(r), gb.DeviceArray.from_numpy(t)
+    z = gb.DeviceArray(n)
+    net.forward(dr, z)
+    Ws = co.unflatten(net.params(), nloc)
+    logk = np.log(kappa[::nloc])
+    loss_ref, g_ref, y = co.loss_grad(Ws, r, t, logk, N, nloc, 0.7)
+    rms = np.sqrt(np.mean(r ** 2))
+    z_ref = (0.7 * rms * y[:, :nloc]).ravel()
+    assert _rel(z.numpy(), z_ref) < 2e-2
+    loss = net.loss_grad(dr, dt)
+    assert abs(loss - loss_ref) < 2e-2 * loss_ref
+    g = co.unflatten(net.grads(), nloc)
+    for i, (a, b) in enumerate(zip(g, g_ref)):
+        cos = np.sum(a * b) / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-300)
+        assert cos > 0.995, (i, cos)
+        assert _rel(a, b) < 0.1, (i, _rel(a, b))
+
+
+def test_training_reduces_the_loss_and_is_reproducible(gb):
+    N, order = 8, 2
+    n = N ** 3 * 27
+    rng = np.random.default_rng(1)
+    r = gb.DeviceArray.from_numpy(rng.uniform(-1, 1, n).astype(np.float32))
+    t = gb.DeviceArray.from_numpy(rng.uniform(-1, 1, n).astype(np.float32))
+    runs = []
+    for _ in range(2):
+        net = gb.CNN(order, N, seed=5)
+        losses = [net.train_step(r, t, 3e-3) for _ in range(40)]
+        runs.append((losses, net.params()))
+    assert runs[0][0][-1] < 0.7 * runs[0][0][0]
+    assert runs[0][0] == runs[1][0]
+    assert np.array_equal(runs[0][1], runs[1][1])
+
+
+def test_checkpoint_roundtrip_and_rejection(gb, tmp_path):
+    net = gb.CNN(3, 8, seed=9)
+    net.scale = 2.5
+    path = str(tmp_path / "net.bin")
+    net.save(path)
+    other = gb.CNN(3, 8, seed=10)
+    other.load(path)
+    assert np.array_equal(other.params(), net.params()) and other.scale == 2.5
+    data = bytearray(open(path, "rb").read())
+    data[40:44] = np.array([np.nan], dtype=np.float32).tobytes()
+    bad = str(tmp_path / "bad.bin")
+    open(bad, "wb").write(bytes(data))
+    with pytest.raises(gb.GbfemError):
+        other.load(bad)
+    with pytest.raises(gb.GbfemError):
+        gb.CNN(2, 8).load(path)  # another space
+
+
+def test_learned_fcg_certifies_and_falls_back_from_a_broken_network(gb):
+    """A network with absurd weights must not spoil the solve: the FP64
+    residual decides, flexible CG falls back to block Jacobi."""
+    import learned
+    cells, order = 16, 2
+    op64, op32, k64, k32, f = learned.sipg_problem(cells, order, 123)
+    bj = gb.Preconditioner.block_jacobi(op64)
+    net = gb.CNN(order, cells, seed=1)
+    net.set_kappa(k64)
+    net.set_params(1e3 * np.random.default_rng(0).normal(size=net.num_params).astype(np.float32))
+    net.scale = 1e6
+    pc = net.preconditioner(bj)
+    inv = gb.KrylovInverseOperator("fcg", tolerance=1e-10, max_iterations=5000, restart=4)
+    inv.bind(op64, pc)
+    u = gb.DeviceArray(op64.size)
+    u.clear()
+    inv(f, u)
+    info = inv.info()
+    assert info["converged"] and info["fallbacks"] >= 1
+    r = gb.DeviceArray(op64.size)
+    op64(u, r)
+    x, ff = r.numpy(), f.numpy()
+    assert np.linalg.norm(ff - x) <= 1.01e-10 * np.linalg.norm(ff)
