@@ -34,7 +34,10 @@ SEED = 20261203
 METRIC = "SIPG apply DoF/s"
 UNIT = "DoF/s"
 BYTES_PER_DOF = 16.0          # read u (8) + write w (8), geometry recomputed, tables on chip
-FLOP_PER_DOF = 402.0          # sum-factorised SIPG Q3, q=5 (volume + faces)
+FLOP_PER_DOF = 402.0          # sum-factorised SIPG Q3, q=5 (volume + faces), the algorithmic count
+# flops the constant-coefficient closed-form kernel executes per dof (n = 4):
+# volume 3 n^4 FMA, faces 6 n^2 (4 n) trace FMA + 12 n^3 expansion FMA, ~10 flop per face point
+KERNEL_FLOP_PER_DOF = (2.0 * (3 * 4 ** 4 + 36 * 4 ** 3) + 6 * 16 * 10) / 64.0
 CONFIG = {"workload": "SIPG DG Q3 apply, 3-D unit cube 64^3 hexes, 16.8M dofs, q=5, penalty 160, FP64",
           "cells": list(CELLS), "order": ORDER, "quad_points": QUAD, "dofs": 64 ** 3 * 64,
           "l2": "inputs exceed L2 (u + w = 268 MB > 129 MB), no flush"}
@@ -111,11 +114,12 @@ def barrier(world):
         dist.barrier()
 
 
-def allreduce_max(x, world):
+def allreduce_max(x, world, device="cuda"):
+    """Max over ranks of a per-rank time (the replicas' job time)."""
     if world > 1:
         import torch
         import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        t = torch.tensor([x], dtype=torch.float64, device=device)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
     return x
@@ -170,9 +174,26 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def time_applies(op, u, w, steps, stream):
+    import torch
+    sptr = stream.cuda_stream
+    for _ in range(3):
+        op(u, w, sptr)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        op(u, w, sptr)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
 def run_gpu(args, world, rank, local):
     import gbfem
     peaks, peak_kind = load_peaks()
+    # default algorithm: constant kappa -> the closed form of the q=5 quadrature
     op = gbfem.DGOperator(CELLS, ORDER, quad_points=QUAD)
     n = op.size
     u_h = np.random.default_rng(SEED + rank).uniform(-1.0, 1.0, n)
@@ -218,9 +239,21 @@ def run_gpu(args, world, rank, local):
     if rank != 0:
         return
 
+    # the Gauss-point quadrature kernel on the same input (variable-kappa path), for reference
+    opq = gbfem.DGOperator(CELLS, ORDER, quad_points=QUAD, algorithm=gbfem.ALGO_QUADRATURE)
+    wq = gbfem.DeviceArray(n)
+    ms_quad = time_applies(opq, u, wq, max(3, min(args.steps, 20)), stream)
+    wa, wb = w.numpy(), wq.numpy()
+    quad_rel = float(np.max(np.abs(wa - wb)) / np.max(np.abs(wb)))
+    op32 = gbfem.DGOperator(CELLS, ORDER, quad_points=QUAD, precision=gbfem.F32)
+    u32 = gbfem.convert(u, gbfem.F32)
+    w32 = gbfem.DeviceArray(n, gbfem.F32)
+    ms_f32 = time_applies(op32, u32, w32, max(3, min(args.steps, 50)), stream)
+    del opq, wq, op32, u32, w32
+
     fp64_peak, fp32_peak = gbfem.measure_fma_peaks()
     achieved_gbs = BYTES_PER_DOF * n / (ms_step * 1e-3) / 1e9
-    achieved_tflops = FLOP_PER_DOF * n / (ms_step * 1e-3) / 1e12
+    achieved_tflops = KERNEL_FLOP_PER_DOF * n / (ms_step * 1e-3) / 1e12
     traffic = None
     prof = os.path.join(ROOT, "profiles", "dg_apply_q3_64cube_f64.json")
     if os.path.exists(prof):
@@ -243,7 +276,16 @@ def run_gpu(args, world, rank, local):
                          "peak_source": peak_kind, "algorithmic_bytes_per_dof": BYTES_PER_DOF},
             "fp64_pipe": {"achieved_tflops": achieved_tflops, "peak_tflops_measured": fp64_peak,
                           "frac": achieved_tflops / fp64_peak if fp64_peak else None,
-                          "algorithmic_flop_per_dof": FLOP_PER_DOF, "fp32_peak_tflops_measured": fp32_peak},
+                          "kernel_flop_per_dof": KERNEL_FLOP_PER_DOF,
+                          "sum_factorised_quadrature_flop_per_dof": FLOP_PER_DOF,
+                          "fp32_peak_tflops_measured": fp32_peak},
+            "algorithm": "constant-kappa closed form of the q=5 Gauss quadrature (exact for these integrands; "
+                         "1-D stiffness along lines + identity tangential face mass)",
+            "quadrature_kernel": {"value": n / (ms_quad * 1e-3), "unit": UNIT, "ms_per_step": ms_quad,
+                                  "rel_max_diff_vs_default": quad_rel,
+                                  "note": "sum-factorised evaluation at the 125 Gauss points (the variable-kappa path)"},
+            "fp32_apply": {"value": n / (ms_f32 * 1e-3), "unit": UNIT, "ms_per_step": ms_f32,
+                           "hbm_frac": 8.0 * n / (ms_f32 * 1e-3) / 1e9 / peaks["hbm_gbs"]},
             "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": nthreads, "kind": "port",
                              "sample": "%d cells (whole z-slabs) of the 64^3 grid applied by the oracle "
                                        "(dense per-element evaluation as dune-fem's GalerkinOperator), ~15 s"
@@ -395,22 +437,68 @@ def workload_mixed(args):
     return out
 
 
+def workload_learned(args):
+    """SIPG Q3 variable kappa (cells^3), CNN preconditioner trained on the
+    solver's own (residual, error) pairs for args.train_seeds kappa seeds,
+    evaluated on args.eval_seeds held-out seeds against FP64 CG."""
+    import gbfem
+    import learned
+    N, p = args.cells, 3
+    net = gbfem.CNN(p, N, seed=2026)
+    log = (lambda m: print(m, file=sys.stderr, flush=True)) if args.verbose else None
+    t0 = time.perf_counter()
+    losses = learned.train(net, N, p, list(range(args.train_seeds)), steps_per_pair=args.train_steps, lr=args.lr,
+                           log=log)
+    t_train = time.perf_counter() - t0
+    if args.save_net:
+        net.save(args.save_net)
+    evals = [learned.evaluate(net, N, p, 100000 + s, plain=not args.skip_plain)
+             for s in range(args.eval_seeds)]
+    def mean(key, field):
+        v = [e[key][field] for e in evals if key in e]
+        return float(np.mean(v)) if v else None
+    out = {"metric": "SIPG Q3 variable-kappa solve time to 1e-10: learned/mixed vs plain FP64 CG", "unit": "s",
+           "higher_is_better": False, "dtype": "f64 outer / f32 inner / bf16 network",
+           "config": {"workload": "SIPG Q3 %d^3 (%d dofs), -div(kappa grad u) = 1, log kappa ~ 256 Fourier modes; "
+                                  "%d training seeds, %d held-out seeds" % (N, N ** 3 * 64, args.train_seeds,
+                                                                          args.eval_seeds)},
+           "value": mean("mixed_learned", "time_s"),
+           "train_s": t_train, "train_steps": len(losses), "loss_first": losses[0], "loss_last": losses[-1],
+           "loss_last_mean20": float(np.mean(losses[-20:])), "evals": evals}
+    for k in ("plain_cg", "bj_cg", "learned_fcg", "mixed_bj", "mixed_learned"):
+        out[k + "_mean_time_s"] = mean(k, "time_s")
+        out[k + "_mean_iterations"] = mean(k, "iterations")
+    if out.get("plain_cg_mean_time_s") and out.get("mixed_learned_mean_time_s"):
+        out["speedup_mixed_learned_vs_plain_fp64_cg"] = out["plain_cg_mean_time_s"] / out["mixed_learned_mean_time_s"]
+    if out.get("bj_cg_mean_time_s") and out.get("learned_fcg_mean_time_s"):
+        out["speedup_learned_fcg_vs_bj_cg"] = out["bj_cg_mean_time_s"] / out["learned_fcg_mean_time_s"]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbfem", choices=["gbfem", "reference"])
-    ap.add_argument("--workload", default="apply", choices=["apply", "q1cg", "rk3", "mixed"])
+    ap.add_argument("--workload", default="apply", choices=["apply", "q1cg", "rk3", "mixed", "learned"])
     ap.add_argument("--rk-steps", type=int, default=100)
     ap.add_argument("--cells", type=int, default=96)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--inner-tol", type=float, default=1e-3)
     ap.add_argument("--fp64-max-iter", type=int, default=20000)
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--train-seeds", type=int, default=256)
+    ap.add_argument("--eval-seeds", type=int, default=32)
+    ap.add_argument("--train-steps", type=int, default=2)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--save-net", default="")
+    ap.add_argument("--verbose", action="store_true")
     args = ap.parse_args()
     if args.workload != "apply":
-        fn = {"q1cg": workload_q1cg, "rk3": workload_rk3, "mixed": workload_mixed}[args.workload]
+        fn = {"q1cg": workload_q1cg, "rk3": workload_rk3, "mixed": workload_mixed,
+              "learned": workload_learned}[args.workload]
         line = fn(args)
         line.update({"n_gpus": 1, "data": "synthetic"})
         print(json.dumps(line), flush=True)

@@ -1,6 +1,7 @@
 // Instantiation and launch of dg_apply_kernel for the supported (n, q)
 // pairs: n = p+1 in 2..5, q in {p+1, p+2}.
 #pragma once
+#include "dg_const_kernel.cuh"
 #include "dg_kernel.cuh"
 #include "gbfem_internal.cuh"
 
@@ -43,6 +44,28 @@ int dg_launch(const DgArgsT<T>& args, const DgTablesT<T>& tabs, int n, int q, bo
   GBFEM_DG_CASE(5, 6)
 #undef GBFEM_DG_CASE
   return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "dg apply: unsupported (p, q)");
+}
+
+template <typename T, int N>
+int dg_const_launch_one(const DgArgsT<T>& args, const DgConstTablesT<T>& tabs, cudaStream_t stream) {
+  constexpr int CPB = N <= 2 ? 32 : (N <= 4 ? 16 : 8);
+  const long long blocks = (args.ncells + CPB - 1) / CPB;
+  if (blocks <= 0) return GBFEM_OK;
+  if (blocks > 2147483647LL) return set_error(GBFEM_ERR_INVALID, "dg apply: grid too large");
+  dg_const_kernel<T, N, CPB><<<unsigned(blocks), 256, 0, stream>>>(args, tabs);
+  GBFEM_CUDA_TRY(cudaGetLastError());
+  return GBFEM_OK;
+}
+
+template <typename T>
+int dg_const_launch(const DgArgsT<T>& args, const DgConstTablesT<T>& tabs, int n, cudaStream_t stream) {
+  switch (n) {
+    case 2: return dg_const_launch_one<T, 2>(args, tabs, stream);
+    case 3: return dg_const_launch_one<T, 3>(args, tabs, stream);
+    case 4: return dg_const_launch_one<T, 4>(args, tabs, stream);
+    case 5: return dg_const_launch_one<T, 5>(args, tabs, stream);
+  }
+  return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "dg apply: unsupported order");
 }
 
 }  // namespace gbfem

@@ -16,6 +16,23 @@ namespace gbfem {
 
 int dg_launch_f64(const DgArgsT<double>&, const DgTablesT<double>&, int, int, bool, cudaStream_t);
 int dg_launch_f32(const DgArgsT<float>&, const DgTablesT<float>&, int, int, bool, cudaStream_t);
+int dg_const_launch_f64(const DgArgsT<double>&, const DgConstTablesT<double>&, int, cudaStream_t);
+int dg_const_launch_f32(const DgArgsT<float>&, const DgConstTablesT<float>&, int, cudaStream_t);
+
+template <typename T>
+static void fill_const_tables(const Tables1D& t, const ConstTables1D& c, DgConstTablesT<T>* out) {
+  std::memset(out, 0, sizeof(*out));
+  for (int i = 0; i < t.n; ++i)
+    for (int j = 0; j < t.n; ++j) {
+      out->K1[i * t.n + j] = T(c.K1[i][j]);
+      out->D1[i * t.n + j] = T(c.D1[i][j]);
+    }
+  for (int s = 0; s < 2; ++s)
+    for (int i = 0; i < t.n; ++i) {
+      out->tr[s * t.n + i] = T(t.tr[s][i]);
+      out->dtr[s * t.n + i] = T(t.dtr[s][i]);
+    }
+}
 
 template <typename T>
 static void fill_dg_tables(const Tables1D& t, DgTablesT<T>* out) {
@@ -70,6 +87,7 @@ int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s,
     a.w = static_cast<double*>(w);
     a.unit_mode = unit_mode;
     a.blocks = static_cast<double*>(blocks);
+    if (unit_mode == 0 && op->coefficient_space) return dg_const_launch_f64(a, op->ctab64, op->n, s);
     return dg_launch_f64(a, op->tab64, op->n, op->q, op->dg.kappa != nullptr, s);
   } else {
     DgArgsT<float> a;
@@ -80,6 +98,7 @@ int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s,
     a.w = static_cast<float*>(w);
     a.unit_mode = unit_mode;
     a.blocks = static_cast<float*>(blocks);
+    if (unit_mode == 0 && op->coefficient_space) return dg_const_launch_f32(a, op->ctab32, op->n, s);
     return dg_launch_f32(a, op->tab32, op->n, op->q, op->dg.kappa != nullptr, s);
   }
 }
@@ -208,9 +227,19 @@ int gbfem_dg_operator_create(const gbfem_dg_desc* desc, gbfem_operator* out) {
   op->nloc = op->n * op->n * op->n;
   op->ncells = (long long)desc->grid.cells[0] * desc->grid.cells[1] * desc->grid.cells[2];
   op->ndofs = op->ncells * op->nloc;
+  for (int k = 0; k < 3; ++k)
+    if (desc->grid.periodic[k] && desc->grid.cells[k] < 2) {
+      delete op;
+      return set_error(GBFEM_ERR_INVALID, "a periodic direction needs at least 2 cells");
+    }
   Tables1D t = make_tables(op->n, q);
   fill_dg_tables(t, &op->tab64);
   fill_dg_tables(t, &op->tab32);
+  ConstTables1D ct = make_const_tables(op->n);
+  fill_const_tables(t, ct, &op->ctab64);
+  fill_const_tables(t, ct, &op->ctab32);
+  // q >= p+1 always holds here, so the quadrature is exact for constant kappa
+  op->coefficient_space = desc->kappa == nullptr && desc->algorithm == GBFEM_ALGO_AUTO;
   *out = op;
   return GBFEM_OK;
 }

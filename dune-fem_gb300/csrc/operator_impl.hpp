@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/gbfem.h"
+#include "dg_const_kernel.cuh"
 #include "dg_kernel.cuh"
 
 namespace gbfem {
@@ -31,6 +32,9 @@ struct gbfem_operator_s {
   long long ncells = 0, ndofs = 0;
   gbfem::DgTablesT<double> tab64{};
   gbfem::DgTablesT<float> tab32{};
+  gbfem::DgConstTablesT<double> ctab64{};
+  gbfem::DgConstTablesT<float> ctab32{};
+  bool coefficient_space = false;  // constant-coefficient closed form (exact quadrature)
   gbfem::Q1Element q1{};
   void* host_u = nullptr;  // device staging of gbfem_operator_apply_host
   void* host_w = nullptr;

@@ -70,16 +70,26 @@ __global__ void k_block_invert(const TI* __restrict__ blocks, TO* __restrict__ i
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) a[e] = double(src[e]);
   __syncthreads();
   for (int k = 0; k < nb; ++k) {
-    if (threadIdx.x == 0) {
-      int p = k;
-      double best = fabs(a[k * nb + k]);
-      for (int i = k + 1; i < nb; ++i) {
+    if (threadIdx.x < 32) {
+      // warp-parallel partial pivoting: largest |a[i][k]|, ties to the smallest i
+      int p = nb;
+      double best = -1.0;
+      for (int i = k + int(threadIdx.x); i < nb; i += 32) {
         const double v = fabs(a[i * nb + k]);
         if (v > best) { best = v; p = i; }
       }
-      s_piv = p;
-      perm[k] = p;
-      if (best == 0.0) atomicExch(singular, 1);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_down_sync(0xffffffffu, best, o);
+        const int op = __shfl_down_sync(0xffffffffu, p, o);
+        if (ob > best || (ob == best && op < p)) { best = ob; p = op; }
+      }
+      if (threadIdx.x == 0) {
+        if (p >= nb) p = k;  // only NaN in the column: keep the row, flag below
+        s_piv = p;
+        perm[k] = p;
+        if (!(best > 0.0)) atomicExch(singular, 1);
+      }
     }
     __syncthreads();
     const int p = s_piv;

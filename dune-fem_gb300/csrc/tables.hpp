@@ -103,4 +103,30 @@ inline Tables1D make_tables(int n, int q) {
   return t;
 }
 
+// 1-D stiffness and advection matrices of the orthonormal Legendre basis on
+// [0,1], by (n+1)-point Gauss quadrature (exact for the degree-2p products).
+struct ConstTables1D {
+  long double K1[kMaxN][kMaxN];  // int L_i' L_j'
+  long double D1[kMaxN][kMaxN];  // int L_i' L_j
+};
+inline ConstTables1D make_const_tables(int n) {
+  ConstTables1D t{};
+  long double p[kMaxQ], w[kMaxQ];
+  gauss01(n + 1, p, w);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      long double k = 0, d = 0;
+      for (int a = 0; a <= n; ++a) {
+        long double vi, di, vj, dj;
+        legendre01(i, p[a], &vi, &di);
+        legendre01(j, p[a], &vj, &dj);
+        k += w[a] * di * dj;
+        d += w[a] * di * vj;
+      }
+      t.K1[i][j] = k;
+      t.D1[i][j] = d;
+    }
+  return t;
+}
+
 }  // namespace gbfem

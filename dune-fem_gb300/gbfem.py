@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libgbfem.so")
 
 F64, F32 = 0, 1
+ALGO_AUTO, ALGO_QUADRATURE = 0, 1
 _DTYPES = {F64: np.float64, F32: np.float32}
 
 
@@ -33,7 +34,8 @@ class GridDesc(C.Structure):
 class DgDesc(C.Structure):
     _fields_ = [("grid", GridDesc), ("order", C.c_int), ("quad_points", C.c_int), ("precision", C.c_int),
                 ("diffusion", C.c_double), ("penalty", C.c_double), ("mass", C.c_double),
-                ("velocity", C.c_double * 3), ("weak_dirichlet", C.c_int), ("kappa", C.c_void_p)]
+                ("velocity", C.c_double * 3), ("weak_dirichlet", C.c_int), ("kappa", C.c_void_p),
+                ("algorithm", C.c_int)]
 
 
 class SolverParams(C.Structure):
@@ -221,7 +223,7 @@ class DGOperator(Operator):
 
     def __init__(self, cells, order, quad_points=0, precision=F64, diffusion=1.0, penalty=None, mass=0.0,
                  velocity=(0.0, 0.0, 0.0), weak_dirichlet=True, periodic=(0, 0, 0), lower=(0.0, 0.0, 0.0),
-                 upper=(1.0, 1.0, 1.0), kappa=None):
+                 upper=(1.0, 1.0, 1.0), kappa=None, algorithm=0):
         d = DgDesc()
         d.grid = grid_desc(cells, lower, upper, periodic)
         d.order = order
@@ -235,6 +237,7 @@ class DGOperator(Operator):
         d.weak_dirichlet = 1 if weak_dirichlet else 0
         self.kappa = kappa  # keep the device array alive
         d.kappa = kappa.ptr if kappa is not None else None
+        d.algorithm = algorithm
         h = C.c_void_p()
         check(lib().gbfem_dg_operator_create(C.byref(d), C.byref(h)))
         self.desc = d

@@ -77,7 +77,17 @@ typedef struct {
   double velocity[3];   /* constant advection b, upwind flux; all zero = no advection */
   int weak_dirichlet;   /* 1 = Nitsche weak u=0 on non-periodic boundary faces, 0 = do-nothing */
   const void* kappa;    /* device DG coefficients of kappa (same layout/precision) or NULL = 1 */
+  int algorithm;        /* GBFEM_ALGO_AUTO or GBFEM_ALGO_QUADRATURE (see below) */
 } gbfem_dg_desc;
+
+/* GBFEM_ALGO_AUTO: with kappa == NULL the apply uses the closed form of the
+ * same integrals (orthonormal basis, affine cells, exact Gauss quadrature:
+ * 1-D stiffness/advection matrices along lines, identity tangential face
+ * mass), which equals the quadrature result up to rounding; otherwise the
+ * sum-factorised quadrature kernel.  GBFEM_ALGO_QUADRATURE always evaluates
+ * at the q^3 volume / q^2 face Gauss points. */
+#define GBFEM_ALGO_AUTO 0
+#define GBFEM_ALGO_QUADRATURE 1
 
 typedef struct gbfem_operator_s* gbfem_operator;
 

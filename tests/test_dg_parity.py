@@ -22,10 +22,13 @@ def _pair(gb, orc, cells, order, q=0, precision=0, kappa=None, **kw):
 
 @pytest.mark.parametrize("order", [1, 2, 3, 4])
 @pytest.mark.parametrize("qoff", [1, 2])
-def test_sipg_apply_fp64(gb, orc, order, qoff):
+@pytest.mark.parametrize("algorithm", [0, 1])
+def test_sipg_apply_fp64(gb, orc, order, qoff, algorithm):
+    """algorithm 0: constant-coefficient closed form; 1: Gauss-point quadrature."""
     cells = (3, 4, 2)
     rng = np.random.default_rng(100 + order)
-    op, prob = _pair(gb, orc, cells, order, q=order + qoff)
+    op = gb.DGOperator(cells, order, quad_points=order + qoff, algorithm=algorithm)
+    prob = orc.DGProblem(cells, order, quad_points=order + qoff)
     u = rng.uniform(-1, 1, prob.ndofs)
     w = gb.DeviceArray(prob.ndofs)
     op(gb.DeviceArray.from_numpy(u), w)
@@ -52,10 +55,12 @@ def test_full_form_fp64(gb, orc, order):
     assert relmax(w.numpy(), prob.apply(u, kappa=kappa)) < TOL64
 
 
-def test_periodic_advection_only(gb, orc):
+@pytest.mark.parametrize("algorithm", [0, 1])
+def test_periodic_advection_only(gb, orc, algorithm):
     cells = (4, 3, 2)
     kw = dict(diffusion=0.0, velocity=(1.0, 0.5, 0.25), periodic=(1, 1, 1), weak_dirichlet=False)
-    op, prob = _pair(gb, orc, cells, 2, **kw)
+    op = gb.DGOperator(cells, 2, algorithm=algorithm, **kw)
+    prob = orc.DGProblem(cells, 2, **kw)
     u = np.random.default_rng(3).uniform(-1, 1, prob.ndofs)
     w = gb.DeviceArray(prob.ndofs)
     op(gb.DeviceArray.from_numpy(u), w)
@@ -63,9 +68,11 @@ def test_periodic_advection_only(gb, orc):
 
 
 @pytest.mark.parametrize("order", [2, 3])
-def test_sipg_apply_fp32(gb, orc, order):
+@pytest.mark.parametrize("algorithm", [0, 1])
+def test_sipg_apply_fp32(gb, orc, order, algorithm):
     cells = (3, 3, 3)
-    op, prob = _pair(gb, orc, cells, order, precision=gb.F32)
+    op = gb.DGOperator(cells, order, precision=gb.F32, algorithm=algorithm)
+    prob = orc.DGProblem(cells, order)
     u = np.random.default_rng(5).uniform(-1, 1, prob.ndofs).astype(np.float32)
     w = gb.DeviceArray(prob.ndofs, gb.F32)
     op(gb.DeviceArray.from_numpy(u), w)
@@ -140,3 +147,18 @@ def test_dot_is_deterministic_fp64_and_fp32(gb):
     fx, fy = gb.DeviceArray.from_numpy(x.astype(np.float32)), gb.DeviceArray.from_numpy(y.astype(np.float32))
     ref = float(x.astype(np.float32).astype(np.float64) @ y.astype(np.float32).astype(np.float64))
     assert abs(gb.dot(fx, fy) - ref) < 1e-9
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_constant_coefficient_form_with_mass_advection_anisotropic(gb, orc, order):
+    """Closed-form (coefficient-space) apply against the quadrature oracle on
+    the full constant-coefficient form."""
+    cells = (3, 2, 4)
+    kw = dict(diffusion=0.7, mass=1.3, velocity=(1.0, -0.5, 0.25), periodic=(0, 1, 0),
+              lower=(0.0, -1.0, 0.5), upper=(1.0, 0.5, 1.5))
+    op = gb.DGOperator(cells, order, **kw)
+    prob = orc.DGProblem(cells, order, **kw)
+    u = np.random.default_rng(17 + order).uniform(-1, 1, prob.ndofs)
+    w = gb.DeviceArray(prob.ndofs)
+    op(gb.DeviceArray.from_numpy(u), w)
+    assert relmax(w.numpy(), prob.apply(u)) < TOL64
