@@ -355,6 +355,20 @@ def workload_q1cg(args):
     xs = np.linspace(0, 1, N + 1)
     X, Y = np.meshgrid(xs, xs)
     err = float(np.max(np.abs(x - (np.sin(np.pi * X) * np.sin(np.pi * Y)).ravel())))
+    # the manufactured rhs is (to 1e-14) an eigenvector of the diagonally
+    # preconditioned operator on this uniform grid, so CG stops after one
+    # iteration (the oracle too); a seeded random interior rhs times the loop
+    br = np.random.default_rng(SEED).uniform(-1, 1, b.size)
+    br.reshape(N + 1, N + 1)[[0, -1], :] = 0.0
+    br.reshape(N + 1, N + 1)[:, [0, -1]] = 0.0
+    brd = gbfem.DeviceArray.from_numpy(br)
+    rt = []
+    for _ in range(args.warmup + args.steps):
+        u.clear()
+        _, tt = _timed(lambda: inv(brd, u))
+        rt.append(tt)
+    it_rand = inv.iterations()
+    t_rand = float(np.median(rt[args.warmup:]))
     dg = oracle.q1_apply((N, N), None, 1.0, 1.0, diag_only=True)
     t0 = time.perf_counter()
     it_ref, x_ref, _ = oracle.cg(lambda v: oracle.q1_apply((N, N), v, 1.0, 1.0), b, prec=lambda r: r / dg,
@@ -363,6 +377,8 @@ def workload_q1cg(args):
     return {"metric": "Q1 64x64 diag-PCG solve time to 1e-10", "value": 1e3 * t, "unit": "ms",
             "higher_is_better": False, "iterations": inv.iterations(), "oracle_iterations": it_ref,
             "max_nodal_error_vs_exact": err, "rel_diff_vs_oracle": float(np.max(np.abs(x - x_ref)) / np.max(np.abs(x_ref))),
+            "random_rhs": {"ms": 1e3 * t_rand, "iterations": it_rand,
+                           "us_per_iteration": 1e6 * t_rand / max(1, it_rand)},
             "e2e": {"value": 1e3 * te, "unit": "ms", "h2d_bytes_per_step": 8 * b.size, "d2h_bytes_per_step": 8 * b.size},
             "cpu_baseline": {"value": 1e3 * t_ref, "unit": "ms", "cores": 1, "kind": "port",
                              "sample": "whole solve: oracle CG (cg.hh restated) + oracle Q1 apply"},
@@ -376,7 +392,23 @@ def workload_rk3(args):
     steps = args.rk_steps
     kw = dict(diffusion=1e-3, velocity=(1.0, 0.5, 0.25), periodic=(1, 1, 1), weak_dirichlet=False)
     bnorm = float(np.sqrt(1 + 0.25 + 0.0625))
-    dt = 0.2 * (1.0 / N) / (bnorm * (2 * p + 1))
+    dt_adv = 0.2 * (1.0 / N) / (bnorm * (2 * p + 1))
+    # The SIPG diffusion (penalty 10 (p+1)^2) bounds the explicit step too:
+    # dt <= 2 / rho(M^{-1} A) keeps dt*lambda inside SSP-RK3's real stability
+    # interval [-2.51, 0].  rho from 30 power iterations on the FP64 operator.
+    opr = gbfem.DGOperator((N, N, N), p, **kw)
+    v = gbfem.DeviceArray.from_numpy(np.random.default_rng(0).uniform(-1, 1, opr.size))
+    av = gbfem.DeviceArray(opr.size)
+    rho = 0.0
+    for _ in range(30):
+        opr(v, av)
+        nrm = np.sqrt(gbfem.dot(av, av))
+        rho = nrm / np.sqrt(gbfem.dot(v, v)) * N ** 3  # M^{-1} = 1/|K| = N^3
+        gbfem.check(gbfem.lib().gbfem_scal(0, av.n, 1.0 / nrm, av.ptr, None))
+        v, av = av, v
+    dt_stab = 2.0 / rho
+    dt = min(dt_adv, dt_stab)
+    del opr, v, av
     res = {}
     for prec, name in ((gbfem.F64, "f64"), (gbfem.F32, "f32")):
         op = gbfem.DGOperator((N, N, N), p, precision=prec, **kw)
@@ -390,7 +422,9 @@ def workload_rk3(args):
     ndofs = N ** 3 * (p + 1) ** 3
     err = float(np.max(np.abs(res["f32"][1] - res["f64"][1])) / np.max(np.abs(res["f64"][1])))
     return {"metric": "SSP-RK3 128^3 Q2 advection-diffusion, time per step", "value": 1e3 * res["f64"][0] / steps,
-            "unit": "ms/step", "higher_is_better": False, "steps": steps, "dt": dt,
+            "unit": "ms/step", "higher_is_better": False, "steps": steps, "dt": dt, "dt_advective_cfl_0.2": dt_adv,
+            "dt_stability": dt_stab, "spectral_radius_minv_a": rho,
+            "f64_max_abs": float(np.max(np.abs(res["f64"][1]))),
             "f32_ms_per_step": 1e3 * res["f32"][0] / steps,
             "f64_dof_stage_per_s": 3 * ndofs * steps / res["f64"][0],
             "f32_dof_stage_per_s": 3 * ndofs * steps / res["f32"][0],

@@ -32,17 +32,17 @@ struct DgConstTablesT {
   T D1[kDgMaxN * kDgMaxN];  // D1[i*n+j] = int L_i' L_j
   T tr[2 * kDgMaxN];        // L_i(s)
   T dtr[2 * kDgMaxN];       // L_i'(s)
+  T M[3][kDgMaxN * kDgMaxN];  // per-axis line operator (filled per operator)
 };
 
 template <typename T, int N, int CPB>
 __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, const DgConstTablesT<T> tabs) {
   constexpr int N2 = N * N, N3 = N * N * N;
-  __shared__ T sK1[N * N], sD1[N * N], str[2 * N], sdtr[2 * N];
+  __shared__ T str[2 * N], sdtr[2 * N];
   __shared__ T su[CPB * N3];
   __shared__ T sr[CPB * N3];
   __shared__ T sF[CPB * 6 * 2 * N2];  // [cell][face][Val/Grad][jk]
   const int tid = threadIdx.x;
-  for (int i = tid; i < N * N; i += blockDim.x) { sK1[i] = tabs.K1[i]; sD1[i] = tabs.D1[i]; }
   for (int i = tid; i < 2 * N; i += blockDim.x) { str[i] = tabs.tr[i]; sdtr[i] = tabs.dtr[i]; }
   const long long ncells = args.ncells;
   const long long c0 = (long long)blockIdx.x * CPB;
@@ -118,46 +118,39 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
     sF[(c * 6 + f) * 2 * N2 + N2 + jk] = grad;
   }
   __syncthreads();
-  // ---- volume (1-D stiffness / advection along each axis) + face expansion -
-  for (int item = tid; item < CPB * N3; item += blockDim.x) {
-    const int c = item / N3, l = item - c * N3;
-    const int i0 = l / N2, i1 = (l / N) % N, i2 = l % N;
-    const T* uc = su + c * N3;
-    T acc = args.mass * args.detK * uc[l];
-    const int idx[3] = {i0, i1, i2};
-    const int strides[3] = {N2, N, 1};
+  // ---- volume + face expansion, one line along axis d per item ---------------
+  // M_d = eps|K|/h_d^2 K1 - b_d |K|/h_d D1 (+ c|K| I for d = 0) is the same for
+  // every line: a warp-uniform operand from the kernel parameters.
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const int b0 = l - idx[d] * strides[d];
-      T ks = T(0), ds = T(0);
+  for (int d = 0; d < 3; ++d) {
+    const int stride = d == 0 ? N2 : (d == 1 ? N : 1);
+    const T sgnh = args.invh[d];
+    for (int item = tid; item < CPB * N2; item += blockDim.x) {
+      const int c = item / N2, jk = item - c * N2;
+      const int j = jk / N, k = jk % N;
+      const int base = d == 0 ? j * N + k : (d == 1 ? j * N2 + k : j * N2 + k * N);
+      const T* uc = su + c * N3 + base;
+      T x[N];
 #pragma unroll
-      for (int jj = 0; jj < N; ++jj) {
-        const T x = uc[b0 + jj * strides[d]];
-        ks = fma(sK1[idx[d] * N + jj], x, ks);
-        if (args.advect) ds = fma(sD1[idx[d] * N + jj], x, ds);
-      }
-      const T ih = args.invh[d];
-      acc = fma(args.eps * args.detK * ih * ih, ks, acc);
-      if (args.advect) acc = fma(-args.b[d] * args.detK * ih, ds, acc);
-    }
-    // faces in fixed order d = 0..2, s = 0..1
+      for (int i = 0; i < N; ++i) x[i] = uc[i * stride];
+      const T* fv0 = sF + (c * 6 + 2 * d) * 2 * N2;
+      const T* fv1 = fv0 + 2 * N2;
+      const T v0 = fv0[jk], g0 = fv0[N2 + jk], v1 = fv1[jk], g1 = fv1[N2 + jk];
+      T* rc = sr + c * N3 + base;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      int i, jk;
-      if (d == 0) { i = i0; jk = i1 * N + i2; }
-      else if (d == 1) { i = i1; jk = i0 * N + i2; }
-      else { i = i2; jk = i0 * N + i1; }
+      for (int i = 0; i < N; ++i) {
+        T acc = d == 0 ? T(0) : rc[i * stride];
 #pragma unroll
-      for (int s = 0; s < 2; ++s) {
-        const T* fv = sF + (c * 6 + 2 * d + s) * 2 * N2;
-        const T sgn = s ? T(1) : T(-1);
-        acc = fma(str[s * N + i], fv[jk], acc);
-        acc = fma(sgn * args.invh[d] * sdtr[s * N + i], fv[N2 + jk], acc);
+        for (int jj = 0; jj < N; ++jj) acc = fma(tabs.M[d][i * N + jj], x[jj], acc);
+        acc = fma(str[i], v0, acc);                       // side s = 0 (L_i(0))
+        acc = fma(-sgnh * sdtr[i], g0, acc);
+        acc = fma(str[N + i], v1, acc);                   // side s = 1 (L_i(1))
+        acc = fma(sgnh * sdtr[N + i], g1, acc);
+        rc[i * stride] = acc;
       }
     }
-    sr[item] = acc;
+    __syncthreads();
   }
-  __syncthreads();
   for (int e = tid; e < CPB * N3; e += blockDim.x) {
     const long long v = c0 + e / N3;
     if (v < ncells) __stcs(args.w + c0 * N3 + e, sr[e]);

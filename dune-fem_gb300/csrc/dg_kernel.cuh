@@ -64,43 +64,54 @@ struct DgArgsT {
   T b[3];             // advection velocity
   int advect;         // b != 0
   int weak_dirichlet; // Nitsche u = 0 on non-periodic boundary faces
-  int unit_mode;      // 1: block-diagonal assembly (own dofs = e_j, neighbour u = 0); 2: diagonal only
+  int unit_mode;      // 1: block-diagonal assembly (own dofs = e_j, neighbour u = 0); 2: diagonal only;
+                      // 3: neighbour couplings (own u = 0, the neighbour through face f holds e_j)
   T* blocks;          // unit_mode 1 output blocks[cell - cell_begin][i][j]; unit_mode 2 output diag[cell][j]
   long long cell_begin;  // unit_mode 1: first cell of the batch
   long long cell_count;  // unit_mode 1: cells in the batch (0 = all)
 };
 
-// out = contraction of `in` along axis AX with matrix M.
-// in  : NCELL arrays of dims [I0][I1][I2] (row-major), cell stride `ics`.
-// out : NCELL arrays of the same dims except OUT on axis AX, cell stride `ocs`.
-// !TR : out[..o..] = sum_i M[o*LDM + i] * in[..i..]
-//  TR : out[..o..] = sum_i M[i*LDM + o] * in[..i..]
-// ACC adds to the existing content of out.
+// Contraction of NCELL arrays `in` (dims [I0][I1][I2], row-major, cell
+// stride ics) along axis AX with the matrix M into `out` (same dims except
+// OUT on axis AX, cell stride ocs):
+//   !TR: out[..o..] = sum_i M[o*LDM + i] in[..i..];  TR: M[i*LDM + o];
+//   ACC adds to the existing content of out.
+// One thread owns a whole line along axis AX, keeps its
+// IN inputs in registers and writes all OUT outputs.  M is warp-uniform (the
+// same entry for every thread at each unrolled step), read from the kernel's
+// parameter space, so a contraction costs IN + OUT shared-memory accesses per
+// IN*OUT FMAs instead of two per FMA.  Same fixed summation order per output
+// as `contract`.
 template <typename T, int AX, int I0, int I1, int I2, int OUT, int LDM, bool TR, bool ACC, int NCELL>
-__device__ __forceinline__ void contract(const T* __restrict__ in, int ics, T* __restrict__ out, int ocs,
-                                         const T* __restrict__ M) {
+__device__ __forceinline__ void contract_lines(const T* __restrict__ in, int ics, T* __restrict__ out, int ocs,
+                                               const T* __restrict__ M) {
   constexpr int IN = AX == 0 ? I0 : (AX == 1 ? I1 : I2);
   constexpr int O0 = AX == 0 ? OUT : I0;
   constexpr int O1 = AX == 1 ? OUT : I1;
   constexpr int O2 = AX == 2 ? OUT : I2;
-  constexpr int OSZ = O0 * O1 * O2;
-  constexpr int IS0 = I1 * I2, IS1 = I2;
-  constexpr int ISA = AX == 0 ? IS0 : (AX == 1 ? IS1 : 1);
-  for (int item = threadIdx.x; item < NCELL * OSZ; item += blockDim.x) {
-    const int cell = item / OSZ;
-    const int r = item - cell * OSZ;
-    const int x0 = r / (O1 * O2);
-    const int x1 = (r / O2) % O1;
-    const int x2 = r % O2;
-    const int o = AX == 0 ? x0 : (AX == 1 ? x1 : x2);
-    const int ib = cell * ics + (AX == 0 ? 0 : x0 * IS0) + (AX == 1 ? 0 : x1 * IS1) + (AX == 2 ? 0 : x2);
-    T acc = ACC ? out[cell * ocs + r] : T(0);
+  // the two axes that are not contracted, in order
+  constexpr int PA = AX == 0 ? 1 : 0, PB = AX == 2 ? 1 : 2;
+  constexpr int DI[3] = {I0, I1, I2};
+  constexpr int SI[3] = {I1 * I2, I2, 1};
+  constexpr int SO[3] = {O1 * O2, O2, 1};
+  constexpr int NA = DI[PA], NB = DI[PB];
+  constexpr int LINES = NA * NB;
+  for (int item = threadIdx.x; item < NCELL * LINES; item += blockDim.x) {
+    const int cell = item / LINES;
+    const int ln = item - cell * LINES;
+    const int xa = ln / NB, xb = ln - xa * NB;
+    const T* src = in + cell * ics + xa * SI[PA] + xb * SI[PB];
+    T* dst = out + cell * ocs + xa * SO[PA] + xb * SO[PB];
+    T x[IN];
 #pragma unroll
-    for (int i = 0; i < IN; ++i) {
-      const T m = TR ? M[i * LDM + o] : M[o * LDM + i];
-      acc = fma(m, in[ib + i * ISA], acc);
+    for (int i = 0; i < IN; ++i) x[i] = src[i * SI[AX]];
+#pragma unroll
+    for (int o = 0; o < OUT; ++o) {
+      T acc = ACC ? dst[o * SO[AX]] : T(0);
+#pragma unroll
+      for (int i = 0; i < IN; ++i) acc = fma(TR ? M[i * LDM + o] : M[o * LDM + i], x[i], acc);
+      dst[o * SO[AX]] = acc;
     }
-    out[cell * ocs + r] = acc;
   }
 }
 
@@ -118,7 +129,8 @@ struct DgSmem {
 };
 
 template <typename T, int N, int Q, bool KAPPA, int CPB>
-__global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args, const DgTablesT<T> tabs) {
+__global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args,
+                                                       const __grid_constant__ DgTablesT<T> tabs) {
   using S = DgSmem<N, Q, KAPPA, CPB>;
   constexpr int N3 = S::N3, Q3 = S::Q3, N2 = S::N2, Q2 = S::Q2, MA = S::MA;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -145,8 +157,10 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args, co
   // In unit mode the "virtual cells" are (cell, j) pairs: vcell = cell*N3 + j,
   // for cells in [cell_begin, cell_begin + cell_count).
   const long long ucount = args.cell_count > 0 ? args.cell_count : ncells;
-  const long long nvirt = args.unit_mode ? (args.cell_begin + ucount) * N3 : ncells;
-  const long long v0 = (long long)blockIdx.x * CPB + (args.unit_mode ? args.cell_begin * N3 : 0);
+  // unit mode 3: virtual cells (cell, f, j) = (cell*6 + f)*N3 + j
+  const int vper = args.unit_mode == 3 ? 6 * N3 : N3;
+  const long long nvirt = args.unit_mode ? (args.cell_begin + ucount) * vper : ncells;
+  const long long v0 = (long long)blockIdx.x * CPB + (args.unit_mode ? args.cell_begin * vper : 0);
   if (v0 >= nvirt) return;
 
   // ---- load own dofs (and kappa) ------------------------------------------
@@ -156,8 +170,8 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args, co
     T val = T(0), kv = T(0);
     if (v < nvirt) {
       if (args.unit_mode) {
-        const long long cell = v / N3;
-        val = (i == int(v - cell * N3)) ? T(1) : T(0);
+        const long long cell = v / vper;
+        val = (args.unit_mode != 3 && i == int(v - cell * N3)) ? T(1) : T(0);
         if (KAPPA) kv = __ldg(args.kappa + cell * N3 + i);
       } else {
         val = __ldg(args.u + v * N3 + i);
@@ -179,39 +193,36 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args, co
     T* G2 = G1 + Q3;
     T* Kq = G2 + Q3;              // [Q3] (KAPPA)
     if (KAPPA) {
-      contract<T, 0, N, N, N, Q, N, false, false, CPB>(sk, N3, t1, WS, sB);
+      contract_lines<T, 0, N, N, N, Q, N, false, false, CPB>(sk, N3, t1, WS, tabs.B);
       __syncthreads();
-      contract<T, 1, Q, N, N, Q, N, false, false, CPB>(t1, WS, t2, WS, sB);
+      contract_lines<T, 1, Q, N, N, Q, N, false, false, CPB>(t1, WS, t2, WS, tabs.B);
       __syncthreads();
-      contract<T, 2, Q, Q, N, Q, N, false, false, CPB>(t2, WS, Kq, WS, sB);
+      contract_lines<T, 2, Q, Q, N, Q, N, false, false, CPB>(t2, WS, Kq, WS, tabs.B);
       __syncthreads();
     }
-    contract<T, 0, N, N, N, Q, N, false, false, CPB>(su, N3, t1, WS, sB);
+    contract_lines<T, 0, N, N, N, Q, N, false, false, CPB>(su, N3, t1, WS, tabs.B);
     __syncthreads();
-    contract<T, 1, Q, N, N, Q, N, false, false, CPB>(t1, WS, t2, WS, sB);
+    contract_lines<T, 1, Q, N, N, Q, N, false, false, CPB>(t1, WS, t2, WS, tabs.B);
     __syncthreads();
-    contract<T, 2, Q, Q, N, Q, N, false, false, CPB>(t2, WS, U, WS, sB);
+    contract_lines<T, 2, Q, Q, N, Q, N, false, false, CPB>(t2, WS, U, WS, tabs.B);
     __syncthreads();
-    // gradients in reference coordinates + pointwise flux
+    // gradients in reference coordinates: collocation derivative along each axis
+    contract_lines<T, 0, Q, Q, Q, Q, Q, false, false, CPB>(U, WS, G0, WS, tabs.Dc);
+    contract_lines<T, 1, Q, Q, Q, Q, Q, false, false, CPB>(U, WS, G1, WS, tabs.Dc);
+    contract_lines<T, 2, Q, Q, Q, Q, Q, false, false, CPB>(U, WS, G2, WS, tabs.Dc);
+    __syncthreads();
+    // pointwise flux (in place: item r reads and writes only point r)
     for (int item = tid; item < CPB * Q3; item += blockDim.x) {
       const int c = item / Q3, r = item - c * Q3;
       const int a = r / Q2, b = (r / Q) % Q, cc = r % Q;
-      const T* Uc = U + c * WS;
-      T g0 = T(0), g1 = T(0), g2 = T(0);
-#pragma unroll
-      for (int o = 0; o < Q; ++o) {
-        g0 = fma(sDc[a * Q + o], Uc[o * Q2 + b * Q + cc], g0);
-        g1 = fma(sDc[b * Q + o], Uc[a * Q2 + o * Q + cc], g1);
-        g2 = fma(sDc[cc * Q + o], Uc[a * Q2 + b * Q + o], g2);
-      }
-      const T uq = Uc[r];
+      const T uq = U[c * WS + r];
       const T kq = KAPPA ? Kq[c * WS + r] : T(1);
       const T W = sw[a] * sw[b] * sw[cc] * args.detK;
       const T ek = args.eps * kq;
       // flux F = eps*kappa*grad u - b*u (physical), tested with grad phi = invh * ref-grad
-      T f0 = ek * g0 * args.invh[0];
-      T f1 = ek * g1 * args.invh[1];
-      T f2 = ek * g2 * args.invh[2];
+      T f0 = ek * G0[c * WS + r] * args.invh[0];
+      T f1 = ek * G1[c * WS + r] * args.invh[1];
+      T f2 = ek * G2[c * WS + r] * args.invh[2];
       if (args.advect) {
         f0 -= args.b[0] * uq;
         f1 -= args.b[1] * uq;
@@ -220,31 +231,21 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args, co
       G0[c * WS + r] = W * f0 * args.invh[0];
       G1[c * WS + r] = W * f1 * args.invh[1];
       G2[c * WS + r] = W * f2 * args.invh[2];
+      U[c * WS + r] = W * args.mass * uq;
     }
     __syncthreads();
-    // V = W*c*u + Dc^T-contractions of the fluxes (in place into U: item r only reads U[r])
-    for (int item = tid; item < CPB * Q3; item += blockDim.x) {
-      const int c = item / Q3, r = item - c * Q3;
-      const int a = r / Q2, b = (r / Q) % Q, cc = r % Q;
-      const T W = sw[a] * sw[b] * sw[cc] * args.detK;
-      T v = W * args.mass * U[c * WS + r];
-      const T* g0 = G0 + c * WS;
-      const T* g1 = G1 + c * WS;
-      const T* g2 = G2 + c * WS;
-#pragma unroll
-      for (int o = 0; o < Q; ++o) {
-        v = fma(sDc[o * Q + a], g0[o * Q2 + b * Q + cc], v);
-        v = fma(sDc[o * Q + b], g1[a * Q2 + o * Q + cc], v);
-        v = fma(sDc[o * Q + cc], g2[a * Q2 + b * Q + o], v);
-      }
-      U[c * WS + r] = v;
-    }
+    // V = W c u + Dc^T contractions of the fluxes, accumulated axis by axis
+    contract_lines<T, 0, Q, Q, Q, Q, Q, true, true, CPB>(G0, WS, U, WS, tabs.Dc);
     __syncthreads();
-    contract<T, 2, Q, Q, Q, N, N, true, false, CPB>(U, WS, t2, WS, sB);
+    contract_lines<T, 1, Q, Q, Q, Q, Q, true, true, CPB>(G1, WS, U, WS, tabs.Dc);
     __syncthreads();
-    contract<T, 1, Q, Q, N, N, N, true, false, CPB>(t2, WS, t1, WS, sB);
+    contract_lines<T, 2, Q, Q, Q, Q, Q, true, true, CPB>(G2, WS, U, WS, tabs.Dc);
     __syncthreads();
-    contract<T, 0, Q, N, N, N, N, true, false, CPB>(t1, WS, sr, N3, sB);
+    contract_lines<T, 2, Q, Q, Q, N, N, true, false, CPB>(U, WS, t2, WS, tabs.B);
+    __syncthreads();
+    contract_lines<T, 1, Q, Q, N, N, N, true, false, CPB>(t2, WS, t1, WS, tabs.B);
+    __syncthreads();
+    contract_lines<T, 0, Q, N, N, N, N, true, false, CPB>(t1, WS, sr, N3, tabs.B);
     __syncthreads();
   }
 
@@ -265,9 +266,12 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args, co
       const int j = jk / N, k = jk % N;
       const T sgn = s ? T(1) : T(-1);
       const long long v = v0 + c;
-      long long cell = args.unit_mode ? v / N3 : v;
+      long long cell = args.unit_mode ? v / vper : v;
       bool valid = v < nvirt;
       if (!valid) cell = 0;
+      // unit mode 3: the face whose neighbour carries e_j, and j
+      const int uf = args.unit_mode == 3 && valid ? int((v - cell * vper) / N3) : -1;
+      const int uj = args.unit_mode == 3 && valid ? int(v - cell * vper - uf * N3) : -1;
       long long cz = cell / ((long long)args.nc[0] * args.nc[1]);
       long long rem = cell - cz * (long long)args.nc[0] * args.nc[1];
       long long cy = rem / args.nc[0];
@@ -300,7 +304,8 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args, co
         const int so = 1 - s;
 #pragma unroll
         for (int i = 0; i < N; ++i) {
-          const T x = args.unit_mode ? T(0) : __ldg(args.u + ncell * N3 + base + i * stride);
+          const T x = args.unit_mode == 3 ? ((uf == 2 * d + s && base + i * stride == uj) ? T(1) : T(0))
+                      : args.unit_mode ? T(0) : __ldg(args.u + ncell * N3 + base + i * stride);
           vp = fma(str[so * N + i], x, vp);
           np = fma(sdtr[so * N + i], x, np);
           if (KAPPA) kp = fma(str[so * N + i], __ldg(args.kappa + ncell * N3 + base + i * stride), kp);
@@ -318,9 +323,9 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args, co
     }
     __syncthreads();
     // F2/F3: 2-D interpolation of all face arrays to the q x q face points
-    contract<T, 1, 2 * MA, N, N, Q, N, false, false, CPB>(FC, WS, FT, WS, sB);
+    contract_lines<T, 1, 2 * MA, N, N, Q, N, false, false, CPB>(FC, WS, FT, WS, tabs.B);
     __syncthreads();
-    contract<T, 2, 2 * MA, Q, N, Q, N, false, false, CPB>(FT, WS, FQ, WS, sB);
+    contract_lines<T, 2, 2 * MA, Q, N, Q, N, false, false, CPB>(FT, WS, FQ, WS, tabs.B);
     __syncthreads();
     // F4: pointwise numerical fluxes
     for (int item = tid; item < CPB * 2 * Q2; item += blockDim.x) {
@@ -330,7 +335,7 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args, co
       const int ab = r - s * Q2;
       const int a = ab / Q, b = ab % Q;
       const long long v = v0 + c;
-      long long cell = args.unit_mode ? v / N3 : v;
+      long long cell = args.unit_mode ? v / vper : v;
       if (v >= nvirt) cell = 0;
       long long cz = cell / ((long long)args.nc[0] * args.nc[1]);
       long long rem = cell - cz * (long long)args.nc[0] * args.nc[1];
@@ -366,9 +371,9 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args, co
     }
     __syncthreads();
     // F5/F6: transposed 2-D contraction back to the n x n tangential coefficients
-    contract<T, 2, 4, Q, Q, N, N, true, false, CPB>(FV, WS, FT, WS, sB);
+    contract_lines<T, 2, 4, Q, Q, N, N, true, false, CPB>(FV, WS, FT, WS, tabs.B);
     __syncthreads();
-    contract<T, 1, 4, Q, N, N, N, true, false, CPB>(FT, WS, FC, WS, sB);
+    contract_lines<T, 1, 4, Q, N, N, N, true, false, CPB>(FT, WS, FC, WS, tabs.B);
     __syncthreads();
     // F7: expand into the cell's test functions, both sides in fixed order
     for (int item = tid; item < CPB * N3; item += blockDim.x) {
@@ -396,7 +401,13 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args, co
     const int c = e / N3, i = e - c * N3;
     const long long v = v0 + c;
     if (v >= nvirt) continue;
-    if (args.unit_mode) {
+    if (args.unit_mode == 3) {
+      // neighbour couplings: blocks[cell - cell_begin][1 + f][i][j]
+      const long long cell = v / vper;
+      const int f = int((v - cell * vper) / N3);
+      const int j = int(v - cell * vper - f * N3);
+      args.blocks[(((cell - args.cell_begin) * 7 + 1 + f) * N3 + i) * N3 + j] = sr[e];
+    } else if (args.unit_mode) {
       const long long cell = v / N3;
       const int j = int(v - cell * N3);
       if (args.unit_mode == 1) args.blocks[((cell - args.cell_begin) * N3 + i) * N3 + j] = sr[e];

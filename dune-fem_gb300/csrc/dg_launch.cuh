@@ -19,7 +19,7 @@ int dg_launch_one(const DgArgsT<T>& args, const DgTablesT<T>& tabs, cudaStream_t
   GBFEM_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   constexpr int N3 = N * N * N;
   const long long ucount = args.cell_count > 0 ? args.cell_count : args.ncells;
-  const long long nvirt = args.unit_mode ? ucount * N3 : args.ncells;
+  const long long nvirt = args.unit_mode ? ucount * (args.unit_mode == 3 ? 6 * N3 : N3) : args.ncells;
   const long long blocks = (nvirt + CPB - 1) / CPB;
   if (blocks <= 0) return GBFEM_OK;
   if (blocks > 2147483647LL) return set_error(GBFEM_ERR_INVALID, "dg apply: grid too large");

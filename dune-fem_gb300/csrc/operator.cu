@@ -76,6 +76,26 @@ static void fill_dg_args(const gbfem_operator_s* op, DgArgsT<T>* a) {
   a->kappa = static_cast<const T*>(d.kappa);
 }
 
+// M_d = eps |K|/h_d^2 K1 - b_d |K|/h_d D1 (+ c |K| I on axis 0), rounded once.
+template <typename T>
+static void fill_line_operators(const gbfem_operator_s* op, DgConstTablesT<T>* ct) {
+  const gbfem_dg_desc& d = op->dg;
+  double h[3], vol = 1.0;
+  for (int k = 0; k < 3; ++k) {
+    h[k] = (d.grid.upper[k] - d.grid.lower[k]) / d.grid.cells[k];
+    vol *= h[k];
+  }
+  const int n = op->n;
+  for (int ax = 0; ax < 3; ++ax)
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        double m = d.diffusion * vol / (h[ax] * h[ax]) * op->cK1[i * n + j] -
+                   d.velocity[ax] * vol / h[ax] * op->cD1[i * n + j];
+        if (ax == 0 && i == j) m += d.mass * vol;
+        ct->M[ax][i * n + j] = T(m);
+      }
+}
+
 int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
              void* blocks, long long cell_begin, long long cell_count) {
   if (op->precision == GBFEM_F64) {
@@ -87,7 +107,11 @@ int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s,
     a.w = static_cast<double*>(w);
     a.unit_mode = unit_mode;
     a.blocks = static_cast<double*>(blocks);
-    if (unit_mode == 0 && op->coefficient_space) return dg_const_launch_f64(a, op->ctab64, op->n, s);
+    if (unit_mode == 0 && op->coefficient_space) {
+      DgConstTablesT<double> ct = op->ctab64;
+      fill_line_operators(op, &ct);
+      return dg_const_launch_f64(a, ct, op->n, s);
+    }
     return dg_launch_f64(a, op->tab64, op->n, op->q, op->dg.kappa != nullptr, s);
   } else {
     DgArgsT<float> a;
@@ -98,7 +122,11 @@ int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s,
     a.w = static_cast<float*>(w);
     a.unit_mode = unit_mode;
     a.blocks = static_cast<float*>(blocks);
-    if (unit_mode == 0 && op->coefficient_space) return dg_const_launch_f32(a, op->ctab32, op->n, s);
+    if (unit_mode == 0 && op->coefficient_space) {
+      DgConstTablesT<float> ct = op->ctab32;
+      fill_line_operators(op, &ct);
+      return dg_const_launch_f32(a, ct, op->n, s);
+    }
     return dg_launch_f32(a, op->tab32, op->n, op->q, op->dg.kappa != nullptr, s);
   }
 }
@@ -238,6 +266,11 @@ int gbfem_dg_operator_create(const gbfem_dg_desc* desc, gbfem_operator* out) {
   ConstTables1D ct = make_const_tables(op->n);
   fill_const_tables(t, ct, &op->ctab64);
   fill_const_tables(t, ct, &op->ctab32);
+  for (int i = 0; i < op->n; ++i)
+    for (int j = 0; j < op->n; ++j) {
+      op->cK1[i * op->n + j] = double(ct.K1[i][j]);
+      op->cD1[i * op->n + j] = double(ct.D1[i][j]);
+    }
   // q >= p+1 always holds here, so the quadrature is exact for constant kappa
   op->coefficient_space = desc->kappa == nullptr && desc->algorithm == GBFEM_ALGO_AUTO;
   *out = op;
@@ -272,6 +305,8 @@ int gbfem_operator_destroy(gbfem_operator op) {
   if (!op) return GBFEM_OK;
   if (op->host_u) cudaFree(op->host_u);
   if (op->host_w) cudaFree(op->host_w);
+  if (op->bsr_blocks) cudaFree(op->bsr_blocks);
+  if (op->bsr_col) cudaFree(op->bsr_col);
   delete op;
   return GBFEM_OK;
 }
@@ -293,6 +328,7 @@ int gbfem_operator_apply(gbfem_operator op, const void* u, void* w, void* stream
   if (u == w) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_apply: u and w must not alias");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (op->kind == OpKind::DG) return dg_apply(op, u, w, s, 0, nullptr);
+  if (op->kind == OpKind::BSR) return bsr_apply(op, u, w, s, 0);
   return q1_apply(op, u, w, s, 0);
 }
 
@@ -312,6 +348,12 @@ int gbfem_operator_apply_host(gbfem_operator op, const void* u_host, void* w_hos
 
 int gbfem_operator_block_diagonal(gbfem_operator op, void* blocks, void* stream) {
   if (!op || !blocks) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_block_diagonal: null argument");
+  if (op->kind == OpKind::BSR) {
+    const size_t bsz = size_t(op->nloc) * op->nloc * (op->precision == GBFEM_F64 ? 8 : 4);
+    GBFEM_CUDA_TRY(cudaMemcpy2DAsync(blocks, bsz, op->bsr_blocks, 7 * bsz, bsz, size_t(op->ncells),
+                                     cudaMemcpyDeviceToDevice, static_cast<cudaStream_t>(stream)));
+    return GBFEM_OK;
+  }
   if (op->kind != OpKind::DG)
     return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "block diagonal is defined for DG operators only");
   return dg_apply(op, nullptr, nullptr, static_cast<cudaStream_t>(stream), 1, blocks);
@@ -323,5 +365,6 @@ extern "C" int gbfem_operator_diagonal(gbfem_operator op, void* diag, void* stre
   if (!op || !diag) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_diagonal: null argument");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (op->kind == OpKind::DG) return dg_apply(op, nullptr, nullptr, s, 2, diag);
+  if (op->kind == OpKind::BSR) return bsr_apply(op, nullptr, diag, s, 1);
   return q1_apply(op, nullptr, diag, s, 1);
 }

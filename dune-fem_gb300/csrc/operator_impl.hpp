@@ -8,7 +8,7 @@
 
 namespace gbfem {
 
-enum class OpKind { DG = 1, Q1 = 2 };
+enum class OpKind { DG = 1, Q1 = 2, BSR = 3 };
 
 // Element matrix of the continuous Q1 operator; local vertex k = kx + 2*ky.
 struct Q1Element {
@@ -20,6 +20,8 @@ struct Q1Element {
 int dg_apply(const struct ::gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
              void* blocks, long long cell_begin = 0, long long cell_count = 0);
 int q1_apply(const struct ::gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int diag_only);
+// assembled operator: y = A x (diag_only: the diagonal into y)
+int bsr_apply(const struct ::gbfem_operator_s* op, const void* x, void* y, cudaStream_t s, int diag_only);
 
 }  // namespace gbfem
 
@@ -35,7 +37,11 @@ struct gbfem_operator_s {
   gbfem::DgConstTablesT<double> ctab64{};
   gbfem::DgConstTablesT<float> ctab32{};
   bool coefficient_space = false;  // constant-coefficient closed form (exact quadrature)
+  double cK1[gbfem::kDgMaxN * gbfem::kDgMaxN] = {};  // 1-D stiffness int L_i' L_j'
+  double cD1[gbfem::kDgMaxN * gbfem::kDgMaxN] = {};  // 1-D advection int L_i' L_j
   gbfem::Q1Element q1{};
+  void* bsr_blocks = nullptr;   // assembled: [cell][7][nloc][nloc]
+  long long* bsr_col = nullptr; // assembled: [cell][7] column cell (-1 = none)
   void* host_u = nullptr;  // device staging of gbfem_operator_apply_host
   void* host_w = nullptr;
 };

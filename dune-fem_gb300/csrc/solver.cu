@@ -653,7 +653,8 @@ int gbfem_preconditioner_diagonal_create(gbfem_operator op, gbfem_preconditioner
 int gbfem_preconditioner_block_jacobi_create(gbfem_operator op, int precision, gbfem_preconditioner* out) {
   if (!op || !out) return set_error(GBFEM_ERR_INVALID, "gbfem_preconditioner_block_jacobi_create: null argument");
   *out = nullptr;
-  if (op->kind != OpKind::DG) return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "block Jacobi needs a DG operator");
+  if (op->kind != OpKind::DG && op->kind != OpKind::BSR)
+    return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "block Jacobi needs a DG operator");
   if (precision != GBFEM_F64 && precision != GBFEM_F32) return set_error(GBFEM_ERR_INVALID, "bad precision");
   auto* pc = new (std::nothrow) gbfem_preconditioner_s();
   if (!pc) return set_error(GBFEM_ERR_INVALID, "out of host memory");
@@ -684,7 +685,14 @@ int gbfem_preconditioner_block_jacobi_create(gbfem_operator op, int precision, g
   const size_t sm = size_t(nb) * nb * 8 + size_t(nb) * 4;
   for (long long c0 = 0; c0 < op->ncells && rc == GBFEM_OK; c0 += batch) {
     const long long cnt = (c0 + batch <= op->ncells) ? batch : op->ncells - c0;
-    rc = dg_apply(op, nullptr, nullptr, nullptr, 1, tmp, c0, cnt);
+    if (op->kind == OpKind::BSR) {
+      const size_t bsz = size_t(nb) * nb * osz;
+      e = cudaMemcpy2D(tmp, bsz, static_cast<char*>(op->bsr_blocks) + size_t(c0) * 7 * bsz, 7 * bsz, bsz,
+                       size_t(cnt), cudaMemcpyDeviceToDevice);
+      if (e != cudaSuccess) { rc = set_cuda_error(e, "block Jacobi from assembled operator"); break; }
+    } else {
+      rc = dg_apply(op, nullptr, nullptr, nullptr, 1, tmp, c0, cnt);
+    }
     if (rc) break;
     if (op->precision == GBFEM_F64 && precision == GBFEM_F64) {
       cudaFuncSetAttribute(k_block_invert<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));

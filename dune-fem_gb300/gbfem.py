@@ -88,6 +88,7 @@ def lib():
         L.gbfem_q1_operator_create.argtypes = [C.POINTER(GridDesc), C.c_int, C.c_double, C.c_double,
                                                C.POINTER(C.c_void_p)]
         L.gbfem_measure_fma_peaks.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.gbfem_operator_assemble.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
         L.gbfem_fourier_modes.argtypes = [C.c_uint64, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double)]
         L.gbfem_dg_project.argtypes = [C.POINTER(GridDesc), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
                                        C.POINTER(C.c_double), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
@@ -203,6 +204,14 @@ class Operator:
         d = DeviceArray(self.size, self.precision)
         check(lib().gbfem_operator_diagonal(self.handle, d.ptr, None))
         return d
+
+    def assemble(self):
+        """The assembled (block-sparse) copy of this operator, as an Operator."""
+        h = C.c_void_p()
+        check(lib().gbfem_operator_assemble(self.handle, C.byref(h)))
+        a = Operator(h, self.precision)
+        a.nloc = getattr(self, "nloc", None)
+        return a
 
     def block_diagonal(self, nloc):
         b = DeviceArray(self.size * nloc, self.precision)

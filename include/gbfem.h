@@ -125,6 +125,15 @@ int gbfem_operator_diagonal(gbfem_operator op, void* diag, void* stream);
  * (operator/linear/blockdiagonal.hh:24-135). */
 int gbfem_operator_block_diagonal(gbfem_operator op, void* blocks, void* stream);
 
+/* Assembled copy of a DG operator: the full Jacobian in block-sparse-row form
+ * (per cell 7 dense nloc x nloc blocks: itself and the six face neighbours),
+ * returned as another gbfem_operator whose apply is the block SpMV.
+ * ≙ DifferentiableGalerkinOperator::jacobian/assemble into a
+ * SparseRowLinearOperator (schemes/galerkin.hh:1548-1643, 1195-1314;
+ * operator/linear/spoperator.hh:17-55, operator/matrix/spmatrix.hh:148-180).
+ * Memory: ncells * 7 * nloc^2 values. */
+int gbfem_operator_assemble(gbfem_operator op, gbfem_operator* assembled);
+
 /* ---- preconditioners ------------------------------------------------------
  * A preconditioner is any map z = P(r) on dof vectors (the reference takes
  * any Operator<D,D>, solver/krylovinverseoperators.hh:36).

@@ -149,3 +149,25 @@ def test_nan_input_reports_nonfinite(gb, orc):
     f[7] = np.nan
     info, _ = _solve(gb, op, f, "cg", max_iterations=50)
     assert not info["converged"]
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(velocity=(0.4, -0.3, 0.2), mass=0.7, periodic=(1, 0, 1))])
+def test_assembled_matrix_times_vector_equals_matrix_free_apply(gb, orc, kw):
+    """apply == assembled Jacobian . vector (dune/fempy/test/testoperator.py:33-71),
+    on both kernels' results, and the assembled operator drives the solvers."""
+    cells, order = (3, 4, 2), 2
+    op = gb.DGOperator(cells, order, algorithm=gb.ALGO_QUADRATURE, **kw)
+    A = op.assemble()
+    prob = orc.DGProblem(cells, order, **kw)
+    u = np.random.default_rng(8).uniform(-1, 1, prob.ndofs)
+    y, ya = gb.DeviceArray(prob.ndofs), gb.DeviceArray(prob.ndofs)
+    du = gb.DeviceArray.from_numpy(u)
+    op(du, y)
+    A(du, ya)
+    assert relmax(ya.numpy(), y.numpy()) < 1e-13
+    assert relmax(ya.numpy(), prob.apply(u)) < 1e-12
+    assert relmax(A.diagonal().numpy(), op.diagonal().numpy()) < 1e-14
+    method = "gmres" if "velocity" in kw else "cg"
+    info, x = _solve(gb, A, u, method, gb.Preconditioner.block_jacobi(A), restart=10)
+    assert info["converged"]
+    assert np.linalg.norm(u - prob.apply(x)) <= 2e-10 * np.linalg.norm(u)
