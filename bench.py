@@ -351,6 +351,7 @@ def workload_q1cg(args):
         u2.clear()
         inv(bd2, u2)
         return u2.numpy()
+    it_manufactured = inv.iterations()
     x, te = _timed(e2e)
     xs = np.linspace(0, 1, N + 1)
     X, Y = np.meshgrid(xs, xs)
@@ -375,7 +376,7 @@ def workload_q1cg(args):
                                  epsilon=1e-10, max_iter=100000)
     t_ref = time.perf_counter() - t0
     return {"metric": "Q1 64x64 diag-PCG solve time to 1e-10", "value": 1e3 * t, "unit": "ms",
-            "higher_is_better": False, "iterations": inv.iterations(), "oracle_iterations": it_ref,
+            "higher_is_better": False, "iterations": it_manufactured, "oracle_iterations": it_ref,
             "max_nodal_error_vs_exact": err, "rel_diff_vs_oracle": float(np.max(np.abs(x - x_ref)) / np.max(np.abs(x_ref))),
             "random_rhs": {"ms": 1e3 * t_rand, "iterations": it_rand,
                            "us_per_iteration": 1e6 * t_rand / max(1, it_rand)},
@@ -509,15 +510,79 @@ def workload_learned(args):
     return out
 
 
+def workload_kernels(args):
+    """CUDA-event timings of the building blocks of one Krylov iteration on the
+    variable-kappa SIPG problem (order args.order, args.cells^3)."""
+    import torch
+    import gbfem
+    import learned
+    N, p = args.cells, args.order
+    op64, op32, k64, k32, f = learned.sipg_problem(N, p, args.seed)
+    n = op64.size
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+
+    def ev(fn, reps=10):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    u64 = gbfem.DeviceArray.from_numpy(np.random.default_rng(0).uniform(-1, 1, n))
+    w64 = gbfem.DeviceArray(n)
+    u32 = gbfem.convert(u64, gbfem.F32)
+    w32 = gbfem.DeviceArray(n, gbfem.F32)
+    out = {"metric": "Krylov building blocks, ms", "unit": "ms", "cells": N, "order": p, "dofs": n}
+    out["apply_f64_quadrature_kappa"] = ev(lambda: op64(u64, w64, sptr))
+    out["apply_f32_quadrature_kappa"] = ev(lambda: op32(u32, w32, sptr))
+    opc = gbfem.DGOperator((N, N, N), p)
+    out["apply_f64_const"] = ev(lambda: opc(u64, w64, sptr))
+    opc32 = gbfem.DGOperator((N, N, N), p, precision=gbfem.F32)
+    out["apply_f32_const"] = ev(lambda: opc32(u32, w32, sptr))
+    t0 = time.perf_counter()
+    bj64 = gbfem.Preconditioner.block_jacobi(op64)
+    torch.cuda.synchronize()
+    out["bj64_setup_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    bj32 = gbfem.Preconditioner.block_jacobi(op32, gbfem.F32)
+    torch.cuda.synchronize()
+    out["bj32_setup_s"] = time.perf_counter() - t0
+    out["bj64_apply"] = ev(lambda: bj64(u64, w64, sptr))
+    out["bj32_apply"] = ev(lambda: bj32(u32, w32, sptr))
+    out["dot_f64_host_result"] = ev(lambda: gbfem.dot(u64, w64, sptr))
+    out["axpy_f64"] = ev(lambda: gbfem.axpy(0.5, u64, w64, sptr))
+    for name, op, pc, fv in (("cg_iter_f64_bj", op64, bj64, f), ("cg_iter_f32_bj", op32, bj32, gbfem.convert(f, gbfem.F32))):
+        x = gbfem.DeviceArray(n, op.precision)
+        inv = gbfem.KrylovInverseOperator("cg", tolerance=1e-30, max_iterations=50)
+        inv.bind(op, pc)
+        x.clear()
+        inv(fv, x)
+        out[name] = inv.info()["time_ms"] / 50.0
+    if N % 8 == 0 and p <= 4:
+        net = gbfem.CNN(p, N, seed=1)
+        net.set_kappa(k64)
+        out["cnn_forward_f64"] = ev(lambda: net.forward(u64, w64))
+        out["cnn_train_step_f32"] = ev(lambda: net.train_step(u32, w32, 1e-4), reps=5)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbfem", choices=["gbfem", "reference"])
-    ap.add_argument("--workload", default="apply", choices=["apply", "q1cg", "rk3", "mixed", "learned"])
+    ap.add_argument("--workload", default="apply", choices=["apply", "q1cg", "rk3", "mixed", "learned", "kernels"])
     ap.add_argument("--rk-steps", type=int, default=100)
     ap.add_argument("--cells", type=int, default=96)
+    ap.add_argument("--order", type=int, default=3)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--inner-tol", type=float, default=1e-3)
     ap.add_argument("--fp64-max-iter", type=int, default=20000)
@@ -532,7 +597,7 @@ def main():
     args = ap.parse_args()
     if args.workload != "apply":
         fn = {"q1cg": workload_q1cg, "rk3": workload_rk3, "mixed": workload_mixed,
-              "learned": workload_learned}[args.workload]
+              "learned": workload_learned, "kernels": workload_kernels}[args.workload]
         line = fn(args)
         line.update({"n_gpus": 1, "data": "synthetic"})
         print(json.dumps(line), flush=True)

@@ -130,29 +130,34 @@ __global__ void k_block_invert(const TI* __restrict__ blocks, TO* __restrict__ i
       }
     __syncthreads();
   }
+  // stored transposed (column j contiguous) for the coalesced apply
   TO* dst = inv + b * nb * nb;
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) dst[e] = TO(a[e]);
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int i = e / nb, j = e - i * nb;
+    dst[j * nb + i] = TO(a[e]);
+  }
 }
 
-// z_K = Binv_K r_K: one warp per row group, CPB cells per CTA, r_K in smem.
+// z_K = Binv_K r_K with Binv_K stored transposed (binvT[K][j][i]): one thread
+// per row i, CPB cells per CTA, r_K broadcast from shared memory.  For fixed j
+// the threads of a cell read consecutive addresses, so the block stream is
+// coalesced; the sum over j has a fixed order.
 template <typename T>
-__global__ void k_block_apply(const T* __restrict__ binv, const T* __restrict__ r, T* __restrict__ z, int nb,
-                              long long ncells) {
+__global__ void k_block_apply(const T* __restrict__ binvT, const T* __restrict__ r, T* __restrict__ z, int nb,
+                              long long ncells, int cpb) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  T* rs = reinterpret_cast<T*>(smraw);
-  const long long c = blockIdx.x;
-  if (c >= ncells) return;
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) rs[i] = r[c * nb + i];
+  T* rs = reinterpret_cast<T*>(smraw);  // [cpb][nb]
+  const long long c0 = (long long)blockIdx.x * cpb;
+  const int ncell = int(ncells - c0 < cpb ? ncells - c0 : cpb);
+  for (int e = threadIdx.x; e < ncell * nb; e += blockDim.x) rs[e] = r[c0 * nb + e];
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  const T* B = binv + c * (long long)nb * nb;
-  for (int row = warp; row < nb; row += nw) {
-    double s = 0.0;
-    for (int j = lane; j < nb; j += 32) s += double(B[(long long)row * nb + j]) * double(rs[j]);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) z[c * nb + row] = T(s);
-  }
+  const int lc = threadIdx.x / nb, i = threadIdx.x - lc * nb;
+  if (lc >= ncell) return;
+  const T* B = binvT + (c0 + lc) * (long long)nb * nb + i;
+  const T* rc = rs + lc * nb;
+  T acc = T(0);
+  for (int j = 0; j < nb; ++j) acc = fma(B[(long long)j * nb], rc[j], acc);
+  z[(c0 + lc) * nb + i] = acc;
 }
 
 // ------------------------------------------------------------ vector ops --
@@ -204,6 +209,8 @@ struct Ctx {
     GBFEM_CUDA_TRY(cudaGetLastError());
     return GBFEM_OK;
   }
+  // x *= a (in place)
+  int scal(double a, void* x) { return gbfem_scal(prec, n, a, x, s); }
   int copy(const void* x, void* y) {
     GBFEM_CUDA_TRY(cudaMemcpyAsync(y, x, bytes(), cudaMemcpyDeviceToDevice, s));
     return GBFEM_OK;
@@ -244,11 +251,16 @@ int precond_apply(const gbfem_preconditioner_s* pc, const void* r, void* z, cuda
     case PcKind::BlockJacobi: {
       const int nb = pc->nloc;
       const long long nc = n / nb;
-      const size_t sm = size_t(nb) * (pc->precision == GBFEM_F64 ? 8 : 4);
+      const int cpb = nb >= 128 ? 1 : 128 / nb;
+      const int threads = ((cpb * nb + 31) / 32) * 32;
+      const size_t sm = size_t(cpb) * nb * (pc->precision == GBFEM_F64 ? 8 : 4);
+      const unsigned blocks = unsigned((nc + cpb - 1) / cpb);
       if (pc->precision == GBFEM_F64)
-        k_block_apply<double><<<unsigned(nc), 128, sm, s>>>((const double*)pc->data, (const double*)r, (double*)z, nb, nc);
+        k_block_apply<double><<<blocks, threads, sm, s>>>((const double*)pc->data, (const double*)r, (double*)z, nb,
+                                                          nc, cpb);
       else
-        k_block_apply<float><<<unsigned(nc), 128, sm, s>>>((const float*)pc->data, (const float*)r, (float*)z, nb, nc);
+        k_block_apply<float><<<blocks, threads, sm, s>>>((const float*)pc->data, (const float*)r, (float*)z, nb,
+                                                         nc, cpb);
       break;
     }
     case PcKind::External:
@@ -365,7 +377,7 @@ static int gmres(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_
     if (res <= tol * (1 + 1e-15)) break;
     g[0] = -res;
     for (int i = 1; i <= m; ++i) g[i] = 0.0;
-    GBFEM_TRY(c.axpby(0.0, v[0], 1.0 / res, v[0]));
+    GBFEM_TRY(c.scal(1.0 / res, v[0]));
     int jlast = 0;
     for (int j = 0; j < m; ++j) {
       void* vj = v[j];
@@ -383,7 +395,7 @@ static int gmres(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_
       double nn;
       GBFEM_TRY(c.dot(vjp, vjp, &nn));
       Hm(j + 1, j) = std::sqrt(nn);
-      GBFEM_TRY(c.axpby(0.0, vjp, 1.0 / Hm(j + 1, j), vjp));
+      GBFEM_TRY(c.scal(1.0 / Hm(j + 1, j), vjp));
       for (int i = 0; i < j; ++i) rotate(&Hm(i + 1, j), &Hm(i, j), cs[i], sn[i]);
       const double hjj = Hm(j, j), hjpj = Hm(j + 1, j);
       const double nrm = std::sqrt(hjj * hjj + hjpj * hjpj);
@@ -792,7 +804,7 @@ int gbfem_solve_mixed(gbfem_operator op64, gbfem_operator op32, gbfem_preconditi
     if (!std::isfinite(rel)) { info->status = GBFEM_ERR_NONFINITE; break; }
     if (rel <= prm->tolerance || outer == prm->max_outer) break;
     GBFEM_TRY(gbfem_convert(n, GBFEM_F64, r, GBFEM_F32, r32, nullptr));
-    GBFEM_TRY(c32.axpby(0.0, r32, 1.0 / rn, r32));
+    GBFEM_TRY(c32.scal(1.0 / rn, r32));
     GBFEM_TRY(c32.clear(d32));
     gbfem_solver_info ii{};
     GBFEM_TRY(solve_impl(op32, pc32, ip, r32, d32, &ii, nullptr));

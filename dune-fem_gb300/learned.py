@@ -39,7 +39,7 @@ def _rms(x):
 def make_pairs(cells, order, seed, ks=(10, 40, 120), inner_tol=1e-3):
     """Training pairs (r_k, target_k) in FP32 for one kappa seed, plus the kappa field."""
     op64, op32, k64, k32, f = sipg_problem(cells, order, seed)
-    bj32 = gbfem.Preconditioner.block_jacobi(op64, gbfem.F32)
+    bj32 = gbfem.Preconditioner.block_jacobi(op32, gbfem.F32)   # blocks from the FP32 operator
     xs = gbfem.DeviceArray(op64.size)
     xs.clear()
     info = gbfem.solve_mixed(op64, op32, bj32, f, xs, tolerance=1e-10, inner_tolerance=inner_tol)
@@ -92,7 +92,7 @@ def evaluate(cnn, cells, order, seed, tol=1e-10, max_iterations=20000, plain=Tru
     op64, op32, k64, k32, f = sipg_problem(cells, order, seed)
     out = {"seed": seed}
     bj64 = gbfem.Preconditioner.block_jacobi(op64)
-    bj32 = gbfem.Preconditioner.block_jacobi(op64, gbfem.F32)
+    bj32 = gbfem.Preconditioner.block_jacobi(op32, gbfem.F32)
     cnn.set_kappa(k64)
     learned64 = cnn.preconditioner(bj64)
     u = gbfem.DeviceArray(op64.size)

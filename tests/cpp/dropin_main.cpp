@@ -32,7 +32,9 @@ int main() {
   f.copyFromHost(fh.data());
   GpuPreconditioner bj = GpuPreconditioner::blockJacobi(op);
   for (int method : {GBFEM_SOLVER_CG, GBFEM_SOLVER_GMRES, GBFEM_SOLVER_BICGSTAB, GBFEM_SOLVER_FCG}) {
-    GpuKrylovInverseOperator inv(method, 1e-10, GBFEM_TOL_RELATIVE);
+    // preconditioned CG/FCG test the preconditioned or true residual against
+    // eps ||b||; 1e-11 leaves room for the difference below 1e-9
+    GpuKrylovInverseOperator inv(method, 1e-11, GBFEM_TOL_RELATIVE);
     inv.bind(op, bj);
     u.clear();
     inv(f, u);
