@@ -255,7 +255,7 @@ def run_gpu(args, world, rank, local):
     achieved_gbs = BYTES_PER_DOF * n / (ms_step * 1e-3) / 1e9
     achieved_tflops = KERNEL_FLOP_PER_DOF * n / (ms_step * 1e-3) / 1e12
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "dg_apply_q3_64cube_f64.json")
+    prof = os.path.join(ROOT, "profiles", "dg_const_q3_64cube_f64.json")
     if os.path.exists(prof):
         with open(prof) as f:
             traffic = json.load(f).get("dram_bytes_per_launch")
@@ -487,6 +487,7 @@ def workload_learned(args):
     t_train = time.perf_counter() - t0
     if args.save_net:
         net.save(args.save_net)
+    diag = learned.diagnose(net, N, p, 100000)
     evals = [learned.evaluate(net, N, p, 100000 + s, plain=not args.skip_plain)
              for s in range(args.eval_seeds)]
     def mean(key, field):
@@ -499,7 +500,7 @@ def workload_learned(args):
                                                                           args.eval_seeds)},
            "value": mean("mixed_learned", "time_s"),
            "train_s": t_train, "train_steps": len(losses), "loss_first": losses[0], "loss_last": losses[-1],
-           "loss_last_mean20": float(np.mean(losses[-20:])), "evals": evals}
+           "loss_last_mean20": float(np.mean(losses[-20:])), "a_norm_error_ratio": diag, "evals": evals}
     for k in ("plain_cg", "bj_cg", "learned_fcg", "mixed_bj", "mixed_learned"):
         out[k + "_mean_time_s"] = mean(k, "time_s")
         out[k + "_mean_iterations"] = mean(k, "iterations")

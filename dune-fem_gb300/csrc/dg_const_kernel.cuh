@@ -16,9 +16,19 @@
 //           (boundary: Val = |F| (eps (sigma v- - dn-) + max(b.n,0) v-), Grad = -|F| eps v-)
 //           w[i,jk] += L_i(s) Val[jk] + (n.e_d/h_d) L_i'(s) Grad[jk]
 //
-// Same owner-computes face scheme and fixed summation order as
-// dg_apply_kernel, so it is deterministic; ~3n^4 FMAs per cell for the volume
-// instead of the ~6 q^4 of the collocation chain.
+// Two kernels (the FP64 pipe is the binding resource, so work is traded for
+// a little extra traffic):
+//  1. dg_trace_kernel: every cell's traces v(s) = sum_i L_i(s) u_i and
+//     d(s) = sum_i L_i'(s) u_i on its 6 faces, into a trace buffer
+//     [cell][face][v|d][n^2].  L_i(1-x) = (-1)^i L_i(x) gives both faces of a
+//     line from one even and one odd partial sum.
+//  2. dg_const_kernel: numerical fluxes from the own and the neighbour's
+//     traces (owner computes, no scatter), then one pass per axis over the
+//     lines of the cell: the 1-D operator M_d (a warp-uniform operand; its
+//     entries with i+j odd vanish without advection and are skipped) plus
+//     the face expansion, again split into even and odd i.
+// Every output is one thread's fixed-order sum: deterministic, independent of
+// the launch shape.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -35,15 +45,50 @@ struct DgConstTablesT {
   T M[3][kDgMaxN * kDgMaxN];  // per-axis line operator (filled per operator)
 };
 
-template <typename T, int N, int CPB>
-__global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, const DgConstTablesT<T> tabs) {
+// traces[cell][f = 2d+s][0: v, 1: d][jk], d(s) without the 1/h and normal sign
+template <typename T, int N>
+__global__ void __launch_bounds__(256) dg_trace_kernel(const T* __restrict__ u, T* __restrict__ traces,
+                                                       long long ncells, const __grid_constant__ DgConstTablesT<T> tabs) {
+  constexpr int N2 = N * N, N3 = N2 * N;
+  const long long total = ncells * 3 * N2;
+  for (long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x; item < total;
+       item += (long long)gridDim.x * blockDim.x) {
+    const long long cell = item / (3 * N2);
+    const int r = int(item - cell * 3 * N2);
+    const int d = r / N2, jk = r - d * N2;
+    const int j = jk / N, k = jk % N;
+    const int base = d == 0 ? j * N + k : (d == 1 ? j * N2 + k : j * N2 + k * N);
+    const int stride = d == 0 ? N2 : (d == 1 ? N : 1);
+    const T* uc = u + cell * N3 + base;
+    T ev = T(0), od = T(0), ed = T(0), odd = T(0);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      const T x = __ldg(uc + i * stride);
+      if (i & 1) {
+        od = fma(tabs.tr[N + i], x, od);
+        odd = fma(tabs.dtr[N + i], x, odd);
+      } else {
+        ev = fma(tabs.tr[N + i], x, ev);
+        ed = fma(tabs.dtr[N + i], x, ed);
+      }
+    }
+    // L_i(1) = tr[N+i]; L_i(0) = (-1)^i L_i(1); L_i'(0) = (-1)^(i+1) L_i'(1)
+    T* tc = traces + cell * (12 * N2);
+    tc[(2 * d + 0) * 2 * N2 + jk] = ev - od;        // v(0)
+    tc[(2 * d + 0) * 2 * N2 + N2 + jk] = odd - ed;  // d(0)
+    tc[(2 * d + 1) * 2 * N2 + jk] = ev + od;        // v(1)
+    tc[(2 * d + 1) * 2 * N2 + N2 + jk] = ed + odd;  // d(1)
+  }
+}
+
+template <typename T, int N, int CPB, bool ADV>
+__global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, const T* __restrict__ traces,
+                                                       const __grid_constant__ DgConstTablesT<T> tabs) {
   constexpr int N2 = N * N, N3 = N * N * N;
-  __shared__ T str[2 * N], sdtr[2 * N];
   __shared__ T su[CPB * N3];
   __shared__ T sr[CPB * N3];
   __shared__ T sF[CPB * 6 * 2 * N2];  // [cell][face][Val/Grad][jk]
   const int tid = threadIdx.x;
-  for (int i = tid; i < 2 * N; i += blockDim.x) { str[i] = tabs.tr[i]; sdtr[i] = tabs.dtr[i]; }
   const long long ncells = args.ncells;
   const long long c0 = (long long)blockIdx.x * CPB;
   if (c0 >= ncells) return;
@@ -51,14 +96,12 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
     const long long v = c0 + e / N3;
     su[e] = v < ncells ? __ldg(args.u + c0 * N3 + e) : T(0);
   }
-  __syncthreads();
-  // ---- faces: traces and numerical fluxes in coefficient space --------------
+  // ---- faces: numerical fluxes from own and neighbour traces -----------------
   for (int item = tid; item < CPB * 6 * N2; item += blockDim.x) {
     const int c = item / (6 * N2);
     const int r = item - c * 6 * N2;
     const int f = r / N2, jk = r - f * N2;
     const int d = f >> 1, s = f & 1;
-    const int j = jk / N, k = jk % N;
     const long long cell = c0 + c;
     const bool valid = cell < ncells;
     const long long cl = valid ? cell : 0;
@@ -74,57 +117,39 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
     }
     cc[d] = nb;
     const long long ncell = cc[0] + (long long)args.nc[0] * (cc[1] + (long long)args.nc[1] * cc[2]);
-    int base, stride;
-    if (d == 0) { base = j * N + k; stride = N2; }
-    else if (d == 1) { base = j * N2 + k; stride = N; }
-    else { base = j * N2 + k * N; stride = 1; }
-    const T sgn = s ? T(1) : T(-1);
-    const T invh = args.invh[d];
-    const T* uo = su + c * N3;
-    T vm = T(0), nm = T(0), vp = T(0), np = T(0);
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      const T x = uo[base + i * stride];
-      vm = fma(str[s * N + i], x, vm);
-      nm = fma(sdtr[s * N + i], x, nm);
-    }
-    nm *= sgn * invh;
+    const T sgnh = s ? args.invh[d] : -args.invh[d];  // (n . e_d) / h_d
+    const T* own = traces + cl * (12 * N2) + f * 2 * N2;
+    const T vm = __ldg(own + jk), nm = sgnh * __ldg(own + N2 + jk);
+    T vp = T(0), np = T(0);
     if (has_nb && valid) {
-      const int so = 1 - s;
-#pragma unroll
-      for (int i = 0; i < N; ++i) {
-        const T x = __ldg(args.u + ncell * N3 + base + i * stride);
-        vp = fma(str[so * N + i], x, vp);
-        np = fma(sdtr[so * N + i], x, np);
-      }
-      np *= sgn * invh;
+      const T* nbt = traces + ncell * (12 * N2) + (2 * d + 1 - s) * 2 * N2;
+      vp = __ldg(nbt + jk);
+      np = sgnh * __ldg(nbt + N2 + jk);
     }
     const T F = args.faceA[d];
-    const T bn = args.advect ? sgn * args.b[d] : T(0);
+    const T bn = ADV ? (s ? args.b[d] : -args.b[d]) : T(0);
     T val = T(0), grad = T(0);
     if (has_nb) {
       const T J = vm - vp;
       val = F * args.eps * (args.sigma[d] * J - T(0.5) * (nm + np));
       grad = F * args.eps * (T(-0.5) * J);
-      if (args.advect) val += F * bn * (bn >= T(0) ? vm : vp);
+      if (ADV) val += F * bn * (bn >= T(0) ? vm : vp);
     } else {
       if (args.weak_dirichlet) {
         val = F * args.eps * (args.sigma[d] * vm - nm);
         grad = F * args.eps * (-vm);
       }
-      if (args.advect && bn > T(0)) val += F * bn * vm;
+      if (ADV && bn > T(0)) val += F * bn * vm;
     }
     sF[(c * 6 + f) * 2 * N2 + jk] = val;
     sF[(c * 6 + f) * 2 * N2 + N2 + jk] = grad;
   }
   __syncthreads();
   // ---- volume + face expansion, one line along axis d per item ---------------
-  // M_d = eps|K|/h_d^2 K1 - b_d |K|/h_d D1 (+ c|K| I for d = 0) is the same for
-  // every line: a warp-uniform operand from the kernel parameters.
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const int stride = d == 0 ? N2 : (d == 1 ? N : 1);
-    const T sgnh = args.invh[d];
+    const T ih = args.invh[d];
     for (int item = tid; item < CPB * N2; item += blockDim.x) {
       const int c = item / N2, jk = item - c * N2;
       const int j = jk / N, k = jk % N;
@@ -135,17 +160,19 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
       for (int i = 0; i < N; ++i) x[i] = uc[i * stride];
       const T* fv0 = sF + (c * 6 + 2 * d) * 2 * N2;
       const T* fv1 = fv0 + 2 * N2;
-      const T v0 = fv0[jk], g0 = fv0[N2 + jk], v1 = fv1[jk], g1 = fv1[N2 + jk];
+      // sum_s L_i(s) Val_s = L_i(1) (Val_1 + (-1)^i Val_0); the gradient
+      // terms likewise with (n.e_d/h) L_i'(s): (1/h) L_i'(1) (G_1 + (-1)^i G_0)
+      const T v0 = fv0[jk], v1 = fv1[jk], g0 = fv0[N2 + jk], g1 = fv1[N2 + jk];
+      const T vs = v1 + v0, vd = v1 - v0, gs = ih * (g1 + g0), gd = ih * (g1 - g0);
       T* rc = sr + c * N3 + base;
 #pragma unroll
       for (int i = 0; i < N; ++i) {
         T acc = d == 0 ? T(0) : rc[i * stride];
 #pragma unroll
-        for (int jj = 0; jj < N; ++jj) acc = fma(tabs.M[d][i * N + jj], x[jj], acc);
-        acc = fma(str[i], v0, acc);                       // side s = 0 (L_i(0))
-        acc = fma(-sgnh * sdtr[i], g0, acc);
-        acc = fma(str[N + i], v1, acc);                   // side s = 1 (L_i(1))
-        acc = fma(sgnh * sdtr[N + i], g1, acc);
+        for (int jj = 0; jj < N; ++jj)
+          if (ADV || !((i + jj) & 1)) acc = fma(tabs.M[d][i * N + jj], x[jj], acc);
+        acc = fma(tabs.tr[N + i], (i & 1) ? vd : vs, acc);
+        acc = fma(tabs.dtr[N + i], (i & 1) ? gd : gs, acc);
         rc[i * stride] = acc;
       }
     }

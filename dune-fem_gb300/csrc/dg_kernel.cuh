@@ -115,6 +115,54 @@ __device__ __forceinline__ void contract_lines(const T* __restrict__ in, int ics
   }
 }
 
+// Per-output variant of the same contraction: one thread per output value,
+// matrix from shared memory.  The FP64 kernels use it: they are FP64-pipe
+// bound, and this form issues fewer instructions per FMA than the line form.
+// in  : NCELL arrays of dims [I0][I1][I2] (row-major), cell stride `ics`.
+// out : NCELL arrays of the same dims except OUT on axis AX, cell stride `ocs`.
+// !TR : out[..o..] = sum_i M[o*LDM + i] * in[..i..]
+//  TR : out[..o..] = sum_i M[i*LDM + o] * in[..i..]
+// ACC adds to the existing content of out.
+template <typename T, int AX, int I0, int I1, int I2, int OUT, int LDM, bool TR, bool ACC, int NCELL>
+__device__ __forceinline__ void contract_items(const T* __restrict__ in, int ics, T* __restrict__ out, int ocs,
+                                         const T* __restrict__ M) {
+  constexpr int IN = AX == 0 ? I0 : (AX == 1 ? I1 : I2);
+  constexpr int O0 = AX == 0 ? OUT : I0;
+  constexpr int O1 = AX == 1 ? OUT : I1;
+  constexpr int O2 = AX == 2 ? OUT : I2;
+  constexpr int OSZ = O0 * O1 * O2;
+  constexpr int IS0 = I1 * I2, IS1 = I2;
+  constexpr int ISA = AX == 0 ? IS0 : (AX == 1 ? IS1 : 1);
+  for (int item = threadIdx.x; item < NCELL * OSZ; item += blockDim.x) {
+    const int cell = item / OSZ;
+    const int r = item - cell * OSZ;
+    const int x0 = r / (O1 * O2);
+    const int x1 = (r / O2) % O1;
+    const int x2 = r % O2;
+    const int o = AX == 0 ? x0 : (AX == 1 ? x1 : x2);
+    const int ib = cell * ics + (AX == 0 ? 0 : x0 * IS0) + (AX == 1 ? 0 : x1 * IS1) + (AX == 2 ? 0 : x2);
+    T acc = ACC ? out[cell * ocs + r] : T(0);
+#pragma unroll
+    for (int i = 0; i < IN; ++i) {
+      const T m = TR ? M[i * LDM + o] : M[o * LDM + i];
+      acc = fma(m, in[ib + i * ISA], acc);
+    }
+    out[cell * ocs + r] = acc;
+  }
+}
+
+// Contraction with the form that suits the precision: lines (register
+// inputs, warp-uniform parameter-space matrix) for FP32, which would
+// otherwise be bound by shared-memory bandwidth; per-output items for FP64.
+template <typename T, int AX, int I0, int I1, int I2, int OUT, int LDM, bool TR, bool ACC, int NCELL>
+__device__ __forceinline__ void contract(const T* __restrict__ in, int ics, T* __restrict__ out, int ocs,
+                                         const T* __restrict__ Msmem, const T* __restrict__ Mparam) {
+  if (sizeof(T) == 8)
+    contract_items<T, AX, I0, I1, I2, OUT, LDM, TR, ACC, NCELL>(in, ics, out, ocs, Msmem);
+  else
+    contract_lines<T, AX, I0, I1, I2, OUT, LDM, TR, ACC, NCELL>(in, ics, out, ocs, Mparam);
+}
+
 // Shared-memory footprint (elements of T) of one CTA.
 template <int N, int Q, bool KAPPA, int CPB>
 struct DgSmem {
@@ -193,23 +241,23 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args,
     T* G2 = G1 + Q3;
     T* Kq = G2 + Q3;              // [Q3] (KAPPA)
     if (KAPPA) {
-      contract_lines<T, 0, N, N, N, Q, N, false, false, CPB>(sk, N3, t1, WS, tabs.B);
+      contract<T, 0, N, N, N, Q, N, false, false, CPB>(sk, N3, t1, WS, sB, tabs.B);
       __syncthreads();
-      contract_lines<T, 1, Q, N, N, Q, N, false, false, CPB>(t1, WS, t2, WS, tabs.B);
+      contract<T, 1, Q, N, N, Q, N, false, false, CPB>(t1, WS, t2, WS, sB, tabs.B);
       __syncthreads();
-      contract_lines<T, 2, Q, Q, N, Q, N, false, false, CPB>(t2, WS, Kq, WS, tabs.B);
+      contract<T, 2, Q, Q, N, Q, N, false, false, CPB>(t2, WS, Kq, WS, sB, tabs.B);
       __syncthreads();
     }
-    contract_lines<T, 0, N, N, N, Q, N, false, false, CPB>(su, N3, t1, WS, tabs.B);
+    contract<T, 0, N, N, N, Q, N, false, false, CPB>(su, N3, t1, WS, sB, tabs.B);
     __syncthreads();
-    contract_lines<T, 1, Q, N, N, Q, N, false, false, CPB>(t1, WS, t2, WS, tabs.B);
+    contract<T, 1, Q, N, N, Q, N, false, false, CPB>(t1, WS, t2, WS, sB, tabs.B);
     __syncthreads();
-    contract_lines<T, 2, Q, Q, N, Q, N, false, false, CPB>(t2, WS, U, WS, tabs.B);
+    contract<T, 2, Q, Q, N, Q, N, false, false, CPB>(t2, WS, U, WS, sB, tabs.B);
     __syncthreads();
     // gradients in reference coordinates: collocation derivative along each axis
-    contract_lines<T, 0, Q, Q, Q, Q, Q, false, false, CPB>(U, WS, G0, WS, tabs.Dc);
-    contract_lines<T, 1, Q, Q, Q, Q, Q, false, false, CPB>(U, WS, G1, WS, tabs.Dc);
-    contract_lines<T, 2, Q, Q, Q, Q, Q, false, false, CPB>(U, WS, G2, WS, tabs.Dc);
+    contract<T, 0, Q, Q, Q, Q, Q, false, false, CPB>(U, WS, G0, WS, sDc, tabs.Dc);
+    contract<T, 1, Q, Q, Q, Q, Q, false, false, CPB>(U, WS, G1, WS, sDc, tabs.Dc);
+    contract<T, 2, Q, Q, Q, Q, Q, false, false, CPB>(U, WS, G2, WS, sDc, tabs.Dc);
     __syncthreads();
     // pointwise flux (in place: item r reads and writes only point r)
     for (int item = tid; item < CPB * Q3; item += blockDim.x) {
@@ -235,17 +283,17 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args,
     }
     __syncthreads();
     // V = W c u + Dc^T contractions of the fluxes, accumulated axis by axis
-    contract_lines<T, 0, Q, Q, Q, Q, Q, true, true, CPB>(G0, WS, U, WS, tabs.Dc);
+    contract<T, 0, Q, Q, Q, Q, Q, true, true, CPB>(G0, WS, U, WS, sDc, tabs.Dc);
     __syncthreads();
-    contract_lines<T, 1, Q, Q, Q, Q, Q, true, true, CPB>(G1, WS, U, WS, tabs.Dc);
+    contract<T, 1, Q, Q, Q, Q, Q, true, true, CPB>(G1, WS, U, WS, sDc, tabs.Dc);
     __syncthreads();
-    contract_lines<T, 2, Q, Q, Q, Q, Q, true, true, CPB>(G2, WS, U, WS, tabs.Dc);
+    contract<T, 2, Q, Q, Q, Q, Q, true, true, CPB>(G2, WS, U, WS, sDc, tabs.Dc);
     __syncthreads();
-    contract_lines<T, 2, Q, Q, Q, N, N, true, false, CPB>(U, WS, t2, WS, tabs.B);
+    contract<T, 2, Q, Q, Q, N, N, true, false, CPB>(U, WS, t2, WS, sB, tabs.B);
     __syncthreads();
-    contract_lines<T, 1, Q, Q, N, N, N, true, false, CPB>(t2, WS, t1, WS, tabs.B);
+    contract<T, 1, Q, Q, N, N, N, true, false, CPB>(t2, WS, t1, WS, sB, tabs.B);
     __syncthreads();
-    contract_lines<T, 0, Q, N, N, N, N, true, false, CPB>(t1, WS, sr, N3, tabs.B);
+    contract<T, 0, Q, N, N, N, N, true, false, CPB>(t1, WS, sr, N3, sB, tabs.B);
     __syncthreads();
   }
 
@@ -323,9 +371,9 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args,
     }
     __syncthreads();
     // F2/F3: 2-D interpolation of all face arrays to the q x q face points
-    contract_lines<T, 1, 2 * MA, N, N, Q, N, false, false, CPB>(FC, WS, FT, WS, tabs.B);
+    contract<T, 1, 2 * MA, N, N, Q, N, false, false, CPB>(FC, WS, FT, WS, sB, tabs.B);
     __syncthreads();
-    contract_lines<T, 2, 2 * MA, Q, N, Q, N, false, false, CPB>(FT, WS, FQ, WS, tabs.B);
+    contract<T, 2, 2 * MA, Q, N, Q, N, false, false, CPB>(FT, WS, FQ, WS, sB, tabs.B);
     __syncthreads();
     // F4: pointwise numerical fluxes
     for (int item = tid; item < CPB * 2 * Q2; item += blockDim.x) {
@@ -371,9 +419,9 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args,
     }
     __syncthreads();
     // F5/F6: transposed 2-D contraction back to the n x n tangential coefficients
-    contract_lines<T, 2, 4, Q, Q, N, N, true, false, CPB>(FV, WS, FT, WS, tabs.B);
+    contract<T, 2, 4, Q, Q, N, N, true, false, CPB>(FV, WS, FT, WS, sB, tabs.B);
     __syncthreads();
-    contract_lines<T, 1, 4, Q, N, N, N, true, false, CPB>(FT, WS, FC, WS, tabs.B);
+    contract<T, 1, 4, Q, N, N, N, true, false, CPB>(FT, WS, FC, WS, sB, tabs.B);
     __syncthreads();
     // F7: expand into the cell's test functions, both sides in fixed order
     for (int item = tid; item < CPB * N3; item += blockDim.x) {

@@ -116,6 +116,7 @@ extern "C" int gbfem_operator_assemble(gbfem_operator op, gbfem_operator* out) {
   a->host_u = a->host_w = nullptr;
   a->bsr_blocks = nullptr;
   a->bsr_col = nullptr;
+  a->trace_buf = nullptr;
   const int nb = op->nloc;
   const size_t es = op->precision == GBFEM_F64 ? 8 : 4;
   const size_t bsz = size_t(nb) * nb * es;

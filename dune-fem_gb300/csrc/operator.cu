@@ -16,8 +16,20 @@ namespace gbfem {
 
 int dg_launch_f64(const DgArgsT<double>&, const DgTablesT<double>&, int, int, bool, cudaStream_t);
 int dg_launch_f32(const DgArgsT<float>&, const DgTablesT<float>&, int, int, bool, cudaStream_t);
-int dg_const_launch_f64(const DgArgsT<double>&, const DgConstTablesT<double>&, int, cudaStream_t);
-int dg_const_launch_f32(const DgArgsT<float>&, const DgConstTablesT<float>&, int, cudaStream_t);
+int dg_const_launch_f64(const DgArgsT<double>&, const DgConstTablesT<double>&, int, double*, cudaStream_t);
+int dg_const_launch_f32(const DgArgsT<float>&, const DgConstTablesT<float>&, int, float*, cudaStream_t);
+
+// Trace buffer of the closed-form kernel: [cell][6 faces][v|d][n^2], allocated
+// on the first apply of an operator.
+static int trace_buffer(const gbfem_operator_s* op, void** buf) {
+  auto* mop = const_cast<gbfem_operator_s*>(op);
+  if (!mop->trace_buf) {
+    const size_t bytes = size_t(op->ncells) * 12 * op->n * op->n * (op->precision == GBFEM_F64 ? 8 : 4);
+    GBFEM_CUDA_TRY(cudaMalloc(&mop->trace_buf, bytes));
+  }
+  *buf = mop->trace_buf;
+  return GBFEM_OK;
+}
 
 template <typename T>
 static void fill_const_tables(const Tables1D& t, const ConstTables1D& c, DgConstTablesT<T>* out) {
@@ -110,7 +122,9 @@ int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s,
     if (unit_mode == 0 && op->coefficient_space) {
       DgConstTablesT<double> ct = op->ctab64;
       fill_line_operators(op, &ct);
-      return dg_const_launch_f64(a, ct, op->n, s);
+      void* tb = nullptr;
+      GBFEM_TRY(trace_buffer(op, &tb));
+      return dg_const_launch_f64(a, ct, op->n, static_cast<double*>(tb), s);
     }
     return dg_launch_f64(a, op->tab64, op->n, op->q, op->dg.kappa != nullptr, s);
   } else {
@@ -125,7 +139,9 @@ int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s,
     if (unit_mode == 0 && op->coefficient_space) {
       DgConstTablesT<float> ct = op->ctab32;
       fill_line_operators(op, &ct);
-      return dg_const_launch_f32(a, ct, op->n, s);
+      void* tb = nullptr;
+      GBFEM_TRY(trace_buffer(op, &tb));
+      return dg_const_launch_f32(a, ct, op->n, static_cast<float*>(tb), s);
     }
     return dg_launch_f32(a, op->tab32, op->n, op->q, op->dg.kappa != nullptr, s);
   }
@@ -306,6 +322,7 @@ int gbfem_operator_destroy(gbfem_operator op) {
   if (op->host_u) cudaFree(op->host_u);
   if (op->host_w) cudaFree(op->host_w);
   if (op->bsr_blocks) cudaFree(op->bsr_blocks);
+  if (op->trace_buf) cudaFree(op->trace_buf);
   if (op->bsr_col) cudaFree(op->bsr_col);
   delete op;
   return GBFEM_OK;

@@ -42,6 +42,7 @@ struct gbfem_operator_s {
   gbfem::Q1Element q1{};
   void* bsr_blocks = nullptr;   // assembled: [cell][7][nloc][nloc]
   long long* bsr_col = nullptr; // assembled: [cell][7] column cell (-1 = none)
+  void* trace_buf = nullptr;    // closed-form kernel: face traces [cell][6][2][n^2]
   void* host_u = nullptr;  // device staging of gbfem_operator_apply_host
   void* host_w = nullptr;
 };

@@ -528,7 +528,7 @@ static int bicgstab(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solv
 static int fcg(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_params& prm, const void* b, void* x,
                Ctx& c, gbfem_solver_info* info) {
   const int mmax = prm.restart > 0 ? prm.restart : 1;
-  constexpr int kStagnation = 25;
+  constexpr int kStagnation = 50;
   Vecs t, dirs, ws;
   GBFEM_TRY(t.alloc(2, c.bytes()));
   GBFEM_TRY(dirs.alloc(mmax + 1, c.bytes()));

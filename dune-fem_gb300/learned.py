@@ -4,8 +4,8 @@ Training pairs come from the solver itself, on seeded log-Gaussian kappa
 fields (256 Fourier modes, std 1, correlation length 0.1):
   1. x* = the FP64-accurate solution of -div(kappa grad u) = 1 (SIPG, weak
      u = 0), from the mixed FP32/FP64 iterative refinement to 1e-10;
-  2. iterates x_k of block-Jacobi PCG at k in `ks` give errors e_k = x* - x_k
-     and residuals r_k = A e_k (FP64 apply);
+  2. iterates x_k of block-Jacobi PCG at k in `ks` (k = 0: x_0 = 0) give
+     errors e_k = x* - x_k and residuals r_k = A e_k (FP64 apply);
   3. the network learns the part of e_k block Jacobi misses:
      target_k = e_k - BJ(r_k).
 The network is then used as z = BJ(r) + NN(r) inside flexible CG, where the
@@ -36,7 +36,7 @@ def _rms(x):
     return np.sqrt(max(gbfem.dot(x, x), 0.0) / x.n)
 
 
-def make_pairs(cells, order, seed, ks=(10, 40, 120), inner_tol=1e-3):
+def make_pairs(cells, order, seed, ks=(0, 10, 40, 120, 400, 1000), inner_tol=1e-3):
     """Training pairs (r_k, target_k) in FP32 for one kappa seed, plus the kappa field."""
     op64, op32, k64, k32, f = sipg_problem(cells, order, seed)
     bj32 = gbfem.Preconditioner.block_jacobi(op32, gbfem.F32)   # blocks from the FP32 operator
@@ -66,7 +66,7 @@ def make_pairs(cells, order, seed, ks=(10, 40, 120), inner_tol=1e-3):
     return pairs, k32
 
 
-def train(cnn, cells, order, seeds, ks=(10, 40, 120), steps_per_pair=4, lr=1e-3, log=None):
+def train(cnn, cells, order, seeds, ks=(0, 10, 40, 120, 400, 1000), steps_per_pair=4, lr=1e-3, log=None):
     """Online training over `seeds`; returns the per-step losses."""
     losses = []
     t0 = time.perf_counter()
@@ -117,4 +117,33 @@ def evaluate(cnn, cells, order, seed, tol=1e-10, max_iterations=20000, plain=Tru
                                  inner_restart=4)
         out[name] = {"iterations": info.iterations, "time_s": time.perf_counter() - t0,
                      "converged": bool(info.converged), "rel_residual": info.residual}
+    return out
+
+
+def diagnose(cnn, cells, order, seed, ks=(0, 40, 400)):
+    """A-norm quality of the preconditioner on held-out solver pairs:
+    ||e - z||_A / ||e||_A for z = BJ(r) and for z = BJ(r) + NN(r)."""
+    op64, op32, k64, k32, f = sipg_problem(cells, order, seed)
+    pairs, _ = make_pairs(cells, order, seed, ks)
+    bj32 = gbfem.Preconditioner.block_jacobi(op32, gbfem.F32)
+    cnn.set_kappa(k32)
+    out = []
+    for (r32, t32), k in zip(pairs, ks):
+        z = gbfem.DeviceArray(op32.size, gbfem.F32)
+        bj32(r32, z)
+        e = gbfem.copy(t32)             # e = target + BJ(r)
+        gbfem.axpy(1.0, z, e)
+        zn = gbfem.copy(z)
+        cnn.forward(r32, zn, accumulate=True)
+        res = {"k": k}
+        for name, zz in (("bj", z), ("learned", zn)):
+            d = gbfem.convert(e, gbfem.F64)
+            gbfem.axpy(-1.0, gbfem.convert(zz, gbfem.F64), d)
+            ad = gbfem.DeviceArray(op64.size)
+            op64(d, ad)
+            e64 = gbfem.convert(e, gbfem.F64)
+            ae = gbfem.DeviceArray(op64.size)
+            op64(e64, ae)
+            res[name] = float(np.sqrt(gbfem.dot(d, ad) / gbfem.dot(e64, ae)))
+        out.append(res)
     return out
