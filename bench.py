@@ -35,9 +35,10 @@ METRIC = "SIPG apply DoF/s"
 UNIT = "DoF/s"
 BYTES_PER_DOF = 16.0          # read u (8) + write w (8), geometry recomputed, tables on chip
 FLOP_PER_DOF = 402.0          # sum-factorised SIPG Q3, q=5 (volume + faces), the algorithmic count
-# flops the constant-coefficient closed-form kernel executes per dof (n = 4):
-# volume 3 n^4 FMA, faces 6 n^2 (4 n) trace FMA + 12 n^3 expansion FMA, ~10 flop per face point
-KERNEL_FLOP_PER_DOF = (2.0 * (3 * 4 ** 4 + 36 * 4 ** 3) + 6 * 16 * 10) / 64.0
+# flops the closed-form kernels execute per cell (n = 4, no advection), divided by n^3:
+# traces 3 n^2 lines x (4 n flop + 4 adds); fluxes 6 n^2 x ~12 flop;
+# lines 3 n^2 x (n outputs x (2 (n/2) + 4) flop + 6)
+KERNEL_FLOP_PER_DOF = (3 * 16 * (16 + 4) + 6 * 16 * 12 + 3 * 16 * (4 * (4 + 4) + 6)) / 64.0
 CONFIG = {"workload": "SIPG DG Q3 apply, 3-D unit cube 64^3 hexes, 16.8M dofs, q=5, penalty 160, FP64",
           "cells": list(CELLS), "order": ORDER, "quad_points": QUAD, "dofs": 64 ** 3 * 64,
           "l2": "inputs exceed L2 (u + w = 268 MB > 129 MB), no flush"}
@@ -255,7 +256,7 @@ def run_gpu(args, world, rank, local):
     achieved_gbs = BYTES_PER_DOF * n / (ms_step * 1e-3) / 1e9
     achieved_tflops = KERNEL_FLOP_PER_DOF * n / (ms_step * 1e-3) / 1e12
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "dg_const_q3_64cube_f64.json")
+    prof = os.path.join(ROOT, "profiles", "dg_const2_q3_64cube_f64.json")
     if os.path.exists(prof):
         with open(prof) as f:
             traffic = json.load(f).get("dram_bytes_per_launch")
@@ -268,7 +269,7 @@ def run_gpu(args, world, rank, local):
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform[-1,1] dofs)",
             "config": dict(CONFIG, parallelism="replicas" if world > 1 else "single GPU"),
-            "gpu_launches": args.steps,
+            "gpu_launches": 2 * args.steps,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                     "steps": e2e_steps, "path": "gbfem_operator_apply_host (pinned host buffers)"},
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
@@ -280,7 +281,8 @@ def run_gpu(args, world, rank, local):
                           "sum_factorised_quadrature_flop_per_dof": FLOP_PER_DOF,
                           "fp32_peak_tflops_measured": fp32_peak},
             "algorithm": "constant-kappa closed form of the q=5 Gauss quadrature (exact for these integrands; "
-                         "1-D stiffness along lines + identity tangential face mass)",
+                         "trace pre-pass + 1-D stiffness along lines + identity tangential face mass); "
+                         "2 kernel launches per apply",
             "quadrature_kernel": {"value": n / (ms_quad * 1e-3), "unit": UNIT, "ms_per_step": ms_quad,
                                   "rel_max_diff_vs_default": quad_rel,
                                   "note": "sum-factorised evaluation at the 125 Gauss points (the variable-kappa path)"},
@@ -482,13 +484,17 @@ def workload_learned(args):
     net = gbfem.CNN(p, N, seed=2026)
     log = (lambda m: print(m, file=sys.stderr, flush=True)) if args.verbose else None
     t0 = time.perf_counter()
-    losses = learned.train(net, N, p, list(range(args.train_seeds)), steps_per_pair=args.train_steps, lr=args.lr,
-                           log=log)
+    if args.loss == "anorm":
+        losses = learned.train_anorm(net, N, p, list(range(args.train_seeds)), steps_per_pair=args.train_steps,
+                                     lr=args.lr, log=log)
+    else:
+        losses = learned.train(net, N, p, list(range(args.train_seeds)), steps_per_pair=args.train_steps,
+                               lr=args.lr, log=log, form=args.form)
     t_train = time.perf_counter() - t0
     if args.save_net:
         net.save(args.save_net)
-    diag = learned.diagnose(net, N, p, 100000)
-    evals = [learned.evaluate(net, N, p, 100000 + s, plain=not args.skip_plain)
+    diag = learned.diagnose(net, N, p, 100000, form=args.form)
+    evals = [learned.evaluate(net, N, p, 100000 + s, plain=not args.skip_plain, form=args.form)
              for s in range(args.eval_seeds)]
     def mean(key, field):
         v = [e[key][field] for e in evals if key in e]
@@ -500,7 +506,9 @@ def workload_learned(args):
                                                                           args.eval_seeds)},
            "value": mean("mixed_learned", "time_s"),
            "train_s": t_train, "train_steps": len(losses), "loss_first": losses[0], "loss_last": losses[-1],
-           "loss_last_mean20": float(np.mean(losses[-20:])), "a_norm_error_ratio": diag, "evals": evals}
+           "loss_last_mean20": float(np.mean(losses[-20:])), "form": args.form, "loss": args.loss,
+           "a_norm_error_ratio": diag,
+           "evals": evals}
     for k in ("plain_cg", "bj_cg", "learned_fcg", "mixed_bj", "mixed_learned"):
         out[k + "_mean_time_s"] = mean(k, "time_s")
         out[k + "_mean_iterations"] = mean(k, "iterations")
@@ -594,6 +602,8 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--save-net", default="")
+    ap.add_argument("--form", default="additive", choices=["additive", "twolevel"])
+    ap.add_argument("--loss", default="anorm", choices=["anorm", "mse"])
     ap.add_argument("--verbose", action="store_true")
     args = ap.parse_args()
     if args.workload != "apply":

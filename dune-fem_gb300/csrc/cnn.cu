@@ -134,6 +134,20 @@ __global__ void loss_grad_kernel(const float* __restrict__ y, const T* __restric
   }
 }
 
+// dy[p][c] = S rms(r) g[p*nloc + c] (chain rule through z = S rms(r) y); 0 on padded channels
+template <typename T>
+__global__ void grad_from_dofs_kernel(const T* __restrict__ g, const double* __restrict__ rr, long long n, int nloc,
+                                      int cout, long long P, float S, bf16* __restrict__ dy) {
+  const double rms = sqrt(rr[0] / double(n));
+  const long long total = P * cout;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+    const int c = int(e % cout);
+    const long long p = e / cout;
+    const double v = c < nloc ? double(S) * rms * double(g[p * nloc + c]) : 0.0;
+    dy[e] = __float2bfloat16_rn(float(v));
+  }
+}
+
 // logk[p] = log(kappa coefficient 0 of cell p) (the cell mean for the orthonormal basis)
 template <typename T>
 __global__ void logkappa_kernel(const T* __restrict__ kappa, int nloc, long long P, float* __restrict__ logk) {
@@ -385,19 +399,52 @@ static int cnn_loss_grad(gbfem_cnn_s* c, int precision, const void* r, const voi
 struct LearnedCtx {
   gbfem_cnn_s* cnn;
   gbfem_preconditioner bj;  // not owned
+  gbfem_operator op;        // not owned; NULL = additive form
+  void* t = nullptr;        // work vectors of the two-level form
+  void* at = nullptr;
+  ~LearnedCtx() {
+    if (t) cudaFree(t);
+    if (at) cudaFree(at);
+  }
 };
 
+template <typename T>
+__global__ void learned_residual_kernel(long long n, const T* __restrict__ r, const T* __restrict__ az,
+                                        T* __restrict__ t) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    t[i] = r[i] - az[i];
+}
+template <typename T>
+__global__ void learned_add_kernel(long long n, const T* __restrict__ a, T* __restrict__ z) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    z[i] += a[i];
+}
+
+// Additive:   z = BJ(r) + NN(r)
+// Two-level:  z = NN(r);  z += BJ(r - A z)   (the network as the coarse
+//             correction, one block-Jacobi smoothing step after it)
 static int ext_learned_apply(void* ctx, const void* r, void* z, cudaStream_t s) {
   LearnedCtx* lc = static_cast<LearnedCtx*>(ctx);
   gbfem_cnn_s* c = lc->cnn;
-  int prec = GBFEM_F64;
-  if (lc->bj) {
-    prec = lc->bj->precision;
-    GBFEM_TRY(precond_apply(lc->bj, r, z, s));
-  } else {
-    GBFEM_CUDA_TRY(cudaMemsetAsync(z, 0, size_t(c->ndofs) * 8, s));
+  const int prec = lc->bj ? lc->bj->precision : GBFEM_F64;
+  if (!lc->op) {
+    if (lc->bj) GBFEM_TRY(precond_apply(lc->bj, r, z, s));
+    else GBFEM_CUDA_TRY(cudaMemsetAsync(z, 0, size_t(c->ndofs) * (prec == GBFEM_F64 ? 8 : 4), s));
+    return cnn_apply(c, prec, r, z, 1, s);
   }
-  return cnn_apply(c, prec, r, z, 1, s);
+  GBFEM_TRY(cnn_apply(c, prec, r, z, 0, s));
+  GBFEM_TRY(gbfem_operator_apply(lc->op, z, lc->at, s));
+  const long long n = c->ndofs;
+  if (prec == GBFEM_F64) {
+    learned_residual_kernel<double><<<grid1(n), 256, 0, s>>>(n, (const double*)r, (const double*)lc->at, (double*)lc->t);
+  } else {
+    learned_residual_kernel<float><<<grid1(n), 256, 0, s>>>(n, (const float*)r, (const float*)lc->at, (float*)lc->t);
+  }
+  GBFEM_TRY(precond_apply(lc->bj, lc->t, lc->at, s));
+  if (prec == GBFEM_F64) learned_add_kernel<double><<<grid1(n), 256, 0, s>>>(n, (const double*)lc->at, (double*)z);
+  else learned_add_kernel<float><<<grid1(n), 256, 0, s>>>(n, (const float*)lc->at, (float*)z);
+  GBFEM_CUDA_TRY(cudaGetLastError());
+  return GBFEM_OK;
 }
 
 static void ext_learned_destroy(void* ctx) { delete static_cast<LearnedCtx*>(ctx); }
@@ -563,6 +610,34 @@ int gbfem_cnn_train_step(gbfem_cnn c, int precision, const void* r, const void* 
   return refresh_bf16(c, s);
 }
 
+int gbfem_cnn_train_step_grad(gbfem_cnn c, int precision, const void* r, const void* grad_z, double lr,
+                              void* stream) {
+  if (!c || !r || !grad_z) return set_error(GBFEM_ERR_INVALID, "gbfem_cnn_train_step_grad: null argument");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (precision == GBFEM_F64) GBFEM_TRY(cnn_input<double>(c, r, s));
+  else GBFEM_TRY(cnn_input<float>(c, r, s));
+  GBFEM_TRY(cnn_forward(c, s));
+  const long long ny = c->P[0] * c->cout0;
+  if (precision == GBFEM_F64)
+    grad_from_dofs_kernel<double><<<grid1(ny), 256, 0, s>>>(static_cast<const double*>(grad_z), c->d_rr, c->ndofs,
+                                                            c->nloc, c->cout0, c->P[0], c->S, c->dy);
+  else
+    grad_from_dofs_kernel<float><<<grid1(ny), 256, 0, s>>>(static_cast<const float*>(grad_z), c->d_rr, c->ndofs,
+                                                           c->nloc, c->cout0, c->P[0], c->S, c->dy);
+  GBFEM_CUDA_TRY(cudaGetLastError());
+  GBFEM_TRY(cnn_backward(c, s));
+  c->adam_t += 1;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = float(1.0 / (1.0 - std::pow(double(b1), c->adam_t)));
+  const float c2 = float(1.0 / (1.0 - std::pow(double(b2), c->adam_t)));
+  for (int i = 0; i < NLAYER; ++i) {
+    Layer& l = c->L[i];
+    adam_kernel<<<grid1(l.nw), 256, 0, s>>>(l.w, l.g, l.m, l.v, l.nw, float(lr), b1, b2, 1e-8f, c1, c2);
+  }
+  GBFEM_CUDA_TRY(cudaGetLastError());
+  return refresh_bf16(c, s);
+}
+
 int gbfem_cnn_num_params(gbfem_cnn c, int64_t* n) {
   if (!c || !n) return set_error(GBFEM_ERR_INVALID, "null argument");
   long long t = 0;
@@ -631,9 +706,12 @@ int gbfem_cnn_load(gbfem_cnn c, const char* path) {
   return cnn_copy_params(c, w.data(), 0, true);
 }
 
-int gbfem_preconditioner_learned_create(gbfem_cnn c, gbfem_preconditioner bj, gbfem_preconditioner* out) {
+int gbfem_preconditioner_learned_create(gbfem_cnn c, gbfem_preconditioner bj, gbfem_operator op,
+                                        gbfem_preconditioner* out) {
   if (!c || !out) return set_error(GBFEM_ERR_INVALID, "gbfem_preconditioner_learned_create: null argument");
   if (bj && bj->n != c->ndofs) return set_error(GBFEM_ERR_INVALID, "learned preconditioner: size mismatch");
+  if (op && (!bj || op->ndofs != c->ndofs || op->precision != bj->precision))
+    return set_error(GBFEM_ERR_INVALID, "learned preconditioner: the two-level form needs bj and a matching op");
   *out = nullptr;
   auto* pc = new (std::nothrow) gbfem_preconditioner_s();
   if (!pc) return set_error(GBFEM_ERR_INVALID, "out of host memory");
@@ -642,8 +720,18 @@ int gbfem_preconditioner_learned_create(gbfem_cnn c, gbfem_preconditioner bj, gb
   pc->n = c->ndofs;
   pc->nloc = c->nloc;
   pc->owns_data = false;
-  auto* lc = new (std::nothrow) LearnedCtx{c, bj};
+  auto* lc = new (std::nothrow) LearnedCtx{c, bj, op};
   if (!lc) { delete pc; return set_error(GBFEM_ERR_INVALID, "out of host memory"); }
+  if (op) {
+    const size_t bytes = size_t(c->ndofs) * (bj->precision == GBFEM_F64 ? 8 : 4);
+    cudaError_t e = cudaMalloc(&lc->t, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&lc->at, bytes);
+    if (e != cudaSuccess) {
+      delete lc;
+      delete pc;
+      return set_cuda_error(e, "learned preconditioner: work vectors");
+    }
+  }
   pc->ext_apply = ext_learned_apply;
   pc->ext_destroy = ext_learned_destroy;
   pc->ext_ctx = lc;

@@ -106,12 +106,14 @@ def lib():
         L.gbfem_cnn_train_step.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_double,
                                            C.POINTER(C.c_double), C.c_void_p]
         L.gbfem_cnn_num_params.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+        L.gbfem_cnn_train_step_grad.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_double,
+                                                C.c_void_p]
         L.gbfem_cnn_get_params.argtypes = [C.c_void_p, C.c_void_p]
         L.gbfem_cnn_set_params.argtypes = [C.c_void_p, C.c_void_p]
         L.gbfem_cnn_get_grads.argtypes = [C.c_void_p, C.c_void_p]
         L.gbfem_cnn_save.argtypes = [C.c_void_p, C.c_char_p]
         L.gbfem_cnn_load.argtypes = [C.c_void_p, C.c_char_p]
-        L.gbfem_preconditioner_learned_create.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]
+        L.gbfem_preconditioner_learned_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]
         L.gbfem_preconditioner_diagonal_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
         L.gbfem_preconditioner_block_jacobi_create.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
         L.gbfem_preconditioner_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -464,6 +466,10 @@ class CNN:
         check(lib().gbfem_cnn_train_step(self.handle, r.precision, r.ptr, target.ptr, lr, C.byref(l), None))
         return l.value
 
+    def train_step_grad(self, r, grad_z, lr=1e-3):
+        """Adam step for a caller-supplied gradient dL/dz of the dof-space output."""
+        check(lib().gbfem_cnn_train_step_grad(self.handle, r.precision, r.ptr, grad_z.ptr, lr, None))
+
     def params(self):
         a = np.zeros(self.num_params, dtype=np.float32)
         check(lib().gbfem_cnn_get_params(self.handle, a.ctypes.data))
@@ -484,12 +490,13 @@ class CNN:
     def load(self, path):
         check(lib().gbfem_cnn_load(self.handle, path.encode()))
 
-    def preconditioner(self, bj):
-        """z = bj(r) + NN(r), with bj as the fallback of flexible solvers."""
+    def preconditioner(self, bj, op=None):
+        """op None: z = bj(r) + NN(r); op given: z = NN(r), z += bj(r - op(z)).
+        bj is the fallback of flexible solvers."""
         h = C.c_void_p()
         check(lib().gbfem_preconditioner_learned_create(self.handle, bj.handle if bj is not None else None,
-                                                        C.byref(h)))
-        return Preconditioner(h, bj.precision if bj is not None else F64, (self, bj))
+                                                        op.handle if op is not None else None, C.byref(h)))
+        return Preconditioner(h, bj.precision if bj is not None else F64, (self, bj, op))
 
     def __del__(self):
         try:

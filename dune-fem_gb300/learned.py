@@ -36,8 +36,9 @@ def _rms(x):
     return np.sqrt(max(gbfem.dot(x, x), 0.0) / x.n)
 
 
-def make_pairs(cells, order, seed, ks=(0, 10, 40, 120, 400, 1000), inner_tol=1e-3):
-    """Training pairs (r_k, target_k) in FP32 for one kappa seed, plus the kappa field."""
+def make_pairs(cells, order, seed, ks=(0, 10, 40, 120, 400, 1000), inner_tol=1e-3, form="additive"):
+    """Training pairs (r_k, target_k) in FP32 for one kappa seed, plus the kappa field.
+    form "additive": target e_k - BJ(r_k); "twolevel": target e_k."""
     op64, op32, k64, k32, f = sipg_problem(cells, order, seed)
     bj32 = gbfem.Preconditioner.block_jacobi(op32, gbfem.F32)   # blocks from the FP32 operator
     xs = gbfem.DeviceArray(op64.size)
@@ -58,20 +59,22 @@ def make_pairs(cells, order, seed, ks=(0, 10, 40, 120, 400, 1000), inner_tol=1e-
         r = gbfem.DeviceArray(op64.size)
         op64(e, r)                              # r = A e
         r32 = gbfem.convert(r, gbfem.F32)
-        z = gbfem.DeviceArray(op32.size, gbfem.F32)
-        bj32(r32, z)
-        t = gbfem.convert(e, gbfem.F32)         # target = e - BJ(r)
-        gbfem.axpy(-1.0, z, t)
+        t = gbfem.convert(e, gbfem.F32)
+        if form == "additive":                  # target = e - BJ(r)
+            z = gbfem.DeviceArray(op32.size, gbfem.F32)
+            bj32(r32, z)
+            gbfem.axpy(-1.0, z, t)
         pairs.append((r32, t))
     return pairs, k32
 
 
-def train(cnn, cells, order, seeds, ks=(0, 10, 40, 120, 400, 1000), steps_per_pair=4, lr=1e-3, log=None):
+def train(cnn, cells, order, seeds, ks=(0, 10, 40, 120, 400, 1000), steps_per_pair=4, lr=1e-3, log=None,
+          form="additive"):
     """Online training over `seeds`; returns the per-step losses."""
     losses = []
     t0 = time.perf_counter()
     for i, seed in enumerate(seeds):
-        pairs, k32 = make_pairs(cells, order, seed, ks)
+        pairs, k32 = make_pairs(cells, order, seed, ks, form=form)
         cnn.set_kappa(k32)
         if i == 0:
             r, t = pairs[-1]
@@ -85,7 +88,44 @@ def train(cnn, cells, order, seeds, ks=(0, 10, 40, 120, 400, 1000), steps_per_pa
     return losses
 
 
-def evaluate(cnn, cells, order, seed, tol=1e-10, max_iterations=20000, plain=True):
+def train_anorm(cnn, cells, order, seeds, ks=(0, 10, 40, 120, 400, 1000), steps_per_pair=4, lr=1e-3, log=None):
+    """Online training with the energy-norm loss of the preconditioned step,
+    L = (z - e)^T A (z - e) / e^T A e with z = BJ(r) + NN(r): the quantity that
+    governs (flexible) CG convergence.  dL/dz = 2 A (z - e) / e^T A e costs one
+    FP32 operator apply per step."""
+    losses = []
+    t0 = time.perf_counter()
+    for i, seed in enumerate(seeds):
+        op64, op32, k64, k32, f = sipg_problem(cells, order, seed)
+        del op64
+        pairs, _ = make_pairs(cells, order, seed, ks, form="twolevel")   # (r, e) in FP32
+        bj32 = gbfem.Preconditioner.block_jacobi(op32, gbfem.F32)
+        cnn.set_kappa(k32)
+        if i == 0:
+            r, e = pairs[0]
+            cnn.scale = _rms(e) / _rms(r)
+        pc = cnn.preconditioner(bj32)
+        n = op32.size
+        z = gbfem.DeviceArray(n, gbfem.F32)
+        ad = gbfem.DeviceArray(n, gbfem.F32)
+        ae = gbfem.DeviceArray(n, gbfem.F32)
+        for _ in range(steps_per_pair):
+            for r, e in pairs:
+                op32(e, ae)
+                eae = gbfem.dot(e, ae)
+                pc(r, z)                          # z = BJ(r) + NN(r)
+                gbfem.axpy(-1.0, e, z)            # z <- z - e
+                op32(z, ad)
+                losses.append(gbfem.dot(z, ad) / eae)
+                gbfem.check(gbfem.lib().gbfem_scal(gbfem.F32, n, 2.0 / eae, ad.ptr, None))
+                cnn.train_step_grad(r, ad, lr)
+        if log:
+            log("seed %d (%d/%d): A-norm loss %.4e  (%.1f s)" % (seed, i + 1, len(seeds), losses[-1],
+                                                                 time.perf_counter() - t0))
+    return losses
+
+
+def evaluate(cnn, cells, order, seed, tol=1e-10, max_iterations=20000, plain=True, form="additive"):
     """Iterations and times on one held-out seed: FP64 flexible CG with the
     learned preconditioner vs FP64 block-Jacobi PCG (and unpreconditioned CG),
     plus the mixed FP32/FP64 solve with the learned preconditioner inside."""
@@ -94,7 +134,7 @@ def evaluate(cnn, cells, order, seed, tol=1e-10, max_iterations=20000, plain=Tru
     bj64 = gbfem.Preconditioner.block_jacobi(op64)
     bj32 = gbfem.Preconditioner.block_jacobi(op32, gbfem.F32)
     cnn.set_kappa(k64)
-    learned64 = cnn.preconditioner(bj64)
+    learned64 = cnn.preconditioner(bj64, op64 if form == "twolevel" else None)
     u = gbfem.DeviceArray(op64.size)
     runs = [("bj_cg", "cg", bj64), ("learned_fcg", "fcg", learned64)]
     if plain:
@@ -109,7 +149,7 @@ def evaluate(cnn, cells, order, seed, tol=1e-10, max_iterations=20000, plain=Tru
         out[name] = {"iterations": i["iterations"], "time_s": time.perf_counter() - t0,
                      "converged": i["converged"], "fallbacks": i["fallbacks"]}
     # mixed precision + learned (FP32 inner flexible CG, FP64 refinement)
-    learned32 = cnn.preconditioner(bj32)
+    learned32 = cnn.preconditioner(bj32, op32 if form == "twolevel" else None)
     for name, pc, method in (("mixed_bj", bj32, "cg"), ("mixed_learned", learned32, "fcg")):
         u.clear()
         t0 = time.perf_counter()
@@ -120,21 +160,20 @@ def evaluate(cnn, cells, order, seed, tol=1e-10, max_iterations=20000, plain=Tru
     return out
 
 
-def diagnose(cnn, cells, order, seed, ks=(0, 40, 400)):
+def diagnose(cnn, cells, order, seed, ks=(0, 40, 400), form="additive"):
     """A-norm quality of the preconditioner on held-out solver pairs:
-    ||e - z||_A / ||e||_A for z = BJ(r) and for z = BJ(r) + NN(r)."""
+    ||e - z||_A / ||e||_A for z = BJ(r) and for the learned z."""
     op64, op32, k64, k32, f = sipg_problem(cells, order, seed)
-    pairs, _ = make_pairs(cells, order, seed, ks)
+    pairs, _ = make_pairs(cells, order, seed, ks, form="twolevel")   # targets = e
     bj32 = gbfem.Preconditioner.block_jacobi(op32, gbfem.F32)
     cnn.set_kappa(k32)
+    pc = cnn.preconditioner(bj32, op32 if form == "twolevel" else None)
     out = []
-    for (r32, t32), k in zip(pairs, ks):
+    for (r32, e), k in zip(pairs, ks):
         z = gbfem.DeviceArray(op32.size, gbfem.F32)
         bj32(r32, z)
-        e = gbfem.copy(t32)             # e = target + BJ(r)
-        gbfem.axpy(1.0, z, e)
-        zn = gbfem.copy(z)
-        cnn.forward(r32, zn, accumulate=True)
+        zn = gbfem.DeviceArray(op32.size, gbfem.F32)
+        pc(r32, zn)
         res = {"k": k}
         for name, zz in (("bj", z), ("learned", zn)):
             d = gbfem.convert(e, gbfem.F64)

@@ -267,6 +267,12 @@ int gbfem_cnn_loss_grad(gbfem_cnn cnn, int precision, const void* r, const void*
 /* loss_grad followed by one Adam step (lr, beta = 0.9/0.999, eps 1e-8). */
 int gbfem_cnn_train_step(gbfem_cnn cnn, int precision, const void* r, const void* target, double lr,
                          double* loss, void* stream);
+/* One Adam step for a loss L whose gradient with respect to the network's
+ * dof-space output z = S rms(r) NN(r/rms(r)) the caller supplies (grad_z, a
+ * dof vector), e.g. the A-norm loss (z-e)^T A (z-e) / e^T A e with
+ * grad_z = 2 A (z-e) / e^T A e. */
+int gbfem_cnn_train_step_grad(gbfem_cnn cnn, int precision, const void* r, const void* grad_z, double lr,
+                              void* stream);
 int gbfem_cnn_num_params(gbfem_cnn cnn, int64_t* n);
 /* Host FP32 copies of weights / gradients, layer by layer, [taps][cout][cin]. */
 int gbfem_cnn_get_params(gbfem_cnn cnn, float* host);
@@ -276,8 +282,12 @@ int gbfem_cnn_get_grads(gbfem_cnn cnn, float* host);
  * with non-finite weights. */
 int gbfem_cnn_save(gbfem_cnn cnn, const char* path);
 int gbfem_cnn_load(gbfem_cnn cnn, const char* path);
-/* z = bj(r) + NN(r); bj is the fallback of flexible solvers (not owned). */
-int gbfem_preconditioner_learned_create(gbfem_cnn cnn, gbfem_preconditioner bj, gbfem_preconditioner* pc);
+/* op == NULL: additive form z = bj(r) + NN(r).
+ * op != NULL: two-level form z = NN(r); z += bj(r - op(z)) (the network as
+ * the coarse correction, one block-Jacobi smoothing step; one extra apply).
+ * bj is the fallback of flexible solvers.  cnn, bj and op are not owned. */
+int gbfem_preconditioner_learned_create(gbfem_cnn cnn, gbfem_preconditioner bj, gbfem_operator op,
+                                        gbfem_preconditioner* pc);
 
 /* ---- BLAS-1 on dof vectors (function/common/discretefunction.hh:781-901,
  *      function/common/scalarproducts.hh:101-127).  Reductions are
