@@ -486,7 +486,7 @@ def workload_learned(args):
     t0 = time.perf_counter()
     if args.loss == "anorm":
         losses = learned.train_anorm(net, N, p, list(range(args.train_seeds)), steps_per_pair=args.train_steps,
-                                     lr=args.lr, log=log)
+                                     lr=args.lr, log=log, form=args.form)
     else:
         losses = learned.train(net, N, p, list(range(args.train_seeds)), steps_per_pair=args.train_steps,
                                lr=args.lr, log=log, form=args.form)

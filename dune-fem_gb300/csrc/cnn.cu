@@ -87,7 +87,7 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g, 
 template <typename T>
 __global__ void assemble_input_kernel(const T* __restrict__ r, const float* __restrict__ logk,
                                       const double* __restrict__ rr, long long n, int nloc, int cin,
-                                      long long P, bf16* __restrict__ x0) {
+                                      long long P, int coarse, bf16* __restrict__ x0) {
   const double ms = rr[0] / double(n);
   const float inv = ms > 0.0 ? float(1.0 / sqrt(ms)) : 0.f;
   const long long total = P * cin;
@@ -95,7 +95,7 @@ __global__ void assemble_input_kernel(const T* __restrict__ r, const float* __re
     const int c = int(e % cin);
     const long long p = e / cin;
     float v = 0.f;
-    if (c < nloc) v = float(r[p * nloc + c]) * inv;
+    if (c < nloc) v = (coarse && c > 0) ? 0.f : float(r[p * nloc + c]) * inv;
     else if (c == nloc) v = logk[p];
     x0[e] = __float2bfloat16_rn(v);
   }
@@ -104,13 +104,13 @@ __global__ void assemble_input_kernel(const T* __restrict__ r, const float* __re
 // z[p*nloc+l] (+)= S * rms(r) * y[p][l]
 template <typename T>
 __global__ void emit_output_kernel(const float* __restrict__ y, const double* __restrict__ rr, long long n, int nloc,
-                                   int cout, long long P, float S, int accumulate, T* __restrict__ z) {
+                                   int cout, long long P, float S, int accumulate, int coarse, T* __restrict__ z) {
   const double rms = sqrt(rr[0] / double(n));
   const long long total = P * nloc;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
     const int l = int(e % nloc);
     const long long p = e / nloc;
-    const double v = double(S) * rms * double(y[p * cout + l]);
+    const double v = (coarse && l > 0) ? 0.0 : double(S) * rms * double(y[p * cout + l]);
     z[e] = accumulate ? T(double(z[e]) + v) : T(v);
   }
 }
@@ -137,13 +137,13 @@ __global__ void loss_grad_kernel(const float* __restrict__ y, const T* __restric
 // dy[p][c] = S rms(r) g[p*nloc + c] (chain rule through z = S rms(r) y); 0 on padded channels
 template <typename T>
 __global__ void grad_from_dofs_kernel(const T* __restrict__ g, const double* __restrict__ rr, long long n, int nloc,
-                                      int cout, long long P, float S, bf16* __restrict__ dy) {
+                                      int cout, long long P, float S, int coarse, bf16* __restrict__ dy) {
   const double rms = sqrt(rr[0] / double(n));
   const long long total = P * cout;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
     const int c = int(e % cout);
     const long long p = e / cout;
-    const double v = c < nloc ? double(S) * rms * double(g[p * nloc + c]) : 0.0;
+    const double v = (c < nloc && !(coarse && c > 0)) ? double(S) * rms * double(g[p * nloc + c]) : 0.0;
     dy[e] = __float2bfloat16_rn(float(v));
   }
 }
@@ -170,6 +170,7 @@ struct gbfem_cnn_s {
   long long ndofs = 0;
   float S = 1.0f;            // output scale
   int adam_t = 0;
+  int coarse = 0;            // coarse mode: input the cell means of r, output the cell means only
   Layer L[NLAYER];
   // activations (BF16, channels-last)
   bf16 *x0 = nullptr, *a0 = nullptr, *s1 = nullptr, *p1 = nullptr, *s2 = nullptr, *p2 = nullptr, *s3 = nullptr,
@@ -353,7 +354,8 @@ template <typename T>
 static int cnn_input(gbfem_cnn_s* c, const void* r, cudaStream_t s) {
   GBFEM_TRY(dot_device(sizeof(T) == 8 ? GBFEM_F64 : GBFEM_F32, c->ndofs, r, r, c->d_rr, c->d_partial, s));
   assemble_input_kernel<T><<<grid1(c->P[0] * c->cin0), 256, 0, s>>>(static_cast<const T*>(r), c->logk, c->d_rr,
-                                                                    c->ndofs, c->nloc, c->cin0, c->P[0], c->x0);
+                                                                    c->ndofs, c->nloc, c->cin0, c->P[0], c->coarse,
+                                                                    c->x0);
   GBFEM_CUDA_TRY(cudaGetLastError());
   return GBFEM_OK;
 }
@@ -364,10 +366,10 @@ static int cnn_apply(gbfem_cnn_s* c, int precision, const void* r, void* z, int 
   GBFEM_TRY(cnn_forward(c, s));
   if (precision == GBFEM_F64)
     emit_output_kernel<double><<<grid1(c->ndofs), 256, 0, s>>>(c->y, c->d_rr, c->ndofs, c->nloc, c->cout0, c->P[0],
-                                                               c->S, accumulate, static_cast<double*>(z));
+                                                               c->S, accumulate, c->coarse, static_cast<double*>(z));
   else
     emit_output_kernel<float><<<grid1(c->ndofs), 256, 0, s>>>(c->y, c->d_rr, c->ndofs, c->nloc, c->cout0, c->P[0],
-                                                              c->S, accumulate, static_cast<float*>(z));
+                                                              c->S, accumulate, c->coarse, static_cast<float*>(z));
   GBFEM_CUDA_TRY(cudaGetLastError());
   return GBFEM_OK;
 }
@@ -571,6 +573,12 @@ int gbfem_cnn_set_kappa(gbfem_cnn c, int precision, const void* kappa, void* str
   return GBFEM_OK;
 }
 
+int gbfem_cnn_set_coarse(gbfem_cnn c, int coarse) {
+  if (!c) return set_error(GBFEM_ERR_INVALID, "gbfem_cnn_set_coarse: null cnn");
+  c->coarse = coarse ? 1 : 0;
+  return GBFEM_OK;
+}
+
 int gbfem_cnn_set_output_scale(gbfem_cnn c, double scale) {
   if (!c || !(scale > 0)) return set_error(GBFEM_ERR_INVALID, "gbfem_cnn_set_output_scale: bad argument");
   c->S = float(scale);
@@ -620,10 +628,10 @@ int gbfem_cnn_train_step_grad(gbfem_cnn c, int precision, const void* r, const v
   const long long ny = c->P[0] * c->cout0;
   if (precision == GBFEM_F64)
     grad_from_dofs_kernel<double><<<grid1(ny), 256, 0, s>>>(static_cast<const double*>(grad_z), c->d_rr, c->ndofs,
-                                                            c->nloc, c->cout0, c->P[0], c->S, c->dy);
+                                                            c->nloc, c->cout0, c->P[0], c->S, c->coarse, c->dy);
   else
     grad_from_dofs_kernel<float><<<grid1(ny), 256, 0, s>>>(static_cast<const float*>(grad_z), c->d_rr, c->ndofs,
-                                                           c->nloc, c->cout0, c->P[0], c->S, c->dy);
+                                                           c->nloc, c->cout0, c->P[0], c->S, c->coarse, c->dy);
   GBFEM_CUDA_TRY(cudaGetLastError());
   GBFEM_TRY(cnn_backward(c, s));
   c->adam_t += 1;

@@ -99,6 +99,7 @@ def lib():
         L.gbfem_cnn_destroy.argtypes = [C.c_void_p]
         L.gbfem_cnn_set_kappa.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
         L.gbfem_cnn_set_output_scale.argtypes = [C.c_void_p, C.c_double]
+        L.gbfem_cnn_set_coarse.argtypes = [C.c_void_p, C.c_int]
         L.gbfem_cnn_get_output_scale.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.gbfem_cnn_forward.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
         L.gbfem_cnn_loss_grad.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_double),
@@ -452,6 +453,10 @@ class CNN:
     @scale.setter
     def scale(self, v):
         check(lib().gbfem_cnn_set_output_scale(self.handle, float(v)))
+
+    def set_coarse(self, coarse=True):
+        """Learned coarse-grid correction: cell means in, cell means out."""
+        check(lib().gbfem_cnn_set_coarse(self.handle, 1 if coarse else 0))
 
     def forward(self, r, z, accumulate=False):
         check(lib().gbfem_cnn_forward(self.handle, r.precision, r.ptr, z.ptr, 1 if accumulate else 0, None))

@@ -88,11 +88,15 @@ def train(cnn, cells, order, seeds, ks=(0, 10, 40, 120, 400, 1000), steps_per_pa
     return losses
 
 
-def train_anorm(cnn, cells, order, seeds, ks=(0, 10, 40, 120, 400, 1000), steps_per_pair=4, lr=1e-3, log=None):
+def train_anorm(cnn, cells, order, seeds, ks=(0, 10, 40, 120, 400, 1000), steps_per_pair=4, lr=1e-3, log=None,
+                form="additive"):
     """Online training with the energy-norm loss of the preconditioned step,
-    L = (z - e)^T A (z - e) / e^T A e with z = BJ(r) + NN(r): the quantity that
-    governs (flexible) CG convergence.  dL/dz = 2 A (z - e) / e^T A e costs one
-    FP32 operator apply per step."""
+    L = (z - e)^T A (z - e) / e^T A e: the quantity that governs (flexible) CG
+    convergence.  dL/dz = 2 A (z - e) / e^T A e costs one FP32 operator apply.
+      additive:  z = BJ(r) + NN(r),             dL/dNN = dL/dz
+      twolevel:  z = NN(r) + BJ(r - A NN(r)),   dL/dNN = (I - A BJ) dL/dz
+    (BJ and A symmetric); in the two-level form the network runs in coarse
+    mode (cell means in, cell means out): a learned coarse-grid correction."""
     losses = []
     t0 = time.perf_counter()
     for i, seed in enumerate(seeds):
@@ -104,20 +108,28 @@ def train_anorm(cnn, cells, order, seeds, ks=(0, 10, 40, 120, 400, 1000), steps_
         if i == 0:
             r, e = pairs[0]
             cnn.scale = _rms(e) / _rms(r)
-        pc = cnn.preconditioner(bj32)
+        twolevel = form == "twolevel"
+        cnn.set_coarse(twolevel)
+        pc = cnn.preconditioner(bj32, op32 if twolevel else None)
         n = op32.size
         z = gbfem.DeviceArray(n, gbfem.F32)
         ad = gbfem.DeviceArray(n, gbfem.F32)
         ae = gbfem.DeviceArray(n, gbfem.F32)
+        t1 = gbfem.DeviceArray(n, gbfem.F32)
+        t2 = gbfem.DeviceArray(n, gbfem.F32)
         for _ in range(steps_per_pair):
             for r, e in pairs:
                 op32(e, ae)
                 eae = gbfem.dot(e, ae)
-                pc(r, z)                          # z = BJ(r) + NN(r)
+                pc(r, z)                          # z = P(r)
                 gbfem.axpy(-1.0, e, z)            # z <- z - e
                 op32(z, ad)
                 losses.append(gbfem.dot(z, ad) / eae)
-                gbfem.check(gbfem.lib().gbfem_scal(gbfem.F32, n, 2.0 / eae, ad.ptr, None))
+                gbfem.check(gbfem.lib().gbfem_scal(gbfem.F32, n, 2.0 / eae, ad.ptr, None))   # g = dL/dz
+                if twolevel:                      # dL/dNN = g - A BJ g
+                    bj32(ad, t1)
+                    op32(t1, t2)
+                    gbfem.axpy(-1.0, t2, ad)
                 cnn.train_step_grad(r, ad, lr)
         if log:
             log("seed %d (%d/%d): A-norm loss %.4e  (%.1f s)" % (seed, i + 1, len(seeds), losses[-1],
@@ -134,6 +146,7 @@ def evaluate(cnn, cells, order, seed, tol=1e-10, max_iterations=20000, plain=Tru
     bj64 = gbfem.Preconditioner.block_jacobi(op64)
     bj32 = gbfem.Preconditioner.block_jacobi(op32, gbfem.F32)
     cnn.set_kappa(k64)
+    cnn.set_coarse(form == "twolevel")
     learned64 = cnn.preconditioner(bj64, op64 if form == "twolevel" else None)
     u = gbfem.DeviceArray(op64.size)
     runs = [("bj_cg", "cg", bj64), ("learned_fcg", "fcg", learned64)]
@@ -167,6 +180,7 @@ def diagnose(cnn, cells, order, seed, ks=(0, 40, 400), form="additive"):
     pairs, _ = make_pairs(cells, order, seed, ks, form="twolevel")   # targets = e
     bj32 = gbfem.Preconditioner.block_jacobi(op32, gbfem.F32)
     cnn.set_kappa(k32)
+    cnn.set_coarse(form == "twolevel")
     pc = cnn.preconditioner(bj32, op32 if form == "twolevel" else None)
     out = []
     for (r32, e), k in zip(pairs, ks):

@@ -256,6 +256,10 @@ int gbfem_cnn_create(int order, int cells, uint64_t seed, gbfem_cnn* cnn);
 int gbfem_cnn_destroy(gbfem_cnn cnn);
 /* Sets the log-kappa input channel from DG kappa coefficients (device; NULL = 1). */
 int gbfem_cnn_set_kappa(gbfem_cnn cnn, int precision, const void* kappa, void* stream);
+/* Coarse mode (1): the network reads only the cell means of r (coefficient 0)
+ * and log kappa, and writes only the cell means of z: a learned coarse-grid
+ * correction for the two-level form of the learned preconditioner. */
+int gbfem_cnn_set_coarse(gbfem_cnn cnn, int coarse);
 int gbfem_cnn_set_output_scale(gbfem_cnn cnn, double scale);
 int gbfem_cnn_get_output_scale(gbfem_cnn cnn, double* scale);
 /* z = S rms(r) NN(r/rms(r)) (accumulate = 1: z += ...). */

@@ -102,3 +102,48 @@ def test_learned_fcg_certifies_and_falls_back_from_a_broken_network(gb):
     op64(u, r)
     x, ff = r.numpy(), f.numpy()
     assert np.linalg.norm(ff - x) <= 1.01e-10 * np.linalg.norm(ff)
+
+
+def test_zero_network_reduces_both_forms_to_block_jacobi(gb):
+    import learned
+    cells, order = 8, 2
+    op64, op32, k64, k32, f = learned.sipg_problem(cells, order, 5)
+    bj = gb.Preconditioner.block_jacobi(op64)
+    net = gb.CNN(order, cells, seed=2)
+    net.set_kappa(k64)
+    net.set_params(np.zeros(net.num_params, dtype=np.float32))
+    r = gb.DeviceArray.from_numpy(np.random.default_rng(0).uniform(-1, 1, op64.size))
+    zb, za, zt = (gb.DeviceArray(op64.size) for _ in range(3))
+    bj(r, zb)
+    net.preconditioner(bj)(r, za)
+    net.preconditioner(bj, op64)(r, zt)
+    assert np.array_equal(za.numpy(), zb.numpy())
+    assert np.array_equal(zt.numpy(), zb.numpy())
+
+
+def test_energy_norm_training_step_lowers_the_energy_loss(gb):
+    """gbfem_cnn_train_step_grad with dL/dz = 2 A (z - e) / e^T A e."""
+    import learned
+    cells, order = 8, 2
+    op64, op32, k64, k32, f = learned.sipg_problem(cells, order, 7)
+    bj = gb.Preconditioner.block_jacobi(op32, gb.F32)
+    n = op32.size
+    rng = np.random.default_rng(1)
+    e = gb.DeviceArray.from_numpy(rng.uniform(-1, 1, n).astype(np.float32))
+    r = gb.DeviceArray(n, gb.F32)
+    op32(e, r)
+    net = gb.CNN(order, cells, seed=4)
+    net.set_kappa(k32)
+    pc = net.preconditioner(bj)
+    z, ad, ae = (gb.DeviceArray(n, gb.F32) for _ in range(3))
+    op32(e, ae)
+    eae = gb.dot(e, ae)
+    losses = []
+    for _ in range(30):
+        pc(r, z)
+        gb.axpy(-1.0, e, z)
+        op32(z, ad)
+        losses.append(gb.dot(z, ad) / eae)
+        gb.check(gb.lib().gbfem_scal(gb.F32, n, 2.0 / eae, ad.ptr, None))
+        net.train_step_grad(r, ad, 1e-3)
+    assert losses[-1] < 0.9 * losses[0]
