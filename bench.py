@@ -494,7 +494,8 @@ def workload_learned(args):
     if args.save_net:
         net.save(args.save_net)
     diag = learned.diagnose(net, N, p, 100000, form=args.form)
-    evals = [learned.evaluate(net, N, p, 100000 + s, plain=not args.skip_plain, form=args.form)
+    evals = [learned.evaluate(net, N, p, 100000 + s, plain=not args.skip_plain, form=args.form,
+                              plain_max_iterations=args.plain_max_iter)
              for s in range(args.eval_seeds)]
     def mean(key, field):
         v = [e[key][field] for e in evals if key in e]
@@ -604,6 +605,7 @@ def main():
     ap.add_argument("--save-net", default="")
     ap.add_argument("--form", default="additive", choices=["additive", "twolevel"])
     ap.add_argument("--loss", default="anorm", choices=["anorm", "mse"])
+    ap.add_argument("--plain-max-iter", type=int, default=0)
     ap.add_argument("--verbose", action="store_true")
     args = ap.parse_args()
     if args.workload != "apply":

@@ -137,7 +137,8 @@ def train_anorm(cnn, cells, order, seeds, ks=(0, 10, 40, 120, 400, 1000), steps_
     return losses
 
 
-def evaluate(cnn, cells, order, seed, tol=1e-10, max_iterations=20000, plain=True, form="additive"):
+def evaluate(cnn, cells, order, seed, tol=1e-10, max_iterations=20000, plain=True, form="additive",
+             plain_max_iterations=None):
     """Iterations and times on one held-out seed: FP64 flexible CG with the
     learned preconditioner vs FP64 block-Jacobi PCG (and unpreconditioned CG),
     plus the mixed FP32/FP64 solve with the learned preconditioner inside."""
@@ -153,7 +154,8 @@ def evaluate(cnn, cells, order, seed, tol=1e-10, max_iterations=20000, plain=Tru
     if plain:
         runs.insert(0, ("plain_cg", "cg", None))
     for name, method, pc in runs:
-        inv = gbfem.KrylovInverseOperator(method, tolerance=tol, max_iterations=max_iterations, restart=4)
+        cap = plain_max_iterations if (name == "plain_cg" and plain_max_iterations) else max_iterations
+        inv = gbfem.KrylovInverseOperator(method, tolerance=tol, max_iterations=cap, restart=4)
         inv.bind(op64, pc)
         u.clear()
         t0 = time.perf_counter()
