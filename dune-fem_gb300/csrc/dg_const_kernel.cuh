@@ -43,6 +43,8 @@ struct DgConstTablesT {
   T tr[2 * kDgMaxN];        // L_i(s)
   T dtr[2 * kDgMaxN];       // L_i'(s)
   T M[3][kDgMaxN * kDgMaxN];  // per-axis line operator (filled per operator)
+  // per-axis flux constants: A1 = |F| eps sigma, A2 = |F| eps / (2 h), A3 = |F| eps / 2
+  T A1[3], A2[3], A3[3];
 };
 
 // traces[cell][f = 2d+s][0: v, 1: d][jk], d(s) without the 1/h and normal sign
@@ -117,29 +119,37 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
     }
     cc[d] = nb;
     const long long ncell = cc[0] + (long long)args.nc[0] * (cc[1] + (long long)args.nc[1] * cc[2]);
-    const T sgnh = s ? args.invh[d] : -args.invh[d];  // (n . e_d) / h_d
+    // n.grad u = (n.e_d / h_d) d(s): the 1/h_d and the face constants are folded
+    // into A1 = |F| eps sigma, A2 = |F| eps / (2 h_d), A3 = |F| eps / 2
     const T* own = traces + cl * (12 * N2) + f * 2 * N2;
-    const T vm = __ldg(own + jk), nm = sgnh * __ldg(own + N2 + jk);
-    T vp = T(0), np = T(0);
+    const T vm = __ldg(own + jk), dm = __ldg(own + N2 + jk);
+    T vp = T(0), dp = T(0);
     if (has_nb && valid) {
       const T* nbt = traces + ncell * (12 * N2) + (2 * d + 1 - s) * 2 * N2;
       vp = __ldg(nbt + jk);
-      np = sgnh * __ldg(nbt + N2 + jk);
+      dp = __ldg(nbt + N2 + jk);
     }
-    const T F = args.faceA[d];
-    const T bn = ADV ? (s ? args.b[d] : -args.b[d]) : T(0);
+    const T a2 = s ? tabs.A2[d] : -tabs.A2[d];  // carries the normal's sign
     T val = T(0), grad = T(0);
     if (has_nb) {
+      // eps |F| (sigma J - {dn u}),  -eps |F| J / 2
       const T J = vm - vp;
-      val = F * args.eps * (args.sigma[d] * J - T(0.5) * (nm + np));
-      grad = F * args.eps * (T(-0.5) * J);
-      if (ADV) val += F * bn * (bn >= T(0) ? vm : vp);
+      val = fma(tabs.A1[d], J, -a2 * (dm + dp));
+      grad = -tabs.A3[d] * J;
+      if (ADV) {
+        const T bn = s ? args.b[d] : -args.b[d];
+        val += args.faceA[d] * bn * (bn >= T(0) ? vm : vp);
+      }
     } else {
       if (args.weak_dirichlet) {
-        val = F * args.eps * (args.sigma[d] * vm - nm);
-        grad = F * args.eps * (-vm);
+        // eps |F| (sigma u - dn u),  -eps |F| u
+        val = fma(tabs.A1[d], vm, T(-2) * a2 * dm);
+        grad = T(-2) * tabs.A3[d] * vm;
       }
-      if (ADV && bn > T(0)) val += F * bn * vm;
+      if (ADV) {
+        const T bn = s ? args.b[d] : -args.b[d];
+        if (bn > T(0)) val += args.faceA[d] * bn * vm;
+      }
     }
     sF[(c * 6 + f) * 2 * N2 + jk] = val;
     sF[(c * 6 + f) * 2 * N2 + N2 + jk] = grad;

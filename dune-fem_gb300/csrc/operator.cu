@@ -106,6 +106,12 @@ static void fill_line_operators(const gbfem_operator_s* op, DgConstTablesT<T>* c
         if (ax == 0 && i == j) m += d.mass * vol;
         ct->M[ax][i * n + j] = T(m);
       }
+  for (int ax = 0; ax < 3; ++ax) {
+    const double area = vol / h[ax];
+    ct->A1[ax] = T(area * d.diffusion * d.penalty / h[ax]);  // sigma = beta / h_F, h_F = |K| / |F| = h
+    ct->A2[ax] = T(area * d.diffusion * 0.5 / h[ax]);
+    ct->A3[ax] = T(area * d.diffusion * 0.5);
+  }
 }
 
 int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
