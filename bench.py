@@ -372,6 +372,35 @@ def workload_q1cg(args):
         rt.append(tt)
     it_rand = inv.iterations()
     t_rand = float(np.median(rt[args.warmup:]))
+    # the same solve with the device-resident loop (scalars on the device,
+    # 32 iterations per CUDA-graph launch, one host read per launch)
+    invg = gbfem.KrylovInverseOperator("cg", tolerance=1e-10, graph_chunk=32)
+    invg.bind(op, pc)
+    gt = []
+    for _ in range(args.warmup + args.steps):
+        u.clear()
+        _, tt = _timed(lambda: invg(brd, u))
+        gt.append(tt)
+    t_graph = float(np.median(gt[args.warmup:]))
+    it_graph = invg.iterations()
+    # and a small 3-D DG solve (16^3 Q2 SIPG, block-Jacobi CG), where the
+    # per-iteration host synchronisations are a large share of the iteration
+    opd = gbfem.DGOperator((16, 16, 16), 2, mass=0.1)
+    pcd = gbfem.Preconditioner.block_jacobi(opd)
+    fd = gbfem.DeviceArray.from_numpy(np.random.default_rng(SEED).uniform(-1, 1, opd.size))
+    ud = gbfem.DeviceArray(opd.size)
+    dg_small = {}
+    for name, chunk in (("host_loop", 0), ("graph32", 32)):
+        invd = gbfem.KrylovInverseOperator("cg", tolerance=1e-10, graph_chunk=chunk)
+        invd.bind(opd, pcd)
+        dt = []
+        for _ in range(args.warmup + args.steps):
+            ud.clear()
+            _, tt = _timed(lambda: invd(fd, ud))
+            dt.append(tt)
+        tm = float(np.median(dt[args.warmup:]))
+        dg_small[name] = {"ms": 1e3 * tm, "iterations": invd.iterations(),
+                          "us_per_iteration": 1e6 * tm / max(1, invd.iterations())}
     dg = oracle.q1_apply((N, N), None, 1.0, 1.0, diag_only=True)
     t0 = time.perf_counter()
     it_ref, x_ref, _ = oracle.cg(lambda v: oracle.q1_apply((N, N), v, 1.0, 1.0), b, prec=lambda r: r / dg,
@@ -382,6 +411,9 @@ def workload_q1cg(args):
             "max_nodal_error_vs_exact": err, "rel_diff_vs_oracle": float(np.max(np.abs(x - x_ref)) / np.max(np.abs(x_ref))),
             "random_rhs": {"ms": 1e3 * t_rand, "iterations": it_rand,
                            "us_per_iteration": 1e6 * t_rand / max(1, it_rand)},
+            "random_rhs_graph32": {"ms": 1e3 * t_graph, "iterations": it_graph,
+                                   "us_per_iteration": 1e6 * t_graph / max(1, it_graph)},
+            "dg_16cube_q2_bj_cg": dg_small,
             "e2e": {"value": 1e3 * te, "unit": "ms", "h2d_bytes_per_step": 8 * b.size, "d2h_bytes_per_step": 8 * b.size},
             "cpu_baseline": {"value": 1e3 * t_ref, "unit": "ms", "cores": 1, "kind": "port",
                              "sample": "whole solve: oracle CG (cg.hh restated) + oracle Q1 apply"},

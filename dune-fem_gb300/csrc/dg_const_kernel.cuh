@@ -47,16 +47,19 @@ struct DgConstTablesT {
   T A1[3], A2[3], A3[3];
 };
 
-// traces[cell][f = 2d+s][0: v, 1: d][jk], d(s) without the 1/h and normal sign
+// traces[cell][f = 2d+s][0: v, 1: d][jk], d(s) without the 1/h and normal sign,
+// for the cells [cell_begin, cell_begin + count)
 template <typename T, int N>
 __global__ void __launch_bounds__(256) dg_trace_kernel(const T* __restrict__ u, T* __restrict__ traces,
-                                                       long long ncells, const __grid_constant__ DgConstTablesT<T> tabs) {
+                                                       long long cell_begin, long long count,
+                                                       const __grid_constant__ DgConstTablesT<T> tabs) {
   constexpr int N2 = N * N, N3 = N2 * N;
-  const long long total = ncells * 3 * N2;
+  const long long total = count * 3 * N2;
   for (long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x; item < total;
        item += (long long)gridDim.x * blockDim.x) {
-    const long long cell = item / (3 * N2);
-    const int r = int(item - cell * 3 * N2);
+    const long long lc = item / (3 * N2);
+    const int r = int(item - lc * 3 * N2);
+    const long long cell = cell_begin + lc;
     const int d = r / N2, jk = r - d * N2;
     const int j = jk / N, k = jk % N;
     const int base = d == 0 ? j * N + k : (d == 1 ? j * N2 + k : j * N2 + k * N);
@@ -91,12 +94,13 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
   __shared__ T sr[CPB * N3];
   __shared__ T sF[CPB * 6 * 2 * N2];  // [cell][face][Val/Grad][jk]
   const int tid = threadIdx.x;
-  const long long ncells = args.ncells;
-  const long long c0 = (long long)blockIdx.x * CPB;
-  if (c0 >= ncells) return;
+  // output cells [cell_begin, cend); neighbours anywhere in the grid
+  const long long cend = args.cell_begin + (args.cell_count > 0 ? args.cell_count : args.ncells);
+  const long long c0 = args.cell_begin + (long long)blockIdx.x * CPB;
+  if (c0 >= cend) return;
   for (int e = tid; e < CPB * N3; e += blockDim.x) {
     const long long v = c0 + e / N3;
-    su[e] = v < ncells ? __ldg(args.u + c0 * N3 + e) : T(0);
+    su[e] = v < cend ? __ldg(args.u + c0 * N3 + e) : T(0);
   }
   // ---- faces: numerical fluxes from own and neighbour traces -----------------
   for (int item = tid; item < CPB * 6 * N2; item += blockDim.x) {
@@ -105,7 +109,7 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
     const int f = r / N2, jk = r - f * N2;
     const int d = f >> 1, s = f & 1;
     const long long cell = c0 + c;
-    const bool valid = cell < ncells;
+    const bool valid = cell < cend;
     const long long cl = valid ? cell : 0;
     const long long cz = cl / ((long long)args.nc[0] * args.nc[1]);
     const long long rem = cl - cz * (long long)args.nc[0] * args.nc[1];
@@ -190,7 +194,7 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
   }
   for (int e = tid; e < CPB * N3; e += blockDim.x) {
     const long long v = c0 + e / N3;
-    if (v < ncells) __stcs(args.w + c0 * N3 + e, sr[e]);
+    if (v < cend) __stcs(args.w + c0 * N3 + e, sr[e]);
   }
 }
 

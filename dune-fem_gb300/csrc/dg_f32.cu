@@ -7,7 +7,8 @@ int dg_launch_f32(const DgArgsT<float>& a, const DgTablesT<float>& t, int n, int
                   cudaStream_t s) {
   return dg_launch<float>(a, t, n, q, kappa, s);
 }
-int dg_const_launch_f32(const DgArgsT<float>& a, const DgConstTablesT<float>& t, int n, float* traces, cudaStream_t s) {
-  return dg_const_launch<float>(a, t, n, traces, s);
+int dg_const_launch_f32(const DgArgsT<float>& a, const DgConstTablesT<float>& t, int n, float* traces, int phase,
+                        cudaStream_t s) {
+  return dg_const_launch<float>(a, t, n, traces, phase, s);
 }
 }  // namespace gbfem

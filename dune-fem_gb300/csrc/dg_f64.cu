@@ -6,7 +6,8 @@ int dg_launch_f64(const DgArgsT<double>& a, const DgTablesT<double>& t, int n, i
                   cudaStream_t s) {
   return dg_launch<double>(a, t, n, q, kappa, s);
 }
-int dg_const_launch_f64(const DgArgsT<double>& a, const DgConstTablesT<double>& t, int n, double* traces, cudaStream_t s) {
-  return dg_const_launch<double>(a, t, n, traces, s);
+int dg_const_launch_f64(const DgArgsT<double>& a, const DgConstTablesT<double>& t, int n, double* traces, int phase,
+                        cudaStream_t s) {
+  return dg_const_launch<double>(a, t, n, traces, phase, s);
 }
 }  // namespace gbfem

@@ -202,13 +202,13 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args,
   for (int i = tid; i < 2 * N; i += blockDim.x) { str[i] = tabs.tr[i]; sdtr[i] = tabs.dtr[i]; }
 
   const long long ncells = args.ncells;
-  // In unit mode the "virtual cells" are (cell, j) pairs: vcell = cell*N3 + j,
-  // for cells in [cell_begin, cell_begin + cell_count).
+  // Cells [cell_begin, cell_begin + cell_count) (cell_count 0 = all).  In
+  // unit mode the "virtual cells" are (cell, j) pairs: vcell = cell*N3 + j;
+  // unit mode 3: (cell, f, j) = (cell*6 + f)*N3 + j.
   const long long ucount = args.cell_count > 0 ? args.cell_count : ncells;
-  // unit mode 3: virtual cells (cell, f, j) = (cell*6 + f)*N3 + j
-  const int vper = args.unit_mode == 3 ? 6 * N3 : N3;
-  const long long nvirt = args.unit_mode ? (args.cell_begin + ucount) * vper : ncells;
-  const long long v0 = (long long)blockIdx.x * CPB + (args.unit_mode ? args.cell_begin * vper : 0);
+  const int vper = args.unit_mode == 3 ? 6 * N3 : (args.unit_mode ? N3 : 1);
+  const long long nvirt = (args.cell_begin + ucount) * vper;
+  const long long v0 = (long long)blockIdx.x * CPB + args.cell_begin * vper;
   if (v0 >= nvirt) return;
 
   // ---- load own dofs (and kappa) ------------------------------------------

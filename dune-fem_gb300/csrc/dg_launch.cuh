@@ -19,7 +19,7 @@ int dg_launch_one(const DgArgsT<T>& args, const DgTablesT<T>& tabs, cudaStream_t
   GBFEM_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   constexpr int N3 = N * N * N;
   const long long ucount = args.cell_count > 0 ? args.cell_count : args.ncells;
-  const long long nvirt = args.unit_mode ? ucount * (args.unit_mode == 3 ? 6 * N3 : N3) : args.ncells;
+  const long long nvirt = args.unit_mode ? ucount * (args.unit_mode == 3 ? 6 * N3 : N3) : ucount;
   const long long blocks = (nvirt + CPB - 1) / CPB;
   if (blocks <= 0) return GBFEM_OK;
   if (blocks > 2147483647LL) return set_error(GBFEM_ERR_INVALID, "dg apply: grid too large");
@@ -46,31 +46,41 @@ int dg_launch(const DgArgsT<T>& args, const DgTablesT<T>& tabs, int n, int q, bo
   return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "dg apply: unsupported (p, q)");
 }
 
+// phase bit 1: traces of the cells [cell_begin, cell_begin + count); bit 2:
+// the apply of those cells (reads the traces of their neighbours, which must
+// be current).  count = cell_count, 0 = all cells.
 template <typename T, int N>
-int dg_const_launch_one(const DgArgsT<T>& args, const DgConstTablesT<T>& tabs, T* traces, cudaStream_t stream) {
+int dg_const_launch_one(const DgArgsT<T>& args, const DgConstTablesT<T>& tabs, T* traces, int phase,
+                        cudaStream_t stream) {
   constexpr int CPB = N <= 2 ? 32 : (N <= 4 ? 16 : 8);
-  const long long blocks = (args.ncells + CPB - 1) / CPB;
+  const long long count = args.cell_count > 0 ? args.cell_count : args.ncells;
+  const long long blocks = (count + CPB - 1) / CPB;
   if (blocks <= 0) return GBFEM_OK;
   if (blocks > 2147483647LL) return set_error(GBFEM_ERR_INVALID, "dg apply: grid too large");
-  const long long titems = args.ncells * 3 * N * N;
-  long long tblocks = (titems + 255) / 256;
-  if (tblocks > 152LL * 32) tblocks = 152LL * 32;
-  dg_trace_kernel<T, N><<<unsigned(tblocks), 256, 0, stream>>>(args.u, traces, args.ncells, tabs);
-  if (args.advect)
-    dg_const_kernel<T, N, CPB, true><<<unsigned(blocks), 256, 0, stream>>>(args, traces, tabs);
-  else
-    dg_const_kernel<T, N, CPB, false><<<unsigned(blocks), 256, 0, stream>>>(args, traces, tabs);
+  if (phase & 1) {
+    const long long titems = count * 3 * N * N;
+    long long tblocks = (titems + 255) / 256;
+    if (tblocks > 152LL * 32) tblocks = 152LL * 32;
+    dg_trace_kernel<T, N><<<unsigned(tblocks), 256, 0, stream>>>(args.u, traces, args.cell_begin, count, tabs);
+  }
+  if (phase & 2) {
+    if (args.advect)
+      dg_const_kernel<T, N, CPB, true><<<unsigned(blocks), 256, 0, stream>>>(args, traces, tabs);
+    else
+      dg_const_kernel<T, N, CPB, false><<<unsigned(blocks), 256, 0, stream>>>(args, traces, tabs);
+  }
   GBFEM_CUDA_TRY(cudaGetLastError());
   return GBFEM_OK;
 }
 
 template <typename T>
-int dg_const_launch(const DgArgsT<T>& args, const DgConstTablesT<T>& tabs, int n, T* traces, cudaStream_t stream) {
+int dg_const_launch(const DgArgsT<T>& args, const DgConstTablesT<T>& tabs, int n, T* traces, int phase,
+                    cudaStream_t stream) {
   switch (n) {
-    case 2: return dg_const_launch_one<T, 2>(args, tabs, traces, stream);
-    case 3: return dg_const_launch_one<T, 3>(args, tabs, traces, stream);
-    case 4: return dg_const_launch_one<T, 4>(args, tabs, traces, stream);
-    case 5: return dg_const_launch_one<T, 5>(args, tabs, traces, stream);
+    case 2: return dg_const_launch_one<T, 2>(args, tabs, traces, phase, stream);
+    case 3: return dg_const_launch_one<T, 3>(args, tabs, traces, phase, stream);
+    case 4: return dg_const_launch_one<T, 4>(args, tabs, traces, phase, stream);
+    case 5: return dg_const_launch_one<T, 5>(args, tabs, traces, phase, stream);
   }
   return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "dg apply: unsupported order");
 }

@@ -114,6 +114,7 @@ extern "C" int gbfem_operator_assemble(gbfem_operator op, gbfem_operator* out) {
   *a = *op;
   a->kind = OpKind::BSR;
   a->host_u = a->host_w = nullptr;
+  a->pipe = nullptr;
   a->bsr_blocks = nullptr;
   a->bsr_col = nullptr;
   a->trace_buf = nullptr;

@@ -6,6 +6,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "dg_kernel.cuh"
 #include "gbfem_internal.cuh"
@@ -16,8 +17,8 @@ namespace gbfem {
 
 int dg_launch_f64(const DgArgsT<double>&, const DgTablesT<double>&, int, int, bool, cudaStream_t);
 int dg_launch_f32(const DgArgsT<float>&, const DgTablesT<float>&, int, int, bool, cudaStream_t);
-int dg_const_launch_f64(const DgArgsT<double>&, const DgConstTablesT<double>&, int, double*, cudaStream_t);
-int dg_const_launch_f32(const DgArgsT<float>&, const DgConstTablesT<float>&, int, float*, cudaStream_t);
+int dg_const_launch_f64(const DgArgsT<double>&, const DgConstTablesT<double>&, int, double*, int, cudaStream_t);
+int dg_const_launch_f32(const DgArgsT<float>&, const DgConstTablesT<float>&, int, float*, int, cudaStream_t);
 
 // Trace buffer of the closed-form kernel: [cell][6 faces][v|d][n^2], allocated
 // on the first apply of an operator.
@@ -115,7 +116,7 @@ static void fill_line_operators(const gbfem_operator_s* op, DgConstTablesT<T>* c
 }
 
 int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
-             void* blocks, long long cell_begin, long long cell_count) {
+             void* blocks, long long cell_begin, long long cell_count, int phase) {
   if (op->precision == GBFEM_F64) {
     DgArgsT<double> a;
     fill_dg_args(op, &a);
@@ -130,7 +131,7 @@ int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s,
       fill_line_operators(op, &ct);
       void* tb = nullptr;
       GBFEM_TRY(trace_buffer(op, &tb));
-      return dg_const_launch_f64(a, ct, op->n, static_cast<double*>(tb), s);
+      return dg_const_launch_f64(a, ct, op->n, static_cast<double*>(tb), phase, s);
     }
     return dg_launch_f64(a, op->tab64, op->n, op->q, op->dg.kappa != nullptr, s);
   } else {
@@ -147,7 +148,7 @@ int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s,
       fill_line_operators(op, &ct);
       void* tb = nullptr;
       GBFEM_TRY(trace_buffer(op, &tb));
-      return dg_const_launch_f32(a, ct, op->n, static_cast<float*>(tb), s);
+      return dg_const_launch_f32(a, ct, op->n, static_cast<float*>(tb), phase, s);
     }
     return dg_launch_f32(a, op->tab32, op->n, op->q, op->dg.kappa != nullptr, s);
   }
@@ -252,6 +253,118 @@ static int check_grid(const gbfem_grid_desc* g, int want_dim) {
   return GBFEM_OK;
 }
 
+namespace gbfem {
+
+// Streams and events of the pipelined host-buffer apply.
+struct HostPipe {
+  cudaStream_t in = nullptr, comp = nullptr, out = nullptr;
+  cudaEvent_t start = nullptr;
+  std::vector<cudaEvent_t> ev_in, ev_comp;
+};
+
+void destroy_host_pipe(HostPipe* p) {
+  if (!p) return;
+  for (cudaEvent_t e : p->ev_in) cudaEventDestroy(e);
+  for (cudaEvent_t e : p->ev_comp) cudaEventDestroy(e);
+  if (p->start) cudaEventDestroy(p->start);
+  if (p->in) cudaStreamDestroy(p->in);
+  if (p->comp) cudaStreamDestroy(p->comp);
+  if (p->out) cudaStreamDestroy(p->out);
+  delete p;
+}
+
+static int host_pipe(gbfem_operator_s* op, int nchunks, HostPipe** out) {
+  if (!op->pipe) {
+    op->pipe = new (std::nothrow) HostPipe();
+    if (!op->pipe) return set_error(GBFEM_ERR_INVALID, "out of host memory");
+    HostPipe* p = op->pipe;
+    GBFEM_CUDA_TRY(cudaStreamCreateWithFlags(&p->in, cudaStreamNonBlocking));
+    GBFEM_CUDA_TRY(cudaStreamCreateWithFlags(&p->comp, cudaStreamNonBlocking));
+    GBFEM_CUDA_TRY(cudaStreamCreateWithFlags(&p->out, cudaStreamNonBlocking));
+    GBFEM_CUDA_TRY(cudaEventCreateWithFlags(&p->start, cudaEventDisableTiming));
+  }
+  HostPipe* p = op->pipe;
+  while (int(p->ev_in.size()) < nchunks) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    GBFEM_CUDA_TRY(cudaEventCreateWithFlags(&a, cudaEventDisableTiming));
+    p->ev_in.push_back(a);
+    GBFEM_CUDA_TRY(cudaEventCreateWithFlags(&b, cudaEventDisableTiming));
+    p->ev_comp.push_back(b);
+  }
+  *out = p;
+  return GBFEM_OK;
+}
+
+// Host-buffer apply of a DG operator, pipelined over slabs of whole z-planes
+// (a slab is a contiguous range of cells and dofs): the host-to-device copy
+// of slab k+1, the apply of slab k and the device-to-host copy of slab k-1
+// run at the same time on three streams.  The apply of a slab needs its
+// z-neighbours' data (their traces for the closed-form kernel, their dofs for
+// the quadrature kernel), so it is issued once the next slab has arrived; with
+// periodic z, slab 0 also needs the last slab and is applied last.  Each cell
+// is computed by the same kernel code as the one-shot apply, so the result is
+// bitwise the same.
+int dg_apply_host_pipelined(gbfem_operator_s* op, const void* u_host, void* w_host) {
+  const size_t es = op->precision == GBFEM_F64 ? 8 : 4;
+  const int nz = op->dg.grid.cells[2];
+  const long long plane = (long long)op->dg.grid.cells[0] * op->dg.grid.cells[1];
+  int nchunks = op->host_chunks;
+  if (nchunks <= 0) {
+    // about 16 slabs, each large enough to fill the GPU (>= 8192 cells)
+    const long long by_size = op->ncells / 8192;
+    nchunks = int(by_size < 16 ? (by_size < 1 ? 1 : by_size) : 16);
+  }
+  if (nchunks > nz) nchunks = nz;
+  if (nchunks > 64) nchunks = 64;
+  const int zper = (nz + nchunks - 1) / nchunks;
+  nchunks = (nz + zper - 1) / zper;
+  HostPipe* p = nullptr;
+  GBFEM_TRY(host_pipe(op, nchunks, &p));
+  const size_t cell_bytes = size_t(op->nloc) * es;
+  auto first_cell = [&](int k) { return (long long)k * zper * plane; };
+  auto cell_count = [&](int k) {
+    const long long z1 = (long long)(k + 1) * zper < nz ? (long long)(k + 1) * zper : nz;
+    return (z1 - (long long)k * zper) * plane;
+  };
+  // order after the work already queued on the legacy default stream
+  GBFEM_CUDA_TRY(cudaEventRecord(p->start, 0));
+  GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->in, p->start, 0));
+  GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->comp, p->start, 0));
+  GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->out, p->start, 0));
+  for (int k = 0; k < nchunks; ++k) {
+    const size_t off = size_t(first_cell(k)) * cell_bytes;
+    GBFEM_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(op->host_u) + off, static_cast<const char*>(u_host) + off,
+                                   size_t(cell_count(k)) * cell_bytes, cudaMemcpyHostToDevice, p->in));
+    GBFEM_CUDA_TRY(cudaEventRecord(p->ev_in[k], p->in));
+  }
+  const bool traces = op->coefficient_space;
+  auto apply = [&](int j) -> int {
+    GBFEM_TRY(dg_apply(op, op->host_u, op->host_w, p->comp, 0, nullptr, first_cell(j), cell_count(j), 2));
+    GBFEM_CUDA_TRY(cudaEventRecord(p->ev_comp[j], p->comp));
+    GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->out, p->ev_comp[j], 0));
+    const size_t off = size_t(first_cell(j)) * cell_bytes;
+    GBFEM_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(w_host) + off, static_cast<const char*>(op->host_w) + off,
+                                   size_t(cell_count(j)) * cell_bytes, cudaMemcpyDeviceToHost, p->out));
+    return GBFEM_OK;
+  };
+  const bool defer0 = op->dg.grid.periodic[2] && nchunks > 1;
+  int rc = GBFEM_OK;
+  for (int k = 0; k < nchunks && rc == GBFEM_OK; ++k) {
+    GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->comp, p->ev_in[k], 0));
+    if (traces) rc = dg_apply(op, op->host_u, nullptr, p->comp, 0, nullptr, first_cell(k), cell_count(k), 1);
+    if (rc == GBFEM_OK && k >= 1 && !(k == 1 && defer0)) rc = apply(k - 1);
+  }
+  if (rc == GBFEM_OK && !(nchunks == 1 && defer0)) rc = apply(nchunks - 1);
+  if (rc == GBFEM_OK && defer0) rc = apply(0);
+  // every slab's copy-out waited on its apply: the out stream ends last
+  const cudaError_t e = cudaStreamSynchronize(p->out);
+  GBFEM_TRY(rc);
+  if (e != cudaSuccess) return set_cuda_error(e, "gbfem_operator_apply_host");
+  return GBFEM_OK;
+}
+
+}  // namespace gbfem
+
 extern "C" {
 
 int gbfem_dg_operator_create(const gbfem_dg_desc* desc, gbfem_operator* out) {
@@ -325,6 +438,7 @@ int gbfem_q1_operator_create(const gbfem_grid_desc* grid, int precision, double 
 
 int gbfem_operator_destroy(gbfem_operator op) {
   if (!op) return GBFEM_OK;
+  if (op->pipe) destroy_host_pipe(op->pipe);
   if (op->host_u) cudaFree(op->host_u);
   if (op->host_w) cudaFree(op->host_w);
   if (op->bsr_blocks) cudaFree(op->bsr_blocks);
@@ -362,10 +476,17 @@ int gbfem_operator_apply_host(gbfem_operator op, const void* u_host, void* w_hos
     GBFEM_CUDA_TRY(cudaMalloc(&op->host_u, bytes));
     GBFEM_CUDA_TRY(cudaMalloc(&op->host_w, bytes));
   }
+  if (op->kind == OpKind::DG) return dg_apply_host_pipelined(op, u_host, w_host);
   GBFEM_CUDA_TRY(cudaMemcpyAsync(op->host_u, u_host, bytes, cudaMemcpyHostToDevice, 0));
   GBFEM_TRY(gbfem_operator_apply(op, op->host_u, op->host_w, nullptr));
   GBFEM_CUDA_TRY(cudaMemcpyAsync(w_host, op->host_w, bytes, cudaMemcpyDeviceToHost, 0));
   GBFEM_CUDA_TRY(cudaStreamSynchronize(0));
+  return GBFEM_OK;
+}
+
+int gbfem_operator_set_host_chunks(gbfem_operator op, int nchunks) {
+  if (!op || nchunks < 0) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_set_host_chunks: invalid argument");
+  op->host_chunks = nchunks;
   return GBFEM_OK;
 }
 

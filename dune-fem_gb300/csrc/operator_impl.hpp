@@ -15,13 +15,19 @@ struct Q1Element {
   double K[16];
 };
 
-// unit_mode 0: w = A u; 1: diagonal blocks of cells [cell_begin, cell_begin+cell_count)
-// (cell_count 0 = all) into blocks; 2: the diagonal into blocks.
+// unit_mode 0: w = A u on the cells [cell_begin, cell_begin+cell_count)
+// (cell_count 0 = all); 1: diagonal blocks of those cells into blocks; 2: the
+// diagonal into blocks.  phase (unit mode 0 of the closed-form kernel): bit 1
+// computes the face traces of the cells, bit 2 the apply (which reads the
+// traces of the neighbours); the other kernels ignore it.
 int dg_apply(const struct ::gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
-             void* blocks, long long cell_begin = 0, long long cell_count = 0);
+             void* blocks, long long cell_begin = 0, long long cell_count = 0, int phase = 3);
 int q1_apply(const struct ::gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int diag_only);
 // assembled operator: y = A x (diag_only: the diagonal into y)
 int bsr_apply(const struct ::gbfem_operator_s* op, const void* x, void* y, cudaStream_t s, int diag_only);
+struct HostPipe;
+void destroy_host_pipe(HostPipe* p);
+int dg_apply_host_pipelined(struct ::gbfem_operator_s* op, const void* u_host, void* w_host);
 
 }  // namespace gbfem
 
@@ -45,4 +51,6 @@ struct gbfem_operator_s {
   void* trace_buf = nullptr;    // closed-form kernel: face traces [cell][6][2][n^2]
   void* host_u = nullptr;  // device staging of gbfem_operator_apply_host
   void* host_w = nullptr;
+  int host_chunks = 0;     // z-slab chunks of the pipelined host apply (0 = automatic)
+  gbfem::HostPipe* pipe = nullptr;  // its streams and events
 };

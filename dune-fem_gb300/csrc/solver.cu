@@ -332,9 +332,172 @@ static int cg(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_par
     }
     if (prm.verbose) std::printf("gbfem CG it: %d : residual %.6e\n", it, std::sqrt(std::fabs(residual)));
   }
+  if (!finite(residual)) info->status = GBFEM_ERR_NONFINITE;  // a NaN ends the loop above as if converged
   info->residual = std::sqrt(std::fabs(residual));
   info->iterations = it < prm.max_iterations ? it : -it;
   info->converged = (it < prm.max_iterations && info->status == GBFEM_OK) ? 1 : 0;
+  return GBFEM_OK;
+}
+
+// ------------------------------------------------ CG, device-resident loop ---
+// The same statements as cg() above, with the Krylov scalars in device memory
+// (written by single-thread kernels) and the vector updates predicated on an
+// "active" flag, so chunks of `chunk` iterations can be captured once into a
+// CUDA graph and relaunched; the host reads the convergence flag once per
+// chunk instead of synchronising on every scalar product.  Divisions and
+// updates are the host loop's, so the iterates are identical.
+enum { DS_RES = 0, DS_PREV, DS_QH, DS_NEW, DS_ALPHA, DS_BETA, DS_TOL, DS_ACTIVE, DS_DIR, DS_CONV, DS_IT, DS_MAX,
+       DS_STATUS, DS_N };
+
+__global__ void k_cg_begin(double* ds) {
+  const bool conv = ds[DS_CONV] != 0.0;
+  ds[DS_ACTIVE] = conv ? 0.0 : 1.0;
+  ds[DS_DIR] = (!conv && ds[DS_IT] > 0.0) ? 1.0 : 0.0;
+  ds[DS_BETA] = (!conv && ds[DS_IT] > 0.0) ? ds[DS_RES] / ds[DS_PREV] : 0.0;
+}
+__global__ void k_cg_alpha(double* ds) {
+  if (ds[DS_ACTIVE] == 0.0) return;
+  const double alpha = ds[DS_RES] / ds[DS_QH];
+  if (!isfinite(alpha)) {
+    ds[DS_STATUS] = 1.0;
+    ds[DS_CONV] = 1.0;
+    ds[DS_ACTIVE] = 0.0;
+    return;
+  }
+  ds[DS_ALPHA] = alpha;
+}
+__global__ void k_cg_end(double* ds) {
+  if (ds[DS_ACTIVE] == 0.0) return;
+  ds[DS_PREV] = ds[DS_RES];
+  ds[DS_RES] = ds[DS_NEW];
+  ds[DS_IT] += 1.0;
+  if (!(ds[DS_RES] > ds[DS_TOL]) || ds[DS_IT] >= ds[DS_MAX]) ds[DS_CONV] = 1.0;
+  if (!isfinite(ds[DS_RES])) { ds[DS_STATUS] = 1.0; ds[DS_CONV] = 1.0; }
+}
+// y = a*x + beta*y with beta from ds (direction update), if ds[DS_DIR]
+template <typename T>
+__global__ void k_cg_dir(long long n, double a, const T* __restrict__ x, T* __restrict__ y, const double* ds) {
+  if (ds[DS_DIR] == 0.0) return;
+  const T b = T(ds[DS_BETA]);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = T(a) * x[i] + b * y[i];
+}
+// x += alpha q;  v += sv*alpha h  (v = p with sv = -1, or r with sv = +1), if active
+template <typename T>
+__global__ void k_cg_update(long long n, const T* __restrict__ q, const T* __restrict__ h, T* __restrict__ x,
+                            T* __restrict__ v, double sv, const double* ds) {
+  if (ds[DS_ACTIVE] == 0.0) return;
+  const T alpha = T(ds[DS_ALPHA]);
+  const T sa = T(sv * ds[DS_ALPHA]);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    x[i] = alpha * q[i] + T(1) * x[i];
+    v[i] = sa * h[i] + T(1) * v[i];
+  }
+}
+
+static int cg_device(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_params& prm, const void* b,
+                     void* x, Ctx& c, gbfem_solver_info* info) {
+  Vecs tmp;
+  GBFEM_TRY(tmp.alloc(pc ? 5 : 3, c.bytes()));
+  void* h = tmp[0];
+  void* r = tmp[1];
+  void* p = tmp[2];
+  void* s = pc ? tmp[3] : p;
+  void* q = pc ? tmp[4] : p;
+  double* ds = nullptr;
+  GBFEM_CUDA_TRY(cudaMalloc(&ds, sizeof(double) * DS_N));
+  struct Free { double* p; ~Free() { cudaFree(p); } } free_ds{ds};
+  // set-up, as cg(): h = A x, r = h - b, p = b - h, q = s = P p
+  GBFEM_TRY(op_apply(op, x, h, c));
+  GBFEM_TRY(c.copy(h, r));
+  GBFEM_TRY(c.axpby(-1.0, b, 1.0, r));
+  GBFEM_TRY(c.copy(b, p));
+  GBFEM_TRY(c.axpby(-1.0, h, 1.0, p));
+  if (pc) {
+    GBFEM_TRY(pc_apply(pc, p, q, c));
+    GBFEM_TRY(c.copy(q, s));
+  }
+  double residual = 0.0, bb = 1.0;
+  GBFEM_TRY(c.dot(p, q, &residual));
+  if (prm.error_measure == GBFEM_TOL_RELATIVE) GBFEM_TRY(c.dot(b, b, &bb));
+  const double tolerance = prm.tolerance * prm.tolerance *
+                           (prm.error_measure == GBFEM_TOL_RELATIVE ? bb
+                            : prm.error_measure == GBFEM_TOL_RESIDUAL_REDUCTION ? residual : 1.0);
+  double h0[DS_N] = {};
+  h0[DS_RES] = residual;
+  h0[DS_TOL] = tolerance;
+  h0[DS_MAX] = double(prm.max_iterations);
+  h0[DS_CONV] = (residual > tolerance && 0 < prm.max_iterations) ? 0.0 : 1.0;
+  if (!finite(residual) || !finite(tolerance)) { h0[DS_CONV] = 1.0; h0[DS_STATUS] = 1.0; }
+  GBFEM_CUDA_TRY(cudaMemcpyAsync(ds, h0, sizeof(h0), cudaMemcpyHostToDevice, c.s));
+  // one iteration, as a function of the stream
+  const long long n = c.n;
+  const int g = stream_grid(n);
+  auto iteration = [&](cudaStream_t st) -> int {
+    k_cg_begin<<<1, 1, 0, st>>>(ds);
+    if (c.prec == GBFEM_F64) {
+      if (pc) k_cg_dir<double><<<g, 256, 0, st>>>(n, 1.0, (const double*)s, (double*)q, ds);
+      else k_cg_dir<double><<<g, 256, 0, st>>>(n, -1.0, (const double*)r, (double*)p, ds);
+    } else {
+      if (pc) k_cg_dir<float><<<g, 256, 0, st>>>(n, 1.0, (const float*)s, (float*)q, ds);
+      else k_cg_dir<float><<<g, 256, 0, st>>>(n, -1.0, (const float*)r, (float*)p, ds);
+    }
+    GBFEM_TRY(gbfem_operator_apply(op, q, h, st));
+    GBFEM_TRY(dot_device(c.prec, n, q, h, ds + DS_QH, c.d_partial, st));
+    k_cg_alpha<<<1, 1, 0, st>>>(ds);
+    void* v = pc ? p : r;
+    const double sv = pc ? -1.0 : 1.0;
+    if (c.prec == GBFEM_F64)
+      k_cg_update<double><<<g, 256, 0, st>>>(n, (const double*)q, (const double*)h, (double*)x, (double*)v, sv, ds);
+    else
+      k_cg_update<float><<<g, 256, 0, st>>>(n, (const float*)q, (const float*)h, (float*)x, (float*)v, sv, ds);
+    if (pc) {
+      GBFEM_TRY(precond_apply(pc, p, s, st));
+      GBFEM_TRY(dot_device(c.prec, n, p, s, ds + DS_NEW, c.d_partial, st));
+    } else {
+      GBFEM_TRY(dot_device(c.prec, n, r, r, ds + DS_NEW, c.d_partial, st));
+    }
+    k_cg_end<<<1, 1, 0, st>>>(ds);
+    GBFEM_CUDA_TRY(cudaGetLastError());
+    return GBFEM_OK;
+  };
+  // capture `chunk` iterations into a graph on a private stream
+  const int chunk = prm.graph_chunk > 0 ? prm.graph_chunk : 16;
+  cudaStream_t st = nullptr;
+  GBFEM_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  struct FreeStream { cudaStream_t s; ~FreeStream() { cudaStreamDestroy(s); } } free_st{st};
+  GBFEM_CUDA_TRY(cudaStreamSynchronize(c.s));
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  GBFEM_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+  int rc = GBFEM_OK;
+  for (int k = 0; k < chunk && rc == GBFEM_OK; ++k) rc = iteration(st);
+  cudaError_t e = cudaStreamEndCapture(st, &graph);
+  if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+  if (e != cudaSuccess) return set_cuda_error(e, "cg graph capture");
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return set_cuda_error(e, "cg graph instantiate");
+  struct FreeExec { cudaGraphExec_t g; ~FreeExec() { cudaGraphExecDestroy(g); } } free_exec{exec};
+  double hs[DS_N];
+  int launches = 0;
+  while (true) {
+    GBFEM_CUDA_TRY(cudaMemcpyAsync(hs, ds, sizeof(hs), cudaMemcpyDeviceToHost, st));
+    GBFEM_CUDA_TRY(cudaStreamSynchronize(st));
+    if (hs[DS_CONV] != 0.0) break;
+    GBFEM_CUDA_TRY(cudaGraphLaunch(exec, st));
+    ++launches;
+    if (prm.verbose) std::printf("gbfem CG (graph) it: %d : residual %.6e\n", int(hs[DS_IT]), std::sqrt(hs[DS_RES]));
+  }
+  const int it = int(hs[DS_IT]);
+  if (hs[DS_STATUS] != 0.0) info->status = GBFEM_ERR_NONFINITE;
+  info->residual = std::sqrt(std::fabs(hs[DS_RES]));
+  info->iterations = it < prm.max_iterations ? it : -it;
+  info->converged = (it < prm.max_iterations && info->status == GBFEM_OK) ? 1 : 0;
+  // applies launched: the set-up's plus every captured iteration (the ones
+  // after convergence recompute unchanged vectors and are not counted in `it`)
+  c.op_applies += chunk * launches + 1;
+  c.pc_applies += pc ? chunk * launches + 1 : 0;
   return GBFEM_OK;
 }
 
@@ -609,7 +772,12 @@ int solve_impl(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_pa
   const auto t0 = std::chrono::steady_clock::now();
   int rc;
   switch (prm.method) {
-    case GBFEM_SOLVER_CG: rc = cg(op, pc, prm, f, u, c, info); break;
+    case GBFEM_SOLVER_CG:
+      // device-resident loop unless the preconditioner is external (its apply
+      // may synchronise the host, which a graph capture cannot hold)
+      rc = (prm.graph_chunk > 0 && !(pc && pc->kind == PcKind::External)) ? cg_device(op, pc, prm, f, u, c, info)
+                                                                          : cg(op, pc, prm, f, u, c, info);
+      break;
     case GBFEM_SOLVER_GMRES: rc = gmres(op, pc, prm, f, u, c, info, false); break;
     case GBFEM_SOLVER_FGMRES: rc = gmres(op, pc, prm, f, u, c, info, true); break;
     case GBFEM_SOLVER_BICGSTAB: rc = bicgstab(op, pc, prm, f, u, c, info); break;
@@ -637,6 +805,7 @@ int gbfem_solver_params_default(gbfem_solver_params* prm) {
   prm->max_iterations = INT_MAX;
   prm->restart = 20;
   prm->verbose = 0;
+  prm->graph_chunk = 0;
   return GBFEM_OK;
 }
 

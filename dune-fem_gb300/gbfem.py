@@ -40,7 +40,7 @@ class DgDesc(C.Structure):
 
 class SolverParams(C.Structure):
     _fields_ = [("method", C.c_int), ("tolerance", C.c_double), ("error_measure", C.c_int),
-                ("max_iterations", C.c_int), ("restart", C.c_int), ("verbose", C.c_int)]
+                ("max_iterations", C.c_int), ("restart", C.c_int), ("verbose", C.c_int), ("graph_chunk", C.c_int)]
 
 
 class SolverInfo(C.Structure):
@@ -80,6 +80,7 @@ def lib():
         L.gbfem_memset.argtypes = [C.c_void_p, C.c_int, C.c_size_t]
         L.gbfem_operator_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.gbfem_operator_apply_host.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.gbfem_operator_set_host_chunks.argtypes = [C.c_void_p, C.c_int]
         L.gbfem_operator_diagonal.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.gbfem_operator_block_diagonal.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.gbfem_operator_destroy.argtypes = [C.c_void_p]
@@ -203,6 +204,10 @@ class Operator:
         """Host-buffer apply: copies u in, applies, copies w out (synchronous)."""
         check(lib().gbfem_operator_apply_host(self.handle, u.ctypes.data, w.ctypes.data))
 
+    def set_host_chunks(self, nchunks):
+        """Slabs of the pipelined host-buffer apply of a DG operator (0 = automatic)."""
+        check(lib().gbfem_operator_set_host_chunks(self.handle, nchunks))
+
     def diagonal(self):
         d = DeviceArray(self.size, self.precision)
         check(lib().gbfem_operator_diagonal(self.handle, d.ptr, None))
@@ -318,7 +323,7 @@ class Preconditioner:
 
 
 def solver_params(method="cg", tolerance=1e-8, error_measure=RELATIVE, max_iterations=None, restart=20,
-                  verbose=False):
+                  verbose=False, graph_chunk=0):
     p = SolverParams()
     check(lib().gbfem_solver_params_default(C.byref(p)))
     p.method = METHODS[method] if isinstance(method, str) else method
@@ -328,6 +333,7 @@ def solver_params(method="cg", tolerance=1e-8, error_measure=RELATIVE, max_itera
         p.max_iterations = max_iterations
     p.restart = restart
     p.verbose = 1 if verbose else 0
+    p.graph_chunk = graph_chunk
     return p
 
 
@@ -337,8 +343,8 @@ class KrylovInverseOperator:
     bind(op[, precond]), __call__(f, u), iterations(), info()."""
 
     def __init__(self, method="cg", tolerance=1e-8, error_measure=RELATIVE, max_iterations=None, restart=20,
-                 verbose=False):
-        self.params = solver_params(method, tolerance, error_measure, max_iterations, restart, verbose)
+                 verbose=False, graph_chunk=0):
+        self.params = solver_params(method, tolerance, error_measure, max_iterations, restart, verbose, graph_chunk)
         self.op = None
         self.precond = None
         self._info = SolverInfo()
@@ -370,12 +376,13 @@ class KrylovInverseOperator:
 
 
 def solve_mixed(op64, op32, pc32, f, u, tolerance=1e-10, max_outer=50, inner_method="cg", inner_tolerance=1e-4,
-                inner_max_iterations=100000, inner_restart=20, verbose=False):
+                inner_max_iterations=100000, inner_restart=20, verbose=False, graph_chunk=0):
     """FP64 iterative refinement around an FP32 inner Krylov solve."""
     p = IRParams()
     p.tolerance = tolerance
     p.max_outer = max_outer
-    p.inner = solver_params(inner_method, inner_tolerance, RELATIVE, inner_max_iterations, inner_restart, verbose)
+    p.inner = solver_params(inner_method, inner_tolerance, RELATIVE, inner_max_iterations, inner_restart, verbose,
+                            graph_chunk)
     info = SolverInfo()
     check(lib().gbfem_solve_mixed(op64.handle, op32.handle, pc32.handle if pc32 is not None else None,
                                   C.byref(p), f.ptr, u.ptr, C.byref(info)))

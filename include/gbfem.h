@@ -112,8 +112,15 @@ int gbfem_operator_precision(gbfem_operator op, int* precision);
  * gbfem_operator_size elements of the operator's precision; must not alias. */
 int gbfem_operator_apply(gbfem_operator op, const void* u, void* w, void* stream);
 /* Same as gbfem_operator_apply with host arrays: copies u to the device,
- * applies, copies w back, synchronously.  Device buffers are cached in op. */
+ * applies, copies w back, synchronously.  Device buffers are cached in op.
+ * DG operators pipeline the call over slabs of z-planes (copy in, apply and
+ * copy out of successive slabs overlap on three streams); with page-locked
+ * host arrays the copies run concurrently.  The result is bitwise that of
+ * gbfem_operator_apply. */
 int gbfem_operator_apply_host(gbfem_operator op, const void* u_host, void* w_host);
+/* Number of slabs of the pipelined gbfem_operator_apply_host (0 = automatic:
+ * up to 16, each >= 8192 cells; capped at the number of z-planes and 64). */
+int gbfem_operator_set_host_chunks(gbfem_operator op, int nchunks);
 
 /* Diagonal of the operator's matrix.  ≙ DifferentiableOperator::jacobian
  * (operator/common/differentiableoperator.hh:54) followed by
@@ -177,6 +184,8 @@ typedef struct {
   int max_iterations;  /* fem.solver.maxiterations */
   int restart;         /* fem.solver.gmres.restart; FCG: directions kept */
   int verbose;         /* print per-iteration residuals to stdout */
+  int graph_chunk;     /* CG only: > 0 runs the loop device-resident, chunks of this many
+                          iterations captured in a CUDA graph; 0 = host loop.  Same iterates. */
 } gbfem_solver_params;
 
 typedef struct {

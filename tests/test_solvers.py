@@ -173,3 +173,41 @@ def test_assembled_matrix_times_vector_equals_matrix_free_apply(gb, orc, kw):
                      restart=10)
     assert info["converged"]
     assert np.linalg.norm(u - prob.apply(x)) <= 2e-10 * np.linalg.norm(u)
+
+
+@pytest.mark.parametrize("case", ["plain", "diagonal", "block_jacobi", "fp32_bj", "q1", "bsr"])
+def test_graph_cg_iterates_equal_host_loop(gb, orc, case):
+    """The device-resident CG (scalars on the device, chunks of iterations in a
+    CUDA graph) runs the host loop's statements: same iteration count, same
+    iterate bit for bit, same residual."""
+    prec = gb.F32 if case == "fp32_bj" else gb.F64
+    if case == "q1":
+        op = gb.Q1Operator((24, 24), diffusion=1.0, mass=1.0)
+        f = q1_rhs(24)
+    else:
+        op = gb.DGOperator((3, 3, 3), 2, mass=0.5, precision=prec)
+        if case == "bsr":
+            op = op.assemble()
+        f = np.random.default_rng(6).uniform(-1, 1, op.size)
+    mk = {"plain": lambda: None, "diagonal": lambda: gb.Preconditioner.diagonal(op),
+          "q1": lambda: gb.Preconditioner.diagonal(op)}.get(case, lambda: gb.Preconditioner.block_jacobi(op))
+    pc = mk()
+    tol = 1e-5 if prec == gb.F32 else 1e-10
+    f = f.astype(np.float32) if prec == gb.F32 else f
+    ih, uh = _solve(gb, op, f, "cg", pc, tol=tol)
+    for chunk in (1, 7, 32):
+        ig, ug = _solve(gb, op, f, "cg", pc, tol=tol, graph_chunk=chunk)
+        assert ig["converged"] and ig["iterations"] == ih["iterations"]
+        assert ig["residual"] == ih["residual"]
+        assert np.array_equal(ug.view(np.uint8), uh.view(np.uint8))
+        assert ig["operator_applies"] >= ig["iterations"] + 1
+
+
+def test_graph_cg_cap_and_nonfinite(gb, orc):
+    op, prob, f = _problem(gb, orc)
+    info, _ = _solve(gb, op, f, "cg", max_iterations=3, graph_chunk=8)
+    assert info["iterations"] == -3 and not info["converged"]
+    g = f.copy()
+    g[7] = np.nan
+    info, _ = _solve(gb, op, g, "cg", max_iterations=50, graph_chunk=8)
+    assert not info["converged"]
