@@ -426,38 +426,38 @@ def workload_rk3(args):
     N, p = 128, 2
     steps = args.rk_steps
     kw = dict(diffusion=1e-3, velocity=(1.0, 0.5, 0.25), periodic=(1, 1, 1), weak_dirichlet=False)
-    bnorm = float(np.sqrt(1 + 0.25 + 0.0625))
-    dt_adv = 0.2 * (1.0 / N) / (bnorm * (2 * p + 1))
-    # The SIPG diffusion (penalty 10 (p+1)^2) bounds the explicit step too:
-    # dt <= 2 / rho(M^{-1} A) keeps dt*lambda inside SSP-RK3's real stability
-    # interval [-2.51, 0].  rho from 30 power iterations on the FP64 operator.
+    # Time step: TimeProvider with CFL factor 0.2 on the operator's estimate
+    # h / (|b| (2p+1)), capped by the SIPG stability bound 2 / rho(M^{-1} A)
+    # (SSP-RK3 is stable on [-2.51, 0]; rho from 30 device power iterations).
     opr = gbfem.DGOperator((N, N, N), p, **kw)
-    v = gbfem.DeviceArray.from_numpy(np.random.default_rng(0).uniform(-1, 1, opr.size))
-    av = gbfem.DeviceArray(opr.size)
-    rho = 0.0
-    for _ in range(30):
-        opr(v, av)
-        nrm = np.sqrt(gbfem.dot(av, av))
-        rho = nrm / np.sqrt(gbfem.dot(v, v)) * N ** 3  # M^{-1} = 1/|K| = N^3
-        gbfem.check(gbfem.lib().gbfem_scal(0, av.n, 1.0 / nrm, av.ptr, None))
-        v, av = av, v
-    dt_stab = 2.0 / rho
-    dt = min(dt_adv, dt_stab)
-    del opr, v, av
+    est, ub = gbfem.time_step_estimate(opr, power_iterations=30)
+    dt_adv, dt_stab = 0.2 * est, ub
+    rho = 2.0 / ub
+    del opr
     res = {}
     for prec, name in ((gbfem.F64, "f64"), (gbfem.F32, "f32")):
         op = gbfem.DGOperator((N, N, N), p, precision=prec, **kw)
         u = gbfem.project((N, N, N), p, gbfem.FN_GAUSSIAN, params=(0.5, 0.5, 0.5, 0.1), precision=prec)
-        rk = gbfem.RK3(op)
-        rk.step(u, dt)  # warm-up step (then restart from the initial condition)
+        gbfem.RK3(op).step(u, min(dt_adv, dt_stab))  # warm-up step (then restart from the initial condition)
         u = gbfem.project((N, N, N), p, gbfem.FN_GAUSSIAN, params=(0.5, 0.5, 0.5, 0.1), precision=prec)
-        _, t = _timed(lambda: [rk.step(u, dt) for _ in range(steps)])
+        tp = gbfem.TimeProvider(cfl=0.2)
+        ode = gbfem.ExplicitRungeKuttaSolver(op, tp, estimate=(est, ub))  # the FP64 estimate for both
+        ode.initialize(u)
+        tp.init()
+        dt = tp.deltaT()
+
+        def loop():
+            for _ in range(steps):
+                ode.solve(u)
+                tp.next()
+        _, t = _timed(loop)
         res[name] = (t, u.numpy().astype(np.float64))
-        del rk, op
+        del ode, op
     ndofs = N ** 3 * (p + 1) ** 3
     err = float(np.max(np.abs(res["f32"][1] - res["f64"][1])) / np.max(np.abs(res["f64"][1])))
     return {"metric": "SSP-RK3 128^3 Q2 advection-diffusion, time per step", "value": 1e3 * res["f64"][0] / steps,
             "unit": "ms/step", "higher_is_better": False, "steps": steps, "dt": dt, "dt_advective_cfl_0.2": dt_adv,
+            "time_loop": "TimeProvider(cfl=0.2) + ExplicitRungeKuttaSolver (SSP-RK3)",
             "dt_stability": dt_stab, "spectral_radius_minv_a": rho,
             "f64_max_abs": float(np.max(np.abs(res["f64"][1]))),
             "f32_ms_per_step": 1e3 * res["f32"][0] / steps,

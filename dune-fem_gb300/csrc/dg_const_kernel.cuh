@@ -25,8 +25,9 @@
 //  2. dg_const_kernel: numerical fluxes from the own and the neighbour's
 //     traces (owner computes, no scatter), then one pass per axis over the
 //     lines of the cell: the 1-D operator M_d (a warp-uniform operand; its
-//     entries with i+j odd vanish without advection and are skipped) plus
-//     the face expansion, again split into even and odd i.
+//     structural zeros are skipped: row 0, since L_0' = 0, and without
+//     advection column 0 and the entries with i+j odd) plus the face
+//     expansion, again split into even and odd i.
 // Every output is one thread's fixed-order sum: deterministic, independent of
 // the launch shape.
 #pragma once
@@ -43,8 +44,8 @@ struct DgConstTablesT {
   T tr[2 * kDgMaxN];        // L_i(s)
   T dtr[2 * kDgMaxN];       // L_i'(s)
   T M[3][kDgMaxN * kDgMaxN];  // per-axis line operator (filled per operator)
-  // per-axis flux constants: A1 = |F| eps sigma, A2 = |F| eps / (2 h), A3 = |F| eps / 2
-  T A1[3], A2[3], A3[3];
+  // per-axis flux constants: A1 = |F| eps sigma, A2 = |F| eps / (2 h)
+  T A1[3], A2[3];
 };
 
 // traces[cell][f = 2d+s][0: v, 1: d][jk], d(s) without the 1/h and normal sign,
@@ -74,7 +75,7 @@ __global__ void __launch_bounds__(256) dg_trace_kernel(const T* __restrict__ u, 
         odd = fma(tabs.dtr[N + i], x, odd);
       } else {
         ev = fma(tabs.tr[N + i], x, ev);
-        ed = fma(tabs.dtr[N + i], x, ed);
+        if (i > 0) ed = fma(tabs.dtr[N + i], x, ed);  // L_0' = 0
       }
     }
     // L_i(1) = tr[N+i]; L_i(0) = (-1)^i L_i(1); L_i'(0) = (-1)^(i+1) L_i'(1)
@@ -124,7 +125,8 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
     cc[d] = nb;
     const long long ncell = cc[0] + (long long)args.nc[0] * (cc[1] + (long long)args.nc[1] * cc[2]);
     // n.grad u = (n.e_d / h_d) d(s): the 1/h_d and the face constants are folded
-    // into A1 = |F| eps sigma, A2 = |F| eps / (2 h_d), A3 = |F| eps / 2
+    // into A1 = |F| eps sigma and A2 = |F| eps / (2 h_d); Grad is stored times
+    // 1/h_d (the factor of L_i'(s) in the expansion), which makes its constant A2 too
     const T* own = traces + cl * (12 * N2) + f * 2 * N2;
     const T vm = __ldg(own + jk), dm = __ldg(own + N2 + jk);
     T vp = T(0), dp = T(0);
@@ -139,7 +141,7 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
       // eps |F| (sigma J - {dn u}),  -eps |F| J / 2
       const T J = vm - vp;
       val = fma(tabs.A1[d], J, -a2 * (dm + dp));
-      grad = -tabs.A3[d] * J;
+      grad = -tabs.A2[d] * J;
       if (ADV) {
         const T bn = s ? args.b[d] : -args.b[d];
         val += args.faceA[d] * bn * (bn >= T(0) ? vm : vp);
@@ -148,7 +150,7 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
       if (args.weak_dirichlet) {
         // eps |F| (sigma u - dn u),  -eps |F| u
         val = fma(tabs.A1[d], vm, T(-2) * a2 * dm);
-        grad = T(-2) * tabs.A3[d] * vm;
+        grad = T(-2) * tabs.A2[d] * vm;
       }
       if (ADV) {
         const T bn = s ? args.b[d] : -args.b[d];
@@ -163,7 +165,6 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const int stride = d == 0 ? N2 : (d == 1 ? N : 1);
-    const T ih = args.invh[d];
     for (int item = tid; item < CPB * N2; item += blockDim.x) {
       const int c = item / N2, jk = item - c * N2;
       const int j = jk / N, k = jk % N;
@@ -175,18 +176,25 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
       const T* fv0 = sF + (c * 6 + 2 * d) * 2 * N2;
       const T* fv1 = fv0 + 2 * N2;
       // sum_s L_i(s) Val_s = L_i(1) (Val_1 + (-1)^i Val_0); the gradient
-      // terms likewise with (n.e_d/h) L_i'(s): (1/h) L_i'(1) (G_1 + (-1)^i G_0)
+      // terms likewise with (n.e_d/h) L_i'(s): L_i'(1) (G_1 + (-1)^i G_0), G
+      // already carrying the 1/h
       const T v0 = fv0[jk], v1 = fv1[jk], g0 = fv0[N2 + jk], g1 = fv1[N2 + jk];
-      const T vs = v1 + v0, vd = v1 - v0, gs = ih * (g1 + g0), gd = ih * (g1 - g0);
+      const T vs = v1 + v0, vd = v1 - v0, gs = g1 + g0, gd = g1 - g0;
       T* rc = sr + c * N3 + base;
 #pragma unroll
       for (int i = 0; i < N; ++i) {
         T acc = d == 0 ? T(0) : rc[i * stride];
 #pragma unroll
-        for (int jj = 0; jj < N; ++jj)
-          if (ADV || !((i + jj) & 1)) acc = fma(tabs.M[d][i * N + jj], x[jj], acc);
+        for (int jj = 0; jj < N; ++jj) {
+          // structural zeros of M_d: row 0 (L_0' = 0 in both the stiffness and
+          // the advection matrix) but for the mass entry (0,0) of axis 0;
+          // without advection also column 0 and the entries with i+j odd
+          const bool mass00 = d == 0 && i == 0 && jj == 0;
+          const bool nz = ADV ? (i != 0 || mass00) : (!((i + jj) & 1) && ((i != 0 && jj != 0) || mass00));
+          if (nz) acc = fma(tabs.M[d][i * N + jj], x[jj], acc);
+        }
         acc = fma(tabs.tr[N + i], (i & 1) ? vd : vs, acc);
-        acc = fma(tabs.dtr[N + i], (i & 1) ? gd : gs, acc);
+        if (i > 0) acc = fma(tabs.dtr[N + i], (i & 1) ? gd : gs, acc);  // L_0'(1) = 0
         rc[i * stride] = acc;
       }
     }

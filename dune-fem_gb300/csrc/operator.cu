@@ -111,7 +111,6 @@ static void fill_line_operators(const gbfem_operator_s* op, DgConstTablesT<T>* c
     const double area = vol / h[ax];
     ct->A1[ax] = T(area * d.diffusion * d.penalty / h[ax]);  // sigma = beta / h_F, h_F = |K| / |F| = h
     ct->A2[ax] = T(area * d.diffusion * 0.5 / h[ax]);
-    ct->A3[ax] = T(area * d.diffusion * 0.5);
   }
 }
 

@@ -12,6 +12,8 @@
 // The stage combinations are single fused passes over the vectors, with the
 // factor -1/|K| folded into the coefficients.
 #include <cuda_runtime.h>
+#include <cfloat>
+#include <cmath>
 #include <new>
 
 #include "blas.cuh"
@@ -31,6 +33,18 @@ __global__ void k_stage(long long n, const T* u, int nw, const T* __restrict__ w
     if (nw > 1) v += a1 * w1[i];
     if (nw > 2) v += a2 * w2[i];
     y[i] = v;
+  }
+}
+
+// v[i] = uniform(-1, 1) from a SplitMix64 hash of (seed, i)
+template <typename T>
+__global__ void k_random_fill(long long n, unsigned long long seed, T* v) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    unsigned long long z = seed + 0x9E3779B97F4A7C15ULL * (unsigned long long)(i + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    v[i] = T(double(z >> 11) * (2.0 / 9007199254740992.0) - 1.0);
   }
 }
 
@@ -110,6 +124,54 @@ int gbfem_rk3_step(gbfem_rk_solver rk, void* u, double dt, void* stream) {
                                                   (const float*)rk->k[1], b[1] * f, (const float*)rk->k[2],
                                                   b[2] * f, (float*)u);
   GBFEM_CUDA_TRY(cudaGetLastError());
+  return GBFEM_OK;
+}
+
+int gbfem_dg_time_step_estimate(gbfem_operator op, int power_iterations, uint64_t seed, double* dt_estimate,
+                                double* dt_upper_bound) {
+  if (!op || !dt_estimate || !dt_upper_bound || power_iterations < 0)
+    return set_error(GBFEM_ERR_INVALID, "gbfem_dg_time_step_estimate: invalid argument");
+  if (op->kind != OpKind::DG) return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "gbfem_dg_time_step_estimate: DG only");
+  const gbfem_dg_desc& d = op->dg;
+  double hmin = 1e300, vol = 1.0, bnorm = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    const double h = (d.grid.upper[k] - d.grid.lower[k]) / d.grid.cells[k];
+    hmin = h < hmin ? h : hmin;
+    vol *= h;
+    bnorm += d.velocity[k] * d.velocity[k];
+  }
+  bnorm = std::sqrt(bnorm);
+  *dt_estimate = bnorm > 0.0 ? hmin / (bnorm * (2 * d.order + 1)) : DBL_MAX;
+  *dt_upper_bound = DBL_MAX;
+  if (power_iterations == 0) return GBFEM_OK;
+  // power iteration for rho(M^{-1} A), M^{-1} = 1/|K|; 2/rho keeps dt*lambda
+  // inside SSP-RK3's real stability interval [-2.51, 0]
+  const long long n = op->ndofs;
+  const int prec = op->precision;
+  const size_t bytes = size_t(n) * (prec == GBFEM_F64 ? 8 : 4);
+  void *v = nullptr, *av = nullptr;
+  cudaError_t e = cudaMalloc(&v, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&av, bytes);
+  struct Free { void** a; void** b; ~Free() { if (*a) cudaFree(*a); if (*b) cudaFree(*b); } } fr{&v, &av};
+  if (e != cudaSuccess) return set_cuda_error(e, "gbfem_dg_time_step_estimate");
+  if (prec == GBFEM_F64) k_random_fill<double><<<stream_grid(n), 256>>>(n, seed, static_cast<double*>(v));
+  else k_random_fill<float><<<stream_grid(n), 256>>>(n, seed, static_cast<float*>(v));
+  GBFEM_CUDA_TRY(cudaGetLastError());
+  double vv = 0.0, rho = 0.0;
+  GBFEM_TRY(gbfem_dot(prec, n, v, v, &vv, nullptr));
+  for (int it = 0; it < power_iterations; ++it) {
+    GBFEM_TRY(gbfem_operator_apply(op, v, av, nullptr));
+    double aa = 0.0;
+    GBFEM_TRY(gbfem_dot(prec, n, av, av, &aa, nullptr));
+    if (!(aa > 0.0) || !std::isfinite(aa)) break;
+    rho = std::sqrt(aa / vv) / vol;
+    GBFEM_TRY(gbfem_scal(prec, n, 1.0 / std::sqrt(aa), av, nullptr));
+    void* t = v;
+    v = av;
+    av = t;
+    vv = 1.0;
+  }
+  if (rho > 0.0) *dt_upper_bound = 2.0 / rho;
   return GBFEM_OK;
 }
 

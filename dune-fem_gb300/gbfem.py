@@ -96,6 +96,8 @@ def lib():
         L.gbfem_rk3_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
         L.gbfem_rk3_step.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]
         L.gbfem_rk3_destroy.argtypes = [C.c_void_p]
+        L.gbfem_dg_time_step_estimate.argtypes = [C.c_void_p, C.c_int, C.c_uint64, C.POINTER(C.c_double),
+                                                  C.POINTER(C.c_double)]
         L.gbfem_cnn_create.argtypes = [C.c_int, C.c_int, C.c_uint64, C.POINTER(C.c_void_p)]
         L.gbfem_cnn_destroy.argtypes = [C.c_void_p]
         L.gbfem_cnn_set_kappa.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
@@ -432,6 +434,148 @@ class RK3:
                 self.handle = None
         except Exception:
             pass
+
+
+def time_step_estimate(op, power_iterations=30, seed=0):
+    """(dt_estimate, dt_upper_bound) of a DG operator: the advective CFL-1 step
+    h_min / (|b| (2p+1)) and 2 / rho(M^{-1} A) from the power method (inf when
+    not applicable)."""
+    est, ub = C.c_double(), C.c_double()
+    check(lib().gbfem_dg_time_step_estimate(op.handle, power_iterations, seed, C.byref(est), C.byref(ub)))
+    big = np.finfo(np.float64).max
+    return (np.inf if est.value >= big else est.value), (np.inf if ub.value >= big else ub.value)
+
+
+class TimeProvider:
+    """Time, step counter and step size of an explicit time loop, as
+    dune-fem's TimeProvider (solver/timeprovider.hh:35-200, 403-592):
+
+        tp = TimeProvider(cfl=0.2)
+        ode.initialize(u)                  # provides the operator's estimate
+        tp.init()
+        while tp.time() < end_time:
+            ode.solve(u)                   # uses tp.deltaT(), provides the next estimate
+            tp.next()
+
+    deltaT = min(cfl * estimate, upper bound), both the minimum of what was
+    provided since the step was fixed; a step with deltaT <= 0 is invalid and
+    does not advance the time."""
+
+    def __init__(self, start_time=0.0, cfl=1.0, update_step=1):
+        self._time = float(start_time)
+        self._step = 0
+        self._cfl = float(cfl)
+        self._update_step = int(update_step)
+        self._counter = self._update_step  # the first initTimeStep fixes dt
+        self._dt = 0.0
+        self._valid = False
+        self._init_estimate()
+
+    def _init_estimate(self):
+        self._dt_estimate = np.finfo(np.float64).max
+        self._dt_upper = np.finfo(np.float64).max
+        self._estimate_valid = False
+
+    def _init_time_step(self, dt_estimate):
+        self._counter += 1
+        if self._counter >= self._update_step:
+            self._dt = min(self._cfl * dt_estimate, self._dt_upper)
+            self._valid = self._dt > 0.0
+            self._counter = 0
+        self._init_estimate()
+
+    def _advance(self):
+        if self._valid:
+            self._time += self._dt
+            self._step += 1
+
+    def init(self, time_step=None):
+        self._init_time_step(self._dt_estimate if time_step is None else time_step)
+
+    def next(self, time_step=None):
+        if time_step is None and not self._estimate_valid:
+            raise RuntimeError("TimeProvider.next: no time step estimate was provided")
+        self._advance()
+        self._init_time_step(self._dt_estimate if time_step is None else time_step)
+
+    def time(self):
+        return self._time
+
+    def timeStep(self):
+        if not self._valid:
+            raise RuntimeError("TimeProvider: the time step is not valid")
+        return self._step
+
+    def deltaT(self):
+        if not self._valid:
+            raise RuntimeError("TimeProvider: the time step is not valid")
+        return self._dt
+
+    def inverseDeltaT(self):
+        return 1.0 / self.deltaT()
+
+    def factor(self):
+        return self._cfl
+
+    def timeStepEstimate(self):
+        return self._dt_estimate
+
+    def provideTimeStepEstimate(self, dt_estimate):
+        self._dt_estimate = min(self._dt_estimate, dt_estimate)
+        self._estimate_valid = True
+
+    def provideTimeStepUpperBound(self, upper_bound):
+        self._dt_upper = min(self._dt_upper, upper_bound)
+        self._estimate_valid = True
+
+    def invalidateTimeStep(self):
+        self._valid = False
+
+    def timeStepValid(self):
+        return self._valid
+
+
+class ExplicitRungeKuttaSolver:
+    """SSP-RK3 driven by a TimeProvider, as dune-fem's ExplicitRungeKuttaSolver
+    (solver/rungekutta/explicit.hh:145-215): initialize() provides the
+    operator's time-step estimate, solve(u) makes one step of tp.deltaT() and
+    provides the estimate for the next one.  The estimate of the linear DG
+    operator does not depend on u, so it is computed once (advective CFL-1
+    step as the estimate, 2/rho(M^{-1}A) as the upper bound)."""
+
+    def __init__(self, op, tp, power_iterations=30, seed=0, estimate=None):
+        """estimate: a precomputed (dt_estimate, dt_upper_bound) pair, e.g. the
+        FP64 operator's for an FP32 run, instead of computing it on op."""
+        self.op, self.tp = op, tp
+        self.rk = RK3(op)
+        self.dt_estimate, self.dt_upper_bound = (time_step_estimate(op, power_iterations, seed)
+                                                 if estimate is None else estimate)
+        self.initialized = False
+
+    def _provide(self):
+        if np.isfinite(self.dt_estimate):
+            self.tp.provideTimeStepEstimate(self.dt_estimate)
+        if np.isfinite(self.dt_upper_bound):
+            self.tp.provideTimeStepUpperBound(self.dt_upper_bound)
+        if not (np.isfinite(self.dt_estimate) or np.isfinite(self.dt_upper_bound)):
+            raise RuntimeError("ExplicitRungeKuttaSolver: the operator gives no time-step bound")
+
+    def initialize(self, u):
+        if not self.initialized:
+            self._provide()
+            self.initialized = True
+
+    def solve(self, u, stream=None):
+        if not self.initialized:
+            raise RuntimeError("ExplicitRungeKuttaSolver wasn't initialized before first call!")
+        self.rk.step(u, self.tp.deltaT(), stream)
+        self._provide()
+
+    def stages(self):
+        return 3
+
+    def order(self):
+        return 3
 
 
 class CNN:

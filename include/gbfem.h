@@ -247,6 +247,17 @@ int gbfem_rk3_create(gbfem_operator op, gbfem_rk_solver* rk);
 /* One step of size dt, in place on the device vector u (op's precision). */
 int gbfem_rk3_step(gbfem_rk_solver rk, void* u, double dt, void* stream);
 int gbfem_rk3_destroy(gbfem_rk_solver rk);
+/* Time-step information for the explicit method, the operator's counterpart
+ * of SpaceOperatorInterface::timeStepEstimate (operator/common/
+ * spaceoperatorif.hh:52-124) fed to TimeProvider::provideTimeStepEstimate /
+ * provideTimeStepUpperBound (solver/timeprovider.hh:142-155):
+ *   dt_estimate    = h_min / (|b| (2p+1)), the advective CFL-1 step (DBL_MAX
+ *                    without advection); the time provider scales it by its CFL factor;
+ *   dt_upper_bound = 2 / rho(M^{-1} A) from power_iterations steps of the power
+ *                    method on the device from a seeded random vector (DBL_MAX
+ *                    for 0 iterations): SSP-RK3 is stable on [-2.51, 0]. */
+int gbfem_dg_time_step_estimate(gbfem_operator op, int power_iterations, uint64_t seed, double* dt_estimate,
+                                double* dt_upper_bound);
 
 /* ---- learned preconditioner ------------------------------------------------
  * A 4-level convolutional network (32 channels, 3x3x3 convolutions, BF16

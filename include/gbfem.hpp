@@ -23,6 +23,8 @@
 #include <cmath>
 #include <cstddef>
 #include <cstdint>
+#include <algorithm>
+#include <limits>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -231,6 +233,112 @@ class GpuKrylovInverseOperator {
   mutable gbfem_solver_info info_{};
   const GpuOperator* op_ = nullptr;
   const GpuPreconditioner* pc_ = nullptr;
+};
+
+// TimeProvider (solver/timeprovider.hh:35-200, 403-592), single process:
+// deltaT = min(factor * estimate, upper bound), re-fixed every updateStep calls
+// of init/next; the estimate and bound are reset after each fix.
+class TimeProvider {
+ public:
+  explicit TimeProvider(double startTime = 0.0, double cfl = 1.0, int updateStep = 1)
+      : time_(startTime), cfl_(cfl), updateStep_(updateStep), counter_(updateStep) {
+    initTimeStepEstimate();
+  }
+  void init() { initTimeStep(dtEstimate_); }
+  void init(double timeStep) { initTimeStep(timeStep); }
+  void next() {
+    if (!dtEstimateValid_) throw Error(GBFEM_ERR_INVALID, "TimeProvider::next: no time step estimate provided");
+    advance();
+    initTimeStep(dtEstimate_);
+  }
+  void next(double timeStep) {
+    advance();
+    initTimeStep(timeStep);
+  }
+  double time() const { return time_; }
+  int timeStep() const { return valid(), timeStep_; }
+  double deltaT() const { return valid(), dt_; }
+  double inverseDeltaT() const { return valid(), 1.0 / dt_; }
+  double factor() const { return cfl_; }
+  double timeStepEstimate() const { return dtEstimate_; }
+  void provideTimeStepEstimate(double dt) {
+    dtEstimate_ = std::min(dtEstimate_, dt);
+    dtEstimateValid_ = true;
+  }
+  void provideTimeStepUpperBound(double bound) {
+    dtUpperBound_ = std::min(dtUpperBound_, bound);
+    dtEstimateValid_ = true;
+  }
+  void invalidateTimeStep() { valid_ = false; }
+  bool timeStepValid() const { return valid_; }
+
+ private:
+  bool valid() const {
+    if (!valid_) throw Error(GBFEM_ERR_INVALID, "TimeProvider: time step not valid");
+    return true;
+  }
+  void advance() {
+    if (valid_) {
+      time_ += dt_;
+      ++timeStep_;
+    }
+  }
+  void initTimeStepEstimate() {
+    dtEstimate_ = std::numeric_limits<double>::max();
+    dtUpperBound_ = std::numeric_limits<double>::max();
+    dtEstimateValid_ = false;
+  }
+  void initTimeStep(double dtEstimate) {
+    if (++counter_ >= updateStep_) {
+      dt_ = std::min(cfl_ * dtEstimate, dtUpperBound_);
+      valid_ = dt_ > 0.0;
+      counter_ = 0;
+    }
+    initTimeStepEstimate();
+  }
+  double time_ = 0.0;
+  int timeStep_ = 0;
+  double dt_ = 0.0;
+  bool valid_ = false;
+  bool dtEstimateValid_ = false;
+  double dtEstimate_ = 0.0, dtUpperBound_ = 0.0;
+  double cfl_;
+  int updateStep_, counter_;
+};
+
+// ExplicitRungeKuttaSolver with the TVD3 table over the MOL DG operator
+// (solver/rungekutta/explicit.hh:145-215): initialize() provides the
+// operator's estimate, solve(u) steps by tp.deltaT() and provides it again.
+class GpuExplicitRungeKuttaSolver {
+ public:
+  GpuExplicitRungeKuttaSolver(const GpuOperator& op, TimeProvider& tp, int powerIterations = 30)
+      : tp_(tp) {
+    gbfem_rk_solver rk = nullptr;
+    check(gbfem_rk3_create(op.handle(), &rk));
+    rk_ = std::shared_ptr<gbfem_rk_solver_s>(rk, [](gbfem_rk_solver p) { gbfem_rk3_destroy(p); });
+    check(gbfem_dg_time_step_estimate(op.handle(), powerIterations, 0, &estimate_, &upperBound_));
+  }
+  void initialize(const GpuDiscreteFunction&) {
+    provide();
+    initialized_ = true;
+  }
+  void solve(GpuDiscreteFunction& u) {
+    if (!initialized_) throw Error(GBFEM_ERR_INVALID, "ExplicitRungeKuttaSolver wasn't initialized before first call!");
+    check(gbfem_rk3_step(rk_.get(), u.leakPointer(), tp_.deltaT(), nullptr));
+    provide();
+  }
+  int stages() const { return 3; }
+
+ private:
+  void provide() {
+    const double big = std::numeric_limits<double>::max();
+    if (estimate_ < big) tp_.provideTimeStepEstimate(estimate_);
+    if (upperBound_ < big) tp_.provideTimeStepUpperBound(upperBound_);
+  }
+  TimeProvider& tp_;
+  std::shared_ptr<gbfem_rk_solver_s> rk_;
+  double estimate_ = 0.0, upperBound_ = 0.0;
+  bool initialized_ = false;
 };
 
 }  // namespace gbfem_cpp

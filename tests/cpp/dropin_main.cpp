@@ -44,5 +44,29 @@ int main() {
     std::printf("method %d: iterations %d, relative residual %.3e\n", method, inv.iterations(), rel);
     if (!inv.info().converged || !(rel < 1e-9)) return 1;
   }
+  // explicit time loop: TimeProvider + SSP-RK3 on a periodic advection operator
+  gbfem_dg_desc a = d;
+  for (int k = 0; k < 3; ++k) a.grid.periodic[k] = 1;
+  a.diffusion = 0.0;
+  a.weak_dirichlet = 0;
+  a.velocity[0] = 1.0;
+  a.velocity[1] = 0.5;
+  GpuOperator adv = GpuOperator::dg(a);
+  TimeProvider tp(0.0, 0.2);
+  GpuExplicitRungeKuttaSolver ode(adv, tp);
+  GpuDiscreteFunction v("v", n);
+  v.copyFromHost(fh.data());
+  ode.initialize(v);
+  int steps = 0;
+  for (tp.init(); tp.time() < 0.05; tp.next()) {
+    ode.solve(v);
+    ++steps;
+  }
+  std::vector<double> vh(n);
+  v.copyToHost(vh.data());
+  double mass = 0.0;
+  for (std::int64_t c = 0; c < n / 27; ++c) mass += vh[c * 27];
+  std::printf("time loop: %d steps of %.4e to t = %.4f, mean %.15f\n", steps, tp.deltaT(), tp.time(), mass);
+  if (steps < 1 || std::fabs(mass - 1.0) > 1e-12) return 2;
   return 0;
 }
