@@ -109,12 +109,16 @@ extern "C" int gbfem_operator_assemble(gbfem_operator op, gbfem_operator* out) {
   if (!op || !out) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_assemble: null argument");
   *out = nullptr;
   if (op->kind != OpKind::DG) return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "gbfem_operator_assemble: DG operators only");
+  if (op->nonlinear)
+    return set_error(GBFEM_ERR_INVALID, "gbfem_operator_assemble: nonlinear operator (assemble its Jacobian)");
   auto* a = new (std::nothrow) gbfem_operator_s();
   if (!a) return set_error(GBFEM_ERR_INVALID, "out of host memory");
   *a = *op;
   a->kind = OpKind::BSR;
   a->host_u = a->host_w = nullptr;
   a->pipe = nullptr;
+  a->jac_points = nullptr;
+  a->nonlinear = 0;
   a->bsr_blocks = nullptr;
   a->bsr_col = nullptr;
   a->trace_buf = nullptr;

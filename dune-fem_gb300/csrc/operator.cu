@@ -114,8 +114,28 @@ static void fill_line_operators(const gbfem_operator_s* op, DgConstTablesT<T>* c
   }
 }
 
+static int dg_apply_linear(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
+                           void* blocks, long long cell_begin, long long cell_count, int phase);
+
 int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
              void* blocks, long long cell_begin, long long cell_count, int phase) {
+  if (op->nonlinear && unit_mode != 0)
+    return set_error(GBFEM_ERR_INVALID, "nonlinear operator: diagonal and blocks belong to its Jacobian");
+  GBFEM_TRY(dg_apply_linear(op, u, w, s, unit_mode, blocks, cell_begin, cell_count, phase));
+  const long long count = cell_count > 0 ? cell_count : op->ncells - cell_begin;
+  if (unit_mode == 0 && (phase & 2)) {
+    if (op->nonlinear) return reaction_launch(op, 0, u, w, nullptr, cell_begin, count, 0, s);
+    if (op->jac_points) return reaction_launch(op, 2, u, w, op->jac_points, cell_begin, count, 0, s);
+  } else if (op->jac_points && unit_mode == 1) {
+    return reaction_launch(op, 0, nullptr, blocks, op->jac_points, cell_begin, count, 1, s);
+  } else if (op->jac_points && unit_mode == 2) {
+    return reaction_launch(op, 0, nullptr, blocks, op->jac_points, 0, op->ncells, 2, s);
+  }
+  return GBFEM_OK;
+}
+
+static int dg_apply_linear(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
+                           void* blocks, long long cell_begin, long long cell_count, int phase) {
   if (op->precision == GBFEM_F64) {
     DgArgsT<double> a;
     fill_dg_args(op, &a);
@@ -438,6 +458,7 @@ int gbfem_q1_operator_create(const gbfem_grid_desc* grid, int precision, double 
 int gbfem_operator_destroy(gbfem_operator op) {
   if (!op) return GBFEM_OK;
   if (op->pipe) destroy_host_pipe(op->pipe);
+  if (op->jac_points) cudaFree(op->jac_points);
   if (op->host_u) cudaFree(op->host_u);
   if (op->host_w) cudaFree(op->host_w);
   if (op->bsr_blocks) cudaFree(op->bsr_blocks);

@@ -25,6 +25,11 @@ int dg_apply(const struct ::gbfem_operator_s* op, const void* u, void* w, cudaSt
 int q1_apply(const struct ::gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int diag_only);
 // assembled operator: y = A x (diag_only: the diagonal into y)
 int bsr_apply(const struct ::gbfem_operator_s* op, const void* x, void* y, cudaStream_t s, int diag_only);
+// reaction term of a nonlinear DG operator / linearised term of a Jacobian
+// (reaction_kernel.cuh): mode 0 w += R(u), 1 pts = linearisation at u, 2 w +=
+// R'(u0) u; blocks_mode 1/2 add the linearised cell blocks / their diagonal.
+int reaction_launch(const struct ::gbfem_operator_s* op, int mode, const void* u, void* w, void* pts,
+                    long long cell_begin, long long count, int blocks_mode, cudaStream_t s);
 struct HostPipe;
 void destroy_host_pipe(HostPipe* p);
 int dg_apply_host_pipelined(struct ::gbfem_operator_s* op, const void* u_host, void* w_host);
@@ -52,5 +57,8 @@ struct gbfem_operator_s {
   void* host_u = nullptr;  // device staging of gbfem_operator_apply_host
   void* host_w = nullptr;
   int host_chunks = 0;     // z-slab chunks of the pipelined host apply (0 = automatic)
+  int nonlinear = 0;       // DG: adds the reaction R(u) = int r(u) v (react = c1, c3, ce)
+  double react[3] = {0.0, 0.0, 0.0};
+  void* jac_points = nullptr;  // Jacobian of a nonlinear DG operator: [cell][q^3] w |K| r'(u0)
   gbfem::HostPipe* pipe = nullptr;  // its streams and events
 };

@@ -53,6 +53,26 @@ class IRParams(C.Structure):
     _fields_ = [("tolerance", C.c_double), ("max_outer", C.c_int), ("inner", SolverParams)]
 
 
+class Reaction(C.Structure):
+    _fields_ = [("linear", C.c_double), ("cubic", C.c_double), ("exponential", C.c_double)]
+
+
+class NewtonParams(C.Structure):
+    _fields_ = [("tolerance", C.c_double), ("max_iterations", C.c_int), ("max_linear_iterations", C.c_int),
+                ("max_line_search_iterations", C.c_int), ("line_search", C.c_int), ("forcing", C.c_int),
+                ("eta_max", C.c_double), ("gamma", C.c_double), ("simplified", C.c_int),
+                ("preconditioner", C.c_int), ("verbose", C.c_int), ("linear", SolverParams)]
+
+
+class NewtonInfo(C.Structure):
+    _fields_ = [("converged", C.c_int), ("iterations", C.c_int), ("linear_iterations", C.c_int),
+                ("residual", C.c_double), ("failure", C.c_int), ("time_ms", C.c_double)]
+
+
+PC_NONE, PC_DIAGONAL, PC_BLOCK_JACOBI = 0, 1, 2
+NEWTON_FAILURES = {0: "Success", 1: "InvalidResidual", 4: "LineSearchFailed", 5: "TooManyIterations",
+                   6: "TooManyLinearIterations", 7: "LinearSolverFailed"}
+
 CG, GMRES, BICGSTAB, FCG, FGMRES = 0, 1, 2, 3, 4
 ABSOLUTE, RELATIVE, RESIDUAL_REDUCTION = 0, 1, 2
 METHODS = {"cg": CG, "gmres": GMRES, "bicgstab": BICGSTAB, "fcg": FCG, "fgmres": FGMRES}
@@ -127,6 +147,14 @@ def lib():
                                   C.POINTER(SolverInfo)]
         L.gbfem_solve_mixed.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(IRParams), C.c_void_p,
                                         C.c_void_p, C.POINTER(SolverInfo)]
+        L.gbfem_dg_nonlinear_operator_create.argtypes = [C.POINTER(DgDesc), C.POINTER(Reaction),
+                                                         C.POINTER(C.c_void_p)]
+        L.gbfem_operator_nonlinear.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
+        L.gbfem_operator_jacobian_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+        L.gbfem_operator_jacobian.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.gbfem_newton_params_default.argtypes = [C.POINTER(NewtonParams)]
+        L.gbfem_newton_solve.argtypes = [C.c_void_p, C.POINTER(NewtonParams), C.c_void_p, C.c_void_p,
+                                         C.POINTER(NewtonInfo)]
         _lib = L
     return _lib
 
@@ -228,6 +256,23 @@ class Operator:
         check(lib().gbfem_operator_block_diagonal(self.handle, b.ptr, None))
         return b
 
+    def nonlinear(self):
+        v = C.c_int()
+        check(lib().gbfem_operator_nonlinear(self.handle, C.byref(v)))
+        return bool(v.value)
+
+    def jacobian(self, u, jac=None):
+        """The Jacobian at u as a linear Operator (jacobian(u, jOp),
+        operator/common/differentiableoperator.hh:54); pass jac to update one."""
+        if jac is None:
+            h = C.c_void_p()
+            check(lib().gbfem_operator_jacobian_create(self.handle, C.byref(h)))
+            jac = Operator(h, self.precision)
+            jac.nloc = getattr(self, "nloc", None)
+            jac._base = self
+        check(lib().gbfem_operator_jacobian(self.handle, u.ptr, jac.handle, None))
+        return jac
+
     def __del__(self):
         try:
             if self.handle:
@@ -263,6 +308,95 @@ class DGOperator(Operator):
         self.order = order
         self.nloc = (order + 1) ** 3
         super().__init__(h, precision)
+
+
+class NonlinearDGOperator(DGOperator):
+    """S(u) = A u + int r(u) v, r(u) = linear u + cubic u^3 + exponential e^u,
+    A the SIPG / upwind / mass DG operator (same arguments as DGOperator)."""
+
+    def __init__(self, cells, order, reaction=(0.0, 0.0, 0.0), quad_points=0, precision=F64, diffusion=1.0,
+                 penalty=None, mass=0.0, velocity=(0.0, 0.0, 0.0), weak_dirichlet=True, periodic=(0, 0, 0),
+                 lower=(0.0, 0.0, 0.0), upper=(1.0, 1.0, 1.0), kappa=None, algorithm=0):
+        d = DgDesc()
+        d.grid = grid_desc(cells, lower, upper, periodic)
+        d.order = order
+        d.quad_points = quad_points
+        d.precision = precision
+        d.diffusion = diffusion
+        d.penalty = 10.0 * (order + 1) ** 2 if penalty is None else penalty
+        d.mass = mass
+        for k in range(3):
+            d.velocity[k] = velocity[k]
+        d.weak_dirichlet = 1 if weak_dirichlet else 0
+        self.kappa = kappa
+        d.kappa = kappa.ptr if kappa is not None else None
+        d.algorithm = algorithm
+        r = Reaction(*reaction)
+        h = C.c_void_p()
+        check(lib().gbfem_dg_nonlinear_operator_create(C.byref(d), C.byref(r), C.byref(h)))
+        self.desc = d
+        self.reaction = tuple(reaction)
+        self.order = order
+        self.nloc = (order + 1) ** 3
+        Operator.__init__(self, h, precision)
+
+
+class NewtonInverseOperator:
+    """w = S^{-1}(rhs) by Newton's method: NewtonInverseOperator
+    (solver/newtoninverseoperator.hh:484-790): bind(op), __call__(rhs, w) with
+    w the initial guess, iterations(), linearIterations(), info().
+
+    linear: a KrylovInverseOperator-style parameter set (method, tolerance,
+    error_measure, max_iterations, restart); preconditioner: PC_* of each
+    Jacobian; line_search "none" | "simple"; forcing "none" | "eisenstatwalker"."""
+
+    def __init__(self, tolerance=1e-6, max_iterations=None, max_linear_iterations=None, line_search="none",
+                 forcing="none", eta_max=0.99, gamma=0.1, simplified=False, preconditioner=PC_BLOCK_JACOBI,
+                 linear_method="cg", linear_tolerance=1e-8, linear_error_measure=RELATIVE,
+                 linear_max_iterations=None, linear_restart=20, max_line_search_iterations=None, verbose=False):
+        p = NewtonParams()
+        check(lib().gbfem_newton_params_default(C.byref(p)))
+        p.tolerance = tolerance
+        if max_iterations is not None:
+            p.max_iterations = max_iterations
+        if max_line_search_iterations is not None:
+            p.max_line_search_iterations = max_line_search_iterations
+        p.line_search = {"none": 0, "simple": 1}[line_search]
+        p.forcing = {"none": 0, "eisenstatwalker": 1}[forcing]
+        p.eta_max, p.gamma = eta_max, gamma
+        p.simplified = 1 if simplified else 0
+        p.preconditioner = preconditioner
+        p.verbose = 1 if verbose else 0
+        p.linear = solver_params(linear_method, linear_tolerance, linear_error_measure, linear_max_iterations,
+                                 linear_restart)
+        p.max_linear_iterations = p.linear.max_iterations if max_linear_iterations is None else max_linear_iterations
+        self.params = p
+        self.op = None
+        self._info = NewtonInfo()
+
+    def bind(self, op):
+        self.op = op
+
+    def unbind(self):
+        self.op = None
+
+    def __call__(self, rhs, w):
+        if self.op is None:
+            raise GbfemError(-1, "NewtonInverseOperator: no operator bound")
+        check(lib().gbfem_newton_solve(self.op.handle, C.byref(self.params), rhs.ptr, w.ptr, C.byref(self._info)))
+        return self._info
+
+    def iterations(self):
+        return self._info.iterations
+
+    def linearIterations(self):
+        return self._info.linear_iterations
+
+    def info(self):
+        i = self._info
+        return {"converged": bool(i.converged), "iterations": i.iterations, "linear_iterations": i.linear_iterations,
+                "residual": i.residual, "failure": NEWTON_FAILURES.get(i.failure, str(i.failure)),
+                "time_ms": i.time_ms}
 
 
 class Q1Operator(Operator):

@@ -218,6 +218,76 @@ typedef struct {
 int gbfem_solve_mixed(gbfem_operator op64, gbfem_operator op32, gbfem_preconditioner pc32,
                       const gbfem_ir_params* prm, const void* f, void* u, gbfem_solver_info* info);
 
+/* ---- nonlinear DG operator, Jacobian, Newton ------------------------------
+ * S(u) = A u + R(u): the DG operator above plus the volume reaction
+ * R(u)_l = int_K r(u_h) phi_l, r(u) = linear u + cubic u^3 + exponential e^u,
+ * by the operator's Gauss rule (q points per direction).  ≙ GalerkinOperator
+ * over a nonlinear UFL integrand (schemes/galerkin.hh:332-360,1383-1504).
+ * gbfem_operator_apply evaluates S; diagonal, block diagonal and assembly are
+ * those of the Jacobian. */
+typedef struct {
+  double linear, cubic, exponential;
+} gbfem_reaction;
+int gbfem_dg_nonlinear_operator_create(const gbfem_dg_desc* desc, const gbfem_reaction* reaction,
+                                       gbfem_operator* op);
+/* ≙ Operator::nonlinear() (operator/common/operator.hh:64). */
+int gbfem_operator_nonlinear(gbfem_operator op, int* nonlinear);
+/* A Jacobian operator for op (storage for the linearisation; initially at u = 0
+ * for a nonlinear op, the op itself for a linear one).  Destroy it with
+ * gbfem_operator_destroy. */
+int gbfem_operator_jacobian_create(gbfem_operator op, gbfem_operator* jac);
+/* Linearises op at the device vector u into jac: jac = A + R'(u), a linear
+ * operator with apply, diagonal, block diagonal and assembly.
+ * ≙ DifferentiableOperator::jacobian(u, jOp) (operator/common/
+ * differentiableoperator.hh:54; schemes/galerkin.hh:1548-1643, 362-410). */
+int gbfem_operator_jacobian(gbfem_operator op, const void* u, gbfem_operator jac, void* stream);
+
+/* Newton's method for S(w) = rhs: NewtonInverseOperator::operator()
+ * (solver/newtoninverseoperator.hh:688-790) statement by statement: residual
+ * r = S(w) - rhs, Jacobian at w, linear solve J dw = r (Krylov `linear`
+ * with the chosen preconditioner of J), w -= dw, new residual, optional
+ * line search (:588-630), Eisenstat-Walker forcing of the linear tolerance
+ * (:44-81, :559-564), stop when |r| < tolerance or on a failure (:570-586). */
+#define GBFEM_PC_NONE 0
+#define GBFEM_PC_DIAGONAL 1
+#define GBFEM_PC_BLOCK_JACOBI 2
+#define GBFEM_LINESEARCH_NONE 0
+#define GBFEM_LINESEARCH_SIMPLE 1
+#define GBFEM_FORCING_NONE 0
+#define GBFEM_FORCING_EISENSTAT_WALKER 1
+typedef struct {
+  double tolerance;             /* |S(w) - rhs|_2 (dof Euclidean norm) < tolerance; default 1e-6 */
+  int max_iterations;           /* default INT_MAX */
+  int max_linear_iterations;    /* total over all linear solves; default linear.max_iterations */
+  int max_line_search_iterations; /* default INT_MAX */
+  int line_search;              /* GBFEM_LINESEARCH_* */
+  int forcing;                  /* GBFEM_FORCING_* */
+  double eta_max, gamma;        /* Eisenstat-Walker parameters (0.99, 0.1) */
+  int simplified;               /* 1: keep the first Jacobian (simplified Newton) */
+  int preconditioner;           /* GBFEM_PC_* of each Jacobian */
+  int verbose;
+  gbfem_solver_params linear;   /* the linear solver (its tolerance is replaced under forcing) */
+} gbfem_newton_params;
+/* NewtonFailure (solver/newtoninverseoperator.hh:389-400) */
+#define GBFEM_NEWTON_SUCCESS 0
+#define GBFEM_NEWTON_INVALID_RESIDUAL 1
+#define GBFEM_NEWTON_LINE_SEARCH_FAILED 4
+#define GBFEM_NEWTON_TOO_MANY_ITERATIONS 5
+#define GBFEM_NEWTON_TOO_MANY_LINEAR_ITERATIONS 6
+#define GBFEM_NEWTON_LINEAR_SOLVER_FAILED 7
+typedef struct {
+  int converged;
+  int iterations;          /* Newton iterations */
+  int linear_iterations;   /* total; negative if a linear solve failed */
+  double residual;         /* final |S(w) - rhs| */
+  int failure;             /* GBFEM_NEWTON_* */
+  double time_ms;
+} gbfem_newton_info;
+int gbfem_newton_params_default(gbfem_newton_params* prm);
+/* w: initial guess in, solution out (device, op's precision). */
+int gbfem_newton_solve(gbfem_operator op, const gbfem_newton_params* prm, const void* rhs, void* w,
+                       gbfem_newton_info* info);
+
 /* ---- projection of closed-form functions (coefficient fields, data) ----- */
 #define GBFEM_FN_EXP_FOURIER 0 /* exp(sum_k a_k cos(2 pi w_k.x + phi_k)): log-Gaussian random field */
 #define GBFEM_FN_GAUSSIAN 1    /* exp(-|x-c|^2/width^2); params = cx, cy, cz, width */
