@@ -615,13 +615,59 @@ def workload_kernels(args):
     return out
 
 
+def workload_newton(args):
+    """Bratu problem -lap u = lambda e^u (lambda = 5, SIPG Q2, weak u = 0) on
+    cells^3 by Newton with block-Jacobi CG for each Jacobian; with and without
+    Eisenstat-Walker forcing.  CPU baseline: the oracle's restated Newton loop
+    with the oracle's Jacobian and a dense solve on a 3^3 grid."""
+    import gbfem
+    N, p = args.cells, 2
+    cells = (N, N, N)
+    reaction = (0.0, 0.0, -5.0)
+    op = gbfem.NonlinearDGOperator(cells, p, reaction=reaction)
+    rhs = gbfem.DeviceArray(op.size)
+    rhs.clear()
+    w = gbfem.DeviceArray(op.size)
+    out = {"metric": "Bratu Newton solve time to |S(u)| < 1e-9 (SIPG Q2, lambda = 5)", "unit": "s",
+           "higher_is_better": False, "dtype": "f64",
+           "config": {"workload": "Bratu -lap u = 5 e^u, SIPG Q2 %d^3, u = 0 weak; Newton + block-Jacobi CG" % N,
+                      "dofs": op.size}}
+    for forcing in ("none", "eisenstatwalker"):
+        newton = gbfem.NewtonInverseOperator(tolerance=1e-9, forcing=forcing, linear_tolerance=1e-10,
+                                             preconditioner=gbfem.PC_BLOCK_JACOBI)
+        newton.bind(op)
+        w.clear()
+        newton(rhs, w)  # warm-up (allocations, first Jacobian)
+        w.clear()
+        _, t = _timed(lambda: newton(rhs, w))
+        info = newton.info()
+        out["forcing_" + forcing] = {"s": t, "newton_iterations": info["iterations"],
+                                     "linear_iterations": info["linear_iterations"], "residual": info["residual"],
+                                     "converged": info["converged"]}
+    out["value"] = min(out["forcing_none"]["s"], out["forcing_eisenstatwalker"]["s"])
+    out["max_u"] = float(np.max(w.numpy()))
+    # oracle on 3^3 (dense Jacobian solves)
+    import oracle
+    import nonlinear_oracle as no
+    prob = oracle.DGProblem((3, 3, 3), p)
+    P = no.NonlinearProblem(prob, reaction)
+    t0 = time.perf_counter()
+    _, io = no.newton(P.apply, lambda ww, r, tol: (np.linalg.solve(P.jacobian_matrix(ww), r), 1),
+                      np.zeros(prob.ndofs), np.zeros(prob.ndofs), tolerance=1e-9)
+    out["cpu_baseline"] = {"value": time.perf_counter() - t0, "unit": "s", "cores": 1, "kind": "port",
+                           "sample": "3^3 cells Q2: oracle Newton, dense Jacobian from the oracle apply, numpy solve",
+                           "newton_iterations": io["iterations"]}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbfem", choices=["gbfem", "reference"])
-    ap.add_argument("--workload", default="apply", choices=["apply", "q1cg", "rk3", "mixed", "learned", "kernels"])
+    ap.add_argument("--workload", default="apply",
+                    choices=["apply", "q1cg", "rk3", "mixed", "learned", "kernels", "newton"])
     ap.add_argument("--rk-steps", type=int, default=100)
     ap.add_argument("--cells", type=int, default=96)
     ap.add_argument("--order", type=int, default=3)
@@ -642,7 +688,7 @@ def main():
     args = ap.parse_args()
     if args.workload != "apply":
         fn = {"q1cg": workload_q1cg, "rk3": workload_rk3, "mixed": workload_mixed,
-              "learned": workload_learned, "kernels": workload_kernels}[args.workload]
+              "learned": workload_learned, "kernels": workload_kernels, "newton": workload_newton}[args.workload]
         line = fn(args)
         line.update({"n_gpus": 1, "data": "synthetic"})
         print(json.dumps(line), flush=True)
