@@ -153,6 +153,8 @@ def lib():
         L.gbfem_operator_jacobian_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
         L.gbfem_operator_jacobian.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.gbfem_newton_params_default.argtypes = [C.POINTER(NewtonParams)]
+        L.gbfem_legendre_hierarchical_permutation.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int)]
+        L.gbfem_dg_permute.argtypes = [C.c_int, C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.gbfem_newton_solve.argtypes = [C.c_void_p, C.POINTER(NewtonParams), C.c_void_p, C.c_void_p,
                                          C.POINTER(NewtonInfo)]
         _lib = L
@@ -568,6 +570,27 @@ class RK3:
                 self.handle = None
         except Exception:
             pass
+
+
+def hierarchical_permutation(order, dim=3):
+    """perm[h] = non-hierarchical local index of the h-th hierarchical Legendre shape function."""
+    perm = (C.c_int * ((order + 1) ** dim))()
+    check(lib().gbfem_legendre_hierarchical_permutation(order, dim, perm))
+    return np.array(perm[:], dtype=np.int64)
+
+
+def to_hierarchical(u, order):
+    """The dof vector u (library order) in the hierarchical local order (a new DeviceArray)."""
+    out = DeviceArray(u.n, u.precision)
+    check(lib().gbfem_dg_permute(u.precision, u.n // (order + 1) ** 3, order, 1, u.ptr, out.ptr, None))
+    return out
+
+
+def from_hierarchical(u, order):
+    """The inverse of to_hierarchical."""
+    out = DeviceArray(u.n, u.precision)
+    check(lib().gbfem_dg_permute(u.precision, u.n // (order + 1) ** 3, order, 0, u.ptr, out.ptr, None))
+    return out
 
 
 def time_step_estimate(op, power_iterations=30, seed=0):

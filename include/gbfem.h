@@ -306,6 +306,19 @@ int gbfem_dg_project(const gbfem_grid_desc* grid, int order, int quad_points, in
                      const double* modes_host, int nmodes, int scale_by_volume, int precision, void* out,
                      void* stream);
 
+/* ---- local dof orderings --------------------------------------------------
+ * The library's local order is the non-hierarchical i0 (p+1)^2 + i1 (p+1) + i2
+ * (i0 the x-degree).  The hierarchical LegendreShapeFunctionSet sorts by
+ * maximal degree, then lexicographically by (i0, i1, i2)
+ * (space/shapefunctionset/legendre.hh:236-249, 294-299; the Python default
+ * dglegendre(hierarchical=True)).  perm[h] = the non-hierarchical index of
+ * the h-th hierarchical shape function ((order+1)^dim entries). */
+int gbfem_legendre_hierarchical_permutation(int order, int dim, int* perm);
+/* Whole 3-D DG dof vectors between the orderings (device arrays, in != out):
+ * to_hierarchical = 1: out[c][h] = in[c][perm[h]]; 0: the inverse. */
+int gbfem_dg_permute(int precision, int64_t ncells, int order, int to_hierarchical, const void* in, void* out,
+                     void* stream);
+
 /* ---- explicit SSP-RK3 of the method-of-lines DG operator --------------------
  * u' = -M^{-1} A(u), M^{-1} = 1/|K| for the orthonormal basis on affine cells.
  * ≙ ExplicitRungeKuttaSolver with tvd3ButcherTable (solver/rungekutta/

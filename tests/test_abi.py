@@ -7,6 +7,8 @@ import glob
 import os
 import re
 
+import pytest
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -44,3 +46,23 @@ def test_invalid_descriptor_is_rejected_without_gpu(gb):
     import pytest
     with pytest.raises(gb.GbfemError):
         gb.DGOperator((2, 2, 2), 9)
+
+
+def _reference_hierarchical_order(order, dim):
+    """LegendreShapeFunctionSet with hierarchical ordering (legendre.hh:236-249,
+    294-299): the multi-indices of DefaultFactory::fill (first index slowest)
+    sorted by maximal degree, then lexicographically."""
+    import itertools
+    idx = list(itertools.product(range(order + 1), repeat=dim))  # fill order: non-hierarchical index = position
+    return sorted(range(len(idx)), key=lambda l: (max(idx[l]), idx[l]))
+
+
+@pytest.mark.parametrize("order", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_hierarchical_permutation_matches_the_reference_sort(gb, order, dim):
+    perm = gb.hierarchical_permutation(order, dim)
+    assert list(perm) == _reference_hierarchical_order(order, dim)
+    if order == 1 and dim == 3:
+        assert list(perm) == list(range(8))  # every Q1 function other than 1 has degree 1: lexicographic = natural
+    if order == 2 and dim == 2:
+        assert list(perm) == [0, 1, 3, 4, 2, 5, 6, 7, 8]

@@ -92,3 +92,18 @@ def test_rk3_conserves_mass_on_periodic_grid(gb, orc):
     x = u.numpy()
     assert np.all(np.isfinite(x))
     assert abs(x[::nl].sum() - m0) < 1e-12 * abs(m0)
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_hierarchical_permute_round_trip(gb, order):
+    nloc = (order + 1) ** 3
+    ncells = 37
+    u = np.random.default_rng(order).uniform(-1, 1, ncells * nloc)
+    perm = gb.hierarchical_permutation(order)
+    d = gb.DeviceArray.from_numpy(u)
+    h = gb.to_hierarchical(d, order)
+    assert np.array_equal(h.numpy(), u.reshape(ncells, nloc)[:, perm].ravel())
+    back = gb.from_hierarchical(h, order)
+    assert np.array_equal(back.numpy(), u)
+    h32 = gb.to_hierarchical(gb.DeviceArray.from_numpy(u.astype(np.float32)), order)
+    assert np.array_equal(h32.numpy(), u.astype(np.float32).reshape(ncells, nloc)[:, perm].ravel())
