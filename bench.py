@@ -492,6 +492,16 @@ def workload_mixed(args):
                 "mixed_operator_applies": info.operator_applies})
     x_mixed = u.numpy()
     del pc32
+    # the same refinement with scaled FP16 block-Jacobi storage (half the
+    # preconditioner traffic of the FP32 inner iteration)
+    (pc16, t_setup16) = _timed(lambda: gbfem.Preconditioner.block_jacobi(op64, gbfem.F16))
+    u.clear()
+    info16, t_mixed16 = _timed(lambda: gbfem.solve_mixed(op64, op32, pc16, f, u, tolerance=1e-10,
+                                                         inner_tolerance=args.inner_tol, max_outer=60))
+    out.update({"mixed_f16_blocks_s": t_mixed16, "mixed_f16_setup_s": t_setup16,
+                "mixed_f16_converged": bool(info16.converged), "mixed_f16_rel_residual": info16.residual,
+                "mixed_f16_inner_iterations": info16.iterations})
+    del pc16
     if not args.skip_fp64:
         (pc64, t_setup64) = _timed(lambda: gbfem.Preconditioner.block_jacobi(op64))
         inv = gbfem.KrylovInverseOperator("cg", tolerance=1e-10, max_iterations=args.fp64_max_iter)
@@ -598,6 +608,9 @@ def workload_kernels(args):
     out["bj32_setup_s"] = time.perf_counter() - t0
     out["bj64_apply"] = ev(lambda: bj64(u64, w64, sptr))
     out["bj32_apply"] = ev(lambda: bj32(u32, w32, sptr))
+    bj16 = gbfem.Preconditioner.block_jacobi(op32, gbfem.F16)
+    out["bj16_apply"] = ev(lambda: bj16(u32, w32, sptr))
+    del bj16
     out["dot_f64_host_result"] = ev(lambda: gbfem.dot(u64, w64, sptr))
     out["axpy_f64"] = ev(lambda: gbfem.axpy(0.5, u64, w64, sptr))
     for name, op, pc, fv in (("cg_iter_f64_bj", op64, bj64, f), ("cg_iter_f32_bj", op32, bj32, gbfem.convert(f, gbfem.F32))):

@@ -10,6 +10,7 @@
 // of blas.cu, read back with one stream synchronisation.  FCG and FGMRES
 // (flexible variants for a preconditioner that changes between iterations,
 // e.g. the learned one) follow Notay (2000) and Saad (1993).
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <chrono>
 #include <climits>
@@ -17,6 +18,7 @@
 #include <cstdio>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "blas.cuh"
@@ -59,7 +61,7 @@ __global__ void k_diag_invert(long long n, T* __restrict__ d) {
 // per CTA, in FP64 shared memory; result stored in TO.
 template <typename TI, typename TO>
 __global__ void k_block_invert(const TI* __restrict__ blocks, TO* __restrict__ inv, int nb, long long nblocks,
-                               int* __restrict__ singular) {
+                               int* __restrict__ singular, float* __restrict__ scales) {
   extern __shared__ __align__(16) unsigned char smraw[];
   double* a = reinterpret_cast<double*>(smraw);  // nb*nb
   int* perm = reinterpret_cast<int*>(a + nb * nb);  // nb
@@ -132,10 +134,51 @@ __global__ void k_block_invert(const TI* __restrict__ blocks, TO* __restrict__ i
   }
   // stored transposed (column j contiguous) for the coalesced apply
   TO* dst = inv + b * nb * nb;
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    const int i = e / nb, j = e - i * nb;
-    dst[j * nb + i] = TO(a[e]);
+  if constexpr (std::is_same<TO, __half>::value) {
+    // FP16 storage: entries / max|entry| of the block, the max as an FP32 scale
+    __shared__ double s_max[32];
+    double m = 0.0;
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) m = fmax(m, fabs(a[e]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double mm = 0.0;
+      for (int w = 0; w < int(blockDim.x >> 5); ++w) mm = fmax(mm, s_max[w]);
+      s_max[0] = mm > 0.0 ? mm : 1.0;
+      scales[b] = float(s_max[0]);
+    }
+    __syncthreads();
+    const double inv_scale = 1.0 / s_max[0];
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+      const int i = e / nb, j = e - i * nb;
+      dst[j * nb + i] = __float2half_rn(float(a[e] * inv_scale));
+    }
+  } else {
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+      const int i = e / nb, j = e - i * nb;
+      dst[j * nb + i] = TO(a[e]);
+    }
   }
+}
+
+// FP16 blocks with per-block scale, FP32 vectors: z_K = s_K (Binv_K / s_K) r_K
+__global__ void k_block_apply_h(const __half* __restrict__ binvT, const float* __restrict__ scales,
+                                const float* __restrict__ r, float* __restrict__ z, int nb, long long ncells, int cpb) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float* rs = reinterpret_cast<float*>(smraw);  // [cpb][nb]
+  const long long c0 = (long long)blockIdx.x * cpb;
+  const int ncell = int(ncells - c0 < cpb ? ncells - c0 : cpb);
+  for (int e = threadIdx.x; e < ncell * nb; e += blockDim.x) rs[e] = r[c0 * nb + e];
+  __syncthreads();
+  const int lc = threadIdx.x / nb, i = threadIdx.x - lc * nb;
+  if (lc >= ncell) return;
+  const __half* B = binvT + (c0 + lc) * (long long)nb * nb + i;
+  const float* rc = rs + lc * nb;
+  float acc = 0.0f;
+  for (int j = 0; j < nb; ++j) acc = fmaf(__half2float(B[(long long)j * nb]), rc[j], acc);
+  z[(c0 + lc) * nb + i] = acc * scales[c0 + lc];
 }
 
 // z_K = Binv_K r_K with Binv_K stored transposed (binvT[K][j][i]): one thread
@@ -255,7 +298,10 @@ int precond_apply(const gbfem_preconditioner_s* pc, const void* r, void* z, cuda
       const int threads = ((cpb * nb + 31) / 32) * 32;
       const size_t sm = size_t(cpb) * nb * (pc->precision == GBFEM_F64 ? 8 : 4);
       const unsigned blocks = unsigned((nc + cpb - 1) / cpb);
-      if (pc->precision == GBFEM_F64)
+      if (pc->storage == GBFEM_F16)
+        k_block_apply_h<<<blocks, threads, sm, s>>>((const __half*)pc->data, pc->scales, (const float*)r, (float*)z,
+                                                    nb, nc, cpb);
+      else if (pc->precision == GBFEM_F64)
         k_block_apply<double><<<blocks, threads, sm, s>>>((const double*)pc->data, (const double*)r, (double*)z, nb,
                                                           nc, cpb);
       else
@@ -836,18 +882,21 @@ int gbfem_preconditioner_block_jacobi_create(gbfem_operator op, int precision, g
   *out = nullptr;
   if (op->kind != OpKind::DG && op->kind != OpKind::BSR)
     return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "block Jacobi needs a DG operator");
-  if (precision != GBFEM_F64 && precision != GBFEM_F32) return set_error(GBFEM_ERR_INVALID, "bad precision");
+  if (precision != GBFEM_F64 && precision != GBFEM_F32 && precision != GBFEM_F16)
+    return set_error(GBFEM_ERR_INVALID, "bad precision");
   auto* pc = new (std::nothrow) gbfem_preconditioner_s();
   if (!pc) return set_error(GBFEM_ERR_INVALID, "out of host memory");
   pc->kind = PcKind::BlockJacobi;
-  pc->precision = precision;
+  pc->storage = precision;
+  pc->precision = precision == GBFEM_F16 ? GBFEM_F32 : precision;  // vectors
   pc->n = op->ndofs;
   pc->nloc = op->nloc;
   const int nb = op->nloc;
-  const size_t isz = precision == GBFEM_F64 ? 8 : 4;
+  const size_t isz = precision == GBFEM_F64 ? 8 : (precision == GBFEM_F32 ? 4 : 2);
   const size_t osz = op->precision == GBFEM_F64 ? 8 : 4;
   cudaError_t e = cudaMalloc(&pc->data, size_t(op->ncells) * nb * nb * isz);
-  if (e != cudaSuccess) { delete pc; return set_cuda_error(e, "block Jacobi storage"); }
+  if (e == cudaSuccess && precision == GBFEM_F16) e = cudaMalloc(&pc->scales, size_t(op->ncells) * sizeof(float));
+  if (e != cudaSuccess) { gbfem_preconditioner_destroy(pc); return set_cuda_error(e, "block Jacobi storage"); }
   // blocks in batches of cells (bounded temporary: <= ~1 GB)
   long long batch = (1LL << 30) / ((long long)nb * nb * (long long)osz);
   if (batch < 1) batch = 1;
@@ -875,22 +924,31 @@ int gbfem_preconditioner_block_jacobi_create(gbfem_operator op, int precision, g
       rc = dg_apply(op, nullptr, nullptr, nullptr, 1, tmp, c0, cnt);
     }
     if (rc) break;
-    if (op->precision == GBFEM_F64 && precision == GBFEM_F64) {
+    float* sc = pc->scales ? pc->scales + c0 : nullptr;
+    if (precision == GBFEM_F16 && op->precision == GBFEM_F64) {
+      cudaFuncSetAttribute(k_block_invert<double, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+      k_block_invert<double, __half><<<unsigned(cnt), 256, sm>>>((const double*)tmp,
+                                                                ((__half*)pc->data) + c0 * nb * nb, nb, cnt, d_sing, sc);
+    } else if (precision == GBFEM_F16) {
+      cudaFuncSetAttribute(k_block_invert<float, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
+      k_block_invert<float, __half><<<unsigned(cnt), 256, sm>>>((const float*)tmp,
+                                                               ((__half*)pc->data) + c0 * nb * nb, nb, cnt, d_sing, sc);
+    } else if (op->precision == GBFEM_F64 && precision == GBFEM_F64) {
       cudaFuncSetAttribute(k_block_invert<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
       k_block_invert<double, double><<<unsigned(cnt), 256, sm>>>((const double*)tmp,
-                                                                ((double*)pc->data) + c0 * nb * nb, nb, cnt, d_sing);
+                                                                ((double*)pc->data) + c0 * nb * nb, nb, cnt, d_sing, sc);
     } else if (op->precision == GBFEM_F64) {
       cudaFuncSetAttribute(k_block_invert<double, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
       k_block_invert<double, float><<<unsigned(cnt), 256, sm>>>((const double*)tmp,
-                                                               ((float*)pc->data) + c0 * nb * nb, nb, cnt, d_sing);
+                                                               ((float*)pc->data) + c0 * nb * nb, nb, cnt, d_sing, sc);
     } else if (precision == GBFEM_F64) {
       cudaFuncSetAttribute(k_block_invert<float, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
       k_block_invert<float, double><<<unsigned(cnt), 256, sm>>>((const float*)tmp,
-                                                               ((double*)pc->data) + c0 * nb * nb, nb, cnt, d_sing);
+                                                               ((double*)pc->data) + c0 * nb * nb, nb, cnt, d_sing, sc);
     } else {
       cudaFuncSetAttribute(k_block_invert<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
       k_block_invert<float, float><<<unsigned(cnt), 256, sm>>>((const float*)tmp,
-                                                              ((float*)pc->data) + c0 * nb * nb, nb, cnt, d_sing);
+                                                              ((float*)pc->data) + c0 * nb * nb, nb, cnt, d_sing, sc);
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) rc = set_cuda_error(e, "block invert launch");
@@ -922,6 +980,7 @@ int gbfem_preconditioner_precision(gbfem_preconditioner pc, int* precision) {
 int gbfem_preconditioner_destroy(gbfem_preconditioner pc) {
   if (!pc) return GBFEM_OK;
   if (pc->data && pc->owns_data) cudaFree(pc->data);
+  if (pc->scales) cudaFree(pc->scales);
   if (pc->ext_destroy) pc->ext_destroy(pc->ext_ctx);
   delete pc;
   return GBFEM_OK;

@@ -19,6 +19,8 @@ struct gbfem_preconditioner_s {
   int nloc = 1;
   void* data = nullptr;  // diagonal inverse or block inverses
   bool owns_data = true;
+  int storage = GBFEM_F64;   // block Jacobi: GBFEM_F64, GBFEM_F32 or GBFEM_F16 (scaled) blocks
+  float* scales = nullptr;   // GBFEM_F16 storage: one scale per block
   // External (e.g. the learned preconditioner): z = P(r)
   int (*ext_apply)(void* ctx, const void* r, void* z, cudaStream_t s) = nullptr;
   void (*ext_destroy)(void* ctx) = nullptr;

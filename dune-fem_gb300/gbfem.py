@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libgbfem.so")
 
 F64, F32 = 0, 1
+F16 = 2  # block-Jacobi storage only (scaled FP16 blocks, FP32 vectors)
 ALGO_AUTO, ALGO_QUADRATURE = 0, 1
 _DTYPES = {F64: np.float64, F32: np.float32}
 
@@ -446,7 +447,7 @@ class Preconditioner:
         precision = op.precision if precision is None else precision
         h = C.c_void_p()
         check(lib().gbfem_preconditioner_block_jacobi_create(op.handle, precision, C.byref(h)))
-        return cls(h, precision, op)
+        return cls(h, F32 if precision == F16 else precision, op)
 
     def __call__(self, r, z, stream=None):
         check(lib().gbfem_preconditioner_apply(self.handle, r.ptr, z.ptr, stream))

@@ -32,6 +32,9 @@ extern "C" {
 /* precisions of dof vectors and of the arithmetic of an operator */
 #define GBFEM_F64 0
 #define GBFEM_F32 1
+/* block-Jacobi storage only: FP16 inverse blocks scaled by one FP32 factor per
+ * block (max |entry|), applied to FP32 vectors (half the FP32 traffic) */
+#define GBFEM_F16 2
 
 /* Returns the calling thread's last error message ("" if none). */
 const char* gbfem_last_error(void);
@@ -150,7 +153,9 @@ typedef struct gbfem_preconditioner_s* gbfem_preconditioner;
  * ≙ DiagonalPreconditioner (solver/diagonalpreconditioner.hh:80-142). */
 int gbfem_preconditioner_diagonal_create(gbfem_operator op, gbfem_preconditioner* pc);
 /* z_K = (A_KK)^{-1} r_K with the exact element-diagonal blocks of op, inverted
- * by Gauss-Jordan with partial pivoting, stored in `precision`.
+ * by Gauss-Jordan with partial pivoting, stored in `precision` (GBFEM_F16:
+ * scaled FP16 blocks for FP32 vectors; the preconditioner's precision is then
+ * GBFEM_F32).
  * ≙ BlockDiagonalLinearOperator::invert + multiply
  * (operator/linear/blockdiagonal.hh:102-135).  op must be a DG operator. */
 int gbfem_preconditioner_block_jacobi_create(gbfem_operator op, int precision, gbfem_preconditioner* pc);

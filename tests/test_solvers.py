@@ -211,3 +211,32 @@ def test_graph_cg_cap_and_nonfinite(gb, orc):
     g[7] = np.nan
     info, _ = _solve(gb, op, g, "cg", max_iterations=50, graph_chunk=8)
     assert not info["converged"]
+
+
+def test_fp16_block_jacobi_storage(gb, orc):
+    """Scaled FP16 blocks: the apply is the dense inverse to FP16 accuracy, and
+    the mixed solve with them still reaches the FP64 tolerance."""
+    cells, order = (3, 3, 2), 3
+    kw = dict(mass=0.5, velocity=(0.2, 0.0, -0.1))
+    op = gb.DGOperator(cells, order, **kw)
+    prob = orc.DGProblem(cells, order, **kw)
+    pc = gb.Preconditioner.block_jacobi(op, gb.F16)
+    assert pc.precision == gb.F32
+    f = np.random.default_rng(9).uniform(-1, 1, op.size)
+    z = gb.DeviceArray(op.size, gb.F32)
+    pc(gb.DeviceArray.from_numpy(f.astype(np.float32)), z)
+    binv = np.linalg.inv(prob.block_diagonal())
+    ref = np.einsum("cij,cj->ci", binv, f.astype(np.float32).reshape(-1, prob.nloc)).ravel()
+    err = relmax(z.numpy(), ref)
+    assert 1e-6 < err < 3e-3  # FP16 rounding is visible but small
+    cells, order = (4, 4, 4), 3
+    op64 = gb.DGOperator(cells, order)
+    op32 = gb.DGOperator(cells, order, precision=gb.F32)
+    pc16 = gb.Preconditioner.block_jacobi(op64, gb.F16)
+    f = np.random.default_rng(10).uniform(-1, 1, op64.size)
+    u = gb.DeviceArray(op64.size)
+    u.clear()
+    info = gb.solve_mixed(op64, op32, pc16, gb.DeviceArray.from_numpy(f), u, tolerance=1e-10, inner_tolerance=1e-3)
+    assert info.converged and info.residual <= 1e-10
+    prob = orc.DGProblem(cells, order)
+    assert np.linalg.norm(f - prob.apply(u.numpy())) <= 1.01e-10 * np.linalg.norm(f)
