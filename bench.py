@@ -478,7 +478,7 @@ def workload_mixed(args):
     f = gbfem.project(cells, p, gbfem.FN_CONSTANT, params=(1.0,), scale_by_volume=True)
     op64 = gbfem.DGOperator(cells, p, kappa=k64)
     op32 = gbfem.DGOperator(cells, p, precision=gbfem.F32, kappa=k32)
-    out = {"metric": "SIPG Q4 variable-kappa solve time to 1e-10 (mixed FP32-in-FP64 IR vs FP64 CG)",
+    out = {"metric": "SIPG Q4 variable-kappa solve time to 1e-10 (mixed FP32-in-FP64 vs FP64 CG)",
            "unit": "s", "higher_is_better": False, "dtype": "f64 outer / f32 inner",
            "config": {"workload": "SIPG Q4 %d^3, -div(kappa grad u) = 1, u = 0 weak, log kappa ~ 256 Fourier modes "
                                   "(std 1, corr 0.1), seed %d" % (N, args.seed), "dofs": op64.size}}
@@ -491,14 +491,30 @@ def workload_mixed(args):
                 "mixed_rel_residual": info.residual, "mixed_inner_iterations": info.iterations,
                 "mixed_operator_applies": info.operator_applies})
     x_mixed = u.numpy()
+    out["mixed_outer_iterations"] = info.outer_iterations
+    # flexible FP64 outer Krylov (FGMRES) with the FP32 inner solve as its
+    # preconditioner: converges where plain refinement stalls on cond(A) eps32
+    u.clear()
+    infog, t_fg = _timed(lambda: gbfem.solve_mixed(op64, op32, pc32, f, u, tolerance=1e-10,
+                                                   inner_tolerance=args.fgmres_inner_tol, max_outer=300,
+                                                   outer="fgmres", outer_restart=30))
+    out.update({"mixed_fgmres_s": t_fg, "mixed_fgmres_converged": bool(infog.converged),
+                "mixed_fgmres_rel_residual": infog.residual, "mixed_fgmres_inner_iterations": infog.iterations,
+                "mixed_fgmres_outer_iterations": infog.outer_iterations})
+    if infog.converged and (not info.converged or t_fg < t_mixed):
+        x_mixed = u.numpy()
+        out["value"] = t_fg
+        out["value_from"] = "mixed_fgmres"
     del pc32
-    # the same refinement with scaled FP16 block-Jacobi storage (half the
+    # the flexible outer solve with scaled FP16 block-Jacobi storage (half the
     # preconditioner traffic of the FP32 inner iteration)
     (pc16, t_setup16) = _timed(lambda: gbfem.Preconditioner.block_jacobi(op64, gbfem.F16))
     u.clear()
     info16, t_mixed16 = _timed(lambda: gbfem.solve_mixed(op64, op32, pc16, f, u, tolerance=1e-10,
-                                                         inner_tolerance=args.inner_tol, max_outer=60))
-    out.update({"mixed_f16_blocks_s": t_mixed16, "mixed_f16_setup_s": t_setup16,
+                                                         inner_tolerance=args.fgmres_inner_tol, max_outer=300,
+                                                         outer="fgmres", outer_restart=30))
+    out.update({"mixed_f16_blocks_fgmres_s": t_mixed16, "mixed_f16_setup_s": t_setup16,
+                "mixed_f16_outer_iterations": info16.outer_iterations,
                 "mixed_f16_converged": bool(info16.converged), "mixed_f16_rel_residual": info16.residual,
                 "mixed_f16_inner_iterations": info16.iterations})
     del pc16
@@ -511,7 +527,7 @@ def workload_mixed(args):
         i64 = inv.info()
         x64 = u.numpy()
         out.update({"fp64_cg_s": t64, "fp64_setup_s": t_setup64, "fp64_converged": i64["converged"],
-                    "fp64_iterations": i64["iterations"], "speedup_mixed_vs_fp64": t64 / t_mixed,
+                    "fp64_iterations": i64["iterations"], "speedup_mixed_vs_fp64": t64 / out["value"],
                     "mixed_vs_fp64_rel_max_diff": float(np.max(np.abs(x_mixed - x64)) / np.max(np.abs(x64)))})
     return out
 
@@ -686,6 +702,7 @@ def main():
     ap.add_argument("--order", type=int, default=3)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--inner-tol", type=float, default=1e-3)
+    ap.add_argument("--fgmres-inner-tol", type=float, default=1e-2)
     ap.add_argument("--fp64-max-iter", type=int, default=20000)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--train-seeds", type=int, default=256)

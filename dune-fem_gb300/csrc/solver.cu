@@ -995,8 +995,53 @@ int gbfem_solve(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_p
   return solve_impl(op, pc, *prm, f, u, info, nullptr);
 }
 
-// FP64 iterative refinement around an FP32 inner solve.
-//   r = f - A64 u;  while ||r|| > tol ||f||:  solve A32 d = r/||r|| (FP32),  u += ||r|| d
+}  // extern "C"
+
+namespace gbfem {
+
+// The FP32 inner solve as an FP64 preconditioner: z = ||r|| A32^{-1}(r / ||r||),
+// A32^{-1} the inner Krylov solve to its relative tolerance.  It is a
+// nonlinear (inexact) preconditioner, so the outer method must be flexible.
+struct InnerSolvePc {
+  gbfem_operator op32;
+  gbfem_preconditioner pc32;
+  gbfem_solver_params ip;
+  long long n;
+  void* r32;
+  void* d32;
+  long long inner_total = 0;
+  int op_applies = 0, pc_applies = 0;
+};
+
+static int inner_solve_apply(void* ctx, const void* r, void* z, cudaStream_t s) {
+  auto* x = static_cast<InnerSolvePc*>(ctx);
+  double rr = 0.0;
+  GBFEM_TRY(gbfem_dot(GBFEM_F64, x->n, r, r, &rr, s));
+  const double rn = std::sqrt(rr);
+  if (!(rn > 0.0) || !std::isfinite(rn)) {
+    GBFEM_CUDA_TRY(cudaMemsetAsync(z, 0, size_t(x->n) * 8, s));
+    return rn == 0.0 ? GBFEM_OK : set_error(GBFEM_ERR_NONFINITE, "mixed: non-finite residual");
+  }
+  GBFEM_TRY(gbfem_convert(x->n, GBFEM_F64, r, GBFEM_F32, x->r32, s));
+  GBFEM_TRY(gbfem_scal(GBFEM_F32, x->n, 1.0 / rn, x->r32, s));
+  GBFEM_CUDA_TRY(cudaMemsetAsync(x->d32, 0, size_t(x->n) * 4, s));
+  gbfem_solver_info ii{};
+  GBFEM_TRY(solve_impl(x->op32, x->pc32, x->ip, x->r32, x->d32, &ii, s));
+  x->inner_total += ii.iterations >= 0 ? ii.iterations : -ii.iterations;
+  x->op_applies += ii.operator_applies;
+  x->pc_applies += ii.preconditioner_applies;
+  GBFEM_TRY(gbfem_convert(x->n, GBFEM_F32, x->d32, GBFEM_F64, z, s));
+  GBFEM_TRY(gbfem_scal(GBFEM_F64, x->n, rn, z, s));
+  return GBFEM_OK;
+}
+
+}  // namespace gbfem
+
+extern "C" {
+
+// FP64 outer iteration around an FP32 inner solve.
+//   refinement: r = f - A64 u;  while ||r|| > tol ||f||:  solve A32 d = r/||r|| (FP32),  u += ||r|| d
+//   flexible:   FGMRES / FCG on A64 u = f with the inner solve as the preconditioner
 int gbfem_solve_mixed(gbfem_operator op64, gbfem_operator op32, gbfem_preconditioner pc32, const gbfem_ir_params* prm,
                       const void* f, void* u, gbfem_solver_info* info) {
   if (!op64 || !op32 || !prm || !f || !u || !info) return set_error(GBFEM_ERR_INVALID, "gbfem_solve_mixed: null argument");
@@ -1004,6 +1049,8 @@ int gbfem_solve_mixed(gbfem_operator op64, gbfem_operator op32, gbfem_preconditi
     return set_error(GBFEM_ERR_INVALID, "gbfem_solve_mixed: needs an FP64 and an FP32 operator");
   if (op64->ndofs != op32->ndofs) return set_error(GBFEM_ERR_INVALID, "gbfem_solve_mixed: operator sizes differ");
   if (pc32 && pc32->precision != GBFEM_F32) return set_error(GBFEM_ERR_INVALID, "gbfem_solve_mixed: pc must be FP32");
+  if (prm->outer_method != 0 && prm->outer_method != GBFEM_SOLVER_FGMRES && prm->outer_method != GBFEM_SOLVER_FCG)
+    return set_error(GBFEM_ERR_INVALID, "gbfem_solve_mixed: outer_method must be 0, FGMRES or FCG");
   *info = gbfem_solver_info{};
   const auto t0 = std::chrono::steady_clock::now();
   const long long n = op64->ndofs;
@@ -1021,6 +1068,46 @@ int gbfem_solve_mixed(gbfem_operator op64, gbfem_operator op32, gbfem_preconditi
   double rel = 0.0;
   gbfem_solver_params ip = prm->inner;
   ip.error_measure = GBFEM_TOL_RELATIVE;
+  if (prm->outer_method != 0) {
+    InnerSolvePc ctx{op32, pc32, ip, n, r32, d32};
+    gbfem_preconditioner_s px;
+    px.kind = PcKind::External;
+    px.precision = GBFEM_F64;
+    px.n = n;
+    px.nloc = op64->nloc;
+    px.owns_data = false;
+    px.ext_apply = inner_solve_apply;
+    px.ext_ctx = &ctx;
+    gbfem_solver_params op{};
+    GBFEM_TRY(gbfem_solver_params_default(&op));
+    op.method = prm->outer_method;
+    op.tolerance = prm->tolerance;
+    op.error_measure = GBFEM_TOL_RELATIVE;
+    op.max_iterations = prm->max_outer;
+    op.restart = prm->outer_restart > 0 ? prm->outer_restart : 20;
+    op.verbose = prm->inner.verbose;
+    gbfem_solver_info oi{};
+    const int rc = solve_impl(op64, &px, op, f, u, &oi, nullptr);
+    px.ext_ctx = nullptr;
+    GBFEM_TRY(rc);
+    // report the true relative residual, as the refinement does
+    GBFEM_TRY(op_apply(op64, u, r, c64));
+    GBFEM_TRY(c64.axpby(1.0, f, -1.0, r));
+    double rr;
+    GBFEM_TRY(c64.dot(r, r, &rr));
+    rel = fnorm > 0 ? std::sqrt(rr) / fnorm : std::sqrt(rr);
+    info->status = oi.status;
+    if (!std::isfinite(rel)) info->status = GBFEM_ERR_NONFINITE;
+    info->time_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    info->residual = rel;
+    info->converged = (rel <= prm->tolerance && info->status == GBFEM_OK) ? 1 : 0;
+    const long long it = ctx.inner_total < INT_MAX ? ctx.inner_total : INT_MAX;
+    info->iterations = info->converged ? int(it) : -int(it);
+    info->outer_iterations = oi.iterations >= 0 ? oi.iterations : -oi.iterations;
+    info->operator_applies = oi.operator_applies + 1 + ctx.op_applies;
+    info->preconditioner_applies = ctx.pc_applies;
+    return GBFEM_OK;
+  }
   for (outer = 0; outer <= prm->max_outer; ++outer) {
     GBFEM_TRY(op_apply(op64, u, r, c64));
     GBFEM_TRY(c64.axpby(1.0, f, -1.0, r));  // r = f - A u
@@ -1047,6 +1134,7 @@ int gbfem_solve_mixed(gbfem_operator op64, gbfem_operator op32, gbfem_preconditi
   info->residual = rel;
   info->converged = (rel <= prm->tolerance && info->status == GBFEM_OK) ? 1 : 0;
   info->iterations = info->converged ? inner_total : -inner_total;
+  info->outer_iterations = outer;
   info->operator_applies = c64.op_applies;
   info->preconditioner_applies = c64.pc_applies;
   return GBFEM_OK;

@@ -47,11 +47,12 @@ class SolverParams(C.Structure):
 class SolverInfo(C.Structure):
     _fields_ = [("converged", C.c_int), ("iterations", C.c_int), ("residual", C.c_double),
                 ("time_ms", C.c_double), ("operator_applies", C.c_int), ("preconditioner_applies", C.c_int),
-                ("status", C.c_int), ("fallbacks", C.c_int)]
+                ("status", C.c_int), ("fallbacks", C.c_int), ("outer_iterations", C.c_int)]
 
 
 class IRParams(C.Structure):
-    _fields_ = [("tolerance", C.c_double), ("max_outer", C.c_int), ("inner", SolverParams)]
+    _fields_ = [("tolerance", C.c_double), ("max_outer", C.c_int), ("inner", SolverParams),
+                ("outer_method", C.c_int), ("outer_restart", C.c_int)]
 
 
 class Reaction(C.Structure):
@@ -515,13 +516,18 @@ class KrylovInverseOperator:
 
 
 def solve_mixed(op64, op32, pc32, f, u, tolerance=1e-10, max_outer=50, inner_method="cg", inner_tolerance=1e-4,
-                inner_max_iterations=100000, inner_restart=20, verbose=False, graph_chunk=0):
-    """FP64 iterative refinement around an FP32 inner Krylov solve."""
+                inner_max_iterations=100000, inner_restart=20, verbose=False, graph_chunk=0, outer="refinement",
+                outer_restart=20):
+    """FP64 outer iteration around an FP32 inner Krylov solve: outer =
+    "refinement" (iterative refinement), "fgmres" or "fcg" (flexible FP64
+    Krylov with the inner solve as preconditioner)."""
     p = IRParams()
     p.tolerance = tolerance
     p.max_outer = max_outer
     p.inner = solver_params(inner_method, inner_tolerance, RELATIVE, inner_max_iterations, inner_restart, verbose,
                             graph_chunk)
+    p.outer_method = {"refinement": 0, "fgmres": FGMRES, "fcg": FCG}[outer]
+    p.outer_restart = outer_restart
     info = SolverInfo()
     check(lib().gbfem_solve_mixed(op64.handle, op32.handle, pc32.handle if pc32 is not None else None,
                                   C.byref(p), f.ptr, u.ptr, C.byref(info)))

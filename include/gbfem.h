@@ -202,6 +202,7 @@ typedef struct {
   int preconditioner_applies;
   int status;            /* GBFEM_OK, GBFEM_ERR_NONFINITE on NaN/Inf */
   int fallbacks;         /* flexible solvers: switches to the fallback preconditioner */
+  int outer_iterations;  /* gbfem_solve_mixed: refinement steps / outer Krylov iterations */
 } gbfem_solver_info;
 
 /* Fills the reference's defaults: cg, tolerance 1e-8, absolute, max
@@ -212,13 +213,22 @@ int gbfem_solver_params_default(gbfem_solver_params* prm);
 int gbfem_solve(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_params* prm, const void* f,
                 void* u, gbfem_solver_info* info);
 
-/* Mixed precision: FP64 iterative refinement (residual f - A u, update and
+/* Mixed precision: an FP64 outer iteration (residual f - A u, update and
  * convergence test in FP64 with op64) around an FP32 inner Krylov solve with
- * op32 and pc32.  No counterpart in the reference (spec extension). */
+ * op32 and pc32.  No counterpart in the reference.
+ * outer_method 0: iterative refinement, u += ||r|| A32^{-1}(r/||r||).  It
+ *   converges while cond(A) times the FP32 rounding of the apply stays well
+ *   below 1.
+ * outer_method GBFEM_SOLVER_FGMRES or GBFEM_SOLVER_FCG: that flexible FP64
+ *   Krylov method (restart outer_restart) with the FP32 inner solve as its
+ *   preconditioner, which also converges where refinement stalls.  max_outer
+ *   then bounds the outer Krylov iterations. */
 typedef struct {
   double tolerance;          /* outer relative residual ||f - A u|| / ||f|| */
-  int max_outer;             /* refinement steps */
+  int max_outer;             /* refinement steps / outer Krylov iterations */
   gbfem_solver_params inner; /* FP32 inner solve; its tolerance is relative */
+  int outer_method;          /* 0 = refinement, GBFEM_SOLVER_FGMRES, GBFEM_SOLVER_FCG */
+  int outer_restart;         /* directions kept by the flexible outer method (0 = 20) */
 } gbfem_ir_params;
 int gbfem_solve_mixed(gbfem_operator op64, gbfem_operator op32, gbfem_preconditioner pc32,
                       const gbfem_ir_params* prm, const void* f, void* u, gbfem_solver_info* info);

@@ -240,3 +240,23 @@ def test_fp16_block_jacobi_storage(gb, orc):
     assert info.converged and info.residual <= 1e-10
     prob = orc.DGProblem(cells, order)
     assert np.linalg.norm(f - prob.apply(u.numpy())) <= 1.01e-10 * np.linalg.norm(f)
+
+
+@pytest.mark.parametrize("outer", ["fgmres", "fcg"])
+def test_mixed_flexible_outer_reaches_fp64_tolerance(gb, orc, outer):
+    """FP64 FGMRES / FCG with the FP32 inner solve as preconditioner."""
+    cells, order = (4, 4, 4), 3
+    modes = gb.fourier_modes(3, 64, 0.2, 1.0)
+    k64 = gb.project(cells, order, gb.FN_EXP_FOURIER, modes=modes)
+    k32 = gb.project(cells, order, gb.FN_EXP_FOURIER, modes=modes, precision=gb.F32)
+    op64 = gb.DGOperator(cells, order, kappa=k64)
+    op32 = gb.DGOperator(cells, order, precision=gb.F32, kappa=k32)
+    pc32 = gb.Preconditioner.block_jacobi(op64, gb.F32)
+    f = np.random.default_rng(12).uniform(-1, 1, op64.size)
+    u = gb.DeviceArray(op64.size)
+    u.clear()
+    info = gb.solve_mixed(op64, op32, pc32, gb.DeviceArray.from_numpy(f), u, tolerance=1e-10, inner_tolerance=1e-2,
+                          outer=outer, max_outer=200)
+    assert info.converged and info.residual <= 1e-10 and info.outer_iterations > 0
+    prob = orc.DGProblem(cells, order)
+    assert np.linalg.norm(f - prob.apply(u.numpy(), kappa=k64.numpy())) <= 1.01e-10 * np.linalg.norm(f)
