@@ -311,6 +311,8 @@ int precond_apply(const gbfem_preconditioner_s* pc, const void* r, void* z, cuda
     }
     case PcKind::External:
       return pc->ext_apply(pc->ext_ctx, r, z, s);
+    case PcKind::Sor:
+      return sor_apply(pc, r, z, s);
   }
   GBFEM_CUDA_TRY(cudaGetLastError());
   return GBFEM_OK;
@@ -981,6 +983,8 @@ int gbfem_preconditioner_destroy(gbfem_preconditioner pc) {
   if (!pc) return GBFEM_OK;
   if (pc->data && pc->owns_data) cudaFree(pc->data);
   if (pc->scales) cudaFree(pc->scales);
+  if (pc->sor_cells) cudaFree(pc->sor_cells);
+  if (pc->sor_tmp) cudaFree(pc->sor_tmp);
   if (pc->ext_destroy) pc->ext_destroy(pc->ext_ctx);
   delete pc;
   return GBFEM_OK;

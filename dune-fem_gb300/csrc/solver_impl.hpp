@@ -2,13 +2,17 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "../../include/gbfem.h"
 
 namespace gbfem {
 
-enum class PcKind { Diagonal = 1, BlockJacobi = 2, External = 3 };
+enum class PcKind { Diagonal = 1, BlockJacobi = 2, External = 3, Sor = 4 };
 
 int precond_apply(const struct ::gbfem_preconditioner_s* pc, const void* r, void* z, cudaStream_t s);
+// Jacobi / Gauss-Seidel / SOR / SSOR sweeps over an assembled operator (sor.cu)
+int sor_apply(const struct ::gbfem_preconditioner_s* pc, const void* r, void* z, cudaStream_t s);
 
 }  // namespace gbfem
 
@@ -28,4 +32,13 @@ struct gbfem_preconditioner_s {
   // Flexible solvers switch to this preconditioner when the iteration with
   // this one stagnates (the learned preconditioner's block-Jacobi fallback).
   struct gbfem_preconditioner_s* fallback = nullptr;
+  // Sor: the assembled operator (not owned), method (GBFEM_SMOOTHER_*),
+  // sweeps, relaxation, cells grouped by level x+y+z with the level offsets,
+  // and the previous iterate of Jacobi; data holds 1/diag
+  const struct gbfem_operator_s* sor_op = nullptr;
+  int sor_method = 0, sor_sweeps = 1;
+  double sor_relax = 1.0;
+  int* sor_cells = nullptr;
+  void* sor_tmp = nullptr;
+  std::vector<long long> sor_level_offsets;
 };

@@ -143,6 +143,8 @@ def lib():
         L.gbfem_preconditioner_diagonal_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
         L.gbfem_preconditioner_block_jacobi_create.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
         L.gbfem_preconditioner_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.gbfem_preconditioner_sor_create.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double,
+                                                      C.POINTER(C.c_void_p)]
         L.gbfem_preconditioner_destroy.argtypes = [C.c_void_p]
         L.gbfem_solver_params_default.argtypes = [C.POINTER(SolverParams)]
         L.gbfem_solve.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(SolverParams), C.c_void_p, C.c_void_p,
@@ -449,6 +451,17 @@ class Preconditioner:
         h = C.c_void_p()
         check(lib().gbfem_preconditioner_block_jacobi_create(op.handle, precision, C.byref(h)))
         return cls(h, F32 if precision == F16 else precision, op)
+
+    SMOOTHERS = {"ssor": 2, "sor": 3, "gauss-seidel": 5, "jacobi": 6}
+
+    @classmethod
+    def sor(cls, assembled, method="ssor", iterations=1, relaxation=1.0):
+        """Jacobi / Gauss-Seidel / SOR / SSOR sweeps of an assembled operator
+        (Operator.assemble()), fem.solver.preconditioning.method."""
+        h = C.c_void_p()
+        check(lib().gbfem_preconditioner_sor_create(assembled.handle, cls.SMOOTHERS[method], iterations, relaxation,
+                                                    C.byref(h)))
+        return cls(h, assembled.precision, assembled)
 
     def __call__(self, r, z, stream=None):
         check(lib().gbfem_preconditioner_apply(self.handle, r.ptr, z.ptr, stream))

@@ -159,6 +159,22 @@ int gbfem_preconditioner_diagonal_create(gbfem_operator op, gbfem_preconditioner
  * ≙ BlockDiagonalLinearOperator::invert + multiply
  * (operator/linear/blockdiagonal.hh:102-135).  op must be a DG operator. */
 int gbfem_preconditioner_block_jacobi_create(gbfem_operator op, int precision, gbfem_preconditioner* pc);
+/* Stationary-iteration preconditioners of an assembled operator (from
+ * gbfem_operator_assemble; it must outlive pc): FemPreconditioning with
+ * fem.solver.preconditioning.method jacobi / gauss-seidel / sor / ssor
+ * (solver/fempreconditioning.hh:59-161, built as in krylovinverseoperators.hh:
+ * 226-250), sweeping x_i = w (b_i - sum_{j!=i} a_ij x_j) / a_ii in natural row
+ * order (operator/matrix/spmatrix.hh:376-480; SSOR adds the backward sweep),
+ * from x = 0, `iterations` times.  The reference's FemPreconditioning
+ * constructor drops its n and w arguments (fempreconditioning.hh:184-186), so
+ * iterations = 1 and relaxation = 1 reproduce it; Gauss-Seidel always relaxes
+ * with 1.  Method ids are the reference's SolverParameter ids. */
+#define GBFEM_SMOOTHER_SSOR 2
+#define GBFEM_SMOOTHER_SOR 3
+#define GBFEM_SMOOTHER_GAUSS_SEIDEL 5
+#define GBFEM_SMOOTHER_JACOBI 6
+int gbfem_preconditioner_sor_create(gbfem_operator assembled, int method, int iterations, double relaxation,
+                                    gbfem_preconditioner* pc);
 int gbfem_preconditioner_apply(gbfem_preconditioner pc, const void* r, void* z, void* stream);
 int gbfem_preconditioner_precision(gbfem_preconditioner pc, int* precision);
 int gbfem_preconditioner_destroy(gbfem_preconditioner pc);

@@ -55,3 +55,22 @@ def test_constant_is_in_kernel_of_periodic_diffusion(orc):
     u = np.zeros(prob.ndofs)
     u[::prob.nloc] = 1.0  # L_0 = 1 in every cell
     assert np.max(np.abs(prob.apply(u))) < 1e-12
+
+
+def test_smoother_oracle_converges_as_a_stationary_iteration():
+    """The restated sweeps are stationary iterations: on a diagonally dominant
+    matrix, many Jacobi / Gauss-Seidel / SSOR sweeps from 0 reach A^{-1} b."""
+    import numpy as np
+    import smoother_oracle
+    rng = np.random.default_rng(0)
+    n = 12
+    A = rng.uniform(-1, 1, (n, n)) * (rng.uniform(0, 1, (n, n)) < 0.4)
+    A = A + A.T + np.diag(2.0 + np.abs(A).sum(axis=1) + np.abs(A).sum(axis=0))
+    b = rng.uniform(-1, 1, n)
+    x = np.linalg.solve(A, b)
+    for method in ("jacobi", "gauss-seidel", "ssor"):
+        y = smoother_oracle.smoother_apply(A, b, method, iterations=200)
+        assert np.max(np.abs(y - x)) < 1e-12 * np.max(np.abs(x)), method
+    # one Gauss-Seidel sweep is the forward substitution with the lower triangle
+    y = smoother_oracle.smoother_apply(A, b, "gauss-seidel", iterations=1)
+    assert np.allclose(y, np.linalg.solve(np.tril(A), b), rtol=0, atol=1e-14)
