@@ -35,10 +35,13 @@ METRIC = "SIPG apply DoF/s"
 UNIT = "DoF/s"
 BYTES_PER_DOF = 16.0          # read u (8) + write w (8), geometry recomputed, tables on chip
 FLOP_PER_DOF = 402.0          # sum-factorised SIPG Q3, q=5 (volume + faces), the algorithmic count
-# flops the closed-form kernels execute per cell (n = 4, no advection), divided by n^3:
-# traces 3 n^2 lines x (4 n flop + 4 adds); fluxes 6 n^2 x ~12 flop;
-# lines 3 n^2 x (n outputs x (2 (n/2) + 4) flop + 6)
-KERNEL_FLOP_PER_DOF = (3 * 16 * (16 + 4) + 6 * 16 * 12 + 3 * 16 * (4 * (4 + 4) + 6)) / 64.0
+# flops the closed-form kernels execute per cell (n = 4, no advection; an FMA
+# counts 2), divided by n^3:
+#  traces: 3 n^2 lines x (7 FMA (L_0' = 0 skipped) + 4 adds) = 48 x 18
+#  fluxes: 6 n^2 face points x 6 (J, dm + dp, a2 x, FMA, grad)  = 96 x 6
+#  lines:  n^2 lines per axis x (4 adds + 2 x (nonzeros of M_d + 7 face FMAs));
+#          M_d has 5 structural nonzeros for n = 4 (6 on axis 0, the mass entry)
+KERNEL_FLOP_PER_DOF = (48 * 18 + 96 * 6 + 16 * (4 + 2 * (6 + 7)) + 32 * (4 + 2 * (5 + 7))) / 64.0  # = 44.0
 CONFIG = {"workload": "SIPG DG Q3 apply, 3-D unit cube 64^3 hexes, 16.8M dofs, q=5, penalty 160, FP64",
           "cells": list(CELLS), "order": ORDER, "quad_points": QUAD, "dofs": 64 ** 3 * 64,
           "l2": "inputs exceed L2 (u + w = 268 MB > 129 MB), no flush"}
@@ -661,8 +664,12 @@ def workload_newton(args):
            "higher_is_better": False, "dtype": "f64",
            "config": {"workload": "Bratu -lap u = 5 e^u, SIPG Q2 %d^3, u = 0 weak; Newton + block-Jacobi CG" % N,
                       "dofs": op.size}}
-    for forcing in ("none", "eisenstatwalker"):
+    runs = (("none", "cg"), ("eisenstatwalker", "gmres"))
+    for forcing, method in runs:
+        # the forcing term bounds the true residual |J dw - r| <= eta |r|: GMRES
+        # (right preconditioning) measures that one, preconditioned CG does not
         newton = gbfem.NewtonInverseOperator(tolerance=1e-9, forcing=forcing, linear_tolerance=1e-10,
+                                             linear_method=method, linear_restart=50, max_iterations=100,
                                              preconditioner=gbfem.PC_BLOCK_JACOBI)
         newton.bind(op)
         w.clear()
@@ -670,10 +677,11 @@ def workload_newton(args):
         w.clear()
         _, t = _timed(lambda: newton(rhs, w))
         info = newton.info()
-        out["forcing_" + forcing] = {"s": t, "newton_iterations": info["iterations"],
+        out["forcing_" + forcing] = {"s": t, "linear_method": method, "newton_iterations": info["iterations"],
                                      "linear_iterations": info["linear_iterations"], "residual": info["residual"],
                                      "converged": info["converged"]}
-    out["value"] = min(out["forcing_none"]["s"], out["forcing_eisenstatwalker"]["s"])
+    done = [v["s"] for v in (out["forcing_none"], out["forcing_eisenstatwalker"]) if v["converged"]]
+    out["value"] = min(done) if done else None
     out["max_u"] = float(np.max(w.numpy()))
     # oracle on 3^3 (dense Jacobian solves)
     import oracle

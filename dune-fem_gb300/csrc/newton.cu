@@ -181,6 +181,7 @@ int gbfem_newton_solve(gbfem_operator op, const gbfem_newton_params* prm_in, con
   GBFEM_TRY(nt.eval_residual(&nt.delta));
   nt.update_linear_tolerance();
   bool compute_jacobian = true;
+  int idle_solves = 0;  // consecutive linear solves that made no iteration
   PcHolder pc;
   if (nt.prm.verbose) std::printf("Start Newton: tol = %.3e\nNewton iteration 0: |residual| = %.6e\n", nt.prm.tolerance, nt.delta);
   while (true) {
@@ -203,6 +204,16 @@ int gbfem_newton_solve(gbfem_operator op, const gbfem_newton_params* prm_in, con
     GBFEM_TRY(gbfem_solve(jac.op, pc.pc, &lp, nt.residual, dw.p, &li));
     if (li.iterations < 0) {
       nt.linear_iterations = li.iterations;
+      break;
+    }
+    // A preconditioned CG stops on <r, B r> <= eps^2 <b, b> (cg.hh:62-67), which a
+    // loose forcing term can meet before the first iteration: dw = 0 and the
+    // step repeats unchanged.  The reference loop would repeat it until
+    // max_iterations; here two such solves in a row end Newton as a linear
+    // solver failure.
+    idle_solves = li.iterations == 0 ? idle_solves + 1 : 0;
+    if (idle_solves >= 2 && nt.delta >= nt.prm.tolerance) {
+      nt.linear_iterations = -(nt.linear_iterations > 0 ? nt.linear_iterations : 1);
       break;
     }
     nt.linear_iterations += li.iterations;

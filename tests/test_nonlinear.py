@@ -136,7 +136,7 @@ def test_newton_bratu_matches_oracle_newton(gb, orc):
     solve = lambda w, r, tol: (np.linalg.solve(P.jacobian_matrix(w), r), 1)
     wo, io = no.newton(P.apply, solve, np.zeros(op.size), np.zeros(op.size), tolerance=1e-10)
     for pc in (gb.PC_BLOCK_JACOBI, gb.PC_DIAGONAL):
-        newton = gb.NewtonInverseOperator(tolerance=1e-10, preconditioner=pc, linear_tolerance=1e-13)
+        newton = gb.NewtonInverseOperator(tolerance=1e-10, preconditioner=pc, linear_tolerance=1e-13, max_iterations=50)
         newton.bind(op)
         w = gb.DeviceArray(op.size)
         w.clear()
@@ -165,7 +165,8 @@ def test_newton_line_search_matches_oracle(gb, orc):
     wo, io = no.newton(P.apply, solve, np.zeros(op.size), w0, tolerance=1e-10, line_search=True)
     assert io["line_search_halvings"] > 0
     newton = gb.NewtonInverseOperator(tolerance=1e-10, line_search="simple", linear_method="gmres",
-                                      linear_tolerance=1e-14, linear_restart=40, preconditioner=gb.PC_BLOCK_JACOBI)
+                                      linear_tolerance=1e-14, linear_restart=40, preconditioner=gb.PC_BLOCK_JACOBI,
+                                      max_iterations=50)
     newton.bind(op)
     w = gb.DeviceArray.from_numpy(w0)
     rhs = gb.DeviceArray(op.size)
@@ -184,7 +185,10 @@ def test_newton_eisenstat_walker_forcing_saves_linear_iterations(gb):
     f = gb.project(cells, order, gb.FN_CONSTANT, params=(10.0,), scale_by_volume=True)
     res = {}
     for forcing in ("none", "eisenstatwalker"):
-        newton = gb.NewtonInverseOperator(tolerance=1e-9, forcing=forcing, linear_tolerance=1e-12)
+        # GMRES: right preconditioning, so its stopping test is the true
+        # residual |J dw - r| <= eta |r| that the forcing term is meant for
+        newton = gb.NewtonInverseOperator(tolerance=1e-9, forcing=forcing, linear_tolerance=1e-12,
+                                          linear_method="gmres", linear_restart=50, max_iterations=50)
         newton.bind(op)
         w = gb.DeviceArray(op.size)
         w.clear()
@@ -201,7 +205,7 @@ def test_newton_on_a_linear_operator_is_one_linear_solve(gb, orc):
     cells, order = (3, 3, 3), 2
     op = gb.DGOperator(cells, order, mass=0.5)
     f = np.random.default_rng(5).uniform(-1, 1, op.size)
-    newton = gb.NewtonInverseOperator(tolerance=1e-10, linear_tolerance=1e-12)
+    newton = gb.NewtonInverseOperator(tolerance=1e-10, linear_tolerance=1e-12, max_iterations=50)
     newton.bind(op)
     w = gb.DeviceArray(op.size)
     w.clear()
@@ -223,3 +227,21 @@ def test_nonlinear_pipelined_host_apply_is_bitwise_the_device_apply(gb):
     wh = np.empty(op.size)
     op.apply_host(u, wh)
     assert np.array_equal(wh.view(np.uint64), w.numpy().view(np.uint64))
+
+
+@pytest.mark.gpu
+def test_newton_stops_when_the_linear_solves_make_no_progress(gb):
+    """Preconditioned CG with a linear tolerance so loose that <r, B r> <=
+    eps^2 <b, b> holds at the start: dw = 0 twice, Newton ends as a linear
+    solver failure instead of repeating the step."""
+    cells, order = (4, 4, 4), 2
+    op = gb.NonlinearDGOperator(cells, order, reaction=(0.0, 1.0, 0.0))
+    f = gb.project(cells, order, gb.FN_CONSTANT, params=(1.0,), scale_by_volume=True)
+    newton = gb.NewtonInverseOperator(tolerance=1e-12, linear_tolerance=0.999, preconditioner=gb.PC_BLOCK_JACOBI,
+                                      max_iterations=1000)
+    newton.bind(op)
+    w = gb.DeviceArray(op.size)
+    w.clear()
+    newton(f, w)
+    info = newton.info()
+    assert not info["converged"] and info["failure"] == "LinearSolverFailed" and info["iterations"] < 1000
