@@ -647,6 +647,31 @@ def workload_kernels(args):
     return out
 
 
+def workload_apply_kappa(args):
+    """The variable-kappa Gauss-point apply (cells^3, Q_order, q = order+2) in
+    FP32 and FP64: the operator of the mixed solve's inner and outer loops."""
+    import gbfem
+    import torch
+    N, p = args.cells, args.order
+    cells = (N, N, N)
+    modes = gbfem.fourier_modes(args.seed, 256, 0.1, 1.0)
+    out = {"metric": "variable-kappa SIPG apply DoF/s (Gauss-point kernel)", "unit": "DoF/s", "higher_is_better": True,
+           "config": {"workload": "SIPG Q%d %d^3, log-Gaussian kappa (256 Fourier modes)" % (p, N)}}
+    stream = torch.cuda.current_stream()
+    for prec, name in ((gbfem.F32, "f32"), (gbfem.F64, "f64")):
+        k = gbfem.project(cells, p, gbfem.FN_EXP_FOURIER, modes=modes, precision=prec)
+        op = gbfem.DGOperator(cells, p, precision=prec, kappa=k)
+        u0 = np.random.default_rng(SEED).uniform(-1, 1, op.size)
+        u = gbfem.DeviceArray.from_numpy(u0.astype(np.float32) if prec == gbfem.F32 else u0)
+        w = gbfem.DeviceArray(op.size, prec)
+        ms = time_applies(op, u, w, max(3, min(args.steps, 20)), stream)
+        out[name] = {"ms": ms, "dof_per_s": op.size / (ms * 1e-3)}
+        del op, k, u, w
+    out["value"] = out["f32"]["dof_per_s"]
+    out["dtype"] = "f32 (and f64)"
+    return out
+
+
 def workload_newton(args):
     """Bratu problem -lap u = lambda e^u (lambda = 5, SIPG Q2, weak u = 0) on
     cells^3 by Newton with block-Jacobi CG for each Jacobian; with and without
@@ -704,7 +729,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbfem", choices=["gbfem", "reference"])
     ap.add_argument("--workload", default="apply",
-                    choices=["apply", "q1cg", "rk3", "mixed", "learned", "kernels", "newton"])
+                    choices=["apply", "q1cg", "rk3", "mixed", "learned", "kernels", "newton", "apply_kappa"])
     ap.add_argument("--rk-steps", type=int, default=100)
     ap.add_argument("--cells", type=int, default=96)
     ap.add_argument("--order", type=int, default=3)
@@ -726,7 +751,8 @@ def main():
     args = ap.parse_args()
     if args.workload != "apply":
         fn = {"q1cg": workload_q1cg, "rk3": workload_rk3, "mixed": workload_mixed,
-              "learned": workload_learned, "kernels": workload_kernels, "newton": workload_newton}[args.workload]
+              "learned": workload_learned, "kernels": workload_kernels, "newton": workload_newton,
+              "apply_kappa": workload_apply_kappa}[args.workload]
         line = fn(args)
         line.update({"n_gpus": 1, "data": "synthetic"})
         print(json.dumps(line), flush=True)
