@@ -259,7 +259,7 @@ def run_gpu(args, world, rank, local):
     achieved_gbs = BYTES_PER_DOF * n / (ms_step * 1e-3) / 1e9
     achieved_tflops = KERNEL_FLOP_PER_DOF * n / (ms_step * 1e-3) / 1e12
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "dg_const2_q3_64cube_f64.json")
+    prof = os.path.join(ROOT, "profiles", "dg_trace_const_q3_64cube_f64.json")
     if os.path.exists(prof):
         with open(prof) as f:
             traffic = json.load(f).get("dram_bytes_per_launch")

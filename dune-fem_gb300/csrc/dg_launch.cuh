@@ -7,13 +7,20 @@
 
 namespace gbfem {
 
+#ifndef GBFEM_QUAD_CPB_MAX_F32
+#define GBFEM_QUAD_CPB_MAX_F32 8
+#endif
+
 template <typename T, int N, int Q, bool KAPPA>
 int dg_launch_one(const DgArgsT<T>& args, const DgTablesT<T>& tabs, cudaStream_t stream) {
-  // Cells per CTA: as many as fit ~100 KB of shared memory, at most 8.
+  // Cells per CTA: as many as fit ~100 KB of shared memory, at most 8 (FP32:
+  // GBFEM_QUAD_CPB_MAX_F32), 32 threads per cell.
   constexpr int PER_CELL = DgSmem<N, Q, KAPPA, 1>::PER_CELL;
   constexpr int CPB0 = (100 * 1024) / (PER_CELL * int(sizeof(T)));
-  constexpr int CPB = CPB0 >= 8 ? 8 : (CPB0 >= 4 ? 4 : (CPB0 >= 2 ? 2 : 1));
-  constexpr int THREADS = 256;
+  constexpr int CAP = sizeof(T) == 4 ? GBFEM_QUAD_CPB_MAX_F32 : 8;
+  constexpr int CPB1 = CPB0 >= 8 ? 8 : (CPB0 >= 4 ? 4 : (CPB0 >= 2 ? 2 : 1));
+  constexpr int CPB = CPB1 < CAP ? CPB1 : CAP;
+  constexpr int THREADS = sizeof(T) == 4 ? 32 * CPB : 256;
   const size_t smem = size_t(DgSmem<N, Q, KAPPA, CPB>::TOTAL) * sizeof(T);
   auto kern = dg_apply_kernel<T, N, Q, KAPPA, CPB>;
   GBFEM_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
