@@ -488,13 +488,17 @@ def workload_mixed(args):
     (pc32, t_setup32) = _timed(lambda: gbfem.Preconditioner.block_jacobi(op64, gbfem.F32))
     u = gbfem.DeviceArray(op64.size)
     u.clear()
-    info, t_mixed = _timed(lambda: gbfem.solve_mixed(op64, op32, pc32, f, u, tolerance=1e-10,
-                                                     inner_tolerance=args.inner_tol, max_outer=60))
-    out.update({"value": t_mixed, "mixed_setup_s": t_setup32, "mixed_converged": bool(info.converged),
-                "mixed_rel_residual": info.residual, "mixed_inner_iterations": info.iterations,
-                "mixed_operator_applies": info.operator_applies})
-    x_mixed = u.numpy()
-    out["mixed_outer_iterations"] = info.outer_iterations
+    t_mixed = float("inf")
+    info = None
+    x_mixed = None
+    if not args.skip_refinement:
+        info, t_mixed = _timed(lambda: gbfem.solve_mixed(op64, op32, pc32, f, u, tolerance=1e-10,
+                                                         inner_tolerance=args.inner_tol, max_outer=60))
+        out.update({"value": t_mixed, "mixed_setup_s": t_setup32, "mixed_converged": bool(info.converged),
+                    "mixed_rel_residual": info.residual, "mixed_inner_iterations": info.iterations,
+                    "mixed_operator_applies": info.operator_applies,
+                    "mixed_outer_iterations": info.outer_iterations})
+        x_mixed = u.numpy()
     # flexible FP64 outer Krylov (FGMRES) with the FP32 inner solve as its
     # preconditioner: converges where plain refinement stalls on cond(A) eps32
     u.clear()
@@ -504,7 +508,7 @@ def workload_mixed(args):
     out.update({"mixed_fgmres_s": t_fg, "mixed_fgmres_converged": bool(infog.converged),
                 "mixed_fgmres_rel_residual": infog.residual, "mixed_fgmres_inner_iterations": infog.iterations,
                 "mixed_fgmres_outer_iterations": infog.outer_iterations})
-    if infog.converged and (not info.converged or t_fg < t_mixed):
+    if infog.converged and (info is None or not info.converged or t_fg < t_mixed):
         x_mixed = u.numpy()
         out["value"] = t_fg
         out["value_from"] = "mixed_fgmres"
@@ -530,8 +534,9 @@ def workload_mixed(args):
         i64 = inv.info()
         x64 = u.numpy()
         out.update({"fp64_cg_s": t64, "fp64_setup_s": t_setup64, "fp64_converged": i64["converged"],
-                    "fp64_iterations": i64["iterations"], "speedup_mixed_vs_fp64": t64 / out["value"],
-                    "mixed_vs_fp64_rel_max_diff": float(np.max(np.abs(x_mixed - x64)) / np.max(np.abs(x64)))})
+                    "fp64_iterations": i64["iterations"], "speedup_mixed_vs_fp64": t64 / out["value"] if out.get("value") else None,
+                    "mixed_vs_fp64_rel_max_diff": (None if x_mixed is None else
+                                                   float(np.max(np.abs(x_mixed - x64)) / np.max(np.abs(x64))))})
     return out
 
 
@@ -738,6 +743,7 @@ def main():
     ap.add_argument("--fgmres-inner-tol", type=float, default=1e-2)
     ap.add_argument("--fp64-max-iter", type=int, default=20000)
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-refinement", action="store_true")
     ap.add_argument("--train-seeds", type=int, default=256)
     ap.add_argument("--eval-seeds", type=int, default=32)
     ap.add_argument("--train-steps", type=int, default=2)
