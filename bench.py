@@ -497,7 +497,7 @@ def workload_mixed(args):
         out.update({"value": t_mixed, "mixed_setup_s": t_setup32, "mixed_converged": bool(info.converged),
                     "mixed_rel_residual": info.residual, "mixed_inner_iterations": info.iterations,
                     "mixed_operator_applies": info.operator_applies,
-                    "mixed_outer_iterations": info.outer_iterations})
+                    "mixed_outer_iterations": info.outer_iterations, "mixed_stagnated": bool(info.stagnated)})
         x_mixed = u.numpy()
     # flexible FP64 outer Krylov (FGMRES) with the FP32 inner solve as its
     # preconditioner: converges where plain refinement stalls on cond(A) eps32
@@ -507,8 +507,13 @@ def workload_mixed(args):
                                                    outer="fgmres", outer_restart=30))
     out.update({"mixed_fgmres_s": t_fg, "mixed_fgmres_converged": bool(infog.converged),
                 "mixed_fgmres_rel_residual": infog.residual, "mixed_fgmres_inner_iterations": infog.iterations,
-                "mixed_fgmres_outer_iterations": infog.outer_iterations})
-    if infog.converged and (info is None or not info.converged or t_fg < t_mixed):
+                "mixed_fgmres_outer_iterations": infog.outer_iterations,
+                "mixed_fgmres_stagnated": bool(infog.stagnated)})
+    # a stagnated solve stopped at the FP64 rounding floor of the true residual
+    # (the FP64 CG's own true residual, below, sits at the same floor)
+    done_g = infog.converged or infog.stagnated
+    done_r = info is not None and (info.converged or info.stagnated)
+    if done_g and (not done_r or t_fg < t_mixed):
         x_mixed = u.numpy()
         out["value"] = t_fg
         out["value_from"] = "mixed_fgmres"
@@ -523,7 +528,7 @@ def workload_mixed(args):
     out.update({"mixed_f16_blocks_fgmres_s": t_mixed16, "mixed_f16_setup_s": t_setup16,
                 "mixed_f16_outer_iterations": info16.outer_iterations,
                 "mixed_f16_converged": bool(info16.converged), "mixed_f16_rel_residual": info16.residual,
-                "mixed_f16_inner_iterations": info16.iterations})
+                "mixed_f16_inner_iterations": info16.iterations, "mixed_f16_stagnated": bool(info16.stagnated)})
     del pc16
     if not args.skip_fp64:
         (pc64, t_setup64) = _timed(lambda: gbfem.Preconditioner.block_jacobi(op64))
@@ -533,6 +538,13 @@ def workload_mixed(args):
         _, t64 = _timed(lambda: inv(f, u))
         i64 = inv.info()
         x64 = u.numpy()
+        # the FP64 CG stops on <r, B r> (preconditioned); its true relative
+        # residual is the accuracy the mixed solves are compared at
+        au = gbfem.DeviceArray(op64.size)
+        op64(u, au)
+        fh = f.numpy()
+        out["fp64_true_rel_residual"] = float(np.linalg.norm(fh - au.numpy()) / np.linalg.norm(fh))
+        del au
         out.update({"fp64_cg_s": t64, "fp64_setup_s": t_setup64, "fp64_converged": i64["converged"],
                     "fp64_iterations": i64["iterations"], "speedup_mixed_vs_fp64": t64 / out["value"] if out.get("value") else None,
                     "mixed_vs_fp64_rel_max_diff": (None if x_mixed is None else

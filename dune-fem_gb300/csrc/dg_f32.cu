@@ -11,4 +11,8 @@ int dg_const_launch_f32(const DgArgsT<float>& a, const DgConstTablesT<float>& t,
                         cudaStream_t s) {
   return dg_const_launch<float>(a, t, n, traces, phase, s);
 }
+int dg_kappa_points_f32(const float* kappa, float* kq, float* kf, long long ncells, const DgTablesT<float>& t, int n,
+                         int q, cudaStream_t s) {
+  return dg_kappa_points<float>(kappa, kq, kf, ncells, t, n, q, s);
+}
 }  // namespace gbfem

@@ -10,4 +10,8 @@ int dg_const_launch_f64(const DgArgsT<double>& a, const DgConstTablesT<double>& 
                         cudaStream_t s) {
   return dg_const_launch<double>(a, t, n, traces, phase, s);
 }
+int dg_kappa_points_f64(const double* kappa, double* kq, double* kf, long long ncells, const DgTablesT<double>& t, int n,
+                         int q, cudaStream_t s) {
+  return dg_kappa_points<double>(kappa, kq, kf, ncells, t, n, q, s);
+}
 }  // namespace gbfem

@@ -51,7 +51,9 @@ template <typename T>
 struct DgArgsT {
   const T* u;
   T* w;
-  const T* kappa;     // DG coefficients of kappa (used when the KAPPA template flag is set)
+  const T* kappa;     // DG coefficients of kappa (the source of kq, kf)
+  const T* kq;        // KAPPA: kappa at the volume Gauss points [cell][a][b][c]
+  const T* kf;        // KAPPA: kappa at the face Gauss points [cell][face 2d+s][a][b] (own side)
   int nc[3];          // cells per direction
   int periodic[3];
   long long ncells;
@@ -167,12 +169,12 @@ __device__ __forceinline__ void contract(const T* __restrict__ in, int ics, T* _
 template <int N, int Q, bool KAPPA, int CPB>
 struct DgSmem {
   static constexpr int N3 = N * N * N, Q3 = Q * Q * Q, N2 = N * N, Q2 = Q * Q;
-  static constexpr int MA = KAPPA ? 6 : 4;  // face arrays: v-, v+, dn-, dn+ (, k-, k+)
-  static constexpr int VOL = Q * N2 + Q2 * N + Q3 * 4 + (KAPPA ? Q3 : 0);
+  static constexpr int MA = 4;  // face arrays: v-, v+, dn-, dn+ (kappa comes from the point cache)
+  static constexpr int VOL = Q * N2 + Q2 * N + Q3 * 4;
   static constexpr int FACE = 2 * MA * (N2 + Q * N + Q2) + 4 * Q2;
   static constexpr int WORK = VOL > FACE ? VOL : FACE;
   static constexpr int TAB = kDgMaxQ * kDgMaxN + kDgMaxQ * kDgMaxQ + kDgMaxQ + 4 * kDgMaxN;
-  static constexpr int PER_CELL = N3 * (KAPPA ? 3 : 2) + WORK;
+  static constexpr int PER_CELL = N3 * 2 + WORK;
   static constexpr int TOTAL = TAB + CPB * PER_CELL;
 };
 
@@ -190,8 +192,7 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args,
   T* sdtr = str + 2 * kDgMaxN;
   T* su = sm + S::TAB;                 // [CPB][N3]
   T* sr = su + CPB * N3;               // [CPB][N3]
-  T* sk = sr + CPB * N3;               // [CPB][N3] (KAPPA)
-  T* work = sk + (KAPPA ? CPB * N3 : 0);  // [CPB][WORK]
+  T* work = sr + CPB * N3;             // [CPB][WORK]
   constexpr int WS = S::WORK;
 
   const int tid = threadIdx.x;
@@ -211,23 +212,20 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args,
   const long long v0 = (long long)blockIdx.x * CPB + args.cell_begin * vper;
   if (v0 >= nvirt) return;
 
-  // ---- load own dofs (and kappa) ------------------------------------------
+  // ---- load own dofs --------------------------------------------------------
   for (int e = tid; e < CPB * N3; e += blockDim.x) {
     const int c = e / N3, i = e - c * N3;
     const long long v = v0 + c;
-    T val = T(0), kv = T(0);
+    T val = T(0);
     if (v < nvirt) {
       if (args.unit_mode) {
         const long long cell = v / vper;
         val = (args.unit_mode != 3 && i == int(v - cell * N3)) ? T(1) : T(0);
-        if (KAPPA) kv = __ldg(args.kappa + cell * N3 + i);
       } else {
         val = __ldg(args.u + v * N3 + i);
-        if (KAPPA) kv = __ldg(args.kappa + v * N3 + i);
       }
     }
     su[e] = val;
-    if (KAPPA) sk[e] = kv;
   }
   __syncthreads();
 
@@ -239,15 +237,6 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args,
     T* G0 = U + Q3;
     T* G1 = G0 + Q3;
     T* G2 = G1 + Q3;
-    T* Kq = G2 + Q3;              // [Q3] (KAPPA)
-    if (KAPPA) {
-      contract<T, 0, N, N, N, Q, N, false, false, CPB>(sk, N3, t1, WS, sB, tabs.B);
-      __syncthreads();
-      contract<T, 1, Q, N, N, Q, N, false, false, CPB>(t1, WS, t2, WS, sB, tabs.B);
-      __syncthreads();
-      contract<T, 2, Q, Q, N, Q, N, false, false, CPB>(t2, WS, Kq, WS, sB, tabs.B);
-      __syncthreads();
-    }
     contract<T, 0, N, N, N, Q, N, false, false, CPB>(su, N3, t1, WS, sB, tabs.B);
     __syncthreads();
     contract<T, 1, Q, N, N, Q, N, false, false, CPB>(t1, WS, t2, WS, sB, tabs.B);
@@ -264,7 +253,12 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args,
       const int c = item / Q3, r = item - c * Q3;
       const int a = r / Q2, b = (r / Q) % Q, cc = r % Q;
       const T uq = U[c * WS + r];
-      const T kq = KAPPA ? Kq[c * WS + r] : T(1);
+      T kq = T(1);
+      if (KAPPA) {
+        const long long v = v0 + c;
+        const long long cell = v < nvirt ? (args.unit_mode ? v / vper : v) : 0;
+        kq = __ldg(args.kq + cell * Q3 + r);
+      }
       const T W = sw[a] * sw[b] * sw[cc] * args.detK;
       const T ek = args.eps * kq;
       // flux F = eps*kappa*grad u - b*u (physical), tested with grad phi = invh * ref-grad
@@ -340,13 +334,12 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args,
       else if (d == 1) { base = j * N2 + k; stride = N; }
       else { base = j * N2 + k * N; stride = 1; }
       const T* uo = su + c * N3;
-      T vm = T(0), nm = T(0), vp = T(0), np = T(0), km = T(0), kp = T(0);
+      T vm = T(0), nm = T(0), vp = T(0), np = T(0);
 #pragma unroll
       for (int i = 0; i < N; ++i) {
         const T x = uo[base + i * stride];
         vm = fma(str[s * N + i], x, vm);
         nm = fma(sdtr[s * N + i], x, nm);
-        if (KAPPA) km = fma(str[s * N + i], sk[c * N3 + base + i * stride], km);
       }
       if (has_nb && valid) {
         const int so = 1 - s;
@@ -356,7 +349,6 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args,
                       : args.unit_mode ? T(0) : __ldg(args.u + ncell * N3 + base + i * stride);
           vp = fma(str[so * N + i], x, vp);
           np = fma(sdtr[so * N + i], x, np);
-          if (KAPPA) kp = fma(str[so * N + i], __ldg(args.kappa + ncell * N3 + base + i * stride), kp);
         }
       }
       T* fc = FC + c * WS + s * MA * N2;
@@ -364,10 +356,6 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args,
       fc[1 * N2 + jk] = vp;
       fc[2 * N2 + jk] = sgn * invh * nm;
       fc[3 * N2 + jk] = sgn * invh * np;
-      if (KAPPA) {
-        fc[4 * N2 + jk] = km;
-        fc[5 * N2 + jk] = kp;
-      }
     }
     __syncthreads();
     // F2/F3: 2-D interpolation of all face arrays to the q x q face points
@@ -394,8 +382,20 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args,
       const T* fq = FQ + c * WS + s * MA * Q2;
       const T vm = fq[0 * Q2 + ab], vp = fq[1 * Q2 + ab];
       const T nm = fq[2 * Q2 + ab], np = fq[3 * Q2 + ab];
-      const T km = KAPPA ? fq[4 * Q2 + ab] : T(1);
-      const T kp = KAPPA ? fq[5 * Q2 + ab] : T(1);
+      T km = T(1), kp = T(1);
+      if (KAPPA) {
+        // own side from this cell's face cache, the other side from the
+        // neighbour's cache of the same face (its face 2d+1-s)
+        km = __ldg(args.kf + (cell * 6 + 2 * d + s) * Q2 + ab);
+        if (!boundary) {
+          long long cc3[3] = {cx, cy, cz};
+          long long nb = cc3[d] + (s ? 1 : -1);
+          if (nb < 0 || nb >= args.nc[d]) nb = (nb + args.nc[d]) % args.nc[d];
+          cc3[d] = nb;
+          const long long ncell = cc3[0] + (long long)args.nc[0] * (cc3[1] + (long long)args.nc[1] * cc3[2]);
+          kp = __ldg(args.kf + (ncell * 6 + 2 * d + 1 - s) * Q2 + ab);
+        }
+      }
       const T W = sw[a] * sw[b] * args.faceA[d];
       const T bn = args.advect ? (s ? args.b[d] : -args.b[d]) : T(0);
       T val = T(0), grad = T(0);
@@ -463,6 +463,59 @@ __global__ void __launch_bounds__(256) dg_apply_kernel(const DgArgsT<T> args,
     } else {
       __stcs(args.w + v * N3 + i, sr[e]);
     }
+  }
+}
+
+// kappa at the Gauss points of the operator, once per operator (and on
+// gbfem_operator_update_coefficients): kq[cell][a][b][c] = sum_ijk k_ijk
+// L_i(x_a) L_j(x_b) L_k(x_c); kf[cell][2d+s][a][b] the same on face (d, s),
+// the normal factor L_i(s), (a, b) the tangential points in axis order, as the
+// kernel's face arrays.  Direct sums, one thread per point.
+template <typename T, int N, int Q>
+__global__ void dg_kappa_points_kernel(const T* __restrict__ kappa, T* __restrict__ kq, T* __restrict__ kf,
+                                       long long ncells, const __grid_constant__ DgTablesT<T> tabs) {
+  constexpr int N2 = N * N, N3 = N2 * N, Q2 = Q * Q, Q3 = Q2 * Q, PER = Q3 + 6 * Q2;
+  const long long total = ncells * PER;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long cell = e / PER;
+    const int r = int(e - cell * PER);
+    const T* kc = kappa + cell * N3;
+    T f0[N], f1[N], f2[N];  // the 1-D factors along x, y, z
+    if (r < Q3) {
+      const int a = r / Q2, b = (r / Q) % Q, c = r % Q;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        f0[i] = tabs.B[a * N + i];
+        f1[i] = tabs.B[b * N + i];
+        f2[i] = tabs.B[c * N + i];
+      }
+    } else {
+      const int fr = r - Q3, f = fr / Q2, ab = fr - f * Q2;
+      const int d = f >> 1, sd = f & 1, a = ab / Q, b = ab % Q;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const T ts = tabs.tr[sd * N + i];
+        f0[i] = d == 0 ? ts : tabs.B[a * N + i];
+        f1[i] = d == 0 ? tabs.B[a * N + i] : (d == 1 ? ts : tabs.B[b * N + i]);
+        f2[i] = d == 2 ? ts : tabs.B[b * N + i];
+      }
+    }
+    T acc = T(0);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      T si = T(0);
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        T sj = T(0);
+#pragma unroll
+        for (int k = 0; k < N; ++k) sj = fma(f2[k], __ldg(kc + i * N2 + j * N + k), sj);
+        si = fma(f1[j], sj, si);
+      }
+      acc = fma(f0[i], si, acc);
+    }
+    if (r < Q3) kq[cell * Q3 + r] = acc;
+    else kf[cell * 6 * Q2 + (r - Q3)] = acc;
   }
 }
 

@@ -10,14 +10,18 @@ namespace gbfem {
 #ifndef GBFEM_QUAD_CPB_MAX_F32
 #define GBFEM_QUAD_CPB_MAX_F32 8
 #endif
+#ifndef GBFEM_QUAD_CPB_MAX_F64
+#define GBFEM_QUAD_CPB_MAX_F64 8
+#endif
 
 template <typename T, int N, int Q, bool KAPPA>
 int dg_launch_one(const DgArgsT<T>& args, const DgTablesT<T>& tabs, cudaStream_t stream) {
-  // Cells per CTA: as many as fit ~100 KB of shared memory, at most 8 (FP32:
-  // GBFEM_QUAD_CPB_MAX_F32), 32 threads per cell.
+  // Cells per CTA: as many as fit ~100 KB of shared memory, at most
+  // GBFEM_QUAD_CPB_MAX_F32 / _F64 (default 8); FP32 uses 32 threads per cell,
+  // FP64 256 threads per CTA.
   constexpr int PER_CELL = DgSmem<N, Q, KAPPA, 1>::PER_CELL;
   constexpr int CPB0 = (100 * 1024) / (PER_CELL * int(sizeof(T)));
-  constexpr int CAP = sizeof(T) == 4 ? GBFEM_QUAD_CPB_MAX_F32 : 8;
+  constexpr int CAP = sizeof(T) == 4 ? GBFEM_QUAD_CPB_MAX_F32 : GBFEM_QUAD_CPB_MAX_F64;
   constexpr int CPB1 = CPB0 >= 8 ? 8 : (CPB0 >= 4 ? 4 : (CPB0 >= 2 ? 2 : 1));
   constexpr int CPB = CPB1 < CAP ? CPB1 : CAP;
   constexpr int THREADS = sizeof(T) == 4 ? 32 * CPB : 256;
@@ -90,6 +94,35 @@ int dg_const_launch(const DgArgsT<T>& args, const DgConstTablesT<T>& tabs, int n
     case 5: return dg_const_launch_one<T, 5>(args, tabs, traces, phase, stream);
   }
   return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "dg apply: unsupported order");
+}
+
+template <typename T, int N, int Q>
+int dg_kappa_points_one(const T* kappa, T* kq, T* kf, long long ncells, const DgTablesT<T>& tabs,
+                        cudaStream_t stream) {
+  const long long total = ncells * (Q * Q * Q + 6 * Q * Q);
+  long long blocks = (total + 255) / 256;
+  if (blocks > 152LL * 64) blocks = 152LL * 64;
+  if (blocks < 1) return GBFEM_OK;
+  dg_kappa_points_kernel<T, N, Q><<<unsigned(blocks), 256, 0, stream>>>(kappa, kq, kf, ncells, tabs);
+  GBFEM_CUDA_TRY(cudaGetLastError());
+  return GBFEM_OK;
+}
+
+template <typename T>
+int dg_kappa_points(const T* kappa, T* kq, T* kf, long long ncells, const DgTablesT<T>& tabs, int n, int q,
+                    cudaStream_t stream) {
+#define GBFEM_KP_CASE(NN, QQ) \
+  if (n == NN && q == QQ) return dg_kappa_points_one<T, NN, QQ>(kappa, kq, kf, ncells, tabs, stream);
+  GBFEM_KP_CASE(2, 2)
+  GBFEM_KP_CASE(2, 3)
+  GBFEM_KP_CASE(3, 3)
+  GBFEM_KP_CASE(3, 4)
+  GBFEM_KP_CASE(4, 4)
+  GBFEM_KP_CASE(4, 5)
+  GBFEM_KP_CASE(5, 5)
+  GBFEM_KP_CASE(5, 6)
+#undef GBFEM_KP_CASE
+  return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "dg kappa points: unsupported (p, q)");
 }
 
 }  // namespace gbfem

@@ -119,6 +119,8 @@ extern "C" int gbfem_operator_assemble(gbfem_operator op, gbfem_operator* out) {
   a->pipe = nullptr;
   a->jac_points = nullptr;
   a->nonlinear = 0;
+  a->kq_cache = a->kf_cache = nullptr;
+  a->owns_kcache = false;
   a->bsr_blocks = nullptr;
   a->bsr_col = nullptr;
   a->trace_buf = nullptr;

@@ -19,6 +19,27 @@ int dg_launch_f64(const DgArgsT<double>&, const DgTablesT<double>&, int, int, bo
 int dg_launch_f32(const DgArgsT<float>&, const DgTablesT<float>&, int, int, bool, cudaStream_t);
 int dg_const_launch_f64(const DgArgsT<double>&, const DgConstTablesT<double>&, int, double*, int, cudaStream_t);
 int dg_const_launch_f32(const DgArgsT<float>&, const DgConstTablesT<float>&, int, float*, int, cudaStream_t);
+int dg_kappa_points_f64(const double*, double*, double*, long long, const DgTablesT<double>&, int, int, cudaStream_t);
+int dg_kappa_points_f32(const float*, float*, float*, long long, const DgTablesT<float>&, int, int, cudaStream_t);
+
+int dg_kappa_cache(gbfem_operator_s* op) {
+  if (!op->dg.kappa) return GBFEM_OK;
+  const size_t es = op->precision == GBFEM_F64 ? 8 : 4;
+  const size_t q2 = size_t(op->q) * op->q;
+  if (!op->kq_cache) {
+    GBFEM_CUDA_TRY(cudaMalloc(&op->kq_cache, size_t(op->ncells) * q2 * op->q * es));
+    op->owns_kcache = true;
+    GBFEM_CUDA_TRY(cudaMalloc(&op->kf_cache, size_t(op->ncells) * 6 * q2 * es));
+  }
+  if (op->precision == GBFEM_F64)
+    GBFEM_TRY(dg_kappa_points_f64(static_cast<const double*>(op->dg.kappa), static_cast<double*>(op->kq_cache),
+                                  static_cast<double*>(op->kf_cache), op->ncells, op->tab64, op->n, op->q, nullptr));
+  else
+    GBFEM_TRY(dg_kappa_points_f32(static_cast<const float*>(op->dg.kappa), static_cast<float*>(op->kq_cache),
+                                  static_cast<float*>(op->kf_cache), op->ncells, op->tab32, op->n, op->q, nullptr));
+  GBFEM_CUDA_TRY(cudaDeviceSynchronize());
+  return GBFEM_OK;
+}
 
 // Trace buffer of the closed-form kernel: [cell][6 faces][v|d][n^2], allocated
 // on the first apply of an operator.
@@ -87,6 +108,8 @@ static void fill_dg_args(const gbfem_operator_s* op, DgArgsT<T>* a) {
   a->advect = (d.velocity[0] != 0.0 || d.velocity[1] != 0.0 || d.velocity[2] != 0.0) ? 1 : 0;
   a->weak_dirichlet = d.weak_dirichlet;
   a->kappa = static_cast<const T*>(d.kappa);
+  a->kq = static_cast<const T*>(op->kq_cache);
+  a->kf = static_cast<const T*>(op->kf_cache);
 }
 
 // M_d = eps |K|/h_d^2 K1 - b_d |K|/h_d D1 (+ c |K| I on axis 0), rounded once.
@@ -427,8 +450,19 @@ int gbfem_dg_operator_create(const gbfem_dg_desc* desc, gbfem_operator* out) {
     }
   // q >= p+1 always holds here, so the quadrature is exact for constant kappa
   op->coefficient_space = desc->kappa == nullptr && desc->algorithm == GBFEM_ALGO_AUTO;
+  const int rc = dg_kappa_cache(op);
+  if (rc) {
+    gbfem_operator_destroy(op);
+    return rc;
+  }
   *out = op;
   return GBFEM_OK;
+}
+
+int gbfem_operator_update_coefficients(gbfem_operator op) {
+  if (!op) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_update_coefficients: null argument");
+  if (op->kind != OpKind::DG) return GBFEM_OK;
+  return dg_kappa_cache(op);
 }
 
 int gbfem_q1_operator_create(const gbfem_grid_desc* grid, int precision, double diffusion, double mass,
@@ -459,6 +493,10 @@ int gbfem_operator_destroy(gbfem_operator op) {
   if (!op) return GBFEM_OK;
   if (op->pipe) destroy_host_pipe(op->pipe);
   if (op->jac_points) cudaFree(op->jac_points);
+  if (op->owns_kcache) {
+    if (op->kq_cache) cudaFree(op->kq_cache);
+    if (op->kf_cache) cudaFree(op->kf_cache);
+  }
   if (op->host_u) cudaFree(op->host_u);
   if (op->host_w) cudaFree(op->host_w);
   if (op->bsr_blocks) cudaFree(op->bsr_blocks);

@@ -33,6 +33,8 @@ int reaction_launch(const struct ::gbfem_operator_s* op, int mode, const void* u
 struct HostPipe;
 void destroy_host_pipe(HostPipe* p);
 int dg_apply_host_pipelined(struct ::gbfem_operator_s* op, const void* u_host, void* w_host);
+// (re)computes kq_cache / kf_cache from the operator's kappa vector
+int dg_kappa_cache(struct ::gbfem_operator_s* op);
 
 }  // namespace gbfem
 
@@ -60,5 +62,8 @@ struct gbfem_operator_s {
   int nonlinear = 0;       // DG: adds the reaction R(u) = int r(u) v (react = c1, c3, ce)
   double react[3] = {0.0, 0.0, 0.0};
   void* jac_points = nullptr;  // Jacobian of a nonlinear DG operator: [cell][q^3] w |K| r'(u0)
+  void* kq_cache = nullptr;    // variable kappa at the volume Gauss points [cell][q^3]
+  void* kf_cache = nullptr;    // variable kappa at the face Gauss points [cell][6][q^2]
+  bool owns_kcache = false;    // false in copies (Jacobian) that share the operator's caches
   gbfem::HostPipe* pipe = nullptr;  // its streams and events
 };

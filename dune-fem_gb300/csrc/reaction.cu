@@ -118,6 +118,7 @@ int gbfem_operator_jacobian_create(gbfem_operator op, gbfem_operator* jac) {
   j->pipe = nullptr;
   j->jac_points = nullptr;
   j->nonlinear = 0;
+  j->owns_kcache = false;  // shares the operator's kappa point caches
   if (op->nonlinear) {
     const size_t bytes = size_t(op->ncells) * op->q * op->q * op->q * (op->precision == GBFEM_F64 ? 8 : 4);
     const cudaError_t e = cudaMalloc(&j->jac_points, bytes);

@@ -1069,7 +1069,7 @@ int gbfem_solve_mixed(gbfem_operator op64, gbfem_operator op32, gbfem_preconditi
   GBFEM_TRY(c64.dot(f, f, &ff));
   const double fnorm = std::sqrt(ff);
   int inner_total = 0, outer = 0;
-  double rel = 0.0;
+  double rel = 0.0, rel_hist[2] = {0.0, 0.0};
   gbfem_solver_params ip = prm->inner;
   ip.error_measure = GBFEM_TOL_RELATIVE;
   if (prm->outer_method != 0) {
@@ -1095,6 +1095,7 @@ int gbfem_solve_mixed(gbfem_operator op64, gbfem_operator op32, gbfem_preconditi
     // true relative residual meets the tolerance (or the budget is spent).
     gbfem_solver_info oi{};
     int outer_total = 0, applies = 0;
+    double prev_rel = 0.0;
     for (int attempt = 0; attempt < 8; ++attempt) {
       op.max_iterations = prm->max_outer - outer_total;
       if (op.max_iterations <= 0) break;
@@ -1115,6 +1116,11 @@ int gbfem_solve_mixed(gbfem_operator op64, gbfem_operator op32, gbfem_preconditi
       if (prm->inner.verbose) std::printf("gbfem mixed flexible outer: %d iterations, true relative residual %.6e\n",
                                           outer_total, rel);
       if (!(rel > prm->tolerance) || its == 0 || oi.status != GBFEM_OK) break;
+      if (attempt > 0 && rel > 0.9 * prev_rel) {
+        info->stagnated = 1;
+        break;
+      }
+      prev_rel = rel;
     }
     px.ext_ctx = nullptr;
     oi.iterations = outer_total;
@@ -1141,6 +1147,13 @@ int gbfem_solve_mixed(gbfem_operator op64, gbfem_operator op32, gbfem_preconditi
     if (prm->inner.verbose) std::printf("gbfem IR outer %d : relative residual %.6e\n", outer, rel);
     if (!std::isfinite(rel)) { info->status = GBFEM_ERR_NONFINITE; break; }
     if (rel <= prm->tolerance || outer == prm->max_outer) break;
+    // no 10 % progress over two refinement steps: the rounding floor of the
+    // FP64 residual is above the tolerance
+    if (outer >= 2 && rel > 0.9 * rel_hist[(outer - 2) % 2]) {
+      info->stagnated = 1;
+      break;
+    }
+    rel_hist[outer % 2] = rel;
     GBFEM_TRY(gbfem_convert(n, GBFEM_F64, r, GBFEM_F32, r32, nullptr));
     GBFEM_TRY(c32.scal(1.0 / rn, r32));
     GBFEM_TRY(c32.clear(d32));

@@ -47,7 +47,8 @@ class SolverParams(C.Structure):
 class SolverInfo(C.Structure):
     _fields_ = [("converged", C.c_int), ("iterations", C.c_int), ("residual", C.c_double),
                 ("time_ms", C.c_double), ("operator_applies", C.c_int), ("preconditioner_applies", C.c_int),
-                ("status", C.c_int), ("fallbacks", C.c_int), ("outer_iterations", C.c_int)]
+                ("status", C.c_int), ("fallbacks", C.c_int), ("outer_iterations", C.c_int),
+                ("stagnated", C.c_int)]
 
 
 class IRParams(C.Structure):
@@ -103,6 +104,7 @@ def lib():
         L.gbfem_operator_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.gbfem_operator_apply_host.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.gbfem_operator_set_host_chunks.argtypes = [C.c_void_p, C.c_int]
+        L.gbfem_operator_update_coefficients.argtypes = [C.c_void_p]
         L.gbfem_operator_diagonal.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.gbfem_operator_block_diagonal.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.gbfem_operator_destroy.argtypes = [C.c_void_p]
@@ -239,6 +241,10 @@ class Operator:
     def apply_host(self, u, w):
         """Host-buffer apply: copies u in, applies, copies w out (synchronous)."""
         check(lib().gbfem_operator_apply_host(self.handle, u.ctypes.data, w.ctypes.data))
+
+    def update_coefficients(self):
+        """Re-evaluates a variable kappa at the Gauss points after its vector changed."""
+        check(lib().gbfem_operator_update_coefficients(self.handle))
 
     def set_host_chunks(self, nchunks):
         """Slabs of the pipelined host-buffer apply of a DG operator (0 = automatic)."""

@@ -97,6 +97,12 @@ typedef struct gbfem_operator_s* gbfem_operator;
 /* Creates the SIPG/upwind DG operator.  ≙ constructing GalerkinOperator +
  * DGConservationLawModelIntegrands (schemes/galerkin.hh:1383-1430). */
 int gbfem_dg_operator_create(const gbfem_dg_desc* desc, gbfem_operator* op);
+/* A variable kappa is evaluated at the operator's Gauss points once, when the
+ * operator is created (kept on the device: q^3 + 6 q^2 values per cell).
+ * After changing the contents of the kappa vector, call this to re-evaluate.
+ * (The reference's integrands read their coefficient function at every
+ * evaluation.)  A Jacobian shares its operator's cache and must not outlive it. */
+int gbfem_operator_update_coefficients(gbfem_operator op);
 /* Continuous Lagrange Q1 operator for -div(eps grad u) + c u on a 2-D grid
  * with strong Dirichlet rows on the whole boundary: w = A u, w_D = u_D.
  * ≙ DirichletWrapperOperator over GalerkinOperator (schemes/dirichletwrapper.hh:
@@ -219,6 +225,8 @@ typedef struct {
   int status;            /* GBFEM_OK, GBFEM_ERR_NONFINITE on NaN/Inf */
   int fallbacks;         /* flexible solvers: switches to the fallback preconditioner */
   int outer_iterations;  /* gbfem_solve_mixed: refinement steps / outer Krylov iterations */
+  int stagnated;         /* gbfem_solve_mixed: stopped because the true FP64 residual no longer
+                            decreased (its rounding floor lies above the tolerance) */
 } gbfem_solver_info;
 
 /* Fills the reference's defaults: cg, tolerance 1e-8, absolute, max
@@ -238,7 +246,11 @@ int gbfem_solve(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_p
  * outer_method GBFEM_SOLVER_FGMRES or GBFEM_SOLVER_FCG: that flexible FP64
  *   Krylov method (restart outer_restart) with the FP32 inner solve as its
  *   preconditioner, which also converges where refinement stalls.  max_outer
- *   then bounds the outer Krylov iterations. */
+ *   then bounds the outer Krylov iterations.
+ * Both stop early, with info->stagnated = 1, when the true relative residual
+ * ||f - A u|| / ||f|| fails to drop by 10 % over two refinement steps (or one
+ * flexible restart): the FP64 apply's rounding floor is then above the
+ * tolerance. */
 typedef struct {
   double tolerance;          /* outer relative residual ||f - A u|| / ||f|| */
   int max_outer;             /* refinement steps / outer Krylov iterations */

@@ -185,3 +185,31 @@ def test_pipelined_host_apply_is_bitwise_the_device_apply(gb, orc, algorithm, pe
         assert np.array_equal(wh.view(np.uint64), ref.view(np.uint64))
     prob = orc.DGProblem(cells, 2, **kw)
     assert relmax(ref, prob.apply(u)) < TOL64
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_kappa_point_cache_follows_update_coefficients(gb, orc, precision):
+    """kappa is evaluated at the Gauss points when the operator is created; a
+    changed kappa vector takes effect after update_coefficients."""
+    cells, order = (3, 2, 3), 2
+    rng = np.random.default_rng(77)
+    nloc = (order + 1) ** 3
+    ncell = int(np.prod(cells))
+    kappa = np.zeros(ncell * nloc)
+    kappa[::nloc] = rng.uniform(0.5, 2.0, ncell)
+    kappa += 0.05 * rng.uniform(-1, 1, ncell * nloc)
+    dt = np.float64 if precision == 0 else np.float32
+    dk = gb.DeviceArray.from_numpy(kappa.astype(dt), precision)
+    kw = dict(mass=0.2, velocity=(0.1, 0.2, -0.3), periodic=(0, 0, 1))
+    op = gb.DGOperator(cells, order, precision=precision, kappa=dk, **kw)
+    prob = orc.DGProblem(cells, order, **kw)
+    u = rng.uniform(-1, 1, prob.ndofs)
+    w = gb.DeviceArray(prob.ndofs, precision)
+    tol = TOL64 if precision == 0 else TOL32
+    op(gb.DeviceArray.from_numpy(u.astype(dt), precision), w)
+    assert relmax(w.numpy(), prob.apply(u.astype(dt).astype(np.float64), kappa=kappa.astype(dt).astype(np.float64))) < tol
+    kappa2 = 1.5 * kappa
+    gb.check(gb.lib().gbfem_memcpy_h2d(dk.ptr, kappa2.astype(dt).ctypes.data, kappa2.size * dk.itemsize))
+    op.update_coefficients()
+    op(gb.DeviceArray.from_numpy(u.astype(dt), precision), w)
+    assert relmax(w.numpy(), prob.apply(u.astype(dt).astype(np.float64), kappa=kappa2.astype(dt).astype(np.float64))) < tol

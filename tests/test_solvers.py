@@ -294,3 +294,20 @@ def test_ssor_preconditioned_cg_converges(gb, orc):
     assert info_ssor["converged"] and info_ssor["iterations"] < info_none["iterations"]
     prob = orc.DGProblem(cells, order, mass=0.1)
     assert np.linalg.norm(f - prob.apply(x)) <= 1e-9 * np.linalg.norm(f)
+
+
+@pytest.mark.parametrize("outer", ["refinement", "fgmres"])
+def test_mixed_stops_at_the_rounding_floor(gb, orc, outer):
+    """A tolerance below the FP64 rounding floor of ||f - A u|| / ||f||: the
+    mixed solve reports stagnation instead of spending its whole budget."""
+    cells, order = (4, 4, 4), 2
+    op64 = gb.DGOperator(cells, order)
+    op32 = gb.DGOperator(cells, order, precision=gb.F32)
+    pc32 = gb.Preconditioner.block_jacobi(op64, gb.F32)
+    f = np.random.default_rng(15).uniform(-1, 1, op64.size)
+    u = gb.DeviceArray(op64.size)
+    u.clear()
+    info = gb.solve_mixed(op64, op32, pc32, gb.DeviceArray.from_numpy(f), u, tolerance=1e-19, max_outer=200,
+                          inner_tolerance=1e-3, outer=outer)
+    assert not info.converged and info.stagnated and info.outer_iterations < 60
+    assert info.residual < 1e-13
