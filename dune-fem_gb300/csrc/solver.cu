@@ -1090,15 +1090,18 @@ int gbfem_solve_mixed(gbfem_operator op64, gbfem_operator op32, gbfem_preconditi
     op.max_iterations = prm->max_outer;
     op.restart = prm->outer_restart > 0 ? prm->outer_restart : 20;
     op.verbose = prm->inner.verbose;
-    // The flexible method stops on its own residual estimate; the true FP64
-    // residual can sit slightly above it.  Restart from the current u until the
-    // true relative residual meets the tolerance (or the budget is spent).
+    // One restart cycle at a time from the current u (restarted FGMRES(m) /
+    // truncated FCG(m)), checking the true FP64 residual after each cycle:
+    // the flexible method stops on its own residual estimate, which can sit
+    // below the true residual, and a cycle without 10 % progress means the
+    // rounding floor has been reached.
     gbfem_solver_info oi{};
     int outer_total = 0, applies = 0;
     double prev_rel = 0.0;
-    for (int attempt = 0; attempt < 8; ++attempt) {
-      op.max_iterations = prm->max_outer - outer_total;
-      if (op.max_iterations <= 0) break;
+    for (int attempt = 0;; ++attempt) {
+      const int remaining = prm->max_outer - outer_total;
+      if (remaining <= 0) break;
+      op.max_iterations = remaining < op.restart ? remaining : op.restart;
       oi = gbfem_solver_info{};
       const int rc = solve_impl(op64, &px, op, f, u, &oi, nullptr);
       if (rc) {
