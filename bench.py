@@ -742,7 +742,7 @@ def workload_newton(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbfem", choices=["gbfem", "reference"])
     ap.add_argument("--workload", default="apply",
