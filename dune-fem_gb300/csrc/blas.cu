@@ -17,7 +17,6 @@
 
 namespace gbfem {
 
-constexpr int kRedThreads = 256;
 constexpr int kMaxPartials = 1024;
 
 int dot_num_partials(long long n) {
@@ -25,28 +24,6 @@ int dot_num_partials(long long n) {
   if (p < 1) p = 1;
   if (p > kMaxPartials) p = kMaxPartials;
   return int(p);
-}
-
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// Fixed-shape block reduction of one value per thread (kRedThreads threads).
-__device__ __forceinline__ double block_sum(double v) {
-  __shared__ double red[kRedThreads / 32];
-  v = warp_sum(v);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) red[wid] = v;
-  __syncthreads();
-  double r = 0.0;
-  if (wid == 0) {
-    r = lane < kRedThreads / 32 ? red[lane] : 0.0;
-    r = warp_sum(r);
-  }
-  __syncthreads();
-  return r;  // valid in thread 0
 }
 
 template <typename T>
@@ -63,9 +40,7 @@ __global__ void __launch_bounds__(kRedThreads) dot_partial_kernel(const T* __res
 
 __global__ void __launch_bounds__(kRedThreads) dot_final_kernel(const double* __restrict__ partial, int np,
                                                                 double* out) {
-  double s = 0.0;
-  for (int i = threadIdx.x; i < np; i += kRedThreads) s += partial[i];
-  s = block_sum(s);
+  const double s = dot_final_sum(partial, np);
   if (threadIdx.x == 0) *out = s;
 }
 
@@ -89,6 +64,21 @@ int library_scratch(double** partial, double** result) {
   }
   *partial = s.partial;
   if (result) *result = s.result;
+  return GBFEM_OK;
+}
+
+int dot_partial_device(int precision, long long n, const void* x, const void* y, double* d_partial, int* npo,
+                       cudaStream_t s) {
+  const int np = dot_num_partials(n);
+  const long long chunk = (n + np - 1) / np;
+  if (precision == GBFEM_F64)
+    dot_partial_kernel<double><<<np, kRedThreads, 0, s>>>(static_cast<const double*>(x),
+                                                         static_cast<const double*>(y), n, chunk, d_partial);
+  else
+    dot_partial_kernel<float><<<np, kRedThreads, 0, s>>>(static_cast<const float*>(x),
+                                                        static_cast<const float*>(y), n, chunk, d_partial);
+  GBFEM_CUDA_TRY(cudaGetLastError());
+  *npo = np;
   return GBFEM_OK;
 }
 

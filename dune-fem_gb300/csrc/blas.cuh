@@ -5,7 +5,48 @@
 namespace gbfem {
 
 // Number of FP64 partial sums pass 1 of a dot product of length n writes.
+// Pass 1 runs dot_num_partials(n) CTAs of kRedThreads threads; CTA b sums the
+// chunk [b c, min(n, (b+1) c)), c = ceil(n / partials), thread t the elements
+// b c + t + k kRedThreads in order, then block_sum.  Kernels that fuse a dot
+// product into other work reproduce exactly this order (bitwise the same sum).
 int dot_num_partials(long long n);
+constexpr int kRedThreads = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Fixed-shape block reduction of one value per thread (kRedThreads threads);
+// the result is valid in thread 0.
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double red[kRedThreads / 32];
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (wid == 0) {
+    r = lane < kRedThreads / 32 ? red[lane] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+// Pass 2 of a dot product, as a device function for kernels that continue
+// with the result: every thread of the (single, kRedThreads-thread) CTA
+// calls it; the sum is valid in thread 0.
+__device__ __forceinline__ double dot_final_sum(const double* __restrict__ partial, int np) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < np; i += kRedThreads) s += partial[i];
+  return block_sum(s);
+}
+
+// Pass 1 only (partials into d_partial); returns through *np the count.
+int dot_partial_device(int precision, long long n, const void* x, const void* y, double* d_partial, int* np,
+                       cudaStream_t s);
 // d_out[0] = x . y (FP64 accumulate), asynchronously on stream s.
 // d_partial must hold dot_num_partials(n) doubles.
 int dot_device(int precision, long long n, const void* x, const void* y, double* d_out, double* d_partial,

@@ -397,15 +397,33 @@ static int cg(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_par
 enum { DS_RES = 0, DS_PREV, DS_QH, DS_NEW, DS_ALPHA, DS_BETA, DS_TOL, DS_ACTIVE, DS_DIR, DS_CONV, DS_IT, DS_MAX,
        DS_STATUS, DS_N };
 
-__global__ void k_cg_begin(double* ds) {
+// begin of an iteration + direction update (q = s + beta q with a
+// preconditioner, p = beta p - r without): every thread derives the flags and
+// beta itself from the fields no kernel of this launch writes; thread 0
+// publishes them for the later kernels.
+template <typename T>
+__global__ void k_cg_begin_dir(long long n, double a, const T* __restrict__ x, T* __restrict__ y, double* ds) {
   const bool conv = ds[DS_CONV] != 0.0;
-  ds[DS_ACTIVE] = conv ? 0.0 : 1.0;
-  ds[DS_DIR] = (!conv && ds[DS_IT] > 0.0) ? 1.0 : 0.0;
-  ds[DS_BETA] = (!conv && ds[DS_IT] > 0.0) ? ds[DS_RES] / ds[DS_PREV] : 0.0;
+  const bool dir = !conv && ds[DS_IT] > 0.0;
+  const double beta = dir ? ds[DS_RES] / ds[DS_PREV] : 0.0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ds[DS_ACTIVE] = conv ? 0.0 : 1.0;
+    ds[DS_DIR] = dir ? 1.0 : 0.0;
+    ds[DS_BETA] = beta;
+  }
+  if (!dir) return;
+  const T b = T(beta);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = T(a) * x[i] + b * y[i];
 }
-__global__ void k_cg_alpha(double* ds) {
+// pass 2 of <q, h>, then alpha = rho / <q, h>
+__global__ void __launch_bounds__(kRedThreads) k_cg_final_alpha(const double* __restrict__ partial, int np,
+                                                                double* ds) {
+  const double qh = dot_final_sum(partial, np);
+  if (threadIdx.x != 0) return;
+  ds[DS_QH] = qh;
   if (ds[DS_ACTIVE] == 0.0) return;
-  const double alpha = ds[DS_RES] / ds[DS_QH];
+  const double alpha = ds[DS_RES] / qh;
   if (!isfinite(alpha)) {
     ds[DS_STATUS] = 1.0;
     ds[DS_CONV] = 1.0;
@@ -414,32 +432,56 @@ __global__ void k_cg_alpha(double* ds) {
   }
   ds[DS_ALPHA] = alpha;
 }
-__global__ void k_cg_end(double* ds) {
+// x += alpha q; v += sv alpha h (v = p, sv = -1 with a preconditioner; v = r,
+// sv = +1 without), if active; then, in the partition of pass 1 of a dot
+// product: PC 0 the partial of <r, r>, PC 1 s = dinv p and the partial of
+// <p, s>, PC 2 nothing (the preconditioner and its dot product follow).
+template <typename T, int PC>
+__global__ void __launch_bounds__(kRedThreads) k_cg_update_dot(long long n, long long chunk, const T* __restrict__ q,
+                                                               const T* __restrict__ h, T* __restrict__ x,
+                                                               T* __restrict__ v, double sv,
+                                                               const T* __restrict__ dinv, T* __restrict__ sz,
+                                                               double* __restrict__ partial, const double* ds) {
+  const bool active = ds[DS_ACTIVE] != 0.0;
+  const T alpha = T(ds[DS_ALPHA]);
+  const T sa = T(sv * ds[DS_ALPHA]);
+  const long long b0 = (long long)blockIdx.x * chunk;
+  long long b1 = b0 + chunk;
+  if (b1 > n) b1 = n;
+  double acc = 0.0;
+  for (long long i = b0 + threadIdx.x; i < b1; i += kRedThreads) {
+    T vi = v[i];
+    if (active) {
+      x[i] = alpha * q[i] + T(1) * x[i];
+      vi = sa * h[i] + T(1) * vi;
+      v[i] = vi;
+    }
+    if (PC == 1) {
+      const T si = vi * dinv[i];
+      sz[i] = si;
+      acc = fma(double(vi), double(si), acc);
+    } else if (PC == 0) {
+      acc = fma(double(vi), double(vi), acc);
+    }
+  }
+  if (PC == 2) return;
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+}
+// pass 2 of the new rho, then the end of the iteration
+__global__ void __launch_bounds__(kRedThreads) k_cg_final_end(const double* __restrict__ partial, int np,
+                                                              double* ds) {
+  const double rho = dot_final_sum(partial, np);
+  if (threadIdx.x != 0) return;
+  ds[DS_NEW] = rho;
   if (ds[DS_ACTIVE] == 0.0) return;
   ds[DS_PREV] = ds[DS_RES];
   ds[DS_RES] = ds[DS_NEW];
   ds[DS_IT] += 1.0;
   if (!(ds[DS_RES] > ds[DS_TOL]) || ds[DS_IT] >= ds[DS_MAX]) ds[DS_CONV] = 1.0;
-  if (!isfinite(ds[DS_RES])) { ds[DS_STATUS] = 1.0; ds[DS_CONV] = 1.0; }
-}
-// y = a*x + beta*y with beta from ds (direction update), if ds[DS_DIR]
-template <typename T>
-__global__ void k_cg_dir(long long n, double a, const T* __restrict__ x, T* __restrict__ y, const double* ds) {
-  if (ds[DS_DIR] == 0.0) return;
-  const T b = T(ds[DS_BETA]);
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    y[i] = T(a) * x[i] + b * y[i];
-}
-// x += alpha q;  v += sv*alpha h  (v = p with sv = -1, or r with sv = +1), if active
-template <typename T>
-__global__ void k_cg_update(long long n, const T* __restrict__ q, const T* __restrict__ h, T* __restrict__ x,
-                            T* __restrict__ v, double sv, const double* ds) {
-  if (ds[DS_ACTIVE] == 0.0) return;
-  const T alpha = T(ds[DS_ALPHA]);
-  const T sa = T(sv * ds[DS_ALPHA]);
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    x[i] = alpha * q[i] + T(1) * x[i];
-    v[i] = sa * h[i] + T(1) * v[i];
+  if (!isfinite(ds[DS_RES])) {
+    ds[DS_STATUS] = 1.0;
+    ds[DS_CONV] = 1.0;
   }
 }
 
@@ -481,31 +523,44 @@ static int cg_device(gbfem_operator op, gbfem_preconditioner pc, const gbfem_sol
   // one iteration, as a function of the stream
   const long long n = c.n;
   const int g = stream_grid(n);
+  const int np = dot_num_partials(n);
+  const long long dchunk = (n + np - 1) / np;
+  const bool diag_pc = pc && pc->kind == PcKind::Diagonal;
+  // one iteration, as a function of the stream: 6 launches (plus the operator
+  // and a general preconditioner with its dot product)
   auto iteration = [&](cudaStream_t st) -> int {
-    k_cg_begin<<<1, 1, 0, st>>>(ds);
     if (c.prec == GBFEM_F64) {
-      if (pc) k_cg_dir<double><<<g, 256, 0, st>>>(n, 1.0, (const double*)s, (double*)q, ds);
-      else k_cg_dir<double><<<g, 256, 0, st>>>(n, -1.0, (const double*)r, (double*)p, ds);
+      if (pc) k_cg_begin_dir<double><<<g, 256, 0, st>>>(n, 1.0, (const double*)s, (double*)q, ds);
+      else k_cg_begin_dir<double><<<g, 256, 0, st>>>(n, -1.0, (const double*)r, (double*)p, ds);
     } else {
-      if (pc) k_cg_dir<float><<<g, 256, 0, st>>>(n, 1.0, (const float*)s, (float*)q, ds);
-      else k_cg_dir<float><<<g, 256, 0, st>>>(n, -1.0, (const float*)r, (float*)p, ds);
+      if (pc) k_cg_begin_dir<float><<<g, 256, 0, st>>>(n, 1.0, (const float*)s, (float*)q, ds);
+      else k_cg_begin_dir<float><<<g, 256, 0, st>>>(n, -1.0, (const float*)r, (float*)p, ds);
     }
     GBFEM_TRY(gbfem_operator_apply(op, q, h, st));
-    GBFEM_TRY(dot_device(c.prec, n, q, h, ds + DS_QH, c.d_partial, st));
-    k_cg_alpha<<<1, 1, 0, st>>>(ds);
+    int npp = 0;
+    GBFEM_TRY(dot_partial_device(c.prec, n, q, h, c.d_partial, &npp, st));
+    k_cg_final_alpha<<<1, kRedThreads, 0, st>>>(c.d_partial, np, ds);
     void* v = pc ? p : r;
     const double sv = pc ? -1.0 : 1.0;
-    if (c.prec == GBFEM_F64)
-      k_cg_update<double><<<g, 256, 0, st>>>(n, (const double*)q, (const double*)h, (double*)x, (double*)v, sv, ds);
-    else
-      k_cg_update<float><<<g, 256, 0, st>>>(n, (const float*)q, (const float*)h, (float*)x, (float*)v, sv, ds);
-    if (pc) {
-      GBFEM_TRY(precond_apply(pc, p, s, st));
-      GBFEM_TRY(dot_device(c.prec, n, p, s, ds + DS_NEW, c.d_partial, st));
+    const int mode = !pc ? 0 : (diag_pc ? 1 : 2);
+#define GBFEM_CG_UPDATE(TT, M)                                                                              \
+  k_cg_update_dot<TT, M><<<np, kRedThreads, 0, st>>>(n, dchunk, (const TT*)q, (const TT*)h, (TT*)x, (TT*)v, sv, \
+                                                     diag_pc ? (const TT*)pc->data : nullptr, (TT*)s, c.d_partial, ds)
+    if (c.prec == GBFEM_F64) {
+      if (mode == 0) GBFEM_CG_UPDATE(double, 0);
+      else if (mode == 1) GBFEM_CG_UPDATE(double, 1);
+      else GBFEM_CG_UPDATE(double, 2);
     } else {
-      GBFEM_TRY(dot_device(c.prec, n, r, r, ds + DS_NEW, c.d_partial, st));
+      if (mode == 0) GBFEM_CG_UPDATE(float, 0);
+      else if (mode == 1) GBFEM_CG_UPDATE(float, 1);
+      else GBFEM_CG_UPDATE(float, 2);
     }
-    k_cg_end<<<1, 1, 0, st>>>(ds);
+#undef GBFEM_CG_UPDATE
+    if (mode == 2) {
+      GBFEM_TRY(precond_apply(pc, p, s, st));
+      GBFEM_TRY(dot_partial_device(c.prec, n, p, s, c.d_partial, &npp, st));
+    }
+    k_cg_final_end<<<1, kRedThreads, 0, st>>>(c.d_partial, np, ds);
     GBFEM_CUDA_TRY(cudaGetLastError());
     return GBFEM_OK;
   };
