@@ -209,7 +209,8 @@ def test_kappa_point_cache_follows_update_coefficients(gb, orc, precision):
     op(gb.DeviceArray.from_numpy(u.astype(dt), precision), w)
     assert relmax(w.numpy(), prob.apply(u.astype(dt).astype(np.float64), kappa=kappa.astype(dt).astype(np.float64))) < tol
     kappa2 = 1.5 * kappa
-    gb.check(gb.lib().gbfem_memcpy_h2d(dk.ptr, kappa2.astype(dt).ctypes.data, kappa2.size * dk.itemsize))
+    k2 = np.ascontiguousarray(kappa2.astype(dt))  # held while the copy reads it
+    gb.check(gb.lib().gbfem_memcpy_h2d(dk.ptr, k2.ctypes.data, k2.nbytes))
     op.update_coefficients()
     op(gb.DeviceArray.from_numpy(u.astype(dt), precision), w)
     assert relmax(w.numpy(), prob.apply(u.astype(dt).astype(np.float64), kappa=kappa2.astype(dt).astype(np.float64))) < tol
