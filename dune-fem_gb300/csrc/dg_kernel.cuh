@@ -43,6 +43,7 @@ struct DgTablesT {
   T B[kDgMaxQ * kDgMaxN];   // B[a*n+i]  = L_i(x_a)
   T Dc[kDgMaxQ * kDgMaxQ];  // Dc[a*q+b] = l_b'(x_a)
   T w[kDgMaxQ];             // Gauss weights on [0,1]
+  T x[kDgMaxQ];             // Gauss points on [0,1]
   T tr[2 * kDgMaxN];        // tr[s*n+i]  = L_i(s)
   T dtr[2 * kDgMaxN];       // dtr[s*n+i] = L_i'(s)
 };

@@ -121,6 +121,7 @@ extern "C" int gbfem_operator_assemble(gbfem_operator op, gbfem_operator* out) {
   a->nonlinear = 0;
   a->kq_cache = a->kf_cache = nullptr;
   a->owns_kcache = false;
+  a->jit_lib = a->jit_kernel = nullptr;
   a->bsr_blocks = nullptr;
   a->bsr_col = nullptr;
   a->trace_buf = nullptr;

@@ -76,6 +76,7 @@ static void fill_dg_tables(const Tables1D& t, DgTablesT<T>* out) {
   for (int a = 0; a < t.q; ++a)
     for (int b = 0; b < t.q; ++b) out->Dc[a * t.q + b] = T(t.Dc[a][b]);
   for (int a = 0; a < t.q; ++a) out->w[a] = T(t.wts[a]);
+  for (int a = 0; a < t.q; ++a) out->x[a] = T(t.pts[a]);
   for (int s = 0; s < 2; ++s)
     for (int i = 0; i < t.n; ++i) {
       out->tr[s * t.n + i] = T(t.tr[s][i]);
@@ -497,6 +498,7 @@ int gbfem_operator_destroy(gbfem_operator op) {
     if (op->kq_cache) cudaFree(op->kq_cache);
     if (op->kf_cache) cudaFree(op->kf_cache);
   }
+  if (op->jit_lib) cudaLibraryUnload(static_cast<cudaLibrary_t>(op->jit_lib));
   if (op->host_u) cudaFree(op->host_u);
   if (op->host_w) cudaFree(op->host_w);
   if (op->bsr_blocks) cudaFree(op->bsr_blocks);

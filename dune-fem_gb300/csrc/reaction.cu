@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 #include <cmath>
 #include <new>
+#include <string>
 
 #include "gbfem_internal.cuh"
 #include "operator_impl.hpp"
@@ -25,8 +26,15 @@ static void fill_react_tabs(const gbfem_operator_s* op, ReactTabsT<T>* t) {
   const DgTablesT<T>& src = tables_of(op, static_cast<const T*>(nullptr));
   for (int e = 0; e < kDgMaxQ * kDgMaxN; ++e) t->B[e] = src.B[e];
   for (int a = 0; a < kDgMaxQ; ++a) t->w[a] = src.w[a];
+  for (int a = 0; a < kDgMaxQ; ++a) t->xq[a] = src.x[a];
   double vol = 1.0;
-  for (int k = 0; k < 3; ++k) vol *= (op->dg.grid.upper[k] - op->dg.grid.lower[k]) / op->dg.grid.cells[k];
+  for (int k = 0; k < 3; ++k) {
+    const double h = (op->dg.grid.upper[k] - op->dg.grid.lower[k]) / op->dg.grid.cells[k];
+    vol *= h;
+    t->lower[k] = T(op->dg.grid.lower[k]);
+    t->h[k] = T(h);
+    t->nc[k] = op->dg.grid.cells[k];
+  }
   t->detK = T(vol);
   t->c1 = T(op->react[0]);
   t->c3 = T(op->react[1]);
@@ -73,9 +81,27 @@ static int reaction_launch_t(const gbfem_operator_s* op, int mode, const void* u
 // mode 0/1/2 of dg_reaction_kernel on cells [cell_begin, cell_begin+count);
 // blocks_mode 1: add the linearised blocks into w (block-diagonal layout
 // relative to cell_begin), 2: add their diagonal into w.
+// the user's run-time compiled reaction (modes 0 and 1: they evaluate r, r')
+template <typename T>
+static int reaction_launch_jit(const gbfem_operator_s* op, int mode, const void* u, void* w, void* pts,
+                               long long cell_begin, long long count, cudaStream_t s) {
+  ReactTabsT<T> tb;
+  fill_react_tabs(op, &tb);
+  constexpr int CPB = 4;
+  const long long grid = (count + CPB - 1) / CPB;
+  if (grid > 2147483647LL) return set_error(GBFEM_ERR_INVALID, "reaction: grid too large");
+  void* args[] = {&mode, const_cast<void**>(&u), &w, &pts, &cell_begin, &count, &tb};
+  GBFEM_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(op->jit_kernel), dim3(unsigned(grid)), dim3(128),
+                                  args, 0, s));
+  return GBFEM_OK;
+}
+
 int reaction_launch(const gbfem_operator_s* op, int mode, const void* u, void* w, void* pts, long long cell_begin,
                     long long count, int blocks_mode, cudaStream_t s) {
   if (count <= 0) return GBFEM_OK;
+  if (op->jit_kernel && !blocks_mode && mode != 2)
+    return op->precision == GBFEM_F64 ? reaction_launch_jit<double>(op, mode, u, w, pts, cell_begin, count, s)
+                                      : reaction_launch_jit<float>(op, mode, u, w, pts, cell_begin, count, s);
   return op->precision == GBFEM_F64 ? reaction_launch_t<double>(op, mode, u, w, pts, cell_begin, count, blocks_mode, s)
                                     : reaction_launch_t<float>(op, mode, u, w, pts, cell_begin, count, blocks_mode, s);
 }
@@ -95,6 +121,36 @@ int gbfem_dg_nonlinear_operator_create(const gbfem_dg_desc* desc, const gbfem_re
   op->react[0] = reaction->linear;
   op->react[1] = reaction->cubic;
   op->react[2] = reaction->exponential;
+  return GBFEM_OK;
+}
+
+int gbfem_dg_nonlinear_operator_create_jit(const gbfem_dg_desc* desc, const char* cubin_path, gbfem_operator* out) {
+  if (!desc || !cubin_path || !out)
+    return set_error(GBFEM_ERR_INVALID, "gbfem_dg_nonlinear_operator_create_jit: null argument");
+  GBFEM_TRY(gbfem_dg_operator_create(desc, out));
+  gbfem_operator op = *out;
+  // the cubin holds one kernel per (precision, n, q), named for it
+  const std::string name = std::string("gbfem_user_reaction_") + (op->precision == GBFEM_F64 ? "f64" : "f32") +
+                           "_n" + std::to_string(op->n) + "_q" + std::to_string(op->q);
+  cudaLibrary_t lib = nullptr;
+  cudaError_t e = cudaLibraryLoadFromFile(&lib, cubin_path, nullptr, nullptr, 0, nullptr, nullptr, 0);
+  if (e != cudaSuccess) {
+    gbfem_operator_destroy(op);
+    *out = nullptr;
+    return set_cuda_error(e, (std::string("gbfem_dg_nonlinear_operator_create_jit: loading ") + cubin_path).c_str());
+  }
+  cudaKernel_t k = nullptr;
+  e = cudaLibraryGetKernel(&k, lib, name.c_str());
+  if (e != cudaSuccess) {
+    cudaLibraryUnload(lib);
+    gbfem_operator_destroy(op);
+    *out = nullptr;
+    return set_cuda_error(e, ("gbfem_dg_nonlinear_operator_create_jit: no kernel " + name +
+                              " in the cubin (compiled for another precision / order / quadrature?)").c_str());
+  }
+  op->jit_lib = lib;
+  op->jit_kernel = reinterpret_cast<void*>(k);
+  op->nonlinear = 1;
   return GBFEM_OK;
 }
 
@@ -119,6 +175,7 @@ int gbfem_operator_jacobian_create(gbfem_operator op, gbfem_operator* jac) {
   j->jac_points = nullptr;
   j->nonlinear = 0;
   j->owns_kcache = false;  // shares the operator's kappa point caches
+  j->jit_lib = j->jit_kernel = nullptr;  // the Jacobian applies the stored linearisation only
   if (op->nonlinear) {
     const size_t bytes = size_t(op->ncells) * op->q * op->q * op->q * (op->precision == GBFEM_F64 ? 8 : 4);
     const cudaError_t e = cudaMalloc(&j->jac_points, bytes);

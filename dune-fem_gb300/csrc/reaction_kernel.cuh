@@ -28,22 +28,31 @@ template <typename T>
 struct ReactTabsT {
   T B[kDgMaxQ * kDgMaxN];  // B[a*n+i] = L_i(x_a)
   T w[kDgMaxQ];
+  T xq[kDgMaxQ];           // Gauss points on [0, 1]
   T detK, c1, c3, ce;
+  T lower[3], h[3];        // grid origin and cell size (point coordinates)
+  int nc[3];               // cells per direction
 };
 
-template <typename T>
-__device__ __forceinline__ T reaction_value(const ReactTabsT<T>& t, T u) {
-  return t.c1 * u + t.c3 * u * u * u + (t.ce != T(0) ? t.ce * exp(u) : T(0));
-}
-template <typename T>
-__device__ __forceinline__ T reaction_derivative(const ReactTabsT<T>& t, T u) {
-  return t.c1 + T(3) * t.c3 * u * u + (t.ce != T(0) ? t.ce * exp(u) : T(0));
-}
+// The built-in family r(u) = c1 u + c3 u^3 + ce e^u.
+struct BuiltinReaction {
+  static constexpr bool kCoordinates = false;
+  template <typename T>
+  __device__ static T value(const ReactTabsT<T>& t, T u, T, T, T) {
+    return t.c1 * u + t.c3 * u * u * u + (t.ce != T(0) ? t.ce * exp(u) : T(0));
+  }
+  template <typename T>
+  __device__ static T derivative(const ReactTabsT<T>& t, T u, T, T, T) {
+    return t.c1 + T(3) * t.c3 * u * u + (t.ce != T(0) ? t.ce * exp(u) : T(0));
+  }
+};
 
-template <typename T, int N, int Q, int CPB>
-__global__ void __launch_bounds__(128) dg_reaction_kernel(int mode, const T* __restrict__ u, T* __restrict__ w,
-                                                          T* __restrict__ pts, long long cell_begin, long long count,
-                                                          const __grid_constant__ ReactTabsT<T> tb) {
+// R: the pointwise function (value and derivative in u), given the point's
+// physical coordinates when R::kCoordinates.
+template <typename T, int N, int Q, int CPB, class R>
+__device__ __forceinline__ void dg_reaction_body(int mode, const T* __restrict__ u, T* __restrict__ w,
+                                                 T* __restrict__ pts, long long cell_begin, long long count,
+                                                 const ReactTabsT<T>& tb) {
   constexpr int N3 = N * N * N, Q3 = Q * Q * Q;
   __shared__ T sX[CPB * N3];      // coefficients [i][j][k]
   __shared__ T sY1[CPB * Q * N * N];  // [a][j][k]
@@ -85,10 +94,18 @@ __global__ void __launch_bounds__(128) dg_reaction_kernel(int mode, const T* __r
     for (int k = 0; k < N; ++k) s = fma(tb.B[cc * N + k], sY2[cl * Q * Q * N + (a * Q + b) * N + k], s);
     const T W = tb.w[a] * tb.w[b] * tb.w[cc] * tb.detK;
     const long long cell = c0 + cl;
+    T px = T(0), py = T(0), pz = T(0);
+    if (R::kCoordinates) {
+      const long long nxy = (long long)tb.nc[0] * tb.nc[1];
+      const long long cz = cell / nxy, rem = cell - cz * nxy, cy = rem / tb.nc[0], cx = rem - cy * tb.nc[0];
+      px = tb.lower[0] + (T(cx) + tb.xq[a]) * tb.h[0];
+      py = tb.lower[1] + (T(cy) + tb.xq[b]) * tb.h[1];
+      pz = tb.lower[2] + (T(cz) + tb.xq[cc]) * tb.h[2];
+    }
     if (mode == 0) {
-      sP[e] = W * reaction_value(tb, s);
+      sP[e] = W * R::value(tb, s, px, py, pz);
     } else if (mode == 1) {
-      if (cl < ncell) pts[cell * Q3 + r] = W * reaction_derivative(tb, s);
+      if (cl < ncell) pts[cell * Q3 + r] = W * R::derivative(tb, s, px, py, pz);
     } else {
       sP[e] = cl < ncell ? pts[cell * Q3 + r] * s : T(0);
     }
@@ -124,6 +141,14 @@ __global__ void __launch_bounds__(128) dg_reaction_kernel(int mode, const T* __r
     for (int a = 0; a < Q; ++a) s = fma(tb.B[a * N + i], sY1[c * Q * N * N + a * N * N + jk], s);
     w[c0 * N3 + e] += s;
   }
+}
+
+// 128 threads per CTA, CPB cells per CTA
+template <typename T, int N, int Q, int CPB, class R = BuiltinReaction>
+__global__ void __launch_bounds__(128) dg_reaction_kernel(int mode, const T* __restrict__ u, T* __restrict__ w,
+                                                          T* __restrict__ pts, long long cell_begin, long long count,
+                                                          const __grid_constant__ ReactTabsT<T> tb) {
+  dg_reaction_body<T, N, Q, CPB, R>(mode, u, w, pts, cell_begin, count, tb);
 }
 
 // blocks[cell - cell_begin][i][j] += sum_abc pts[abc] phi_i(x_abc) phi_j(x_abc)

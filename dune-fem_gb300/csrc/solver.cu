@@ -468,6 +468,19 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_update_dot(long long n, long
   acc = block_sum(acc);
   if (threadIdx.x == 0) partial[blockIdx.x] = acc;
 }
+// x += alpha q; p -= alpha h, if active (a general preconditioner follows):
+// grid-stride, since no dot-product partition has to be kept
+template <typename T>
+__global__ void k_cg_update(long long n, const T* __restrict__ q, const T* __restrict__ h, T* __restrict__ x,
+                            T* __restrict__ v, double sv, const double* ds) {
+  if (ds[DS_ACTIVE] == 0.0) return;
+  const T alpha = T(ds[DS_ALPHA]);
+  const T sa = T(sv * ds[DS_ALPHA]);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    x[i] = alpha * q[i] + T(1) * x[i];
+    v[i] = sa * h[i] + T(1) * v[i];
+  }
+}
 // pass 2 of the new rho, then the end of the iteration
 __global__ void __launch_bounds__(kRedThreads) k_cg_final_end(const double* __restrict__ partial, int np,
                                                               double* ds) {
@@ -549,11 +562,11 @@ static int cg_device(gbfem_operator op, gbfem_preconditioner pc, const gbfem_sol
     if (c.prec == GBFEM_F64) {
       if (mode == 0) GBFEM_CG_UPDATE(double, 0);
       else if (mode == 1) GBFEM_CG_UPDATE(double, 1);
-      else GBFEM_CG_UPDATE(double, 2);
+      else k_cg_update<double><<<g, 256, 0, st>>>(n, (const double*)q, (const double*)h, (double*)x, (double*)v, sv, ds);
     } else {
       if (mode == 0) GBFEM_CG_UPDATE(float, 0);
       else if (mode == 1) GBFEM_CG_UPDATE(float, 1);
-      else GBFEM_CG_UPDATE(float, 2);
+      else k_cg_update<float><<<g, 256, 0, st>>>(n, (const float*)q, (const float*)h, (float*)x, (float*)v, sv, ds);
     }
 #undef GBFEM_CG_UPDATE
     if (mode == 2) {

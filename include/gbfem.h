@@ -273,6 +273,14 @@ typedef struct {
 } gbfem_reaction;
 int gbfem_dg_nonlinear_operator_create(const gbfem_dg_desc* desc, const gbfem_reaction* reaction,
                                        gbfem_operator* op);
+/* The same operator with a user-defined pointwise reaction r(u, x, y, z),
+ * compiled at run time: cubin_path is an sm_103a cubin holding the kernel
+ * gbfem_user_reaction_<f64|f32>_n<p+1>_q<q> for this operator's precision,
+ * order and quadrature (the Python package's integrands module generates and
+ * compiles it from an expression; r' comes from dual numbers).  ≙ a
+ * GalerkinOperator over UFL-generated integrands (python/dune/models/
+ * integrands/ufl.py). */
+int gbfem_dg_nonlinear_operator_create_jit(const gbfem_dg_desc* desc, const char* cubin_path, gbfem_operator* op);
 /* ≙ Operator::nonlinear() (operator/common/operator.hh:64). */
 int gbfem_operator_nonlinear(gbfem_operator op, int* nonlinear);
 /* A Jacobian operator for op (storage for the linearisation; initially at u = 0

@@ -22,9 +22,16 @@ import oracle
 
 
 class NonlinearProblem:
+    """reaction: the coefficients (c1, c3, ce) of the built-in family, or a
+    pair of callables (r, dr) of (u, x, y, z) for a user-defined reaction."""
+
     def __init__(self, prob, reaction):
         self.prob = prob
-        self.c1, self.c3, self.ce = (float(c) for c in reaction)
+        self.user = callable(reaction[0])
+        if self.user:
+            self.ufun, self.udfun = reaction
+        else:
+            self.c1, self.c3, self.ce = (float(c) for c in reaction)
         n, q = prob.order + 1, prob.quad
         x, w = oracle.gauss(q)
         self.L = np.array([[oracle.legendre(i, xa) for i in range(n)] for xa in x])  # [a][i]
@@ -35,11 +42,23 @@ class NonlinearProblem:
         # Phi[abc, ijk] = L_i(x_a) L_j(x_b) L_k(x_c); W[abc] = w_a w_b w_c |K|
         self.Phi = np.einsum("ai,bj,ck->abcijk", self.L, self.L, self.L).reshape(q ** 3, n ** 3)
         self.W = np.einsum("a,b,c->abc", w, w, w).ravel() * self.detK
+        # physical coordinates of every cell's points [cell][abc] (cell = ix + Nx (iy + Ny iz))
+        nx, ny, nz = (int(c) for c in prob.cells)
+        iz, iy, ix = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+        ix, iy, iz = ix.ravel(), iy.ravel(), iz.ravel()
+        A, B, Cc = np.meshgrid(x, x, x, indexing="ij")
+        self.X = prob.lower[0] + (ix[:, None] + A.ravel()[None, :]) * h[0]
+        self.Y = prob.lower[1] + (iy[:, None] + B.ravel()[None, :]) * h[1]
+        self.Z = prob.lower[2] + (iz[:, None] + Cc.ravel()[None, :]) * h[2]
 
     def r(self, u):
+        if self.user:
+            return self.ufun(u, self.X, self.Y, self.Z)
         return self.c1 * u + self.c3 * u ** 3 + self.ce * np.exp(u)
 
     def dr(self, u):
+        if self.user:
+            return self.udfun(u, self.X, self.Y, self.Z)
         return self.c1 + 3.0 * self.c3 * u ** 2 + self.ce * np.exp(u)
 
     def _points(self, u):

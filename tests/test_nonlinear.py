@@ -245,3 +245,102 @@ def test_newton_stops_when_the_linear_solves_make_no_progress(gb):
     newton(f, w)
     info = newton.info()
     assert not info["converged"] and info["failure"] == "LinearSolverFailed" and info["iterations"] < 1000
+
+
+# ------------------------------------------------- run-time compiled reactions --
+_USER = ("ipow<3>(u) + 0.5*exp(u) - sin(3.0*x)*y + 0.25*z*u",
+         lambda u, x, y, z: u ** 3 + 0.5 * np.exp(u) - np.sin(3.0 * x) * y + 0.25 * z * u,
+         lambda u, x, y, z: 3 * u ** 2 + 0.5 * np.exp(u) + 0.25 * z)
+
+
+def test_user_reaction_source_compiles_for_sm103a():
+    """The generated kernel compiles (nvcc, sm_103a cubin) for both precisions;
+    expressions with other characters are refused."""
+    import shutil
+    if shutil.which("nvcc") is None and not __import__("os").path.exists("/usr/local/cuda/bin/nvcc"):
+        pytest.skip("nvcc not present")
+    import gbfem
+    import integrands
+    for prec in (gbfem.F64, gbfem.F32):
+        path = integrands.compile_reaction(_USER[0], prec, 2)
+        assert path.endswith(".cubin") and __import__("os").path.getsize(path) > 0
+    with pytest.raises(ValueError):
+        integrands.reaction_source("u; system(1)", gbfem.F64, 2)
+    src = integrands.reaction_source("u*u", gbfem.F32, 3, 4)
+    assert "gbfem_user_reaction_f32_n4_q4" in src
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_user_reaction_apply_and_jacobian_match_oracle(gb, orc, order):
+    import integrands
+    no = _no()
+    cells = (3, 2, 4)
+    kw = dict(mass=0.3, velocity=(0.2, 0.0, -0.1), lower=(0.0, -1.0, 0.5), upper=(1.0, 0.5, 1.5))
+    op = integrands.UserNonlinearDGOperator(cells, order, _USER[0], **kw)
+    assert op.nonlinear()
+    P = no.NonlinearProblem(orc.DGProblem(cells, order, **kw), (_USER[1], _USER[2]))
+    rng = np.random.default_rng(60 + order)
+    u, d = rng.uniform(-1, 1, op.size), rng.uniform(-1, 1, op.size)
+    w = gb.DeviceArray(op.size)
+    op(gb.DeviceArray.from_numpy(u), w)
+    assert relmax(w.numpy(), P.apply(u)) < TOL64
+    jac = op.jacobian(gb.DeviceArray.from_numpy(u))
+    y = gb.DeviceArray(op.size)
+    jac(gb.DeviceArray.from_numpy(d), y)
+    assert relmax(y.numpy(), P.jacobian_apply(u, d)) < TOL64
+    nl = op.nloc
+    assert relmax(jac.block_diagonal(nl).numpy().reshape(-1, nl, nl), P.jacobian_blocks(u)) < TOL64
+
+
+@pytest.mark.gpu
+def test_user_reaction_newton_matches_oracle_newton(gb, orc):
+    import integrands
+    no = _no()
+    cells, order = (3, 3, 3), 2
+    expr = "ipow<3>(u) - 2.0*exp(u)*(1.0 + 0.5*x*y) + 0.0*z"
+    r = lambda u, x, y, z: u ** 3 - 2.0 * np.exp(u) * (1.0 + 0.5 * x * y)
+    dr = lambda u, x, y, z: 3 * u ** 2 - 2.0 * np.exp(u) * (1.0 + 0.5 * x * y)
+    op = integrands.UserNonlinearDGOperator(cells, order, expr)
+    P = no.NonlinearProblem(orc.DGProblem(cells, order), (r, dr))
+    solve = lambda w, res, tol: (np.linalg.solve(P.jacobian_matrix(w), res), 1)
+    wo, io = no.newton(P.apply, solve, np.zeros(op.size), np.zeros(op.size), tolerance=1e-10)
+    newton = gb.NewtonInverseOperator(tolerance=1e-10, linear_tolerance=1e-13, max_iterations=50)
+    newton.bind(op)
+    w = gb.DeviceArray(op.size)
+    w.clear()
+    rhs = gb.DeviceArray(op.size)
+    rhs.clear()
+    newton(rhs, w)
+    info = newton.info()
+    assert info["converged"] and info["iterations"] == io["iterations"], (info, io)
+    assert relmax(w.numpy(), wo) < 1e-9
+
+
+@pytest.mark.gpu
+def test_user_reaction_fp32(gb, orc):
+    import integrands
+    no = _no()
+    cells, order = (3, 3, 2), 2
+    op = integrands.UserNonlinearDGOperator(cells, order, _USER[0], precision=gb.F32)
+    P = no.NonlinearProblem(orc.DGProblem(cells, order), (_USER[1], _USER[2]))
+    u = np.random.default_rng(3).uniform(-1, 1, op.size).astype(np.float32)
+    w = gb.DeviceArray(op.size, gb.F32)
+    op(gb.DeviceArray.from_numpy(u), w)
+    assert relmax(w.numpy(), P.apply(u.astype(np.float64))) < 2e-5
+
+
+def test_oracle_user_reaction_coordinates(orc):
+    """r(u, x, y, z) = x + 2 y - z: the coefficient of phi_0 of R is |K| times
+    that function at the cell centre (orthonormal basis, linear integrand)."""
+    no = _no()
+    cells = (2, 3, 2)
+    prob = orc.DGProblem(cells, 1, lower=(0.0, -1.0, 0.5), upper=(1.0, 0.5, 1.5))
+    P = no.NonlinearProblem(prob, (lambda u, x, y, z: x + 2 * y - z + 0 * u, lambda u, x, y, z: 0 * u))
+    R = P.reaction(np.zeros(prob.ndofs)).reshape(-1, prob.nloc)
+    h = (prob.upper - prob.lower) / prob.cells
+    vol = float(np.prod(h))
+    for c in range(prob.ncells):
+        ix, iy, iz = c % 2, (c // 2) % 3, c // 6
+        xc, yc, zc = prob.lower + (np.array([ix, iy, iz]) + 0.5) * h
+        assert abs(R[c, 0] - vol * (xc + 2 * yc - zc)) < 1e-14
