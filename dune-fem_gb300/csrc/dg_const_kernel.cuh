@@ -25,8 +25,8 @@
 //  2. dg_const_kernel: numerical fluxes from the own and the neighbour's
 //     traces (owner computes, no scatter), then one pass per axis over the
 //     lines of the cell: the 1-D operator M_d (a warp-uniform operand; its
-//     structural zeros are skipped: row 0, since L_0' = 0, and without
-//     advection column 0 and the entries with i+j odd) plus the face
+//     structural zeros are skipped: the stiffness part lives on i, j >= 1
+//     with i+j even, the advection part on j < i with i+j odd) plus the face
 //     expansion, again split into even and odd i.
 // Every output is one thread's fixed-order sum: deterministic, independent of
 // the launch shape.
@@ -186,11 +186,14 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
         T acc = d == 0 ? T(0) : rc[i * stride];
 #pragma unroll
         for (int jj = 0; jj < N; ++jj) {
-          // structural zeros of M_d: row 0 (L_0' = 0 in both the stiffness and
-          // the advection matrix) but for the mass entry (0,0) of axis 0;
-          // without advection also column 0 and the entries with i+j odd
+          // structural zeros of M_d = eps K1 - b D1 (+ mass on axis 0):
+          // K1[i][j] = int L_i' L_j' vanishes in row and column 0 and for i+j
+          // odd; D1[i][j] = int L_i' L_j vanishes for j >= i (L_i' has degree
+          // i-1) and for i+j even; the mass entry (0,0) sits on axis 0
           const bool mass00 = d == 0 && i == 0 && jj == 0;
-          const bool nz = ADV ? (i != 0 || mass00) : (!((i + jj) & 1) && ((i != 0 && jj != 0) || mass00));
+          const bool k1 = i != 0 && jj != 0 && !((i + jj) & 1);
+          const bool d1 = jj < i && ((i + jj) & 1);
+          const bool nz = k1 || mass00 || (ADV && d1);
           if (nz) acc = fma(tabs.M[d][i * N + jj], x[jj], acc);
         }
         acc = fma(tabs.tr[N + i], (i & 1) ? vd : vs, acc);
