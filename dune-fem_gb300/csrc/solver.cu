@@ -432,10 +432,10 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_final_alpha(const double* __
   }
   ds[DS_ALPHA] = alpha;
 }
-// x += alpha q; v += sv alpha h (v = p, sv = -1 with a preconditioner; v = r,
-// sv = +1 without), if active; then, in the partition of pass 1 of a dot
-// product: PC 0 the partial of <r, r>, PC 1 s = dinv p and the partial of
-// <p, s>, PC 2 nothing (the preconditioner and its dot product follow).
+// x += alpha q; v += sv alpha h (v = p, sv = -1 with the diagonal
+// preconditioner; v = r, sv = +1 without), if active; then, in the partition
+// of pass 1 of a dot product: PC 0 the partial of <r, r>, PC 1 s = dinv p and
+// the partial of <p, s>.
 template <typename T, int PC>
 __global__ void __launch_bounds__(kRedThreads) k_cg_update_dot(long long n, long long chunk, const T* __restrict__ q,
                                                                const T* __restrict__ h, T* __restrict__ x,
@@ -460,11 +460,10 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_update_dot(long long n, long
       const T si = vi * dinv[i];
       sz[i] = si;
       acc = fma(double(vi), double(si), acc);
-    } else if (PC == 0) {
+    } else {
       acc = fma(double(vi), double(vi), acc);
     }
   }
-  if (PC == 2) return;
   acc = block_sum(acc);
   if (threadIdx.x == 0) partial[blockIdx.x] = acc;
 }
