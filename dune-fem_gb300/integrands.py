@@ -125,3 +125,29 @@ class UserNonlinearDGOperator(gbfem.DGOperator):
         self.order = order
         self.nloc = (order + 1) ** 3
         gbfem.Operator.__init__(self, h, precision)
+
+
+def load_vector(cells, order, expr, quad_points=0, precision=gbfem.F64, lower=(0.0, 0.0, 0.0),
+                upper=(1.0, 1.0, 1.0)):
+    """b_l = int f phi_l for f(x, y, z) = expr (a CUDA expression in x, y, z), by
+    the Gauss rule with quad_points per direction (0: order + 2): the reaction
+    kernel with r = f applied to u = 0.  A DeviceArray in the DG dof layout."""
+    op = UserNonlinearDGOperator(cells, order, expr, quad_points=quad_points, precision=precision, diffusion=0.0,
+                                 penalty=0.0, weak_dirichlet=False, lower=lower, upper=upper)
+    zero = gbfem.DeviceArray(op.size, precision)
+    zero.clear()
+    b = gbfem.DeviceArray(op.size, precision)
+    op(zero, b)
+    return b
+
+
+def project(cells, order, expr, quad_points=0, precision=gbfem.F64, lower=(0.0, 0.0, 0.0), upper=(1.0, 1.0, 1.0)):
+    """L2 projection of f(x, y, z) = expr onto DG Q_order (space.interpolate of a
+    UFL expression): the load vector divided by |K|, the orthonormal basis
+    making the mass matrix |K| I."""
+    b = load_vector(cells, order, expr, quad_points, precision, lower, upper)
+    vol = 1.0
+    for k in range(3):
+        vol *= (upper[k] - lower[k]) / cells[k]
+    gbfem.check(gbfem.lib().gbfem_scal(precision, b.n, 1.0 / vol, b.ptr, None))
+    return b

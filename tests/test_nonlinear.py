@@ -344,3 +344,24 @@ def test_oracle_user_reaction_coordinates(orc):
         ix, iy, iz = c % 2, (c // 2) % 3, c // 6
         xc, yc, zc = prob.lower + (np.array([ix, iy, iz]) + 0.5) * h
         assert abs(R[c, 0] - vol * (xc + 2 * yc - zc)) < 1e-14
+
+
+@pytest.mark.gpu
+def test_projection_of_a_generated_expression(gb, orc):
+    """integrands.project: exact for a polynomial in Q_p, and the same as the
+    built-in projection for the Gaussian bump."""
+    import integrands
+    cells, order = (3, 2, 4), 2
+    lower, upper = (0.0, -1.0, 0.5), (1.0, 0.5, 1.5)
+    u = integrands.project(cells, order, "1.0 + 2.0*x - y + x*y*z + z*z", lower=lower, upper=upper).numpy()
+    import vtkio
+    vals = vtkio.evaluate_subcells(u, cells, order, level=1)
+    h = [(upper[k] - lower[k]) / cells[k] for k in range(3)]
+    zc = lower[2] + (np.arange(cells[2] * 2) + 0.5) * h[2] / 2
+    yc = lower[1] + (np.arange(cells[1] * 2) + 0.5) * h[1] / 2
+    xc = lower[0] + (np.arange(cells[0] * 2) + 0.5) * h[0] / 2
+    X, Y, Z = xc[None, None, :], yc[None, :, None], zc[:, None, None]
+    assert relmax(vals, 1.0 + 2.0 * X - Y + X * Y * Z + Z * Z) < 1e-13
+    bump = integrands.project((4, 4, 4), 2, "exp(-((x-0.5)*(x-0.5) + (y-0.5)*(y-0.5) + (z-0.5)*(z-0.5))/(0.1*0.1))")
+    ref = gb.project((4, 4, 4), 2, gb.FN_GAUSSIAN, params=(0.5, 0.5, 0.5, 0.1))
+    assert relmax(bump.numpy(), ref.numpy()) < 1e-12
