@@ -400,8 +400,8 @@ int gbfem_dg_time_step_estimate(gbfem_operator op, int power_iterations, uint64_
  * 1/rms) and log of the cell mean of kappa, output per-cell coefficients.
  * Trained on the GPU by its own forward/backward kernels.  Used as
  * z = BJ(r) + S rms(r) NN(r/rms(r)) inside flexible CG/GMRES, with block
- * Jacobi as the fallback.  No counterpart in the reference (north-star
- * extension); it plugs in where the reference takes a user preconditioner
+ * Jacobi as the fallback.  No counterpart in the reference (an extension of
+ * the path); it plugs in where the reference takes a user preconditioner
  * (solver/preconditionfunctionwrapper.hh:18-47, schemes/femscheme.hh:202-209).
  * ----------------------------------------------------------------------- */
 typedef struct gbfem_cnn_s* gbfem_cnn;

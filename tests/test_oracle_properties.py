@@ -1,6 +1,7 @@
 """Properties of the CPU oracle itself (no GPU): the invariants the reference's
-tests rely on (SURVEY of dune-fem tests: apply = assembled Jacobian . vector,
-symmetry of SIPG, thread-count invariance)."""
+own tests rely on (apply = assembled Jacobian . vector,
+dune/fempy/test/testoperator.py:33-71; symmetry of SIPG; thread-count
+invariance)."""
 import numpy as np
 import pytest
 
