@@ -161,7 +161,32 @@ class GpuOperator {
   void operator()(const GpuDiscreteFunction& u, GpuDiscreteFunction& w) const {
     check(gbfem_operator_apply(op_.get(), u.leakPointer(), w.leakPointer(), nullptr));
   }
-  bool nonlinear() const { return false; }
+  bool nonlinear() const {
+    int v = 0;
+    check(gbfem_operator_nonlinear(op_.get(), &v));
+    return v != 0;
+  }
+  // S(u) = A u + int r(u) v, r = linear u + cubic u^3 + exponential e^u
+  static GpuOperator nonlinearDG(const gbfem_dg_desc& d, const gbfem_reaction& r) {
+    gbfem_operator op = nullptr;
+    check(gbfem_dg_nonlinear_operator_create(&d, &r, &op));
+    return GpuOperator(op);
+  }
+  // DifferentiableOperator::jacobian(u, jOp): jOp from jacobianOperator()
+  GpuOperator jacobianOperator() const {
+    gbfem_operator j = nullptr;
+    check(gbfem_operator_jacobian_create(op_.get(), &j));
+    return GpuOperator(j);
+  }
+  void jacobian(const GpuDiscreteFunction& u, GpuOperator& jOp) const {
+    check(gbfem_operator_jacobian(op_.get(), u.leakPointer(), jOp.handle(), nullptr));
+  }
+  // the assembled (block-sparse) copy
+  GpuOperator assemble() const {
+    gbfem_operator a = nullptr;
+    check(gbfem_operator_assemble(op_.get(), &a));
+    return GpuOperator(a);
+  }
   std::int64_t size() const {
     std::int64_t n = 0;
     check(gbfem_operator_size(op_.get(), &n));
@@ -186,6 +211,13 @@ class GpuPreconditioner {
   static GpuPreconditioner blockJacobi(const GpuOperator& op, int precision = GBFEM_F64) {
     gbfem_preconditioner pc = nullptr;
     check(gbfem_preconditioner_block_jacobi_create(op.handle(), precision, &pc));
+    return GpuPreconditioner(pc);
+  }
+  // FemPreconditioning jacobi / gauss-seidel / sor / ssor of an assembled
+  // operator (GBFEM_SMOOTHER_*); the operator must outlive the preconditioner
+  static GpuPreconditioner sor(const GpuOperator& assembled, int method, int n = 1, double w = 1.0) {
+    gbfem_preconditioner pc = nullptr;
+    check(gbfem_preconditioner_sor_create(assembled.handle(), method, n, w, &pc));
     return GpuPreconditioner(pc);
   }
   void operator()(const GpuDiscreteFunction& r, GpuDiscreteFunction& z) const {
@@ -233,6 +265,32 @@ class GpuKrylovInverseOperator {
   mutable gbfem_solver_info info_{};
   const GpuOperator* op_ = nullptr;
   const GpuPreconditioner* pc_ = nullptr;
+};
+
+// NewtonInverseOperator (solver/newtoninverseoperator.hh:484-790):
+// bind(op), operator()(rhs, w) with w the initial guess, iterations(),
+// linearIterations(), info(); parameters as gbfem_newton_params.
+class GpuNewtonInverseOperator {
+ public:
+  GpuNewtonInverseOperator() { check(gbfem_newton_params_default(&prm_)); }
+  explicit GpuNewtonInverseOperator(const gbfem_newton_params& prm) : prm_(prm) {}
+  gbfem_newton_params& parameter() { return prm_; }
+  void bind(const GpuOperator& op) { op_ = &op; }
+  void unbind() { op_ = nullptr; }
+  void operator()(const GpuDiscreteFunction& rhs, GpuDiscreteFunction& w) const {
+    if (!op_) throw Error(GBFEM_ERR_INVALID, "GpuNewtonInverseOperator: no operator bound");
+    check(gbfem_newton_solve(op_->handle(), &prm_, rhs.leakPointer(), w.leakPointer(), &info_));
+  }
+  int iterations() const { return info_.iterations; }
+  int linearIterations() const { return info_.linear_iterations; }
+  bool converged() const { return info_.converged != 0; }
+  int failed() const { return info_.failure; }  // NewtonFailure
+  double residual() const { return info_.residual; }
+
+ private:
+  gbfem_newton_params prm_{};
+  mutable gbfem_newton_info info_{};
+  const GpuOperator* op_ = nullptr;
 };
 
 // TimeProvider (solver/timeprovider.hh:35-200, 403-592), single process:

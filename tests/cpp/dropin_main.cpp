@@ -68,5 +68,35 @@ int main() {
   for (std::int64_t c = 0; c < n / 27; ++c) mass += vh[c * 27];
   std::printf("time loop: %d steps of %.4e to t = %.4f, mean %.15f\n", steps, tp.deltaT(), tp.time(), mass);
   if (steps < 1 || std::fabs(mass - 1.0) > 1e-12) return 2;
+  // Newton on the Bratu problem -lap u = 3 e^u through NewtonInverseOperator
+  gbfem_reaction r{0.0, 0.0, -3.0};
+  GpuOperator bratu = GpuOperator::nonlinearDG(d, r);
+  if (!bratu.nonlinear()) return 3;
+  GpuNewtonInverseOperator newton;
+  newton.parameter().tolerance = 1e-10;
+  newton.parameter().max_iterations = 50;
+  newton.parameter().preconditioner = GBFEM_PC_BLOCK_JACOBI;
+  newton.parameter().linear.tolerance = 1e-12;
+  newton.parameter().linear.error_measure = GBFEM_TOL_RELATIVE;
+  newton.bind(bratu);
+  GpuDiscreteFunction zero("zero", n), sol("sol", n);
+  newton(zero, sol);
+  std::printf("Newton (Bratu): %d iterations, %d linear, |residual| %.3e\n", newton.iterations(),
+              newton.linearIterations(), newton.residual());
+  if (!newton.converged() || newton.iterations() > 8) return 4;
+  // jacobian(u, jOp), assembled, with an SSOR-preconditioned CG
+  GpuOperator jac = bratu.jacobianOperator();
+  bratu.jacobian(sol, jac);
+  GpuOperator assembled = jac.assemble();
+  GpuPreconditioner ssor = GpuPreconditioner::sor(assembled, GBFEM_SMOOTHER_SSOR);
+  GpuKrylovInverseOperator cg(GBFEM_SOLVER_CG, 1e-12, GBFEM_TOL_RELATIVE);
+  cg.bind(assembled, ssor);
+  u.clear();
+  cg(f, u);
+  jac(u, w);
+  w -= f;
+  const double relj = std::sqrt(w.normSquaredDofs() / f.normSquaredDofs());
+  std::printf("SSOR-CG on the assembled Jacobian: %d iterations, relative residual %.3e\n", cg.iterations(), relj);
+  if (!cg.info().converged || !(relj < 1e-9)) return 5;
   return 0;
 }

@@ -214,3 +214,35 @@ def test_kappa_point_cache_follows_update_coefficients(gb, orc, precision):
     op.update_coefficients()
     op(gb.DeviceArray.from_numpy(u.astype(dt), precision), w)
     assert relmax(w.numpy(), prob.apply(u.astype(dt).astype(np.float64), kappa=kappa2.astype(dt).astype(np.float64))) < tol
+
+
+@pytest.mark.parametrize("cells,periodic", [((1, 1, 1), (0, 0, 0)), ((1, 3, 1), (0, 0, 0)), ((2, 1, 2), (1, 0, 1)),
+                                            ((5, 1, 1), (1, 0, 0))])
+@pytest.mark.parametrize("algorithm", [0, 1])
+def test_degenerate_grids(gb, orc, cells, periodic, algorithm):
+    """One cell, one cell thick in some directions, periodic with two cells:
+    every face of a direction with one non-periodic cell is a boundary face."""
+    kw = dict(mass=0.4, velocity=(0.3, -0.2, 0.1), periodic=periodic)
+    op = gb.DGOperator(cells, 2, algorithm=algorithm, **kw)
+    prob = orc.DGProblem(cells, 2, **kw)
+    u = np.random.default_rng(sum(cells)).uniform(-1, 1, prob.ndofs)
+    w = gb.DeviceArray(prob.ndofs)
+    op(gb.DeviceArray.from_numpy(u), w)
+    assert relmax(w.numpy(), prob.apply(u)) < TOL64
+    wh = np.empty(prob.ndofs)
+    op.set_host_chunks(0)
+    op.apply_host(u, wh)
+    assert np.array_equal(wh.view(np.uint64), w.numpy().view(np.uint64))
+    nl = prob.nloc
+    assert relmax(op.block_diagonal(nl).numpy().reshape(-1, nl, nl), prob.block_diagonal()) < TOL64
+
+
+def test_invalid_descriptors_are_refused(gb):
+    with pytest.raises(gb.GbfemError):
+        gb.DGOperator((0, 2, 2), 2)          # no cells
+    with pytest.raises(gb.GbfemError):
+        gb.DGOperator((2, 2, 2), 5)          # order outside 1..4
+    with pytest.raises(gb.GbfemError):
+        gb.DGOperator((2, 2, 2), 2, quad_points=7)
+    with pytest.raises(gb.GbfemError):
+        gb.DGOperator((1, 2, 2), 2, periodic=(1, 0, 0))  # periodic needs two cells
