@@ -49,11 +49,14 @@ struct DgConstTablesT {
 };
 
 // traces[cell][f = 2d+s][0: v, 1: d][jk], d(s) without the 1/h and normal sign,
-// for the cells [cell_begin, cell_begin + count)
+// for the cells [cell_begin, cell_begin + count).  ucopy (optional): the
+// x-lines also store the dofs they read there, so a u read from host memory
+// is copied to the device on the way (every dof exactly once).
 template <typename T, int N>
 __global__ void __launch_bounds__(256) dg_trace_kernel(const T* __restrict__ u, T* __restrict__ traces,
                                                        long long cell_begin, long long count,
-                                                       const __grid_constant__ DgConstTablesT<T> tabs) {
+                                                       const __grid_constant__ DgConstTablesT<T> tabs,
+                                                       T* __restrict__ ucopy) {
   constexpr int N2 = N * N, N3 = N2 * N;
   const long long total = count * 3 * N2;
   for (long long item = blockIdx.x * (long long)blockDim.x + threadIdx.x; item < total;
@@ -70,6 +73,7 @@ __global__ void __launch_bounds__(256) dg_trace_kernel(const T* __restrict__ u, 
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       const T x = __ldg(uc + i * stride);
+      if (ucopy && d == 0) ucopy[cell * N3 + base + i * stride] = x;
       if (i & 1) {
         od = fma(tabs.tr[N + i], x, od);
         odd = fma(tabs.dtr[N + i], x, odd);

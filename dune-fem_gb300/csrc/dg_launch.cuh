@@ -62,7 +62,7 @@ int dg_launch(const DgArgsT<T>& args, const DgTablesT<T>& tabs, int n, int q, bo
 // be current).  count = cell_count, 0 = all cells.
 template <typename T, int N>
 int dg_const_launch_one(const DgArgsT<T>& args, const DgConstTablesT<T>& tabs, T* traces, int phase,
-                        cudaStream_t stream) {
+                        cudaStream_t stream, T* ucopy) {
   constexpr int CPB = N <= 2 ? 32 : (N <= 4 ? 16 : 8);
   const long long count = args.cell_count > 0 ? args.cell_count : args.ncells;
   const long long blocks = (count + CPB - 1) / CPB;
@@ -72,7 +72,8 @@ int dg_const_launch_one(const DgArgsT<T>& args, const DgConstTablesT<T>& tabs, T
     const long long titems = count * 3 * N * N;
     long long tblocks = (titems + 255) / 256;
     if (tblocks > 152LL * 32) tblocks = 152LL * 32;
-    dg_trace_kernel<T, N><<<unsigned(tblocks), 256, 0, stream>>>(args.u, traces, args.cell_begin, count, tabs);
+    dg_trace_kernel<T, N><<<unsigned(tblocks), 256, 0, stream>>>(args.u, traces, args.cell_begin, count, tabs,
+                                                                 ucopy);
   }
   if (phase & 2) {
     if (args.advect)
@@ -86,12 +87,12 @@ int dg_const_launch_one(const DgArgsT<T>& args, const DgConstTablesT<T>& tabs, T
 
 template <typename T>
 int dg_const_launch(const DgArgsT<T>& args, const DgConstTablesT<T>& tabs, int n, T* traces, int phase,
-                    cudaStream_t stream) {
+                    cudaStream_t stream, T* ucopy = nullptr) {
   switch (n) {
-    case 2: return dg_const_launch_one<T, 2>(args, tabs, traces, phase, stream);
-    case 3: return dg_const_launch_one<T, 3>(args, tabs, traces, phase, stream);
-    case 4: return dg_const_launch_one<T, 4>(args, tabs, traces, phase, stream);
-    case 5: return dg_const_launch_one<T, 5>(args, tabs, traces, phase, stream);
+    case 2: return dg_const_launch_one<T, 2>(args, tabs, traces, phase, stream, ucopy);
+    case 3: return dg_const_launch_one<T, 3>(args, tabs, traces, phase, stream, ucopy);
+    case 4: return dg_const_launch_one<T, 4>(args, tabs, traces, phase, stream, ucopy);
+    case 5: return dg_const_launch_one<T, 5>(args, tabs, traces, phase, stream, ucopy);
   }
   return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "dg apply: unsupported order");
 }

@@ -17,8 +17,10 @@ namespace gbfem {
 
 int dg_launch_f64(const DgArgsT<double>&, const DgTablesT<double>&, int, int, bool, cudaStream_t);
 int dg_launch_f32(const DgArgsT<float>&, const DgTablesT<float>&, int, int, bool, cudaStream_t);
-int dg_const_launch_f64(const DgArgsT<double>&, const DgConstTablesT<double>&, int, double*, int, cudaStream_t);
-int dg_const_launch_f32(const DgArgsT<float>&, const DgConstTablesT<float>&, int, float*, int, cudaStream_t);
+int dg_const_launch_f64(const DgArgsT<double>&, const DgConstTablesT<double>&, int, double*, int, cudaStream_t,
+                        double* ucopy = nullptr);
+int dg_const_launch_f32(const DgArgsT<float>&, const DgConstTablesT<float>&, int, float*, int, cudaStream_t,
+                        float* ucopy = nullptr);
 int dg_kappa_points_f64(const double*, double*, double*, long long, const DgTablesT<double>&, int, int, cudaStream_t);
 int dg_kappa_points_f32(const float*, float*, float*, long long, const DgTablesT<float>&, int, int, cudaStream_t);
 
@@ -139,13 +141,13 @@ static void fill_line_operators(const gbfem_operator_s* op, DgConstTablesT<T>* c
 }
 
 static int dg_apply_linear(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
-                           void* blocks, long long cell_begin, long long cell_count, int phase);
+                           void* blocks, long long cell_begin, long long cell_count, int phase, void* ucopy);
 
 int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
-             void* blocks, long long cell_begin, long long cell_count, int phase) {
+             void* blocks, long long cell_begin, long long cell_count, int phase, void* ucopy) {
   if (op->nonlinear && unit_mode != 0)
     return set_error(GBFEM_ERR_INVALID, "nonlinear operator: diagonal and blocks belong to its Jacobian");
-  GBFEM_TRY(dg_apply_linear(op, u, w, s, unit_mode, blocks, cell_begin, cell_count, phase));
+  GBFEM_TRY(dg_apply_linear(op, u, w, s, unit_mode, blocks, cell_begin, cell_count, phase, ucopy));
   const long long count = cell_count > 0 ? cell_count : op->ncells - cell_begin;
   if (unit_mode == 0 && (phase & 2)) {
     if (op->nonlinear) return reaction_launch(op, 0, u, w, nullptr, cell_begin, count, 0, s);
@@ -159,7 +161,7 @@ int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s,
 }
 
 static int dg_apply_linear(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
-                           void* blocks, long long cell_begin, long long cell_count, int phase) {
+                           void* blocks, long long cell_begin, long long cell_count, int phase, void* ucopy) {
   if (op->precision == GBFEM_F64) {
     DgArgsT<double> a;
     fill_dg_args(op, &a);
@@ -174,7 +176,7 @@ static int dg_apply_linear(const gbfem_operator_s* op, const void* u, void* w, c
       fill_line_operators(op, &ct);
       void* tb = nullptr;
       GBFEM_TRY(trace_buffer(op, &tb));
-      return dg_const_launch_f64(a, ct, op->n, static_cast<double*>(tb), phase, s);
+      return dg_const_launch_f64(a, ct, op->n, static_cast<double*>(tb), phase, s, static_cast<double*>(ucopy));
     }
     return dg_launch_f64(a, op->tab64, op->n, op->q, op->dg.kappa != nullptr, s);
   } else {
@@ -191,7 +193,7 @@ static int dg_apply_linear(const gbfem_operator_s* op, const void* u, void* w, c
       fill_line_operators(op, &ct);
       void* tb = nullptr;
       GBFEM_TRY(trace_buffer(op, &tb));
-      return dg_const_launch_f32(a, ct, op->n, static_cast<float*>(tb), phase, s);
+      return dg_const_launch_f32(a, ct, op->n, static_cast<float*>(tb), phase, s, static_cast<float*>(ucopy));
     }
     return dg_launch_f32(a, op->tab32, op->n, op->q, op->dg.kappa != nullptr, s);
   }
@@ -347,7 +349,76 @@ static int host_pipe(gbfem_operator_s* op, int nchunks, HostPipe** out) {
 // periodic z, slab 0 also needs the last slab and is applied last.  Each cell
 // is computed by the same kernel code as the one-shot apply, so the result is
 // bitwise the same.
+// The device address of page-locked (registered or cudaHostAlloc'ed) host
+// memory, or nullptr for anything else.  Only such memory is ever read or
+// written by a kernel.
+static void* mapped_device_pointer(const void* host) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost) return nullptr;
+  return a.devicePointer;
+}
+
+// Host-buffer apply of the closed-form kernel on page-locked buffers: the
+// trace pass reads u straight from host memory over NVLink-C2C (and leaves a
+// device copy for the main kernel), the main kernel writes w straight to host
+// memory.  Slabs of z-planes as in the copy pipeline: traces of slab k on one
+// stream, the apply of slab k-1 on another once slab k's traces exist, so the
+// C2C reads overlap the FP64 work.  Same kernels and arithmetic as the
+// device apply.
+static int dg_apply_host_mapped(gbfem_operator_s* op, const void* du, void* dw) {
+  const int nz = op->dg.grid.cells[2];
+  const long long plane = (long long)op->dg.grid.cells[0] * op->dg.grid.cells[1];
+  int nchunks = op->host_chunks;
+  if (nchunks <= 0) {
+    const long long by_size = op->ncells / 8192;
+    nchunks = int(by_size < 16 ? (by_size < 1 ? 1 : by_size) : 16);
+  }
+  if (nchunks > nz) nchunks = nz;
+  if (nchunks > 64) nchunks = 64;
+  const int zper = (nz + nchunks - 1) / nchunks;
+  nchunks = (nz + zper - 1) / zper;
+  HostPipe* p = nullptr;
+  GBFEM_TRY(host_pipe(op, nchunks, &p));
+  auto first_cell = [&](int k) { return (long long)k * zper * plane; };
+  auto cell_count = [&](int k) {
+    const long long z1 = (long long)(k + 1) * zper < nz ? (long long)(k + 1) * zper : nz;
+    return (z1 - (long long)k * zper) * plane;
+  };
+  GBFEM_CUDA_TRY(cudaEventRecord(p->start, 0));
+  GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->in, p->start, 0));
+  GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->comp, p->start, 0));
+  for (int k = 0; k < nchunks; ++k) {
+    GBFEM_TRY(dg_apply(op, du, nullptr, p->in, 0, nullptr, first_cell(k), cell_count(k), 1, op->host_u));
+    GBFEM_CUDA_TRY(cudaEventRecord(p->ev_in[k], p->in));
+  }
+  const bool defer0 = op->dg.grid.periodic[2] && nchunks > 1;
+  auto apply = [&](int j) -> int {
+    // slab j reads the traces of slabs j-1, j, j+1 (and wraps with periodic z)
+    const int need = j + 1 < nchunks ? j + 1 : nchunks - 1;
+    GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->comp, p->ev_in[defer0 && j == 0 ? nchunks - 1 : need], 0));
+    return dg_apply(op, op->host_u, dw, p->comp, 0, nullptr, first_cell(j), cell_count(j), 2);
+  };
+  int rc = GBFEM_OK;
+  for (int j = defer0 ? 1 : 0; j < nchunks && rc == GBFEM_OK; ++j) rc = apply(j);
+  if (rc == GBFEM_OK && defer0) rc = apply(0);
+  const cudaError_t e1 = cudaStreamSynchronize(p->comp);
+  const cudaError_t e2 = cudaStreamSynchronize(p->in);
+  GBFEM_TRY(rc);
+  if (e1 != cudaSuccess) return set_cuda_error(e1, "gbfem_operator_apply_host");
+  if (e2 != cudaSuccess) return set_cuda_error(e2, "gbfem_operator_apply_host");
+  return GBFEM_OK;
+}
+
 int dg_apply_host_pipelined(gbfem_operator_s* op, const void* u_host, void* w_host) {
+  if (op->coefficient_space && !op->host_copy_only) {
+    void* du = mapped_device_pointer(u_host);
+    void* dw = du ? mapped_device_pointer(w_host) : nullptr;
+    if (du && dw) return dg_apply_host_mapped(op, du, dw);
+  }
   const size_t es = op->precision == GBFEM_F64 ? 8 : 4;
   const int nz = op->dg.grid.cells[2];
   const long long plane = (long long)op->dg.grid.cells[0] * op->dg.grid.cells[1];
@@ -541,6 +612,12 @@ int gbfem_operator_apply_host(gbfem_operator op, const void* u_host, void* w_hos
   GBFEM_TRY(gbfem_operator_apply(op, op->host_u, op->host_w, nullptr));
   GBFEM_CUDA_TRY(cudaMemcpyAsync(w_host, op->host_w, bytes, cudaMemcpyDeviceToHost, 0));
   GBFEM_CUDA_TRY(cudaStreamSynchronize(0));
+  return GBFEM_OK;
+}
+
+int gbfem_operator_set_host_transfer(gbfem_operator op, int mode) {
+  if (!op || mode < 0 || mode > 1) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_set_host_transfer: invalid argument");
+  op->host_copy_only = mode;
   return GBFEM_OK;
 }
 

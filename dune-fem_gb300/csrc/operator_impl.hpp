@@ -21,7 +21,8 @@ struct Q1Element {
 // computes the face traces of the cells, bit 2 the apply (which reads the
 // traces of the neighbours); the other kernels ignore it.
 int dg_apply(const struct ::gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
-             void* blocks, long long cell_begin = 0, long long cell_count = 0, int phase = 3);
+             void* blocks, long long cell_begin = 0, long long cell_count = 0, int phase = 3,
+             void* ucopy = nullptr);  // closed form, phase 1: also copy the dofs read to ucopy
 int q1_apply(const struct ::gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int diag_only);
 // assembled operator: y = A x (diag_only: the diagonal into y)
 int bsr_apply(const struct ::gbfem_operator_s* op, const void* x, void* y, cudaStream_t s, int diag_only);
@@ -59,6 +60,7 @@ struct gbfem_operator_s {
   void* host_u = nullptr;  // device staging of gbfem_operator_apply_host
   void* host_w = nullptr;
   int host_chunks = 0;     // z-slab chunks of the pipelined host apply (0 = automatic)
+  int host_copy_only = 0;  // 1: page-locked host buffers go through the copy pipeline too
   int nonlinear = 0;       // DG: adds the reaction R(u) = int r(u) v (react = c1, c3, ce)
   double react[3] = {0.0, 0.0, 0.0};
   void* jac_points = nullptr;  // Jacobian of a nonlinear DG operator: [cell][q^3] w |K| r'(u0)

@@ -104,6 +104,7 @@ def lib():
         L.gbfem_operator_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.gbfem_operator_apply_host.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.gbfem_operator_set_host_chunks.argtypes = [C.c_void_p, C.c_int]
+        L.gbfem_operator_set_host_transfer.argtypes = [C.c_void_p, C.c_int]
         L.gbfem_operator_update_coefficients.argtypes = [C.c_void_p]
         L.gbfem_operator_diagonal.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.gbfem_operator_block_diagonal.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
@@ -245,6 +246,11 @@ class Operator:
     def update_coefficients(self):
         """Re-evaluates a variable kappa at the Gauss points after its vector changed."""
         check(lib().gbfem_operator_update_coefficients(self.handle))
+
+    def set_host_transfer(self, copy_only):
+        """True: page-locked host buffers go through the copy pipeline instead of
+        being read / written by the kernels in place."""
+        check(lib().gbfem_operator_set_host_transfer(self.handle, 1 if copy_only else 0))
 
     def set_host_chunks(self, nchunks):
         """Slabs of the pipelined host-buffer apply of a DG operator (0 = automatic)."""

@@ -246,3 +246,29 @@ def test_invalid_descriptors_are_refused(gb):
         gb.DGOperator((2, 2, 2), 2, quad_points=7)
     with pytest.raises(gb.GbfemError):
         gb.DGOperator((1, 2, 2), 2, periodic=(1, 0, 0))  # periodic needs two cells
+
+
+@pytest.mark.parametrize("periodic_z", [0, 1])
+@pytest.mark.parametrize("chunks", [1, 3, 0])
+@pytest.mark.parametrize("nonlinear", [False, True])
+def test_host_apply_on_page_locked_buffers_is_bitwise_the_device_apply(gb, orc, periodic_z, chunks, nonlinear):
+    """Page-locked host buffers: the kernels read u and write w in host memory
+    (NVLink-C2C); the result is the device apply's, bit for bit, and the same as
+    the copy pipeline's."""
+    torch = pytest.importorskip("torch")
+    cells = (3, 4, 7)
+    kw = dict(mass=0.3, velocity=(0.2, -0.4, 0.7), periodic=(0, 1, periodic_z))
+    op = (gb.NonlinearDGOperator(cells, 2, reaction=(0.1, 0.5, -0.2), **kw) if nonlinear
+          else gb.DGOperator(cells, 2, **kw))
+    op.set_host_chunks(chunks)
+    u = np.random.default_rng(22).uniform(-1, 1, op.size)
+    w = gb.DeviceArray(op.size)
+    op(gb.DeviceArray.from_numpy(u), w)
+    ref = w.numpy()
+    uh = torch.from_numpy(u).pin_memory()
+    wh = torch.full((op.size,), float("nan"), dtype=torch.float64).pin_memory()
+    for copy_only in (False, True, False):
+        op.set_host_transfer(copy_only)
+        wh.fill_(float("nan"))
+        op.apply_host(uh.numpy(), wh.numpy())
+        assert np.array_equal(wh.numpy().view(np.uint64), ref.view(np.uint64)), copy_only
