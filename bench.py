@@ -240,13 +240,14 @@ def run_gpu(args, world, rank, local):
     el = time.perf_counter() - t0
     el = allreduce_max(el, world)
     e2e_value = world * n * e2e_steps / el
-    # the same call with the copy pipeline instead of in-place host access
+    # the same call with the kernels reading / writing the host buffers in
+    # place over NVLink-C2C instead of the copy pipeline
     op.set_host_transfer(True)
     op.apply_host(uh_np, wh_np)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         op.apply_host(uh_np, wh_np)
-    e2e_copy_value = world * n * e2e_steps / allreduce_max(time.perf_counter() - t0, world)
+    e2e_in_place = world * n * e2e_steps / allreduce_max(time.perf_counter() - t0, world)
     op.set_host_transfer(False)
     if rank != 0:
         return
@@ -283,9 +284,9 @@ def run_gpu(args, world, rank, local):
             "gpu_launches": 2 * args.steps,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                     "steps": e2e_steps,
-                    "path": "gbfem_operator_apply_host on page-locked host buffers: the kernels read u and write w "
-                            "in host memory over NVLink-C2C, 16 z-slabs, trace pass and apply overlapped",
-                    "copy_pipeline_value": e2e_copy_value},
+                    "path": "gbfem_operator_apply_host (page-locked host buffers; copy in, apply and copy out "
+                            "pipelined over 16 z-slabs on three streams)",
+                    "in_place_c2c_value": e2e_in_place},
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": traffic,
                          "peak_source": peak_kind, "algorithmic_bytes_per_dof": BYTES_PER_DOF},

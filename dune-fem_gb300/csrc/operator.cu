@@ -414,7 +414,7 @@ static int dg_apply_host_mapped(gbfem_operator_s* op, const void* du, void* dw) 
 }
 
 int dg_apply_host_pipelined(gbfem_operator_s* op, const void* u_host, void* w_host) {
-  if (op->coefficient_space && !op->host_copy_only) {
+  if (op->coefficient_space && op->host_in_place) {
     void* du = mapped_device_pointer(u_host);
     void* dw = du ? mapped_device_pointer(w_host) : nullptr;
     if (du && dw) return dg_apply_host_mapped(op, du, dw);
@@ -617,7 +617,7 @@ int gbfem_operator_apply_host(gbfem_operator op, const void* u_host, void* w_hos
 
 int gbfem_operator_set_host_transfer(gbfem_operator op, int mode) {
   if (!op || mode < 0 || mode > 1) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_set_host_transfer: invalid argument");
-  op->host_copy_only = mode;
+  op->host_in_place = mode;
   return GBFEM_OK;
 }
 

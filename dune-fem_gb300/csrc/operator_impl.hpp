@@ -60,7 +60,7 @@ struct gbfem_operator_s {
   void* host_u = nullptr;  // device staging of gbfem_operator_apply_host
   void* host_w = nullptr;
   int host_chunks = 0;     // z-slab chunks of the pipelined host apply (0 = automatic)
-  int host_copy_only = 0;  // 1: page-locked host buffers go through the copy pipeline too
+  int host_in_place = 0;   // 1: page-locked host buffers are read / written by the kernels over C2C
   int nonlinear = 0;       // DG: adds the reaction R(u) = int r(u) v (react = c1, c3, ce)
   double react[3] = {0.0, 0.0, 0.0};
   void* jac_points = nullptr;  // Jacobian of a nonlinear DG operator: [cell][q^3] w |K| r'(u0)

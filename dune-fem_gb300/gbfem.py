@@ -247,10 +247,10 @@ class Operator:
         """Re-evaluates a variable kappa at the Gauss points after its vector changed."""
         check(lib().gbfem_operator_update_coefficients(self.handle))
 
-    def set_host_transfer(self, copy_only):
-        """True: page-locked host buffers go through the copy pipeline instead of
-        being read / written by the kernels in place."""
-        check(lib().gbfem_operator_set_host_transfer(self.handle, 1 if copy_only else 0))
+    def set_host_transfer(self, in_place):
+        """True: the kernels read u and write w in page-locked host memory over
+        NVLink-C2C; False (default): the slab copy pipeline."""
+        check(lib().gbfem_operator_set_host_transfer(self.handle, 1 if in_place else 0))
 
     def set_host_chunks(self, nchunks):
         """Slabs of the pipelined host-buffer apply of a DG operator (0 = automatic)."""

@@ -123,18 +123,20 @@ int gbfem_operator_apply(gbfem_operator op, const void* u, void* w, void* stream
 /* Same as gbfem_operator_apply with host arrays: copies u to the device,
  * applies, copies w back, synchronously.  Device buffers are cached in op.
  * DG operators pipeline the call over slabs of z-planes (copy in, apply and
- * copy out of successive slabs overlap on three streams).  With page-locked
- * host arrays the constant-coefficient kernel reads u and writes w in host
- * memory directly (see gbfem_operator_set_host_transfer).  The result is
- * bitwise that of gbfem_operator_apply. */
+ * copy out of successive slabs overlap on three streams; page-locked host
+ * arrays let the copies run asynchronously; see also
+ * gbfem_operator_set_host_transfer).  The result is bitwise that of
+ * gbfem_operator_apply. */
 int gbfem_operator_apply_host(gbfem_operator op, const void* u_host, void* w_host);
 /* Number of slabs of the pipelined gbfem_operator_apply_host (0 = automatic:
  * up to 16, each >= 8192 cells; capped at the number of z-planes and 64). */
 int gbfem_operator_set_host_chunks(gbfem_operator op, int nchunks);
 /* How gbfem_operator_apply_host moves page-locked host buffers of the
- * constant-coefficient DG kernel: 0 (default) = the kernels read u and write w
- * in host memory directly over NVLink-C2C (cudaPointerGetAttributes decides;
- * pageable buffers always take the copy pipeline); 1 = copy pipeline. */
+ * constant-coefficient DG kernel: 0 (default) = the slab copy pipeline;
+ * 1 = the kernels read u and write w in host memory directly over NVLink-C2C
+ * (only for buffers cudaPointerGetAttributes reports as page-locked; pageable
+ * ones always take the copy pipeline).  On GB300 the copy pipeline is the
+ * faster of the two at 8-16 slabs; in place wins without slabs. */
 int gbfem_operator_set_host_transfer(gbfem_operator op, int mode);
 
 /* Diagonal of the operator's matrix.  ≙ DifferentiableOperator::jacobian

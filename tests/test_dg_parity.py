@@ -267,8 +267,8 @@ def test_host_apply_on_page_locked_buffers_is_bitwise_the_device_apply(gb, orc, 
     ref = w.numpy()
     uh = torch.from_numpy(u).pin_memory()
     wh = torch.full((op.size,), float("nan"), dtype=torch.float64).pin_memory()
-    for copy_only in (False, True, False):
-        op.set_host_transfer(copy_only)
+    for in_place in (True, False, True):
+        op.set_host_transfer(in_place)
         wh.fill_(float("nan"))
         op.apply_host(uh.numpy(), wh.numpy())
-        assert np.array_equal(wh.numpy().view(np.uint64), ref.view(np.uint64)), copy_only
+        assert np.array_equal(wh.numpy().view(np.uint64), ref.view(np.uint64)), in_place
