@@ -46,6 +46,7 @@ struct DgConstTablesT {
   T M[3][kDgMaxN * kDgMaxN];  // per-axis line operator (filled per operator)
   // per-axis flux constants: A1 = |F| eps sigma, A2 = |F| eps / (2 h)
   T A1[3], A2[3];
+  T massK;  // cellwise kappa: c |K| (the mass term, kept out of M)
 };
 
 // traces[cell][f = 2d+s][0: v, 1: d][jk], d(s) without the 1/h and normal sign,
@@ -91,13 +92,19 @@ __global__ void __launch_bounds__(256) dg_trace_kernel(const T* __restrict__ u, 
   }
 }
 
-template <typename T, int N, int CPB, bool ADV>
+// KC: a constant kappa per cell (args.kcell), no advection: the diffusion
+// part of M_d is scaled by the cell's kappa, the fluxes use the two cells'
+// values as the quadrature of kappa_bar [u][v] - {kappa grad u}.n [v] -
+// [u] {kappa grad v}.n does; the mass term is one FMA on axis 0.
+template <typename T, int N, int CPB, bool ADV, bool KC = false>
 __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, const T* __restrict__ traces,
                                                        const __grid_constant__ DgConstTablesT<T> tabs) {
   constexpr int N2 = N * N, N3 = N * N * N;
+  static_assert(!(KC && ADV), "cellwise kappa without advection");
   __shared__ T su[CPB * N3];
   __shared__ T sr[CPB * N3];
   __shared__ T sF[CPB * 6 * 2 * N2];  // [cell][face][Val/Grad][jk]
+  __shared__ T sK[KC ? CPB : 1];
   const int tid = threadIdx.x;
   // output cells [cell_begin, cend); neighbours anywhere in the grid
   const long long cend = args.cell_begin + (args.cell_count > 0 ? args.cell_count : args.ncells);
@@ -107,6 +114,8 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
     const long long v = c0 + e / N3;
     su[e] = v < cend ? __ldg(args.u + c0 * N3 + e) : T(0);
   }
+  if (KC)
+    for (int c = tid; c < CPB; c += blockDim.x) sK[c] = c0 + c < cend ? __ldg(args.kcell + c0 + c) : T(0);
   // ---- faces: numerical fluxes from own and neighbour traces -----------------
   for (int item = tid; item < CPB * 6 * N2; item += blockDim.x) {
     const int c = item / (6 * N2);
@@ -141,7 +150,19 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
     }
     const T a2 = s ? tabs.A2[d] : -tabs.A2[d];  // carries the normal's sign
     T val = T(0), grad = T(0);
-    if (has_nb) {
+    if (KC) {
+      const T km = __ldg(args.kcell + cl);
+      if (has_nb) {
+        // eps |F| (sigma kbar J - {kappa dn u}),  -eps |F| kappa- J / 2
+        const T kp = __ldg(args.kcell + ncell);
+        const T J = vm - vp;
+        val = fma(tabs.A1[d] * (T(0.5) * (km + kp)), J, -a2 * (km * dm + kp * dp));
+        grad = -tabs.A2[d] * km * J;
+      } else if (args.weak_dirichlet) {
+        val = fma(tabs.A1[d] * km, vm, T(-2) * a2 * km * dm);
+        grad = T(-2) * tabs.A2[d] * km * vm;
+      }
+    } else if (has_nb) {
       // eps |F| (sigma J - {dn u}),  -eps |F| J / 2
       const T J = vm - vp;
       val = fma(tabs.A1[d], J, -a2 * (dm + dp));
@@ -185,6 +206,23 @@ __global__ void __launch_bounds__(256) dg_const_kernel(const DgArgsT<T> args, co
       const T v0 = fv0[jk], v1 = fv1[jk], g0 = fv0[N2 + jk], g1 = fv1[N2 + jk];
       const T vs = v1 + v0, vd = v1 - v0, gs = g1 + g0, gd = g1 - g0;
       T* rc = sr + c * N3 + base;
+      if (KC) {
+        const T kc = sK[c];
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          T acc = d == 0 ? T(0) : rc[i * stride];
+          T t = T(0);
+#pragma unroll
+          for (int jj = 0; jj < N; ++jj)
+            if (i != 0 && jj != 0 && !((i + jj) & 1)) t = fma(tabs.M[d][i * N + jj], x[jj], t);
+          acc = fma(kc, t, acc);
+          if (d == 0 && tabs.massK != T(0)) acc = fma(tabs.massK, x[i], acc);
+          acc = fma(tabs.tr[N + i], (i & 1) ? vd : vs, acc);
+          if (i > 0) acc = fma(tabs.dtr[N + i], (i & 1) ? gd : gs, acc);
+          rc[i * stride] = acc;
+        }
+        continue;
+      }
 #pragma unroll
       for (int i = 0; i < N; ++i) {
         T acc = d == 0 ? T(0) : rc[i * stride];

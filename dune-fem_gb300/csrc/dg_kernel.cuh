@@ -55,6 +55,7 @@ struct DgArgsT {
   const T* kappa;     // DG coefficients of kappa (the source of kq, kf)
   const T* kq;        // KAPPA: kappa at the volume Gauss points [cell][a][b][c]
   const T* kf;        // KAPPA: kappa at the face Gauss points [cell][face 2d+s][a][b] (own side)
+  const T* kcell;     // closed form with a constant kappa per cell: [cell]
   int nc[3];          // cells per direction
   int periodic[3];
   long long ncells;

@@ -76,7 +76,9 @@ int dg_const_launch_one(const DgArgsT<T>& args, const DgConstTablesT<T>& tabs, T
                                                                  ucopy);
   }
   if (phase & 2) {
-    if (args.advect)
+    if (args.kcell)
+      dg_const_kernel<T, N, CPB, false, true><<<unsigned(blocks), 256, 0, stream>>>(args, traces, tabs);
+    else if (args.advect)
       dg_const_kernel<T, N, CPB, true><<<unsigned(blocks), 256, 0, stream>>>(args, traces, tabs);
     else
       dg_const_kernel<T, N, CPB, false><<<unsigned(blocks), 256, 0, stream>>>(args, traces, tabs);

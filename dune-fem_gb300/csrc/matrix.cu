@@ -122,6 +122,7 @@ extern "C" int gbfem_operator_assemble(gbfem_operator op, gbfem_operator* out) {
   a->kq_cache = a->kf_cache = nullptr;
   a->owns_kcache = false;
   a->jit_lib = a->jit_kernel = nullptr;
+  a->owns_kfield = false;
   a->bsr_blocks = nullptr;
   a->bsr_col = nullptr;
   a->trace_buf = nullptr;

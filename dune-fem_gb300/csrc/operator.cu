@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "blas.cuh"
 #include "dg_kernel.cuh"
 #include "gbfem_internal.cuh"
 #include "operator_impl.hpp"
@@ -24,7 +25,34 @@ int dg_const_launch_f32(const DgArgsT<float>&, const DgConstTablesT<float>&, int
 int dg_kappa_points_f64(const double*, double*, double*, long long, const DgTablesT<double>&, int, int, cudaStream_t);
 int dg_kappa_points_f32(const float*, float*, float*, long long, const DgTablesT<float>&, int, int, cudaStream_t);
 
+template <typename T>
+__global__ void k_kappa_field(long long ncells, int nloc, const T* __restrict__ kcell, T* __restrict__ field) {
+  const long long n = ncells * nloc;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const long long c = e / nloc;
+    field[e] = e - c * nloc == 0 ? kcell[c] : T(0);
+  }
+}
+
 int dg_kappa_cache(gbfem_operator_s* op) {
+  if (op->dg.kappa_cell) {
+    // the cellwise kappa as a DG field: mean = kappa_c, higher coefficients 0
+    const size_t es = op->precision == GBFEM_F64 ? 8 : 4;
+    if (!op->kappa_field) {
+      GBFEM_CUDA_TRY(cudaMalloc(&op->kappa_field, size_t(op->ndofs) * es));
+      op->owns_kfield = true;
+    }
+    if (op->precision == GBFEM_F64)
+      k_kappa_field<double><<<stream_grid(op->ndofs), 256>>>(op->ncells, op->nloc,
+                                                             static_cast<const double*>(op->dg.kappa_cell),
+                                                             static_cast<double*>(op->kappa_field));
+    else
+      k_kappa_field<float><<<stream_grid(op->ndofs), 256>>>(op->ncells, op->nloc,
+                                                            static_cast<const float*>(op->dg.kappa_cell),
+                                                            static_cast<float*>(op->kappa_field));
+    GBFEM_CUDA_TRY(cudaGetLastError());
+    op->dg.kappa = op->kappa_field;
+  }
   if (!op->dg.kappa) return GBFEM_OK;
   const size_t es = op->precision == GBFEM_F64 ? 8 : 4;
   const size_t q2 = size_t(op->q) * op->q;
@@ -113,6 +141,7 @@ static void fill_dg_args(const gbfem_operator_s* op, DgArgsT<T>* a) {
   a->kappa = static_cast<const T*>(d.kappa);
   a->kq = static_cast<const T*>(op->kq_cache);
   a->kf = static_cast<const T*>(op->kf_cache);
+  a->kcell = static_cast<const T*>(d.kappa_cell);
 }
 
 // M_d = eps |K|/h_d^2 K1 - b_d |K|/h_d D1 (+ c |K| I on axis 0), rounded once.
@@ -125,14 +154,16 @@ static void fill_line_operators(const gbfem_operator_s* op, DgConstTablesT<T>* c
     vol *= h[k];
   }
   const int n = op->n;
+  const bool kc = d.kappa_cell != nullptr;  // M: the diffusion part only, scaled per cell in the kernel
   for (int ax = 0; ax < 3; ++ax)
     for (int i = 0; i < n; ++i)
       for (int j = 0; j < n; ++j) {
         double m = d.diffusion * vol / (h[ax] * h[ax]) * op->cK1[i * n + j] -
                    d.velocity[ax] * vol / h[ax] * op->cD1[i * n + j];
-        if (ax == 0 && i == j) m += d.mass * vol;
+        if (!kc && ax == 0 && i == j) m += d.mass * vol;
         ct->M[ax][i * n + j] = T(m);
       }
+  ct->massK = T(kc ? d.mass * vol : 0.0);
   for (int ax = 0; ax < 3; ++ax) {
     const double area = vol / h[ax];
     ct->A1[ax] = T(area * d.diffusion * d.penalty / h[ax]);  // sigma = beta / h_F, h_F = |K| / |F| = h
@@ -492,6 +523,10 @@ int gbfem_dg_operator_create(const gbfem_dg_desc* desc, gbfem_operator* out) {
     return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "quad_points must be p+1 or p+2 (or 0 for p+2)");
   if (desc->precision != GBFEM_F64 && desc->precision != GBFEM_F32)
     return set_error(GBFEM_ERR_INVALID, "precision must be GBFEM_F64 or GBFEM_F32");
+  if (desc->kappa_cell && desc->kappa)
+    return set_error(GBFEM_ERR_INVALID, "give either kappa or kappa_cell, not both");
+  if (desc->kappa_cell && (desc->velocity[0] != 0.0 || desc->velocity[1] != 0.0 || desc->velocity[2] != 0.0))
+    return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "kappa_cell with advection");
   auto* op = new (std::nothrow) gbfem_operator_s();
   if (!op) return set_error(GBFEM_ERR_INVALID, "out of host memory");
   op->kind = OpKind::DG;
@@ -570,6 +605,7 @@ int gbfem_operator_destroy(gbfem_operator op) {
     if (op->kf_cache) cudaFree(op->kf_cache);
   }
   if (op->jit_lib) cudaLibraryUnload(static_cast<cudaLibrary_t>(op->jit_lib));
+  if (op->owns_kfield && op->kappa_field) cudaFree(op->kappa_field);
   if (op->host_u) cudaFree(op->host_u);
   if (op->host_w) cudaFree(op->host_w);
   if (op->bsr_blocks) cudaFree(op->bsr_blocks);

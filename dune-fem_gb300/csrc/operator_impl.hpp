@@ -67,6 +67,8 @@ struct gbfem_operator_s {
   void* kq_cache = nullptr;    // variable kappa at the volume Gauss points [cell][q^3]
   void* kf_cache = nullptr;    // variable kappa at the face Gauss points [cell][6][q^2]
   bool owns_kcache = false;    // false in copies (Jacobian) that share the operator's caches
+  void* kappa_field = nullptr; // cellwise kappa as a DG field (the mean only), for the Gauss-point paths
+  bool owns_kfield = false;
   void* jit_lib = nullptr;     // run-time compiled reaction (cudaLibrary_t), owned by the operator
   void* jit_kernel = nullptr;  // its kernel (cudaKernel_t): modes 0 and 1 of the reaction
   gbfem::HostPipe* pipe = nullptr;  // its streams and events

@@ -63,6 +63,12 @@ __global__ void k_permute(long long ncells, int nloc, int to_hier, const T* __re
   }
 }
 
+template <typename T>
+__global__ void k_cell_means(long long ncells, int nloc, const T* __restrict__ in, T* __restrict__ out) {
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncells; c += (long long)gridDim.x * blockDim.x)
+    out[c] = in[c * nloc];
+}
+
 }  // namespace gbfem
 
 using namespace gbfem;
@@ -93,6 +99,22 @@ int gbfem_dg_permute(int precision, int64_t ncells, int order, int to_hierarchic
                                                     static_cast<float*>(out), perm);
   else
     return set_error(GBFEM_ERR_INVALID, "gbfem_dg_permute: precision");
+  GBFEM_CUDA_TRY(cudaGetLastError());
+  return GBFEM_OK;
+}
+
+int gbfem_dg_cell_means(int precision, int64_t ncells, int order, const void* in, void* out, void* stream) {
+  if (!in || !out || order < 0 || order > 4 || ncells < 0)
+    return set_error(GBFEM_ERR_INVALID, "gbfem_dg_cell_means: invalid argument");
+  const int nloc = (order + 1) * (order + 1) * (order + 1);
+  if (ncells == 0) return GBFEM_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (precision == GBFEM_F64)
+    k_cell_means<double><<<stream_grid(ncells), 256, 0, s>>>(ncells, nloc, static_cast<const double*>(in),
+                                                            static_cast<double*>(out));
+  else
+    k_cell_means<float><<<stream_grid(ncells), 256, 0, s>>>(ncells, nloc, static_cast<const float*>(in),
+                                                           static_cast<float*>(out));
   GBFEM_CUDA_TRY(cudaGetLastError());
   return GBFEM_OK;
 }

@@ -176,6 +176,7 @@ int gbfem_operator_jacobian_create(gbfem_operator op, gbfem_operator* jac) {
   j->nonlinear = 0;
   j->owns_kcache = false;  // shares the operator's kappa point caches
   j->jit_lib = j->jit_kernel = nullptr;  // the Jacobian applies the stored linearisation only
+  j->owns_kfield = false;
   if (op->nonlinear) {
     const size_t bytes = size_t(op->ncells) * op->q * op->q * op->q * (op->precision == GBFEM_F64 ? 8 : 4);
     const cudaError_t e = cudaMalloc(&j->jac_points, bytes);

@@ -36,7 +36,7 @@ class DgDesc(C.Structure):
     _fields_ = [("grid", GridDesc), ("order", C.c_int), ("quad_points", C.c_int), ("precision", C.c_int),
                 ("diffusion", C.c_double), ("penalty", C.c_double), ("mass", C.c_double),
                 ("velocity", C.c_double * 3), ("weak_dirichlet", C.c_int), ("kappa", C.c_void_p),
-                ("algorithm", C.c_int)]
+                ("algorithm", C.c_int), ("kappa_cell", C.c_void_p)]
 
 
 class SolverParams(C.Structure):
@@ -162,6 +162,7 @@ def lib():
         L.gbfem_newton_params_default.argtypes = [C.POINTER(NewtonParams)]
         L.gbfem_legendre_hierarchical_permutation.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int)]
         L.gbfem_dg_permute.argtypes = [C.c_int, C.c_int64, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.gbfem_dg_cell_means.argtypes = [C.c_int, C.c_int64, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.gbfem_newton_solve.argtypes = [C.c_void_p, C.POINTER(NewtonParams), C.c_void_p, C.c_void_p,
                                          C.POINTER(NewtonInfo)]
         _lib = L
@@ -305,8 +306,10 @@ class DGOperator(Operator):
 
     def __init__(self, cells, order, quad_points=0, precision=F64, diffusion=1.0, penalty=None, mass=0.0,
                  velocity=(0.0, 0.0, 0.0), weak_dirichlet=True, periodic=(0, 0, 0), lower=(0.0, 0.0, 0.0),
-                 upper=(1.0, 1.0, 1.0), kappa=None, algorithm=0):
+                 upper=(1.0, 1.0, 1.0), kappa=None, algorithm=0, kappa_cell=None):
         d = DgDesc()
+        self.kappa_cell = kappa_cell
+        d.kappa_cell = kappa_cell.ptr if kappa_cell is not None else None
         d.grid = grid_desc(cells, lower, upper, periodic)
         d.order = order
         d.quad_points = quad_points
@@ -609,6 +612,14 @@ def hierarchical_permutation(order, dim=3):
     perm = (C.c_int * ((order + 1) ** dim))()
     check(lib().gbfem_legendre_hierarchical_permutation(order, dim, perm))
     return np.array(perm[:], dtype=np.int64)
+
+
+def cell_means(u, order):
+    """The cell means of a DG field (one value per cell, a new DeviceArray)."""
+    nc = u.n // (order + 1) ** 3
+    out = DeviceArray(nc, u.precision)
+    check(lib().gbfem_dg_cell_means(u.precision, nc, order, u.ptr, out.ptr, None))
+    return out
 
 
 def to_hierarchical(u, order):

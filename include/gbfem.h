@@ -81,6 +81,9 @@ typedef struct {
   int weak_dirichlet;   /* 1 = Nitsche weak u=0 on non-periodic boundary faces, 0 = do-nothing */
   const void* kappa;    /* device DG coefficients of kappa (same layout/precision) or NULL = 1 */
   int algorithm;        /* GBFEM_ALGO_AUTO or GBFEM_ALGO_QUADRATURE (see below) */
+  const void* kappa_cell; /* device array of one kappa per cell (same precision), or NULL; excludes
+                             kappa and velocity.  A cellwise-constant coefficient: the closed form
+                             applies it exactly (as a DG kappa field with only the mean) */
 } gbfem_dg_desc;
 
 /* GBFEM_ALGO_AUTO: with kappa == NULL the apply uses the closed form of the
@@ -373,6 +376,9 @@ int gbfem_dg_project(const gbfem_grid_desc* grid, int order, int quad_points, in
  * dglegendre(hierarchical=True)).  perm[h] = the non-hierarchical index of
  * the h-th hierarchical shape function ((order+1)^dim entries). */
 int gbfem_legendre_hierarchical_permutation(int order, int dim, int* perm);
+/* The cell means of a DG field (the coefficient of the constant basis
+ * function, the basis being orthonormal): out[c] = in[c (order+1)^3]. */
+int gbfem_dg_cell_means(int precision, int64_t ncells, int order, const void* in, void* out, void* stream);
 /* Whole 3-D DG dof vectors between the orderings (device arrays, in != out):
  * to_hierarchical = 1: out[c][h] = in[c][perm[h]]; 0: the inverse. */
 int gbfem_dg_permute(int precision, int64_t ncells, int order, int to_hierarchical, const void* in, void* out,

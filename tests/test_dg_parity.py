@@ -272,3 +272,38 @@ def test_host_apply_on_page_locked_buffers_is_bitwise_the_device_apply(gb, orc, 
         wh.fill_(float("nan"))
         op.apply_host(uh.numpy(), wh.numpy())
         assert np.array_equal(wh.numpy().view(np.uint64), ref.view(np.uint64)), in_place
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_cellwise_kappa_closed_form(gb, orc, order, precision):
+    """A constant kappa per cell: the closed form (per-cell diffusion scaling,
+    two-sided flux weights) equals the Gauss-point oracle on the DG field with
+    only the means, and the Gauss-point kernel on the same operator."""
+    cells = (3, 2, 4)
+    kw = dict(mass=0.6, periodic=(0, 1, 0), lower=(0.0, -1.0, 0.5), upper=(1.0, 0.5, 1.5))
+    rng = np.random.default_rng(90 + order)
+    ncell = int(np.prod(cells))
+    nloc = (order + 1) ** 3
+    kc = rng.uniform(0.2, 3.0, ncell)
+    field = np.zeros(ncell * nloc)
+    field[::nloc] = kc
+    dt = np.float64 if precision == 0 else np.float32
+    dkc = gb.DeviceArray.from_numpy(kc.astype(dt), precision)
+    op = gb.DGOperator(cells, order, precision=precision, kappa_cell=dkc, **kw)
+    opq = gb.DGOperator(cells, order, precision=precision, kappa_cell=dkc, algorithm=gb.ALGO_QUADRATURE, **kw)
+    prob = orc.DGProblem(cells, order, **kw)
+    u = rng.uniform(-1, 1, prob.ndofs)
+    du = gb.DeviceArray.from_numpy(u.astype(dt), precision)
+    w, wq = gb.DeviceArray(prob.ndofs, precision), gb.DeviceArray(prob.ndofs, precision)
+    op(du, w)
+    opq(du, wq)
+    ref = prob.apply(u.astype(dt).astype(np.float64), kappa=field.astype(dt).astype(np.float64))
+    tol = TOL64 if precision == 0 else TOL32
+    assert relmax(w.numpy(), ref) < tol
+    assert relmax(wq.numpy(), ref) < tol
+    if precision == 0:
+        nl = prob.nloc
+        assert relmax(op.block_diagonal(nl).numpy().reshape(-1, nl, nl), prob.block_diagonal(kappa=field)) < TOL64
+        means = gb.cell_means(gb.DeviceArray.from_numpy(field), order).numpy()
+        assert np.array_equal(means, kc)
