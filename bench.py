@@ -497,67 +497,80 @@ def workload_mixed(args):
            "unit": "s", "higher_is_better": False, "dtype": "f64 outer / f32 inner",
            "config": {"workload": "SIPG Q4 %d^3, -div(kappa grad u) = 1, u = 0 weak, log kappa ~ 256 Fourier modes "
                                   "(std 1, corr 0.1), seed %d" % (N, args.seed), "dofs": op64.size}}
-    (pc32, t_setup32) = _timed(lambda: gbfem.Preconditioner.block_jacobi(op64, gbfem.F32))
+    variants = set(args.mixed_variants.split(","))
+    pc32, t_setup32 = None, 0.0
+    if variants & {"refinement", "fgmres"}:
+        (pc32, t_setup32) = _timed(lambda: gbfem.Preconditioner.block_jacobi(op64, gbfem.F32))
     u = gbfem.DeviceArray(op64.size)
     u.clear()
     t_mixed = float("inf")
     info = None
     x_mixed = None
-    if not args.skip_refinement:
+    best = {}  # variant -> time of the solves that converged or reached the FP64 rounding floor
+
+    def consider(name, inf, t):
+        nonlocal x_mixed
+        if inf.converged or inf.stagnated:
+            best[name] = t
+            if min(best.values()) == t:
+                x_mixed = u.numpy()
+    if not args.skip_refinement and "refinement" in variants:
         info, t_mixed = _timed(lambda: gbfem.solve_mixed(op64, op32, pc32, f, u, tolerance=1e-10,
                                                          inner_tolerance=args.inner_tol, max_outer=60))
         out.update({"value": t_mixed, "mixed_setup_s": t_setup32, "mixed_converged": bool(info.converged),
                     "mixed_rel_residual": info.residual, "mixed_inner_iterations": info.iterations,
                     "mixed_operator_applies": info.operator_applies,
                     "mixed_outer_iterations": info.outer_iterations, "mixed_stagnated": bool(info.stagnated)})
-        x_mixed = u.numpy()
+        consider("refinement", info, t_mixed)
     # flexible FP64 outer Krylov (FGMRES) with the FP32 inner solve as its
     # preconditioner: converges where plain refinement stalls on cond(A) eps32
-    u.clear()
-    infog, t_fg = _timed(lambda: gbfem.solve_mixed(op64, op32, pc32, f, u, tolerance=1e-10,
-                                                   inner_tolerance=args.fgmres_inner_tol, max_outer=300,
-                                                   outer="fgmres", outer_restart=30))
-    out.update({"mixed_fgmres_s": t_fg, "mixed_fgmres_converged": bool(infog.converged),
-                "mixed_fgmres_rel_residual": infog.residual, "mixed_fgmres_inner_iterations": infog.iterations,
-                "mixed_fgmres_outer_iterations": infog.outer_iterations,
-                "mixed_fgmres_stagnated": bool(infog.stagnated)})
-    # a stagnated solve stopped at the FP64 rounding floor of the true residual
-    # (the FP64 CG's own true residual, below, sits at the same floor)
-    done_g = infog.converged or infog.stagnated
-    done_r = info is not None and (info.converged or info.stagnated)
-    if done_g and (not done_r or t_fg < t_mixed):
-        x_mixed = u.numpy()
-        out["value"] = t_fg
-        out["value_from"] = "mixed_fgmres"
+    if "fgmres" in variants:
+        u.clear()
+        infog, t_fg = _timed(lambda: gbfem.solve_mixed(op64, op32, pc32, f, u, tolerance=1e-10,
+                                                       inner_tolerance=args.fgmres_inner_tol, max_outer=300,
+                                                       outer="fgmres", outer_restart=30))
+        out.update({"mixed_fgmres_s": t_fg, "mixed_fgmres_converged": bool(infog.converged),
+                    "mixed_fgmres_rel_residual": infog.residual, "mixed_fgmres_inner_iterations": infog.iterations,
+                    "mixed_fgmres_outer_iterations": infog.outer_iterations,
+                    "mixed_fgmres_stagnated": bool(infog.stagnated)})
+        consider("fgmres", infog, t_fg)
     del pc32
     # the flexible outer solve with scaled FP16 block-Jacobi storage (half the
     # preconditioner traffic of the FP32 inner iteration)
-    (pc16, t_setup16) = _timed(lambda: gbfem.Preconditioner.block_jacobi(op64, gbfem.F16))
-    u.clear()
-    info16, t_mixed16 = _timed(lambda: gbfem.solve_mixed(op64, op32, pc16, f, u, tolerance=1e-10,
-                                                         inner_tolerance=args.fgmres_inner_tol, max_outer=300,
-                                                         outer="fgmres", outer_restart=30))
-    out.update({"mixed_f16_blocks_fgmres_s": t_mixed16, "mixed_f16_setup_s": t_setup16,
-                "mixed_f16_outer_iterations": info16.outer_iterations,
-                "mixed_f16_converged": bool(info16.converged), "mixed_f16_rel_residual": info16.residual,
-                "mixed_f16_inner_iterations": info16.iterations, "mixed_f16_stagnated": bool(info16.stagnated)})
-    del pc16
+    if "f16" in variants:
+        (pc16, t_setup16) = _timed(lambda: gbfem.Preconditioner.block_jacobi(op64, gbfem.F16))
+        u.clear()
+        info16, t_mixed16 = _timed(lambda: gbfem.solve_mixed(op64, op32, pc16, f, u, tolerance=1e-10,
+                                                             inner_tolerance=args.fgmres_inner_tol, max_outer=300,
+                                                             outer="fgmres", outer_restart=30))
+        out.update({"mixed_f16_blocks_fgmres_s": t_mixed16, "mixed_f16_setup_s": t_setup16,
+                    "mixed_f16_outer_iterations": info16.outer_iterations,
+                    "mixed_f16_converged": bool(info16.converged), "mixed_f16_rel_residual": info16.residual,
+                    "mixed_f16_inner_iterations": info16.iterations, "mixed_f16_stagnated": bool(info16.stagnated)})
+        consider("fgmres_f16_blocks", info16, t_mixed16)
+        del pc16
     # the FP32 inner operator with kappa replaced by its cell means: the
     # closed-form kernel applies it exactly (cheaper than the Gauss-point
     # kernel); the FP64 FGMRES still iterates on the full kappa
-    kbar = gbfem.cell_means(k32, p)
-    op32c = gbfem.DGOperator(cells, p, precision=gbfem.F32, kappa_cell=kbar)
-    (pc16c, t_setup16c) = _timed(lambda: gbfem.Preconditioner.block_jacobi(op32c, gbfem.F16))
-    u.clear()
-    infoc, t_c = _timed(lambda: gbfem.solve_mixed(op64, op32c, pc16c, f, u, tolerance=1e-10,
-                                                  inner_tolerance=args.fgmres_inner_tol, max_outer=300,
-                                                  outer="fgmres", outer_restart=30))
-    out.update({"mixed_cellkappa_f16_fgmres_s": t_c, "mixed_cellkappa_setup_s": t_setup16c,
-                "mixed_cellkappa_converged": bool(infoc.converged), "mixed_cellkappa_rel_residual": infoc.residual,
-                "mixed_cellkappa_inner_iterations": infoc.iterations,
-                "mixed_cellkappa_outer_iterations": infoc.outer_iterations,
-                "mixed_cellkappa_stagnated": bool(infoc.stagnated)})
-    del pc16c, op32c
+    if "cellkappa" in variants:
+        kbar = gbfem.cell_means(k32, p)
+        op32c = gbfem.DGOperator(cells, p, precision=gbfem.F32, kappa_cell=kbar)
+        (pc16c, t_setup16c) = _timed(lambda: gbfem.Preconditioner.block_jacobi(op32c, gbfem.F16))
+        u.clear()
+        infoc, t_c = _timed(lambda: gbfem.solve_mixed(op64, op32c, pc16c, f, u, tolerance=1e-10,
+                                                      inner_tolerance=args.fgmres_inner_tol, max_outer=300,
+                                                      outer="fgmres", outer_restart=30))
+        out.update({"mixed_cellkappa_f16_fgmres_s": t_c, "mixed_cellkappa_setup_s": t_setup16c,
+                    "mixed_cellkappa_converged": bool(infoc.converged),
+                    "mixed_cellkappa_rel_residual": infoc.residual,
+                    "mixed_cellkappa_inner_iterations": infoc.iterations,
+                    "mixed_cellkappa_outer_iterations": infoc.outer_iterations,
+                    "mixed_cellkappa_stagnated": bool(infoc.stagnated)})
+        consider("fgmres_cellkappa_f16_blocks", infoc, t_c)
+        del pc16c, op32c
+    if best:
+        name = min(best, key=best.get)
+        out["value"], out["value_from"] = best[name], name
     if not args.skip_fp64:
         (pc64, t_setup64) = _timed(lambda: gbfem.Preconditioner.block_jacobi(op64))
         inv = gbfem.KrylovInverseOperator("cg", tolerance=1e-10, max_iterations=args.fp64_max_iter)
@@ -784,6 +797,7 @@ def main():
     ap.add_argument("--fp64-max-iter", type=int, default=20000)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-refinement", action="store_true")
+    ap.add_argument("--mixed-variants", default="refinement,fgmres,f16,cellkappa")
     ap.add_argument("--train-seeds", type=int, default=256)
     ap.add_argument("--eval-seeds", type=int, default=32)
     ap.add_argument("--train-steps", type=int, default=2)
