@@ -483,9 +483,10 @@ def workload_rk3(args):
 
 
 def workload_mixed(args):
-    """3-D SIPG -div(kappa grad u) = 1, 96^3 Q4 (or --cells), log-Gaussian kappa; mixed IR vs FP64 CG."""
+    """3-D SIPG -div(kappa grad u) = 1, 96^3 Q4 (or --cells, --mixed-order), log-Gaussian kappa; the
+    mixed-precision solves against FP64 block-Jacobi CG."""
     import gbfem
-    N, p = args.cells, 4
+    N, p = args.cells, args.mixed_order
     cells = (N, N, N)
     modes = gbfem.fourier_modes(args.seed, 256, 0.1, 1.0)
     k64 = gbfem.project(cells, p, gbfem.FN_EXP_FOURIER, modes=modes)
@@ -493,10 +494,10 @@ def workload_mixed(args):
     f = gbfem.project(cells, p, gbfem.FN_CONSTANT, params=(1.0,), scale_by_volume=True)
     op64 = gbfem.DGOperator(cells, p, kappa=k64)
     op32 = gbfem.DGOperator(cells, p, precision=gbfem.F32, kappa=k32)
-    out = {"metric": "SIPG Q4 variable-kappa solve time to 1e-10 (mixed FP32-in-FP64 vs FP64 CG)",
+    out = {"metric": "SIPG Q%d variable-kappa solve time to 1e-10 (mixed FP32-in-FP64 vs FP64 CG)" % p,
            "unit": "s", "higher_is_better": False, "dtype": "f64 outer / f32 inner",
-           "config": {"workload": "SIPG Q4 %d^3, -div(kappa grad u) = 1, u = 0 weak, log kappa ~ 256 Fourier modes "
-                                  "(std 1, corr 0.1), seed %d" % (N, args.seed), "dofs": op64.size}}
+           "config": {"workload": "SIPG Q%d %d^3, -div(kappa grad u) = 1, u = 0 weak, log kappa ~ 256 Fourier modes "
+                                  "(std 1, corr 0.1), seed %d" % (p, N, args.seed), "dofs": op64.size}}
     variants = set(args.mixed_variants.split(","))
     pc32, t_setup32 = None, 0.0
     if variants & {"refinement", "fgmres"}:
@@ -798,6 +799,7 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-refinement", action="store_true")
     ap.add_argument("--mixed-variants", default="refinement,fgmres,f16,cellkappa")
+    ap.add_argument("--mixed-order", type=int, default=4)
     ap.add_argument("--train-seeds", type=int, default=256)
     ap.add_argument("--eval-seeds", type=int, default=32)
     ap.add_argument("--train-steps", type=int, default=2)
