@@ -150,10 +150,14 @@ __global__ void k_block_invert(const TI* __restrict__ blocks, TO* __restrict__ i
       scales[b] = float(s_max[0]);
     }
     __syncthreads();
+    // rows of the transposed block padded to an even length ld (pad = 0), so
+    // the apply reads two rows per __half2 load
+    const int ld = nb + (nb & 1);
+    TO* dsth = inv + b * (long long)nb * ld;
     const double inv_scale = 1.0 / s_max[0];
-    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-      const int i = e / nb, j = e - i * nb;
-      dst[j * nb + i] = __float2half_rn(float(a[e] * inv_scale));
+    for (int e = threadIdx.x; e < nb * ld; e += blockDim.x) {
+      const int j = e / ld, i = e - j * ld;
+      dsth[e] = i < nb ? __float2half_rn(float(a[i * nb + j] * inv_scale)) : __float2half_rn(0.0f);
     }
   } else {
     for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
@@ -163,22 +167,33 @@ __global__ void k_block_invert(const TI* __restrict__ blocks, TO* __restrict__ i
   }
 }
 
-// FP16 blocks with per-block scale, FP32 vectors: z_K = s_K (Binv_K / s_K) r_K
+// FP16 blocks with per-block scale, FP32 vectors: z_K = s_K (Binv_K / s_K) r_K.
+// The transposed blocks have rows of even length ld = nb + (nb & 1); a thread
+// computes rows 2t and 2t+1 from __half2 loads (ld / 2 threads per cell), so a
+// warp load is 128 bytes as in the FP32 apply.
 __global__ void k_block_apply_h(const __half* __restrict__ binvT, const float* __restrict__ scales,
                                 const float* __restrict__ r, float* __restrict__ z, int nb, long long ncells, int cpb) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float* rs = reinterpret_cast<float*>(smraw);  // [cpb][nb]
+  const int ld = nb + (nb & 1), tpc = ld / 2;
   const long long c0 = (long long)blockIdx.x * cpb;
   const int ncell = int(ncells - c0 < cpb ? ncells - c0 : cpb);
   for (int e = threadIdx.x; e < ncell * nb; e += blockDim.x) rs[e] = r[c0 * nb + e];
   __syncthreads();
-  const int lc = threadIdx.x / nb, i = threadIdx.x - lc * nb;
+  const int lc = threadIdx.x / tpc, t = threadIdx.x - lc * tpc;
   if (lc >= ncell) return;
-  const __half* B = binvT + (c0 + lc) * (long long)nb * nb + i;
+  const __half2* B = reinterpret_cast<const __half2*>(binvT + (c0 + lc) * (long long)nb * ld) + t;
   const float* rc = rs + lc * nb;
-  float acc = 0.0f;
-  for (int j = 0; j < nb; ++j) acc = fmaf(__half2float(B[(long long)j * nb]), rc[j], acc);
-  z[(c0 + lc) * nb + i] = acc * scales[c0 + lc];
+  float a0 = 0.0f, a1 = 0.0f;
+  for (int j = 0; j < nb; ++j) {
+    const float2 bb = __half22float2(B[(long long)j * (ld / 2)]);
+    a0 = fmaf(bb.x, rc[j], a0);
+    a1 = fmaf(bb.y, rc[j], a1);
+  }
+  const float sc = scales[c0 + lc];
+  const int i = 2 * t;
+  z[(c0 + lc) * nb + i] = a0 * sc;
+  if (i + 1 < nb) z[(c0 + lc) * nb + i + 1] = a1 * sc;
 }
 
 // z_K = Binv_K r_K with Binv_K stored transposed (binvT[K][j][i]): one thread
@@ -298,9 +313,14 @@ int precond_apply(const gbfem_preconditioner_s* pc, const void* r, void* z, cuda
       const int threads = ((cpb * nb + 31) / 32) * 32;
       const size_t sm = size_t(cpb) * nb * (pc->precision == GBFEM_F64 ? 8 : 4);
       const unsigned blocks = unsigned((nc + cpb - 1) / cpb);
-      if (pc->storage == GBFEM_F16)
-        k_block_apply_h<<<blocks, threads, sm, s>>>((const __half*)pc->data, pc->scales, (const float*)r, (float*)z,
-                                                    nb, nc, cpb);
+      if (pc->storage == GBFEM_F16) {
+        const int tpc = (nb + (nb & 1)) / 2;  // threads per cell: two rows each
+        const int cpbh = tpc >= 128 ? 1 : 128 / tpc;
+        const int th = ((cpbh * tpc + 31) / 32) * 32;
+        const unsigned bh = unsigned((nc + cpbh - 1) / cpbh);
+        k_block_apply_h<<<bh, th, size_t(cpbh) * nb * 4, s>>>((const __half*)pc->data, pc->scales, (const float*)r,
+                                                            (float*)z, nb, nc, cpbh);
+      }
       else if (pc->precision == GBFEM_F64)
         k_block_apply<double><<<blocks, threads, sm, s>>>((const double*)pc->data, (const double*)r, (double*)z, nb,
                                                           nc, cpb);
@@ -963,7 +983,9 @@ int gbfem_preconditioner_block_jacobi_create(gbfem_operator op, int precision, g
   const int nb = op->nloc;
   const size_t isz = precision == GBFEM_F64 ? 8 : (precision == GBFEM_F32 ? 4 : 2);
   const size_t osz = op->precision == GBFEM_F64 ? 8 : 4;
-  cudaError_t e = cudaMalloc(&pc->data, size_t(op->ncells) * nb * nb * isz);
+  const int ldh = nb + (nb & 1);  // FP16: rows padded to an even length
+  const size_t block_elems = precision == GBFEM_F16 ? size_t(nb) * ldh : size_t(nb) * nb;
+  cudaError_t e = cudaMalloc(&pc->data, size_t(op->ncells) * block_elems * isz);
   if (e == cudaSuccess && precision == GBFEM_F16) e = cudaMalloc(&pc->scales, size_t(op->ncells) * sizeof(float));
   if (e != cudaSuccess) { gbfem_preconditioner_destroy(pc); return set_cuda_error(e, "block Jacobi storage"); }
   // blocks in batches of cells (bounded temporary: <= ~1 GB)
@@ -997,11 +1019,13 @@ int gbfem_preconditioner_block_jacobi_create(gbfem_operator op, int precision, g
     if (precision == GBFEM_F16 && op->precision == GBFEM_F64) {
       cudaFuncSetAttribute(k_block_invert<double, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
       k_block_invert<double, __half><<<unsigned(cnt), 256, sm>>>((const double*)tmp,
-                                                                ((__half*)pc->data) + c0 * nb * nb, nb, cnt, d_sing, sc);
+                                                                ((__half*)pc->data) + c0 * (long long)block_elems, nb,
+                                                                cnt, d_sing, sc);
     } else if (precision == GBFEM_F16) {
       cudaFuncSetAttribute(k_block_invert<float, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
       k_block_invert<float, __half><<<unsigned(cnt), 256, sm>>>((const float*)tmp,
-                                                               ((__half*)pc->data) + c0 * nb * nb, nb, cnt, d_sing, sc);
+                                                               ((__half*)pc->data) + c0 * (long long)block_elems, nb,
+                                                               cnt, d_sing, sc);
     } else if (op->precision == GBFEM_F64 && precision == GBFEM_F64) {
       cudaFuncSetAttribute(k_block_invert<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm));
       k_block_invert<double, double><<<unsigned(cnt), 256, sm>>>((const double*)tmp,
