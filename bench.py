@@ -569,7 +569,20 @@ def workload_mixed(args):
                     "mixed_cellkappa_outer_iterations": infoc.outer_iterations,
                     "mixed_cellkappa_stagnated": bool(infoc.stagnated)})
         consider("fgmres_cellkappa_f16_blocks", infoc, t_c)
-        del pc16c, op32c
+        del pc16c
+        # the same with the scaled shared-block Jacobi (27 kappa = 1 blocks)
+        pcs = gbfem.Preconditioner.scaled_block_jacobi(op32c)
+        u.clear()
+        infos, t_s = _timed(lambda: gbfem.solve_mixed(op64, op32c, pcs, f, u, tolerance=1e-10,
+                                                      inner_tolerance=args.fgmres_inner_tol, max_outer=300,
+                                                      outer="fgmres", outer_restart=30))
+        out.update({"mixed_cellkappa_scaledbj_fgmres_s": t_s, "mixed_cellkappa_scaledbj_converged": bool(infos.converged),
+                    "mixed_cellkappa_scaledbj_rel_residual": infos.residual,
+                    "mixed_cellkappa_scaledbj_inner_iterations": infos.iterations,
+                    "mixed_cellkappa_scaledbj_outer_iterations": infos.outer_iterations,
+                    "mixed_cellkappa_scaledbj_stagnated": bool(infos.stagnated)})
+        consider("fgmres_cellkappa_scaled_bj", infos, t_s)
+        del pcs, op32c
     if best:
         name = min(best, key=best.get)
         out["value"], out["value_from"] = best[name], name

@@ -218,6 +218,51 @@ __global__ void k_block_apply(const T* __restrict__ binvT, const T* __restrict__
   z[(c0 + lc) * nb + i] = acc;
 }
 
+// Scaled shared-block Jacobi of an operator with a constant kappa per cell
+// (no mass, no advection): z_c = Hinv_t(c) r_c / kappa_c.  Hinv_t is the
+// inverse diagonal block of the kappa = 1 operator for the cell's boundary
+// type t (at most 27 per grid), stored transposed like the block-Jacobi
+// blocks; one thread per row, cpb cells per CTA.
+__device__ __forceinline__ int cell_type(long long c, const int* nc, const int* per) {
+  const long long nxy = (long long)nc[0] * nc[1];
+  const long long z = c / nxy, rem = c - z * nxy, y = rem / nc[0], x = rem - y * nc[0];
+  const long long xyz[3] = {x, y, z};
+  int t = 0, mul = 1;
+  for (int d = 0; d < 3; ++d) {
+    int td, md;
+    if (per[d]) { td = 0; md = 2; }
+    else if (nc[d] <= 2) { td = int(xyz[d]); md = nc[d]; }
+    else { td = xyz[d] == 0 ? 0 : (xyz[d] == nc[d] - 1 ? 2 : 1); md = 3; }
+    t += td * mul;
+    mul *= md;
+  }
+  return t;
+}
+
+struct GridShape {
+  int nc[3];
+  int per[3];
+};
+
+__global__ void k_scaled_block_apply(const float* __restrict__ hinvT, const float* __restrict__ kcell,
+                                     const float* __restrict__ r, float* __restrict__ z, int nb, long long ncells,
+                                     int cpb, GridShape g) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float* rs = reinterpret_cast<float*>(smraw);  // [cpb][nb]
+  const long long c0 = (long long)blockIdx.x * cpb;
+  const int ncell = int(ncells - c0 < cpb ? ncells - c0 : cpb);
+  for (int e = threadIdx.x; e < ncell * nb; e += blockDim.x) rs[e] = r[c0 * nb + e];
+  __syncthreads();
+  const int lc = threadIdx.x / nb, i = threadIdx.x - lc * nb;
+  if (lc >= ncell) return;
+  const long long c = c0 + lc;
+  const float* B = hinvT + (long long)cell_type(c, g.nc, g.per) * nb * nb + i;
+  const float* rc = rs + lc * nb;
+  float acc = 0.0f;
+  for (int j = 0; j < nb; ++j) acc = fmaf(__ldg(B + (long long)j * nb), rc[j], acc);
+  z[c * nb + i] = acc / kcell[c];
+}
+
 // ------------------------------------------------------------ vector ops --
 struct Ctx {
   int prec;
@@ -333,6 +378,21 @@ int precond_apply(const gbfem_preconditioner_s* pc, const void* r, void* z, cuda
       return pc->ext_apply(pc->ext_ctx, r, z, s);
     case PcKind::Sor:
       return sor_apply(pc, r, z, s);
+    case PcKind::ScaledBlock: {
+      const int nb = pc->nloc;
+      const long long nc = n / nb;
+      const int cpb = nb >= 128 ? 1 : 128 / nb;
+      const int threads = ((cpb * nb + 31) / 32) * 32;
+      GridShape g;
+      for (int d = 0; d < 3; ++d) {
+        g.nc[d] = pc->sor_op->dg.grid.cells[d];
+        g.per[d] = pc->sor_op->dg.grid.periodic[d];
+      }
+      k_scaled_block_apply<<<unsigned((nc + cpb - 1) / cpb), threads, size_t(cpb) * nb * 4, s>>>(
+          (const float*)pc->data, (const float*)pc->sor_op->dg.kappa_cell, (const float*)r, (float*)z, nb, nc, cpb,
+          g);
+      break;
+    }
   }
   GBFEM_CUDA_TRY(cudaGetLastError());
   return GBFEM_OK;
@@ -1055,6 +1115,48 @@ int gbfem_preconditioner_block_jacobi_create(gbfem_operator op, int precision, g
   cudaFree(d_sing);
   if (rc == GBFEM_OK && sing) rc = set_error(GBFEM_ERR_INVALID, "block Jacobi: a diagonal block is singular");
   if (rc) { gbfem_preconditioner_destroy(pc); return rc; }
+  *out = pc;
+  return GBFEM_OK;
+}
+
+int gbfem_preconditioner_scaled_block_jacobi_create(gbfem_operator op, gbfem_preconditioner* out) {
+  if (!op || !out) return set_error(GBFEM_ERR_INVALID, "gbfem_preconditioner_scaled_block_jacobi_create: null argument");
+  *out = nullptr;
+  const gbfem_dg_desc& d = op->dg;
+  if (op->kind != OpKind::DG || !d.kappa_cell || op->precision != GBFEM_F32 || d.mass != 0.0 || op->nonlinear)
+    return set_error(GBFEM_ERR_INVALID,
+                     "scaled block Jacobi: needs an FP32 DG operator with kappa_cell, no mass, not nonlinear");
+  // the kappa = 1 operator on a grid with one cell per boundary type, same cell size
+  gbfem_dg_desc t = d;
+  t.kappa = nullptr;
+  t.kappa_cell = nullptr;
+  t.precision = GBFEM_F64;
+  t.algorithm = GBFEM_ALGO_QUADRATURE;
+  for (int k = 0; k < 3; ++k) {
+    const double h = (d.grid.upper[k] - d.grid.lower[k]) / d.grid.cells[k];
+    const int m = d.grid.periodic[k] ? 2 : (d.grid.cells[k] <= 2 ? d.grid.cells[k] : 3);
+    t.grid.cells[k] = m;
+    t.grid.lower[k] = 0.0;
+    t.grid.upper[k] = m * h;
+  }
+  gbfem_operator top = nullptr;
+  GBFEM_TRY(gbfem_dg_operator_create(&t, &top));
+  struct OpFree { gbfem_operator o; ~OpFree() { gbfem_operator_destroy(o); } } top_free{top};
+  gbfem_preconditioner tbj = nullptr;
+  GBFEM_TRY(gbfem_preconditioner_block_jacobi_create(top, GBFEM_F32, &tbj));  // inverted, transposed, FP32
+  auto* pc = new (std::nothrow) gbfem_preconditioner_s();
+  if (!pc) {
+    gbfem_preconditioner_destroy(tbj);
+    return set_error(GBFEM_ERR_INVALID, "out of host memory");
+  }
+  pc->kind = PcKind::ScaledBlock;
+  pc->precision = GBFEM_F32;
+  pc->n = op->ndofs;
+  pc->nloc = op->nloc;
+  pc->sor_op = op;
+  pc->data = tbj->data;  // take over the inverted type blocks
+  tbj->data = nullptr;
+  gbfem_preconditioner_destroy(tbj);
   *out = pc;
   return GBFEM_OK;
 }

@@ -8,7 +8,7 @@
 
 namespace gbfem {
 
-enum class PcKind { Diagonal = 1, BlockJacobi = 2, External = 3, Sor = 4 };
+enum class PcKind { Diagonal = 1, BlockJacobi = 2, External = 3, Sor = 4, ScaledBlock = 5 };
 
 int precond_apply(const struct ::gbfem_preconditioner_s* pc, const void* r, void* z, cudaStream_t s);
 // Jacobi / Gauss-Seidel / SOR / SSOR sweeps over an assembled operator (sor.cu)
@@ -32,7 +32,7 @@ struct gbfem_preconditioner_s {
   // Flexible solvers switch to this preconditioner when the iteration with
   // this one stagnates (the learned preconditioner's block-Jacobi fallback).
   struct gbfem_preconditioner_s* fallback = nullptr;
-  // Sor: the assembled operator (not owned), method (GBFEM_SMOOTHER_*),
+  // Sor (and ScaledBlock: the cellwise-kappa operator): the operator (not owned), method (GBFEM_SMOOTHER_*),
   // sweeps, relaxation, cells grouped by level x+y+z with the level offsets,
   // and the previous iterate of Jacobi; data holds 1/diag
   const struct gbfem_operator_s* sor_op = nullptr;

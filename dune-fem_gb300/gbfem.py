@@ -148,6 +148,7 @@ def lib():
         L.gbfem_preconditioner_apply.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.gbfem_preconditioner_sor_create.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double,
                                                       C.POINTER(C.c_void_p)]
+        L.gbfem_preconditioner_scaled_block_jacobi_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
         L.gbfem_preconditioner_destroy.argtypes = [C.c_void_p]
         L.gbfem_solver_params_default.argtypes = [C.POINTER(SolverParams)]
         L.gbfem_solve.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(SolverParams), C.c_void_p, C.c_void_p,
@@ -466,6 +467,14 @@ class Preconditioner:
         h = C.c_void_p()
         check(lib().gbfem_preconditioner_block_jacobi_create(op.handle, precision, C.byref(h)))
         return cls(h, F32 if precision == F16 else precision, op)
+
+    @classmethod
+    def scaled_block_jacobi(cls, op):
+        """For an FP32 operator with kappa_cell (no mass): z_c = H_t^-1 r_c / kappa_c
+        with the shared kappa = 1 blocks H_t of the cell's boundary type."""
+        h = C.c_void_p()
+        check(lib().gbfem_preconditioner_scaled_block_jacobi_create(op.handle, C.byref(h)))
+        return cls(h, F32, op)
 
     SMOOTHERS = {"ssor": 2, "sor": 3, "gauss-seidel": 5, "jacobi": 6}
 

@@ -192,6 +192,13 @@ int gbfem_preconditioner_block_jacobi_create(gbfem_operator op, int precision, g
 #define GBFEM_SMOOTHER_JACOBI 6
 int gbfem_preconditioner_sor_create(gbfem_operator assembled, int method, int iterations, double relaxation,
                                     gbfem_preconditioner* pc);
+/* For an FP32 DG operator with kappa_cell (no mass): z_c = H_t^{-1} r_c /
+ * kappa_c, H_t the diagonal block of the kappa = 1 operator for the cell's
+ * boundary type t (at most 27 inverses kept, instead of one block per cell).
+ * It equals block Jacobi where kappa is constant across a cell's faces and
+ * approximates it (the penalty's face average) elsewhere.  No counterpart in
+ * the reference.  op must outlive pc. */
+int gbfem_preconditioner_scaled_block_jacobi_create(gbfem_operator op, gbfem_preconditioner* pc);
 int gbfem_preconditioner_apply(gbfem_preconditioner pc, const void* r, void* z, void* stream);
 int gbfem_preconditioner_precision(gbfem_preconditioner pc, int* precision);
 int gbfem_preconditioner_destroy(gbfem_preconditioner pc);

@@ -311,3 +311,31 @@ def test_mixed_stops_at_the_rounding_floor(gb, orc, outer):
                           inner_tolerance=1e-3, outer=outer)
     assert not info.converged and info.stagnated and info.outer_iterations < 60
     assert info.residual < 1e-13
+
+
+@pytest.mark.parametrize("cells,periodic", [((4, 3, 5), (0, 0, 0)), ((4, 2, 3), (1, 0, 0)), ((1, 4, 3), (0, 0, 1))])
+def test_scaled_block_jacobi_for_cellwise_kappa(gb, orc, cells, periodic):
+    """z_c = H_t^-1 r_c / kappa_c with H_t the kappa = 1 diagonal block of the
+    cell's boundary type: against the oracle's blocks of the kappa = 1
+    operator on the same grid; equal to block Jacobi when kappa is constant."""
+    order = 2
+    kw = dict(periodic=periodic)
+    ncell = int(np.prod(cells))
+    rng = np.random.default_rng(int(np.prod(cells)))
+    kc = rng.uniform(0.5, 2.0, ncell).astype(np.float32)
+    op = gb.DGOperator(cells, order, precision=gb.F32, kappa_cell=gb.DeviceArray.from_numpy(kc, gb.F32), **kw)
+    pc = gb.Preconditioner.scaled_block_jacobi(op)
+    prob = orc.DGProblem(cells, order, **kw)
+    r = rng.uniform(-1, 1, prob.ndofs).astype(np.float32)
+    z = gb.DeviceArray(prob.ndofs, gb.F32)
+    pc(gb.DeviceArray.from_numpy(r, gb.F32), z)
+    hinv = np.linalg.inv(prob.block_diagonal())  # kappa = 1
+    ref = np.einsum("cij,cj->ci", hinv, r.astype(np.float64).reshape(-1, prob.nloc)) / kc[:, None].astype(np.float64)
+    assert relmax(z.numpy(), ref.ravel()) < 2e-5
+    # constant kappa: the same as block Jacobi of the operator itself
+    const = gb.DGOperator(cells, order, precision=gb.F32,
+                          kappa_cell=gb.DeviceArray.from_numpy(np.full(ncell, 1.7, np.float32), gb.F32), **kw)
+    z1, z2 = gb.DeviceArray(prob.ndofs, gb.F32), gb.DeviceArray(prob.ndofs, gb.F32)
+    gb.Preconditioner.scaled_block_jacobi(const)(gb.DeviceArray.from_numpy(r, gb.F32), z1)
+    gb.Preconditioner.block_jacobi(const)(gb.DeviceArray.from_numpy(r, gb.F32), z2)
+    assert relmax(z1.numpy(), z2.numpy()) < 2e-5
