@@ -561,7 +561,8 @@ def workload_mixed(args):
         u.clear()
         infoc, t_c = _timed(lambda: gbfem.solve_mixed(op64, op32c, pc16c, f, u, tolerance=1e-10,
                                                       inner_tolerance=args.fgmres_inner_tol, max_outer=300,
-                                                      outer="fgmres", outer_restart=30))
+                                                      outer="fgmres", outer_restart=30,
+                                                      graph_chunk=args.inner_graph_chunk))
         out.update({"mixed_cellkappa_f16_fgmres_s": t_c, "mixed_cellkappa_setup_s": t_setup16c,
                     "mixed_cellkappa_converged": bool(infoc.converged),
                     "mixed_cellkappa_rel_residual": infoc.residual,
@@ -575,7 +576,8 @@ def workload_mixed(args):
         u.clear()
         infos, t_s = _timed(lambda: gbfem.solve_mixed(op64, op32c, pcs, f, u, tolerance=1e-10,
                                                       inner_tolerance=args.fgmres_inner_tol, max_outer=300,
-                                                      outer="fgmres", outer_restart=30))
+                                                      outer="fgmres", outer_restart=30,
+                                                      graph_chunk=args.inner_graph_chunk))
         out.update({"mixed_cellkappa_scaledbj_fgmres_s": t_s, "mixed_cellkappa_scaledbj_converged": bool(infos.converged),
                     "mixed_cellkappa_scaledbj_rel_residual": infos.residual,
                     "mixed_cellkappa_scaledbj_inner_iterations": infos.iterations,
@@ -814,6 +816,7 @@ def main():
     ap.add_argument("--skip-refinement", action="store_true")
     ap.add_argument("--mixed-variants", default="refinement,fgmres,f16,cellkappa")
     ap.add_argument("--mixed-order", type=int, default=4)
+    ap.add_argument("--inner-graph-chunk", type=int, default=0)
     ap.add_argument("--train-seeds", type=int, default=256)
     ap.add_argument("--eval-seeds", type=int, default=32)
     ap.add_argument("--train-steps", type=int, default=2)

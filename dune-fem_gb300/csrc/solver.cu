@@ -263,6 +263,76 @@ __global__ void k_scaled_block_apply(const float* __restrict__ hinvT, const floa
   z[c * nb + i] = acc / kcell[c];
 }
 
+// The same on tiles of 32 consecutive cells (nb <= 128): where the tile's
+// cells share one boundary type (most interior tiles), the CTA stages that
+// type's inverse in shared memory (rows padded to 128) and forms the 125 x 32
+// product with 4 x 4 register tiles per thread, so the matrix is read once per
+// 32 cells instead of once per cell; mixed tiles take one thread per row.
+constexpr int kSbTile = 32;
+__global__ void __launch_bounds__(256) k_scaled_block_apply_tiled(const float* __restrict__ hinvT,
+                                                                  const float* __restrict__ kcell,
+                                                                  const float* __restrict__ r, float* __restrict__ z,
+                                                                  int nb, long long ncells, GridShape g) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float* Hs = reinterpret_cast<float*>(smraw);  // [nb][128]  (transposed inverse: Hs[j][i])
+  float* Rs = Hs + nb * 128;                    // [nb][32]   (Rs[j][cell])
+  __shared__ int s_type[kSbTile];
+  __shared__ int s_uniform;
+  const long long c0 = (long long)blockIdx.x * kSbTile;
+  const int ncell = int(ncells - c0 < kSbTile ? ncells - c0 : kSbTile);
+  const int tid = threadIdx.x;
+  if (tid < kSbTile) s_type[tid] = tid < ncell ? cell_type(c0 + tid, g.nc, g.per) : -1;
+  __syncthreads();
+  if (tid == 0) {
+    int u = ncell == kSbTile ? 1 : 0;
+    for (int k = 1; k < ncell && u; ++k) u = s_type[k] == s_type[0];
+    s_uniform = u;
+  }
+  for (int e = tid; e < nb * kSbTile; e += blockDim.x) {
+    const int c = e / nb, j = e - c * nb;
+    Rs[j * kSbTile + c] = c < ncell ? r[(c0 + c) * nb + j] : 0.0f;
+  }
+  __syncthreads();
+  if (!s_uniform) {
+    // one thread per (cell, row)
+    for (int e = tid; e < ncell * nb; e += blockDim.x) {
+      const int c = e / nb, i = e - c * nb;
+      const float* B = hinvT + (long long)s_type[c] * nb * nb + i;
+      float acc = 0.0f;
+      for (int j = 0; j < nb; ++j) acc = fmaf(__ldg(B + (long long)j * nb), Rs[j * kSbTile + c], acc);
+      z[(c0 + c) * nb + i] = acc / kcell[c0 + c];
+    }
+    return;
+  }
+  const float* Hg = hinvT + (long long)s_type[0] * nb * nb;
+  for (int e = tid; e < nb * 128; e += blockDim.x) {
+    const int j = e >> 7, i = e & 127;
+    Hs[e] = i < nb ? __ldg(Hg + (long long)j * nb + i) : 0.0f;
+  }
+  __syncthreads();
+  const int rg = tid & 31, cg = tid >> 5;  // rows 4 rg .. 4 rg + 3, cells 4 cg .. 4 cg + 3
+  float acc[4][4] = {};
+  for (int j = 0; j < nb; ++j) {
+    const float4 a = *reinterpret_cast<const float4*>(Hs + j * 128 + 4 * rg);
+    const float4 b = *reinterpret_cast<const float4*>(Rs + j * kSbTile + 4 * cg);
+    const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+    for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) acc[ii][cc] = fmaf(av[ii], bv[cc], acc[ii][cc]);
+  }
+#pragma unroll
+  for (int cc = 0; cc < 4; ++cc) {
+    const long long c = c0 + 4 * cg + cc;
+    const float ik = 1.0f / kcell[c];
+#pragma unroll
+    for (int ii = 0; ii < 4; ++ii) {
+      const int i = 4 * rg + ii;
+      if (i < nb) z[c * nb + i] = acc[ii][cc] * ik;
+    }
+  }
+}
+
 // ------------------------------------------------------------ vector ops --
 struct Ctx {
   int prec;
@@ -388,9 +458,17 @@ int precond_apply(const gbfem_preconditioner_s* pc, const void* r, void* z, cuda
         g.nc[d] = pc->sor_op->dg.grid.cells[d];
         g.per[d] = pc->sor_op->dg.grid.periodic[d];
       }
-      k_scaled_block_apply<<<unsigned((nc + cpb - 1) / cpb), threads, size_t(cpb) * nb * 4, s>>>(
-          (const float*)pc->data, (const float*)pc->sor_op->dg.kappa_cell, (const float*)r, (float*)z, nb, nc, cpb,
-          g);
+      if (nb > 32 && nb <= 128) {
+        const size_t sm = size_t(nb) * (128 + kSbTile) * 4;
+        GBFEM_CUDA_TRY(cudaFuncSetAttribute(k_scaled_block_apply_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            int(sm)));
+        k_scaled_block_apply_tiled<<<unsigned((nc + kSbTile - 1) / kSbTile), 256, sm, s>>>(
+            (const float*)pc->data, (const float*)pc->sor_op->dg.kappa_cell, (const float*)r, (float*)z, nb, nc, g);
+      } else {
+        k_scaled_block_apply<<<unsigned((nc + cpb - 1) / cpb), threads, size_t(cpb) * nb * 4, s>>>(
+            (const float*)pc->data, (const float*)pc->sor_op->dg.kappa_cell, (const float*)r, (float*)z, nb, nc, cpb,
+            g);
+      }
       break;
     }
   }
