@@ -12,6 +12,7 @@
 // e.g. the learned one) follow Notay (2000) and Saad (1993).
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <chrono>
 #include <climits>
 #include <cmath>
@@ -263,54 +264,35 @@ __global__ void k_scaled_block_apply(const float* __restrict__ hinvT, const floa
   z[c * nb + i] = acc / kcell[c];
 }
 
-// The same on tiles of 32 consecutive cells (nb <= 128): where the tile's
-// cells share one boundary type (most interior tiles), the CTA stages that
-// type's inverse in shared memory (rows padded to 128) and forms the 125 x 32
-// product with 4 x 4 register tiles per thread, so the matrix is read once per
-// 32 cells instead of once per cell; mixed tiles take one thread per row.
+// The same on tiles of up to 32 cells of one boundary type (nb <= 128): the
+// cells sorted by type at creation, each type's list cut into tiles (interior
+// tiles are runs of consecutive cells).  A CTA stages its type's inverse in
+// shared memory (rows padded to 128), gathers the tile's residuals and forms
+// the nb x 32 product with 4 x 4 register tiles per thread, so the matrix is
+// read once per tile instead of once per cell.
 constexpr int kSbTile = 32;
 __global__ void __launch_bounds__(256) k_scaled_block_apply_tiled(const float* __restrict__ hinvT,
                                                                   const float* __restrict__ kcell,
+                                                                  const int* __restrict__ cells,
+                                                                  const int* __restrict__ tiles,
                                                                   const float* __restrict__ r, float* __restrict__ z,
-                                                                  int nb, long long ncells, GridShape g) {
+                                                                  int nb) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float* Hs = reinterpret_cast<float*>(smraw);  // [nb][128]  (transposed inverse: Hs[j][i])
   float* Rs = Hs + nb * 128;                    // [nb][32]   (Rs[j][cell])
-  __shared__ int s_type[kSbTile];
-  __shared__ int s_uniform;
-  const long long c0 = (long long)blockIdx.x * kSbTile;
-  const int ncell = int(ncells - c0 < kSbTile ? ncells - c0 : kSbTile);
+  const int type = tiles[3 * blockIdx.x], start = tiles[3 * blockIdx.x + 1], count = tiles[3 * blockIdx.x + 2];
   const int tid = threadIdx.x;
-  if (tid < kSbTile) s_type[tid] = tid < ncell ? cell_type(c0 + tid, g.nc, g.per) : -1;
-  __syncthreads();
-  if (tid == 0) {
-    int u = ncell == kSbTile ? 1 : 0;
-    for (int k = 1; k < ncell && u; ++k) u = s_type[k] == s_type[0];
-    s_uniform = u;
-  }
-  for (int e = tid; e < nb * kSbTile; e += blockDim.x) {
-    const int c = e / nb, j = e - c * nb;
-    Rs[j * kSbTile + c] = c < ncell ? r[(c0 + c) * nb + j] : 0.0f;
-  }
-  __syncthreads();
-  if (!s_uniform) {
-    // one thread per (cell, row)
-    for (int e = tid; e < ncell * nb; e += blockDim.x) {
-      const int c = e / nb, i = e - c * nb;
-      const float* B = hinvT + (long long)s_type[c] * nb * nb + i;
-      float acc = 0.0f;
-      for (int j = 0; j < nb; ++j) acc = fmaf(__ldg(B + (long long)j * nb), Rs[j * kSbTile + c], acc);
-      z[(c0 + c) * nb + i] = acc / kcell[c0 + c];
-    }
-    return;
-  }
-  const float* Hg = hinvT + (long long)s_type[0] * nb * nb;
+  const float* Hg = hinvT + (long long)type * nb * nb;
   for (int e = tid; e < nb * 128; e += blockDim.x) {
     const int j = e >> 7, i = e & 127;
     Hs[e] = i < nb ? __ldg(Hg + (long long)j * nb + i) : 0.0f;
   }
+  for (int e = tid; e < nb * kSbTile; e += blockDim.x) {
+    const int c = e / nb, j = e - c * nb;
+    Rs[j * kSbTile + c] = c < count ? r[(long long)cells[start + c] * nb + j] : 0.0f;
+  }
   __syncthreads();
-  const int rg = tid & 31, cg = tid >> 5;  // rows 4 rg .. 4 rg + 3, cells 4 cg .. 4 cg + 3
+  const int rg = tid & 31, cg = tid >> 5;  // rows 4 rg .. 4 rg + 3, tile cells 4 cg .. 4 cg + 3
   float acc[4][4] = {};
   for (int j = 0; j < nb; ++j) {
     const float4 a = *reinterpret_cast<const float4*>(Hs + j * 128 + 4 * rg);
@@ -323,7 +305,9 @@ __global__ void __launch_bounds__(256) k_scaled_block_apply_tiled(const float* _
   }
 #pragma unroll
   for (int cc = 0; cc < 4; ++cc) {
-    const long long c = c0 + 4 * cg + cc;
+    const int tc = 4 * cg + cc;
+    if (tc >= count) break;
+    const long long c = cells[start + tc];
     const float ik = 1.0f / kcell[c];
 #pragma unroll
     for (int ii = 0; ii < 4; ++ii) {
@@ -458,12 +442,13 @@ int precond_apply(const gbfem_preconditioner_s* pc, const void* r, void* z, cuda
         g.nc[d] = pc->sor_op->dg.grid.cells[d];
         g.per[d] = pc->sor_op->dg.grid.periodic[d];
       }
-      if (nb > 32 && nb <= 128) {
+      if (pc->sb_tiles) {
         const size_t sm = size_t(nb) * (128 + kSbTile) * 4;
         GBFEM_CUDA_TRY(cudaFuncSetAttribute(k_scaled_block_apply_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             int(sm)));
-        k_scaled_block_apply_tiled<<<unsigned((nc + kSbTile - 1) / kSbTile), 256, sm, s>>>(
-            (const float*)pc->data, (const float*)pc->sor_op->dg.kappa_cell, (const float*)r, (float*)z, nb, nc, g);
+        k_scaled_block_apply_tiled<<<unsigned(pc->sb_ntiles), 256, sm, s>>>(
+            (const float*)pc->data, (const float*)pc->sor_op->dg.kappa_cell, pc->sor_cells, pc->sb_tiles,
+            (const float*)r, (float*)z, nb);
       } else {
         k_scaled_block_apply<<<unsigned((nc + cpb - 1) / cpb), threads, size_t(cpb) * nb * 4, s>>>(
             (const float*)pc->data, (const float*)pc->sor_op->dg.kappa_cell, (const float*)r, (float*)z, nb, nc, cpb,
@@ -1235,6 +1220,46 @@ int gbfem_preconditioner_scaled_block_jacobi_create(gbfem_operator op, gbfem_pre
   pc->data = tbj->data;  // take over the inverted type blocks
   tbj->data = nullptr;
   gbfem_preconditioner_destroy(tbj);
+  if (op->nloc > 32 && op->nloc <= 128) {
+    // cells sorted by boundary type (stable: interior runs stay consecutive), tiles of <= 32
+    const int* nc = d.grid.cells;
+    std::vector<std::vector<int>> by_type(27);
+    for (long long c = 0; c < op->ncells; ++c) {
+      const long long nxy = (long long)nc[0] * nc[1];
+      const long long zz = c / nxy, rem = c - zz * nxy, yy = rem / nc[0], xx = rem - yy * nc[0];
+      const long long xyz[3] = {xx, yy, zz};
+      int t = 0, mul = 1;
+      for (int k = 0; k < 3; ++k) {
+        int td, md;
+        if (d.grid.periodic[k]) { td = 0; md = 2; }
+        else if (nc[k] <= 2) { td = int(xyz[k]); md = nc[k]; }
+        else { td = xyz[k] == 0 ? 0 : (xyz[k] == nc[k] - 1 ? 2 : 1); md = 3; }
+        t += td * mul;
+        mul *= md;
+      }
+      by_type[t].push_back(int(c));
+    }
+    std::vector<int> list, tiles;
+    list.reserve(size_t(op->ncells));
+    for (int t = 0; t < 27; ++t) {
+      for (size_t k = 0; k < by_type[t].size(); k += kSbTile) {
+        const int cnt = int(std::min<size_t>(kSbTile, by_type[t].size() - k));
+        tiles.push_back(t);
+        tiles.push_back(int(list.size()));
+        tiles.push_back(cnt);
+        list.insert(list.end(), by_type[t].begin() + k, by_type[t].begin() + k + cnt);
+      }
+    }
+    cudaError_t e = cudaMalloc(&pc->sor_cells, list.size() * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&pc->sb_tiles, tiles.size() * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpy(pc->sor_cells, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(pc->sb_tiles, tiles.data(), tiles.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      gbfem_preconditioner_destroy(pc);
+      return set_cuda_error(e, "scaled block Jacobi: tiles");
+    }
+    pc->sb_ntiles = (long long)(tiles.size() / 3);
+  }
   *out = pc;
   return GBFEM_OK;
 }
@@ -1255,6 +1280,7 @@ int gbfem_preconditioner_destroy(gbfem_preconditioner pc) {
   if (pc->data && pc->owns_data) cudaFree(pc->data);
   if (pc->scales) cudaFree(pc->scales);
   if (pc->sor_cells) cudaFree(pc->sor_cells);
+  if (pc->sb_tiles) cudaFree(pc->sb_tiles);
   if (pc->sor_tmp) cudaFree(pc->sor_tmp);
   if (pc->ext_destroy) pc->ext_destroy(pc->ext_ctx);
   delete pc;

@@ -41,4 +41,8 @@ struct gbfem_preconditioner_s {
   int* sor_cells = nullptr;
   void* sor_tmp = nullptr;
   std::vector<long long> sor_level_offsets;
+  // ScaledBlock: sor_cells holds the cells sorted by boundary type; tiles of
+  // (type, start, count) into it
+  int* sb_tiles = nullptr;
+  long long sb_ntiles = 0;
 };
