@@ -705,6 +705,12 @@ def workload_kernels(args):
     bj16 = gbfem.Preconditioner.block_jacobi(op32, gbfem.F16)
     out["bj16_apply"] = ev(lambda: bj16(u32, w32, sptr))
     del bj16
+    # the cellwise-kappa FP32 operator and its scaled shared-block Jacobi
+    opc = gbfem.DGOperator((N, N, N), p, precision=gbfem.F32, kappa_cell=gbfem.cell_means(k32, p))
+    out["apply_f32_cellkappa"] = ev(lambda: opc(u32, w32, sptr))
+    sbj = gbfem.Preconditioner.scaled_block_jacobi(opc)
+    out["scaled_bj_apply"] = ev(lambda: sbj(u32, w32, sptr))
+    del sbj, opc
     out["dot_f64_host_result"] = ev(lambda: gbfem.dot(u64, w64, sptr))
     out["axpy_f64"] = ev(lambda: gbfem.axpy(0.5, u64, w64, sptr))
     for name, op, pc, fv in (("cg_iter_f64_bj", op64, bj64, f), ("cg_iter_f32_bj", op32, bj32, gbfem.convert(f, gbfem.F32))):
