@@ -35,13 +35,17 @@ METRIC = "SIPG apply DoF/s"
 UNIT = "DoF/s"
 BYTES_PER_DOF = 16.0          # read u (8) + write w (8), geometry recomputed, tables on chip
 FLOP_PER_DOF = 402.0          # sum-factorised SIPG Q3, q=5 (volume + faces), the algorithmic count
-# flops the closed-form kernels execute per cell (n = 4, no advection; an FMA
-# counts 2), divided by n^3:
-#  traces: 3 n^2 lines x (7 FMA (L_0' = 0 skipped) + 4 adds) = 48 x 18
-#  fluxes: 6 n^2 face points x 6 (J, dm + dp, a2 x, FMA, grad)  = 96 x 6
-#  lines:  n^2 lines per axis x (4 adds + 2 x (nonzeros of M_d + 7 face FMAs));
-#          M_d has 5 structural nonzeros for n = 4 (6 on axis 0, the mass entry)
-KERNEL_FLOP_PER_DOF = (48 * 18 + 96 * 6 + 16 * (4 + 2 * (6 + 7)) + 32 * (4 + 2 * (5 + 7))) / 64.0  # = 44.0
+# flops the closed-form kernels execute per cell (n = 4, constant kappa, no
+# mass, no advection; an FMA counts 2), divided by n^3:
+#  traces: 3 n^2 lines x (even/odd partial sums of v and P: 4 FMA + 2 MUL,
+#          u_0 enters both even sums as is; 4 adds for the two faces) = 48 x 14
+#  fluxes: 6 n^2 face points x 2 (J = v- - v+, P- - P+)             = 96 x 2
+#  lines:  n^2 lines per axis x (4 adds + 2 x (5 structural nonzeros of M_d
+#          + 7 face-expansion FMAs))                                = 48 x 28
+KERNEL_FLOP_PER_DOF = (48 * 14 + 96 * 2 + 48 * (4 + 2 * (5 + 7))) / 64.0  # = 34.5
+# FP64 instructions per dof, which is what the FP64 pipe issues (an add takes
+# the slot of an FMA): (48 x 10 + 96 x 2 + 48 x 16) / 64
+KERNEL_FP64_INSTR_PER_DOF = (48 * 10 + 96 * 2 + 48 * 16) / 64.0  # = 22.5
 CONFIG = {"workload": "SIPG DG Q3 apply, 3-D unit cube 64^3 hexes, 16.8M dofs, q=5, penalty 160, FP64",
           "cells": list(CELLS), "order": ORDER, "quad_points": QUAD, "dofs": 64 ** 3 * 64,
           "l2": "inputs exceed L2 (u + w = 268 MB > 129 MB), no flush"}
@@ -293,6 +297,9 @@ def run_gpu(args, world, rank, local):
             "fp64_pipe": {"achieved_tflops": achieved_tflops, "peak_tflops_measured": fp64_peak,
                           "frac": achieved_tflops / fp64_peak if fp64_peak else None,
                           "kernel_flop_per_dof": KERNEL_FLOP_PER_DOF,
+                          "kernel_fp64_instructions_per_dof": KERNEL_FP64_INSTR_PER_DOF,
+                          "issue_frac": (KERNEL_FP64_INSTR_PER_DOF * n / (ms_step * 1e-3) / 1e12) / (fp64_peak / 2)
+                          if fp64_peak else None,
                           "sum_factorised_quadrature_flop_per_dof": FLOP_PER_DOF,
                           "fp32_peak_tflops_measured": fp32_peak},
             "algorithm": "constant-kappa closed form of the q=5 Gauss quadrature (exact for these integrands; "

@@ -72,8 +72,12 @@ int dg_const_launch_one(const DgArgsT<T>& args, const DgConstTablesT<T>& tabs, T
     const long long titems = count * 3 * N * N;
     long long tblocks = (titems + 255) / 256;
     if (tblocks > 152LL * 32) tblocks = 152LL * 32;
-    dg_trace_kernel<T, N><<<unsigned(tblocks), 256, 0, stream>>>(args.u, traces, args.cell_begin, count, tabs,
-                                                                 ucopy);
+    if (args.kcell)
+      dg_trace_kernel<T, N, true><<<unsigned(tblocks), 256, 0, stream>>>(args.u, traces, args.cell_begin, count,
+                                                                         tabs, ucopy);
+    else
+      dg_trace_kernel<T, N, false><<<unsigned(tblocks), 256, 0, stream>>>(args.u, traces, args.cell_begin, count,
+                                                                          tabs, ucopy);
   }
   if (phase & 2) {
     if (args.kcell)

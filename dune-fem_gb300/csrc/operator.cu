@@ -164,10 +164,31 @@ static void fill_line_operators(const gbfem_operator_s* op, DgConstTablesT<T>* c
         ct->M[ax][i * n + j] = T(m);
       }
   ct->massK = T(kc ? d.mass * vol : 0.0);
+  // Folded flux constants of the closed-form kernel: the second trace P and
+  // the expansion factors (kappa per cell: P is the outward normal derivative
+  // and the expansion uses L_i(1), L_i'(1) unscaled).  C = A1, or 1 where A1
+  // vanishes (no diffusion or no penalty); A1 / C is then the same on every
+  // axis.
+  const double aC = d.diffusion * d.penalty != 0.0 ? 1.0 : 0.0;
+  ct->am1 = T(aC - 1.0);
+  ct->am2 = T(aC - 2.0);
   for (int ax = 0; ax < 3; ++ax) {
     const double area = vol / h[ax];
-    ct->A1[ax] = T(area * d.diffusion * d.penalty / h[ax]);  // sigma = beta / h_F, h_F = |K| / |F| = h
-    ct->A2[ax] = T(area * d.diffusion * 0.5 / h[ax]);
+    const double A1 = area * d.diffusion * d.penalty / h[ax];  // sigma = beta / h_F, h_F = |K| / |F| = h
+    const double A2 = area * d.diffusion * 0.5 / h[ax];
+    ct->A1[ax] = T(A1);
+    ct->A2[ax] = T(A2);
+    const double C = aC != 0.0 ? A1 : 1.0, r = A2 / C;
+    for (int i = 0; i < n; ++i) {
+      const double L1 = op->ctab64.tr[n + i], dL1 = op->ctab64.dtr[n + i];
+      ct->pc[ax][i] = T(kc ? dL1 : L1 - r * dL1);
+      ct->etr[ax][i] = T(C * L1);
+      ct->edtr[ax][i] = T(-A2 * dL1);
+    }
+    for (int side = 0; side < 2; ++side) {
+      const double bn = side ? d.velocity[ax] : -d.velocity[ax];
+      ct->adv[2 * ax + side] = T(area * bn / C);
+    }
   }
 }
 

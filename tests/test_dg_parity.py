@@ -67,6 +67,26 @@ def test_periodic_advection_only(gb, orc, algorithm):
     assert relmax(w.numpy(), prob.apply(u)) < TOL64
 
 
+@pytest.mark.parametrize("algorithm", [0, 1])
+@pytest.mark.parametrize("case", ["no_penalty", "advection_boundaries", "tiny_diffusion"])
+def test_flux_constant_edge_cases(gb, orc, algorithm, case):
+    """The closed form folds A1 = |F| eps beta / h into its expansion tables and
+    keeps P = v - sigma (A2 / A1) dv as its second trace; with A1 = 0 (no
+    penalty, or no diffusion) it uses 1 in its place.  Each case against the
+    oracle: penalty 0 with diffusion, pure advection with inflow and outflow
+    boundary faces, and a diffusion small against the advection."""
+    cells = (3, 4, 2)
+    kw = {"no_penalty": dict(diffusion=0.8, penalty=0.0, mass=0.4),
+          "advection_boundaries": dict(diffusion=0.0, velocity=(1.0, -0.5, 0.25), periodic=(0, 0, 1)),
+          "tiny_diffusion": dict(diffusion=1e-6, velocity=(-0.3, 0.5, 1.0))}[case]
+    op = gb.DGOperator(cells, 3, algorithm=algorithm, **kw)
+    prob = orc.DGProblem(cells, 3, **kw)
+    u = np.random.default_rng(11).uniform(-1, 1, prob.ndofs)
+    w = gb.DeviceArray(prob.ndofs)
+    op(gb.DeviceArray.from_numpy(u), w)
+    assert relmax(w.numpy(), prob.apply(u)) < TOL64
+
+
 @pytest.mark.parametrize("order", [2, 3])
 @pytest.mark.parametrize("algorithm", [0, 1])
 def test_sipg_apply_fp32(gb, orc, order, algorithm):
