@@ -288,8 +288,8 @@ def run_gpu(args, world, rank, local):
             "gpu_launches": 2 * args.steps,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                     "steps": e2e_steps,
-                    "path": "gbfem_operator_apply_host (page-locked host buffers; copy in, apply and copy out "
-                            "pipelined over 16 z-slabs on three streams)",
+                    "path": "gbfem_operator_apply_host (page-locked host buffers; copy in, trace pass, apply and "
+                            "copy out pipelined over 16 z-slabs on four streams, replayed as one CUDA graph)",
                     "in_place_c2c_value": e2e_in_place},
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved_gbs / peaks["hbm_gbs"], "traffic": traffic,

@@ -71,7 +71,7 @@ int dg_kappa_cache(gbfem_operator_s* op) {
   return GBFEM_OK;
 }
 
-// Trace buffer of the closed-form kernel: [cell][6 faces][v|d][n^2], allocated
+// Trace buffer of the closed-form kernel: [cell][6 faces][v|P][n^2], allocated
 // on the first apply of an operator.
 static int trace_buffer(const gbfem_operator_s* op, void** buf) {
   auto* mop = const_cast<gbfem_operator_s*>(op);
@@ -354,19 +354,40 @@ namespace gbfem {
 
 // Streams and events of the pipelined host-buffer apply.
 struct HostPipe {
-  cudaStream_t in = nullptr, comp = nullptr, out = nullptr;
+  cudaStream_t in = nullptr, comp = nullptr, out = nullptr, tr = nullptr;
   cudaEvent_t start = nullptr;
-  std::vector<cudaEvent_t> ev_in, ev_comp;
+  std::vector<cudaEvent_t> ev_in, ev_comp, ev_tr;
+  // the copy pipeline captured as a graph, for one pair of page-locked buffers
+  cudaGraphExec_t gexec = nullptr;
+  const void* g_u = nullptr;
+  void* g_w = nullptr;
+  int g_chunks = 0;
+  cudaEvent_t join[3] = {nullptr, nullptr, nullptr};
 };
+
+static void drop_host_graph(HostPipe* p) {
+  if (p && p->gexec) {
+    cudaGraphExecDestroy(p->gexec);
+    p->gexec = nullptr;
+    p->g_u = nullptr;
+    p->g_w = nullptr;
+    p->g_chunks = 0;
+  }
+}
 
 void destroy_host_pipe(HostPipe* p) {
   if (!p) return;
+  drop_host_graph(p);
+  for (cudaEvent_t e : p->join)
+    if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : p->ev_in) cudaEventDestroy(e);
   for (cudaEvent_t e : p->ev_comp) cudaEventDestroy(e);
+  for (cudaEvent_t e : p->ev_tr) cudaEventDestroy(e);
   if (p->start) cudaEventDestroy(p->start);
   if (p->in) cudaStreamDestroy(p->in);
   if (p->comp) cudaStreamDestroy(p->comp);
   if (p->out) cudaStreamDestroy(p->out);
+  if (p->tr) cudaStreamDestroy(p->tr);
   delete p;
 }
 
@@ -378,7 +399,9 @@ static int host_pipe(gbfem_operator_s* op, int nchunks, HostPipe** out) {
     GBFEM_CUDA_TRY(cudaStreamCreateWithFlags(&p->in, cudaStreamNonBlocking));
     GBFEM_CUDA_TRY(cudaStreamCreateWithFlags(&p->comp, cudaStreamNonBlocking));
     GBFEM_CUDA_TRY(cudaStreamCreateWithFlags(&p->out, cudaStreamNonBlocking));
+    GBFEM_CUDA_TRY(cudaStreamCreateWithFlags(&p->tr, cudaStreamNonBlocking));
     GBFEM_CUDA_TRY(cudaEventCreateWithFlags(&p->start, cudaEventDisableTiming));
+    for (cudaEvent_t& e : p->join) GBFEM_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
   HostPipe* p = op->pipe;
   while (int(p->ev_in.size()) < nchunks) {
@@ -387,6 +410,9 @@ static int host_pipe(gbfem_operator_s* op, int nchunks, HostPipe** out) {
     p->ev_in.push_back(a);
     GBFEM_CUDA_TRY(cudaEventCreateWithFlags(&b, cudaEventDisableTiming));
     p->ev_comp.push_back(b);
+    cudaEvent_t c = nullptr;
+    GBFEM_CUDA_TRY(cudaEventCreateWithFlags(&c, cudaEventDisableTiming));
+    p->ev_tr.push_back(c);
   }
   *out = p;
   return GBFEM_OK;
@@ -465,15 +491,113 @@ static int dg_apply_host_mapped(gbfem_operator_s* op, const void* du, void* dw) 
   return GBFEM_OK;
 }
 
-int dg_apply_host_pipelined(gbfem_operator_s* op, const void* u_host, void* w_host) {
-  if (op->coefficient_space && op->host_in_place) {
-    void* du = mapped_device_pointer(u_host);
-    void* dw = du ? mapped_device_pointer(w_host) : nullptr;
-    if (du && dw) return dg_apply_host_mapped(op, du, dw);
-  }
+// Enqueues the copy pipeline after the work already queued on `origin`.
+static int enqueue_copy_pipeline(gbfem_operator_s* op, HostPipe* p, const void* u_host, void* w_host, int nchunks,
+                                 int zper, cudaStream_t origin) {
   const size_t es = op->precision == GBFEM_F64 ? 8 : 4;
   const int nz = op->dg.grid.cells[2];
   const long long plane = (long long)op->dg.grid.cells[0] * op->dg.grid.cells[1];
+  const size_t cell_bytes = size_t(op->nloc) * es;
+  auto first_cell = [&](int k) { return (long long)k * zper * plane; };
+  auto cell_count = [&](int k) {
+    const long long z1 = (long long)(k + 1) * zper < nz ? (long long)(k + 1) * zper : nz;
+    return (z1 - (long long)k * zper) * plane;
+  };
+  GBFEM_CUDA_TRY(cudaEventRecord(p->start, origin));
+  GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->in, p->start, 0));
+  GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->comp, p->start, 0));
+  GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->out, p->start, 0));
+  for (int k = 0; k < nchunks; ++k) {
+    const size_t off = size_t(first_cell(k)) * cell_bytes;
+    GBFEM_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(op->host_u) + off, static_cast<const char*>(u_host) + off,
+                                   size_t(cell_count(k)) * cell_bytes, cudaMemcpyHostToDevice, p->in));
+    GBFEM_CUDA_TRY(cudaEventRecord(p->ev_in[k], p->in));
+  }
+  // The closed form's trace pass of slab k runs on its own stream as soon as
+  // slab k has arrived, so it fills the SMs left idle by the tail of the apply
+  // of slab k-1 (a slab is only a wave or two of CTAs).  The apply of slab j
+  // reads the traces (or, for the quadrature kernel, the dofs) of slabs j-1,
+  // j and j+1, so it waits for slab j+1's traces (or arrival).
+  const bool traces = op->coefficient_space;
+  if (traces) {
+    GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->tr, p->start, 0));
+    for (int k = 0; k < nchunks; ++k) {
+      GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->tr, p->ev_in[k], 0));
+      GBFEM_TRY(dg_apply(op, op->host_u, nullptr, p->tr, 0, nullptr, first_cell(k), cell_count(k), 1));
+      GBFEM_CUDA_TRY(cudaEventRecord(p->ev_tr[k], p->tr));
+    }
+  }
+  const std::vector<cudaEvent_t>& ready = traces ? p->ev_tr : p->ev_in;
+  auto apply = [&](int j) -> int {
+    const int need = j + 1 < nchunks ? j + 1 : nchunks - 1;
+    GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->comp, ready[need], 0));
+    GBFEM_TRY(dg_apply(op, op->host_u, op->host_w, p->comp, 0, nullptr, first_cell(j), cell_count(j), 2));
+    GBFEM_CUDA_TRY(cudaEventRecord(p->ev_comp[j], p->comp));
+    GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->out, p->ev_comp[j], 0));
+    const size_t off = size_t(first_cell(j)) * cell_bytes;
+    GBFEM_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(w_host) + off, static_cast<const char*>(op->host_w) + off,
+                                   size_t(cell_count(j)) * cell_bytes, cudaMemcpyDeviceToHost, p->out));
+    return GBFEM_OK;
+  };
+  // with periodic z, slab 0 also reads the last slab: it is applied last
+  const bool defer0 = op->dg.grid.periodic[2] && nchunks > 1;
+  for (int j = defer0 ? 1 : 0; j < nchunks; ++j) GBFEM_TRY(apply(j));
+  if (defer0) {
+    GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->comp, ready[nchunks - 1], 0));
+    GBFEM_TRY(apply(0));
+  }
+  return GBFEM_OK;
+}
+
+// Captures the copy pipeline for (u_host, w_host, nchunks) into a graph:
+// one launch then replaces the ~10 API calls and cross-stream waits per slab.
+// Every buffer the graph touches exists before the capture starts.
+static int capture_copy_pipeline(gbfem_operator_s* op, HostPipe* p, const void* u_host, void* w_host, int nchunks,
+                                 int zper) {
+  drop_host_graph(p);
+  if (op->coefficient_space) {
+    void* tb = nullptr;
+    GBFEM_TRY(trace_buffer(op, &tb));
+  }
+  GBFEM_CUDA_TRY(cudaStreamBeginCapture(p->in, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_copy_pipeline(op, p, u_host, w_host, nchunks, zper, p->in);
+  if (rc == GBFEM_OK) {
+    // join every forked stream back into the origin
+    cudaStream_t forked[3] = {p->comp, p->out, op->coefficient_space ? p->tr : nullptr};
+    for (int i = 0; i < 3 && rc == GBFEM_OK; ++i) {
+      if (!forked[i]) continue;
+      cudaError_t e = cudaEventRecord(p->join[i], forked[i]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(p->in, p->join[i], 0);
+      if (e != cudaSuccess) rc = set_cuda_error(e, "gbfem_operator_apply_host: graph capture");
+    }
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(p->in, &g);
+  if (rc != GBFEM_OK || ce != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (rc != GBFEM_OK) return rc;
+    return set_cuda_error(ce, "gbfem_operator_apply_host: graph capture");
+  }
+  cudaGraphExec_t ex = nullptr;
+  const cudaError_t ie = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) return set_cuda_error(ie, "gbfem_operator_apply_host: graph instantiate");
+  p->gexec = ex;
+  p->g_u = u_host;
+  p->g_w = w_host;
+  p->g_chunks = nchunks;
+  return GBFEM_OK;
+}
+
+int dg_apply_host_pipelined(gbfem_operator_s* op, const void* u_host, void* w_host) {
+  const bool pinned = mapped_device_pointer(u_host) && mapped_device_pointer(w_host);
+  if (op->coefficient_space && op->host_in_place && pinned) {
+    void* du = mapped_device_pointer(u_host);
+    void* dw = mapped_device_pointer(w_host);
+    return dg_apply_host_mapped(op, du, dw);
+  }
+  const int nz = op->dg.grid.cells[2];
   int nchunks = op->host_chunks;
   if (nchunks <= 0) {
     // about 16 slabs, each large enough to fill the GPU (>= 8192 cells)
@@ -486,42 +610,18 @@ int dg_apply_host_pipelined(gbfem_operator_s* op, const void* u_host, void* w_ho
   nchunks = (nz + zper - 1) / zper;
   HostPipe* p = nullptr;
   GBFEM_TRY(host_pipe(op, nchunks, &p));
-  const size_t cell_bytes = size_t(op->nloc) * es;
-  auto first_cell = [&](int k) { return (long long)k * zper * plane; };
-  auto cell_count = [&](int k) {
-    const long long z1 = (long long)(k + 1) * zper < nz ? (long long)(k + 1) * zper : nz;
-    return (z1 - (long long)k * zper) * plane;
-  };
-  // order after the work already queued on the legacy default stream
-  GBFEM_CUDA_TRY(cudaEventRecord(p->start, 0));
-  GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->in, p->start, 0));
-  GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->comp, p->start, 0));
-  GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->out, p->start, 0));
-  for (int k = 0; k < nchunks; ++k) {
-    const size_t off = size_t(first_cell(k)) * cell_bytes;
-    GBFEM_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(op->host_u) + off, static_cast<const char*>(u_host) + off,
-                                   size_t(cell_count(k)) * cell_bytes, cudaMemcpyHostToDevice, p->in));
-    GBFEM_CUDA_TRY(cudaEventRecord(p->ev_in[k], p->in));
-  }
-  const bool traces = op->coefficient_space;
-  auto apply = [&](int j) -> int {
-    GBFEM_TRY(dg_apply(op, op->host_u, op->host_w, p->comp, 0, nullptr, first_cell(j), cell_count(j), 2));
-    GBFEM_CUDA_TRY(cudaEventRecord(p->ev_comp[j], p->comp));
-    GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->out, p->ev_comp[j], 0));
-    const size_t off = size_t(first_cell(j)) * cell_bytes;
-    GBFEM_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(w_host) + off, static_cast<const char*>(op->host_w) + off,
-                                   size_t(cell_count(j)) * cell_bytes, cudaMemcpyDeviceToHost, p->out));
+  // A graph needs page-locked buffers (asynchronous copies) and kernel
+  // arguments that stay valid: the plain linear operators.  The graph is
+  // kept for the last pair of buffers.
+  if (pinned && !op->nonlinear && !op->jac_points) {
+    if (!(p->gexec && p->g_u == u_host && p->g_w == w_host && p->g_chunks == nchunks))
+      GBFEM_TRY(capture_copy_pipeline(op, p, u_host, w_host, nchunks, zper));
+    // on the legacy default stream: after the work already queued there
+    GBFEM_CUDA_TRY(cudaGraphLaunch(p->gexec, 0));
+    GBFEM_CUDA_TRY(cudaStreamSynchronize(0));
     return GBFEM_OK;
-  };
-  const bool defer0 = op->dg.grid.periodic[2] && nchunks > 1;
-  int rc = GBFEM_OK;
-  for (int k = 0; k < nchunks && rc == GBFEM_OK; ++k) {
-    GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->comp, p->ev_in[k], 0));
-    if (traces) rc = dg_apply(op, op->host_u, nullptr, p->comp, 0, nullptr, first_cell(k), cell_count(k), 1);
-    if (rc == GBFEM_OK && k >= 1 && !(k == 1 && defer0)) rc = apply(k - 1);
   }
-  if (rc == GBFEM_OK && !(nchunks == 1 && defer0)) rc = apply(nchunks - 1);
-  if (rc == GBFEM_OK && defer0) rc = apply(0);
+  const int rc = enqueue_copy_pipeline(op, p, u_host, w_host, nchunks, zper, 0);
   // every slab's copy-out waited on its apply: the out stream ends last
   const cudaError_t e = cudaStreamSynchronize(p->out);
   GBFEM_TRY(rc);
@@ -590,6 +690,7 @@ int gbfem_dg_operator_create(const gbfem_dg_desc* desc, gbfem_operator* out) {
 int gbfem_operator_update_coefficients(gbfem_operator op) {
   if (!op) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_update_coefficients: null argument");
   if (op->kind != OpKind::DG) return GBFEM_OK;
+  drop_host_graph(op->pipe);
   return dg_kappa_cache(op);
 }
 

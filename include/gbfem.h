@@ -125,10 +125,13 @@ int gbfem_operator_precision(gbfem_operator op, int* precision);
 int gbfem_operator_apply(gbfem_operator op, const void* u, void* w, void* stream);
 /* Same as gbfem_operator_apply with host arrays: copies u to the device,
  * applies, copies w back, synchronously.  Device buffers are cached in op.
- * DG operators pipeline the call over slabs of z-planes (copy in, apply and
- * copy out of successive slabs overlap on three streams; page-locked host
- * arrays let the copies run asynchronously; see also
- * gbfem_operator_set_host_transfer).  The result is bitwise that of
+ * DG operators pipeline the call over slabs of z-planes (copy in, trace pass,
+ * apply and copy out of successive slabs overlap on four streams; page-locked
+ * host arrays let the copies run asynchronously; see also
+ * gbfem_operator_set_host_transfer).  For page-locked arrays and a linear
+ * operator the pipeline is captured once as a CUDA graph for that pair of
+ * arrays and slab count, and replayed while they stay the same (the arrays'
+ * contents are read at each call).  The result is bitwise that of
  * gbfem_operator_apply. */
 int gbfem_operator_apply_host(gbfem_operator op, const void* u_host, void* w_host);
 /* Number of slabs of the pipelined gbfem_operator_apply_host (0 = automatic:

@@ -294,6 +294,42 @@ def test_host_apply_on_page_locked_buffers_is_bitwise_the_device_apply(gb, orc, 
         assert np.array_equal(wh.numpy().view(np.uint64), ref.view(np.uint64)), in_place
 
 
+@pytest.mark.parametrize("algorithm", [0, 1])
+def test_host_apply_graph_follows_buffers_and_contents(gb, orc, algorithm):
+    """With page-locked buffers the copy pipeline runs as a captured graph.  It
+    must read the buffers' contents at each call, be captured again for other
+    buffers or another slab count, and agree bit for bit with the device
+    apply; pageable buffers take the direct path."""
+    torch = pytest.importorskip("torch")
+    cells = (4, 3, 8)
+    op = gb.DGOperator(cells, 2, mass=0.2, velocity=(0.3, 0.0, -0.5), periodic=(0, 0, 1), algorithm=algorithm)
+    rng = np.random.default_rng(31)
+
+    def device_apply(u):
+        w = gb.DeviceArray(op.size)
+        op(gb.DeviceArray.from_numpy(u), w)
+        return w.numpy()
+
+    ua, ub = (torch.from_numpy(rng.uniform(-1, 1, op.size)).pin_memory() for _ in range(2))
+    wa, wb = (torch.empty(op.size, dtype=torch.float64).pin_memory() for _ in range(2))
+    steps = [(ua, wa, 0, False), (ua, wa, 0, True), (ub, wb, 0, False), (ua, wa, 0, False), (ua, wa, 5, False),
+             (ub, wb, 5, True)]
+    for u, w, chunks, refill in steps:
+        if refill:  # same buffer, new contents
+            u.copy_(torch.from_numpy(rng.uniform(-1, 1, op.size)))
+        op.set_host_chunks(chunks)
+        w.fill_(float("nan"))
+        op.apply_host(u.numpy(), w.numpy())
+        ref = device_apply(u.numpy())
+        assert np.array_equal(w.numpy().view(np.uint64), ref.view(np.uint64)), (chunks, refill)
+    u_pageable = rng.uniform(-1, 1, op.size)
+    w_pageable = np.full(op.size, np.nan)
+    op.apply_host(u_pageable, w_pageable)
+    assert np.array_equal(w_pageable.view(np.uint64), device_apply(u_pageable).view(np.uint64))
+    assert relmax(w_pageable, orc.DGProblem(cells, 2, mass=0.2, velocity=(0.3, 0.0, -0.5),
+                                            periodic=(0, 0, 1)).apply(u_pageable)) < TOL64
+
+
 @pytest.mark.parametrize("order", [1, 2, 3, 4])
 @pytest.mark.parametrize("precision", [0, 1])
 def test_cellwise_kappa_closed_form(gb, orc, order, precision):
