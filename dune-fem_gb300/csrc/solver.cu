@@ -266,55 +266,112 @@ __global__ void k_scaled_block_apply(const float* __restrict__ hinvT, const floa
 
 // The same on tiles of up to 32 cells of one boundary type (nb <= 128): the
 // cells sorted by type at creation, each type's list cut into tiles (interior
-// tiles are runs of consecutive cells).  A CTA stages its type's inverse in
-// shared memory (rows padded to 128), gathers the tile's residuals and forms
-// the nb x 32 product with 4 x 4 register tiles per thread, so the matrix is
-// read once per tile instead of once per cell.
+// tiles are runs of consecutive cells).  Each CTA owns a contiguous range of
+// tiles, so it stages its type's inverse in shared memory (rows padded to 128)
+// once, not once per tile: the tiles are sorted by type, and the matrix is
+// reloaded only where the type changes inside the range.  The residuals of
+// tile t+1 are gathered (transposed, [j][cell]) with cp.async while the
+// nb x 32 product of tile t runs with 4 x 4 register tiles per thread; the
+// product is staged back through shared memory so that each cell's nb
+// results go out as one contiguous run.
 constexpr int kSbTile = 32;
+
+__device__ __forceinline__ void sb_cp_async4(float* dst, const float* src) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void sb_cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void sb_cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 __global__ void __launch_bounds__(256) k_scaled_block_apply_tiled(const float* __restrict__ hinvT,
                                                                   const float* __restrict__ kcell,
                                                                   const int* __restrict__ cells,
                                                                   const int* __restrict__ tiles,
                                                                   const float* __restrict__ r, float* __restrict__ z,
-                                                                  int nb) {
+                                                                  int nb, int ntiles) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float* Hs = reinterpret_cast<float*>(smraw);  // [nb][128]  (transposed inverse: Hs[j][i])
-  float* Rs = Hs + nb * 128;                    // [nb][32]   (Rs[j][cell])
-  const int type = tiles[3 * blockIdx.x], start = tiles[3 * blockIdx.x + 1], count = tiles[3 * blockIdx.x + 2];
+  float* Rb = Hs + nb * 128;                    // 2 x [nb][32]: residuals Rs[j][cell], then results [cell][i]
+  __shared__ float sInvK[kSbTile];
   const int tid = threadIdx.x;
-  const float* Hg = hinvT + (long long)type * nb * nb;
-  for (int e = tid; e < nb * 128; e += blockDim.x) {
-    const int j = e >> 7, i = e & 127;
-    Hs[e] = i < nb ? __ldg(Hg + (long long)j * nb + i) : 0.0f;
-  }
-  for (int e = tid; e < nb * kSbTile; e += blockDim.x) {
-    const int c = e / nb, j = e - c * nb;
-    Rs[j * kSbTile + c] = c < count ? r[(long long)cells[start + c] * nb + j] : 0.0f;
-  }
-  __syncthreads();
-  const int rg = tid & 31, cg = tid >> 5;  // rows 4 rg .. 4 rg + 3, tile cells 4 cg .. 4 cg + 3
-  float acc[4][4] = {};
-  for (int j = 0; j < nb; ++j) {
-    const float4 a = *reinterpret_cast<const float4*>(Hs + j * 128 + 4 * rg);
-    const float4 b = *reinterpret_cast<const float4*>(Rs + j * kSbTile + 4 * cg);
-    const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-    for (int ii = 0; ii < 4; ++ii)
-#pragma unroll
-      for (int cc = 0; cc < 4; ++cc) acc[ii][cc] = fmaf(av[ii], bv[cc], acc[ii][cc]);
-  }
-#pragma unroll
-  for (int cc = 0; cc < 4; ++cc) {
-    const int tc = 4 * cg + cc;
-    if (tc >= count) break;
-    const long long c = cells[start + tc];
-    const float ik = 1.0f / kcell[c];
-#pragma unroll
-    for (int ii = 0; ii < 4; ++ii) {
-      const int i = 4 * rg + ii;
-      if (i < nb) z[c * nb + i] = acc[ii][cc] * ik;
+  const int t0 = int((long long)blockIdx.x * ntiles / gridDim.x);
+  const int t1 = int((long long)(blockIdx.x + 1) * ntiles / gridDim.x);
+  if (t0 >= t1) return;
+  const int rstride = nb * kSbTile;
+  auto gather = [&](int t, float* R) {
+    const int start = tiles[3 * t + 1], count = tiles[3 * t + 2];
+    for (int e = tid; e < rstride; e += blockDim.x) {
+      const int c = e / nb, j = e - c * nb;
+      float* dst = R + j * kSbTile + c;
+      if (c < count) sb_cp_async4(dst, r + (long long)cells[start + c] * nb + j);
+      else *dst = 0.0f;
     }
+    sb_cp_async_commit();
+  };
+  gather(t0, Rb);
+  int cur_type = -1;
+  const int rg = tid & 31, cg = tid >> 5;  // rows 4 rg .. 4 rg + 3, tile cells 4 cg .. 4 cg + 3
+  for (int t = t0; t < t1; ++t) {
+    float* R = Rb + ((t - t0) & 1) * rstride;
+    const int type = tiles[3 * t], start = tiles[3 * t + 1], count = tiles[3 * t + 2];
+    if (type != cur_type) {  // the same for every thread of the CTA
+      const float* Hg = hinvT + (long long)type * nb * nb;
+      for (int e = tid; e < nb * 128; e += blockDim.x) {
+        const int j = e >> 7, i = e & 127;
+        Hs[e] = i < nb ? __ldg(Hg + (long long)j * nb + i) : 0.0f;
+      }
+      cur_type = type;
+    }
+    if (tid < kSbTile) sInvK[tid] = tid < count ? 1.0f / kcell[cells[start + tid]] : 0.0f;
+    if (t + 1 < t1) {
+      gather(t + 1, Rb + ((t + 1 - t0) & 1) * rstride);
+      sb_cp_async_wait<1>();  // tile t's group is complete, tile t+1's may still run
+    } else {
+      sb_cp_async_wait<0>();
+    }
+    __syncthreads();  // H, R and the inverse kappas of tile t are visible
+    float acc[4][4] = {};
+    for (int j = 0; j < nb; ++j) {
+      const float4 a = *reinterpret_cast<const float4*>(Hs + j * 128 + 4 * rg);
+      const float4 b = *reinterpret_cast<const float4*>(R + j * kSbTile + 4 * cg);
+      const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+      for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) acc[ii][cc] = fmaf(av[ii], bv[cc], acc[ii][cc]);
+    }
+    __syncthreads();  // every read of R done: it takes the results [cell][i]
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc)
+#pragma unroll
+      for (int ii = 0; ii < 4; ++ii) {
+        const int i = 4 * rg + ii;
+        if (i < nb) R[(4 * cg + cc) * nb + i] = acc[ii][cc] * sInvK[4 * cg + cc];
+      }
+    __syncthreads();
+    for (int e = tid; e < count * nb; e += blockDim.x) {
+      const int c = e / nb, i = e - c * nb;
+      z[(long long)cells[start + c] * nb + i] = R[e];
+    }
+    __syncthreads();  // R and sInvK are free for the gather of tile t+2 and the next tile
   }
+}
+
+// SMs of the current device (152 on GB300), for persistent grids.
+static int num_sms() {
+  static int n = 0;
+  if (n <= 0) {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) ==
+                                                  cudaSuccess && v > 0)
+      n = v;
+    else
+      n = 152;
+  }
+  return n;
 }
 
 // ------------------------------------------------------------ vector ops --
@@ -443,12 +500,14 @@ int precond_apply(const gbfem_preconditioner_s* pc, const void* r, void* z, cuda
         g.per[d] = pc->sor_op->dg.grid.periodic[d];
       }
       if (pc->sb_tiles) {
-        const size_t sm = size_t(nb) * (128 + kSbTile) * 4;
+        // two CTAs of 96 KB per SM, each over a contiguous range of tiles
+        const size_t sm = size_t(nb) * (128 + 2 * kSbTile) * 4;
         GBFEM_CUDA_TRY(cudaFuncSetAttribute(k_scaled_block_apply_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             int(sm)));
-        k_scaled_block_apply_tiled<<<unsigned(pc->sb_ntiles), 256, sm, s>>>(
+        const long long grid = pc->sb_ntiles < 2LL * num_sms() ? pc->sb_ntiles : 2LL * num_sms();
+        k_scaled_block_apply_tiled<<<unsigned(grid), 256, sm, s>>>(
             (const float*)pc->data, (const float*)pc->sor_op->dg.kappa_cell, pc->sor_cells, pc->sb_tiles,
-            (const float*)r, (float*)z, nb);
+            (const float*)r, (float*)z, nb, int(pc->sb_ntiles));
       } else {
         k_scaled_block_apply<<<unsigned((nc + cpb - 1) / cpb), threads, size_t(cpb) * nb * 4, s>>>(
             (const float*)pc->data, (const float*)pc->sor_op->dg.kappa_cell, (const float*)r, (float*)z, nb, nc, cpb,

@@ -313,6 +313,34 @@ def test_mixed_stops_at_the_rounding_floor(gb, orc, outer):
     assert info.residual < 1e-13
 
 
+@pytest.mark.parametrize("cells,order", [((24, 24, 24), 1), ((22, 21, 22), 4)])
+def test_scaled_block_jacobi_many_tiles(gb, orc, cells, order):
+    """Grids with more tiles than the persistent grid has CTAs, so that a CTA
+    runs several tiles, double-buffers their residuals and meets type
+    changes inside its range: against the oracle's kappa = 1 blocks (order 1)
+    and against block Jacobi of the same operator (constant kappa)."""
+    ncell = int(np.prod(cells))
+    nloc = (order + 1) ** 3
+    rng = np.random.default_rng(ncell)
+    r = rng.uniform(-1, 1, ncell * nloc).astype(np.float32)
+    if order == 1:
+        kc = rng.uniform(0.5, 2.0, ncell).astype(np.float32)
+        op = gb.DGOperator(cells, order, precision=gb.F32, kappa_cell=gb.DeviceArray.from_numpy(kc, gb.F32))
+        z = gb.DeviceArray(ncell * nloc, gb.F32)
+        gb.Preconditioner.scaled_block_jacobi(op)(gb.DeviceArray.from_numpy(r, gb.F32), z)
+        hinv = np.linalg.inv(orc.DGProblem(cells, order).block_diagonal())
+        ref = np.einsum("cij,cj->ci", hinv, r.astype(np.float64).reshape(-1, nloc)) / kc[:, None].astype(np.float64)
+        assert relmax(z.numpy(), ref.ravel()) < 2e-5
+    const = gb.DGOperator(cells, order, precision=gb.F32,
+                          kappa_cell=gb.DeviceArray.from_numpy(np.full(ncell, 0.8, np.float32), gb.F32))
+    z1, z2 = gb.DeviceArray(ncell * nloc, gb.F32), gb.DeviceArray(ncell * nloc, gb.F32)
+    gb.Preconditioner.scaled_block_jacobi(const)(gb.DeviceArray.from_numpy(r, gb.F32), z1)
+    gb.Preconditioner.block_jacobi(const)(gb.DeviceArray.from_numpy(r, gb.F32), z2)
+    # FP32 blocks of two assemblies: their rounding grows with the Q4 blocks'
+    # condition; a tile or index mix-up would be O(1)
+    assert relmax(z1.numpy(), z2.numpy()) < (5e-5 if order == 1 else 1e-3)
+
+
 @pytest.mark.parametrize("cells,periodic", [((4, 3, 5), (0, 0, 0)), ((4, 2, 3), (1, 0, 0)), ((1, 4, 3), (0, 0, 1))])
 def test_scaled_block_jacobi_for_cellwise_kappa(gb, orc, cells, periodic):
     """z_c = H_t^-1 r_c / kappa_c with H_t the kappa = 1 diagonal block of the
