@@ -300,13 +300,21 @@ __global__ void __launch_bounds__(256) k_scaled_block_apply_tiled(const float* _
   const int t0 = int((long long)blockIdx.x * ntiles / gridDim.x);
   const int t1 = int((long long)(blockIdx.x + 1) * ntiles / gridDim.x);
   if (t0 >= t1) return;
-  const int rstride = nb * kSbTile;
-  auto gather = [&](int t, float* R) {
+  const int rstride = nb * kSbTile;  // a multiple of 32: every loop below keeps whole warps
+  const int lane = tid & 31;
+  // lane l holds the index of the tile's cell l; the others take it by shuffle
+  auto lane_cell = [&](int t) {
     const int start = tiles[3 * t + 1], count = tiles[3 * t + 2];
+    return lane < count ? cells[start + lane] : 0;
+  };
+  auto gather = [&](int t, float* R) {
+    const int count = tiles[3 * t + 2];
+    const int mine = lane_cell(t);
     for (int e = tid; e < rstride; e += blockDim.x) {
-      const int c = e / nb, j = e - c * nb;
+      const int c = e / nb, j = e - c * nb;  // c < 32
+      const int cell = __shfl_sync(0xffffffffu, mine, c);
       float* dst = R + j * kSbTile + c;
-      if (c < count) sb_cp_async4(dst, r + (long long)cells[start + c] * nb + j);
+      if (c < count) sb_cp_async4(dst, r + (long long)cell * nb + j);
       else *dst = 0.0f;
     }
     sb_cp_async_commit();
@@ -316,7 +324,7 @@ __global__ void __launch_bounds__(256) k_scaled_block_apply_tiled(const float* _
   const int rg = tid & 31, cg = tid >> 5;  // rows 4 rg .. 4 rg + 3, tile cells 4 cg .. 4 cg + 3
   for (int t = t0; t < t1; ++t) {
     float* R = Rb + ((t - t0) & 1) * rstride;
-    const int type = tiles[3 * t], start = tiles[3 * t + 1], count = tiles[3 * t + 2];
+    const int type = tiles[3 * t], count = tiles[3 * t + 2];
     if (type != cur_type) {  // the same for every thread of the CTA
       const float* Hg = hinvT + (long long)type * nb * nb;
       for (int e = tid; e < nb * 128; e += blockDim.x) {
@@ -325,7 +333,8 @@ __global__ void __launch_bounds__(256) k_scaled_block_apply_tiled(const float* _
       }
       cur_type = type;
     }
-    if (tid < kSbTile) sInvK[tid] = tid < count ? 1.0f / kcell[cells[start + tid]] : 0.0f;
+    const int mine = lane_cell(t);
+    if (tid < kSbTile) sInvK[tid] = tid < count ? 1.0f / kcell[mine] : 0.0f;
     if (t + 1 < t1) {
       gather(t + 1, Rb + ((t + 1 - t0) & 1) * rstride);
       sb_cp_async_wait<1>();  // tile t's group is complete, tile t+1's may still run
@@ -352,9 +361,11 @@ __global__ void __launch_bounds__(256) k_scaled_block_apply_tiled(const float* _
         if (i < nb) R[(4 * cg + cc) * nb + i] = acc[ii][cc] * sInvK[4 * cg + cc];
       }
     __syncthreads();
-    for (int e = tid; e < count * nb; e += blockDim.x) {
-      const int c = e / nb, i = e - c * nb;
-      z[(long long)cells[start + c] * nb + i] = R[e];
+    const int total = count * nb;
+    for (int e0 = tid - lane; e0 < total; e0 += blockDim.x) {  // warp-uniform bound
+      const int e = e0 + lane, c = e / nb;
+      const int cell = __shfl_sync(0xffffffffu, mine, c < kSbTile ? c : kSbTile - 1);
+      if (e < total) z[(long long)cell * nb + (e - c * nb)] = R[e];
     }
     __syncthreads();  // R and sInvK are free for the gather of tile t+2 and the next tile
   }
