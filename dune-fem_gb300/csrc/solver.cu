@@ -266,15 +266,20 @@ __global__ void k_scaled_block_apply(const float* __restrict__ hinvT, const floa
 
 // The same on tiles of up to 32 cells of one boundary type (nb <= 128): the
 // cells sorted by type at creation, each type's list cut into tiles (interior
-// tiles are runs of consecutive cells).  Each CTA owns a contiguous range of
-// tiles, so it stages its type's inverse in shared memory (rows padded to 128)
-// once, not once per tile: the tiles are sorted by type, and the matrix is
-// reloaded only where the type changes inside the range.  The residuals of
-// tile t+1 are gathered (transposed, [j][cell]) with cp.async while the
-// nb x 32 product of tile t runs with 4 x 4 register tiles per thread; the
-// product is staged back through shared memory so that each cell's nb
-// results go out as one contiguous run.
+// tiles are runs of consecutive cells) and padded with empty tiles to a
+// multiple of kSbGroups, so that a quad of consecutive tiles has one type.
+// One CTA per SM owns a contiguous range of quads and stages their type's
+// inverse in shared memory (rows padded to 128) once, reloading it only where
+// the type changes.  Its kSbGroups groups of 8 warps each take one tile of a
+// quad: they gather the residuals of their next tile (transposed, [j][cell])
+// with cp.async while the nb x 32 product of the current one runs with 4 x 4
+// register tiles per thread, and stage the product back through shared
+// memory so that each cell's nb results go out as one contiguous run.  A
+// group synchronises on its own named barrier; the whole CTA only where the
+// inverse changes.
 constexpr int kSbTile = 32;
+constexpr int kSbGroups = 4;
+constexpr int kSbGroupThreads = 256;
 
 __device__ __forceinline__ void sb_cp_async4(float* dst, const float* src) {
   const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
@@ -285,22 +290,25 @@ template <int N>
 __device__ __forceinline__ void sb_cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
+// barrier 1 + g among the kSbGroupThreads threads of group g (0 is __syncthreads)
+__device__ __forceinline__ void sb_group_sync(int g) {
+  asm volatile("bar.sync %0, %1;\n" ::"r"(1 + g), "n"(kSbGroupThreads) : "memory");
+}
 
-__global__ void __launch_bounds__(256) k_scaled_block_apply_tiled(const float* __restrict__ hinvT,
-                                                                  const float* __restrict__ kcell,
-                                                                  const int* __restrict__ cells,
-                                                                  const int* __restrict__ tiles,
-                                                                  const float* __restrict__ r, float* __restrict__ z,
-                                                                  int nb, int ntiles) {
+__global__ void __launch_bounds__(kSbGroups * kSbGroupThreads, 1)
+    k_scaled_block_apply_tiled(const float* __restrict__ hinvT, const float* __restrict__ kcell,
+                               const int* __restrict__ cells, const int* __restrict__ tiles,
+                               const float* __restrict__ r, float* __restrict__ z, int nb, int nquads) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  float* Hs = reinterpret_cast<float*>(smraw);  // [nb][128]  (transposed inverse: Hs[j][i])
-  float* Rb = Hs + nb * 128;                    // 2 x [nb][32]: residuals Rs[j][cell], then results [cell][i]
-  __shared__ float sInvK[kSbTile];
+  __shared__ float sInvK[kSbGroups][kSbTile];
   const int tid = threadIdx.x;
-  const int t0 = int((long long)blockIdx.x * ntiles / gridDim.x);
-  const int t1 = int((long long)(blockIdx.x + 1) * ntiles / gridDim.x);
-  if (t0 >= t1) return;
+  const int g = tid / kSbGroupThreads, gt = tid - g * kSbGroupThreads;
   const int rstride = nb * kSbTile;  // a multiple of 32: every loop below keeps whole warps
+  float* Hs = reinterpret_cast<float*>(smraw);      // [nb][128]  (transposed inverse: Hs[j][i])
+  float* Rb = Hs + nb * 128 + g * 2 * rstride;      // this group's 2 x [nb][32]
+  const int q0 = int((long long)blockIdx.x * nquads / gridDim.x);
+  const int q1 = int((long long)(blockIdx.x + 1) * nquads / gridDim.x);
+  if (q0 >= q1) return;  // the same for the whole CTA
   const int lane = tid & 31;
   // lane l holds the index of the tile's cell l; the others take it by shuffle
   auto lane_cell = [&](int t) {
@@ -310,7 +318,7 @@ __global__ void __launch_bounds__(256) k_scaled_block_apply_tiled(const float* _
   auto gather = [&](int t, float* R) {
     const int count = tiles[3 * t + 2];
     const int mine = lane_cell(t);
-    for (int e = tid; e < rstride; e += blockDim.x) {
+    for (int e = gt; e < rstride; e += kSbGroupThreads) {
       const int c = e / nb, j = e - c * nb;  // c < 32
       const int cell = __shfl_sync(0xffffffffu, mine, c);
       float* dst = R + j * kSbTile + c;
@@ -319,29 +327,32 @@ __global__ void __launch_bounds__(256) k_scaled_block_apply_tiled(const float* _
     }
     sb_cp_async_commit();
   };
-  gather(t0, Rb);
+  gather(kSbGroups * q0 + g, Rb);
   int cur_type = -1;
-  const int rg = tid & 31, cg = tid >> 5;  // rows 4 rg .. 4 rg + 3, tile cells 4 cg .. 4 cg + 3
-  for (int t = t0; t < t1; ++t) {
-    float* R = Rb + ((t - t0) & 1) * rstride;
-    const int type = tiles[3 * t], count = tiles[3 * t + 2];
-    if (type != cur_type) {  // the same for every thread of the CTA
+  const int rg = gt & 31, cg = gt >> 5;  // rows 4 rg .. 4 rg + 3, tile cells 4 cg .. 4 cg + 3
+  for (int q = q0; q < q1; ++q) {
+    const int t = kSbGroups * q + g;
+    float* R = Rb + ((q - q0) & 1) * rstride;
+    const int type = tiles[3 * t], count = tiles[3 * t + 2];  // type: the same for the quad
+    if (type != cur_type) {
+      __syncthreads();  // every group is done with the previous inverse
       const float* Hg = hinvT + (long long)type * nb * nb;
       for (int e = tid; e < nb * 128; e += blockDim.x) {
         const int j = e >> 7, i = e & 127;
         Hs[e] = i < nb ? __ldg(Hg + (long long)j * nb + i) : 0.0f;
       }
+      __syncthreads();
       cur_type = type;
     }
     const int mine = lane_cell(t);
-    if (tid < kSbTile) sInvK[tid] = tid < count ? 1.0f / kcell[mine] : 0.0f;
-    if (t + 1 < t1) {
-      gather(t + 1, Rb + ((t + 1 - t0) & 1) * rstride);
-      sb_cp_async_wait<1>();  // tile t's group is complete, tile t+1's may still run
+    if (gt < kSbTile) sInvK[g][gt] = gt < count ? 1.0f / kcell[mine] : 0.0f;
+    if (q + 1 < q1) {
+      gather(t + kSbGroups, Rb + ((q + 1 - q0) & 1) * rstride);
+      sb_cp_async_wait<1>();  // this tile's group is complete, the next one's may still run
     } else {
       sb_cp_async_wait<0>();
     }
-    __syncthreads();  // H, R and the inverse kappas of tile t are visible
+    sb_group_sync(g);  // R and the inverse kappas of this tile are visible to the group
     float acc[4][4] = {};
     for (int j = 0; j < nb; ++j) {
       const float4 a = *reinterpret_cast<const float4*>(Hs + j * 128 + 4 * rg);
@@ -352,22 +363,22 @@ __global__ void __launch_bounds__(256) k_scaled_block_apply_tiled(const float* _
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc) acc[ii][cc] = fmaf(av[ii], bv[cc], acc[ii][cc]);
     }
-    __syncthreads();  // every read of R done: it takes the results [cell][i]
+    sb_group_sync(g);  // every read of R done: it takes the results [cell][i]
 #pragma unroll
     for (int cc = 0; cc < 4; ++cc)
 #pragma unroll
       for (int ii = 0; ii < 4; ++ii) {
         const int i = 4 * rg + ii;
-        if (i < nb) R[(4 * cg + cc) * nb + i] = acc[ii][cc] * sInvK[4 * cg + cc];
+        if (i < nb) R[(4 * cg + cc) * nb + i] = acc[ii][cc] * sInvK[g][4 * cg + cc];
       }
-    __syncthreads();
+    sb_group_sync(g);
     const int total = count * nb;
-    for (int e0 = tid - lane; e0 < total; e0 += blockDim.x) {  // warp-uniform bound
+    for (int e0 = gt - lane; e0 < total; e0 += kSbGroupThreads) {  // warp-uniform bound
       const int e = e0 + lane, c = e / nb;
       const int cell = __shfl_sync(0xffffffffu, mine, c < kSbTile ? c : kSbTile - 1);
       if (e < total) z[(long long)cell * nb + (e - c * nb)] = R[e];
     }
-    __syncthreads();  // R and sInvK are free for the gather of tile t+2 and the next tile
+    sb_group_sync(g);  // R and sInvK[g] are free for the gather after next and the next tile
   }
 }
 
@@ -511,14 +522,16 @@ int precond_apply(const gbfem_preconditioner_s* pc, const void* r, void* z, cuda
         g.per[d] = pc->sor_op->dg.grid.periodic[d];
       }
       if (pc->sb_tiles) {
-        // two CTAs of 96 KB per SM, each over a contiguous range of tiles
-        const size_t sm = size_t(nb) * (128 + 2 * kSbTile) * 4;
+        // one CTA per SM over a contiguous range of quads: the inverse and
+        // two residual tiles per group, 192 KB at nb = 125
+        const size_t sm = size_t(nb) * (128 + 2 * kSbGroups * kSbTile) * 4;
         GBFEM_CUDA_TRY(cudaFuncSetAttribute(k_scaled_block_apply_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             int(sm)));
-        const long long grid = pc->sb_ntiles < 2LL * num_sms() ? pc->sb_ntiles : 2LL * num_sms();
-        k_scaled_block_apply_tiled<<<unsigned(grid), 256, sm, s>>>(
+        const long long nquads = pc->sb_ntiles / kSbGroups;
+        const long long grid = nquads < num_sms() ? nquads : num_sms();
+        k_scaled_block_apply_tiled<<<unsigned(grid), kSbGroups * kSbGroupThreads, sm, s>>>(
             (const float*)pc->data, (const float*)pc->sor_op->dg.kappa_cell, pc->sor_cells, pc->sb_tiles,
-            (const float*)r, (float*)z, nb, int(pc->sb_ntiles));
+            (const float*)r, (float*)z, nb, int(nquads));
       } else {
         k_scaled_block_apply<<<unsigned((nc + cpb - 1) / cpb), threads, size_t(cpb) * nb * 4, s>>>(
             (const float*)pc->data, (const float*)pc->sor_op->dg.kappa_cell, (const float*)r, (float*)z, nb, nc, cpb,
@@ -1312,12 +1325,19 @@ int gbfem_preconditioner_scaled_block_jacobi_create(gbfem_operator op, gbfem_pre
     std::vector<int> list, tiles;
     list.reserve(size_t(op->ncells));
     for (int t = 0; t < 27; ++t) {
-      for (size_t k = 0; k < by_type[t].size(); k += kSbTile) {
+      int ntype = 0;
+      for (size_t k = 0; k < by_type[t].size(); k += kSbTile, ++ntype) {
         const int cnt = int(std::min<size_t>(kSbTile, by_type[t].size() - k));
         tiles.push_back(t);
         tiles.push_back(int(list.size()));
         tiles.push_back(cnt);
         list.insert(list.end(), by_type[t].begin() + k, by_type[t].begin() + k + cnt);
+      }
+      // empty tiles up to a whole quad of this type
+      for (; ntype % kSbGroups != 0; ++ntype) {
+        tiles.push_back(t);
+        tiles.push_back(0);
+        tiles.push_back(0);
       }
     }
     cudaError_t e = cudaMalloc(&pc->sor_cells, list.size() * sizeof(int));
