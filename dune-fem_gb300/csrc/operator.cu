@@ -491,18 +491,45 @@ static int dg_apply_host_mapped(gbfem_operator_s* op, const void* du, void* dw) 
   return GBFEM_OK;
 }
 
-// Enqueues the copy pipeline after the work already queued on `origin`.
-static int enqueue_copy_pipeline(gbfem_operator_s* op, HostPipe* p, const void* u_host, void* w_host, int nchunks,
-                                 int zper, cudaStream_t origin) {
+// z-plane boundaries of the copy pipeline's slabs: slab k holds the planes
+// [zb[k], zb[k+1]).  About nchunks slabs of zper planes; with zper >= 3 the
+// first two and the last two slabs are single planes instead.  The first
+// apply waits for its upper neighbour slab, so it can then start once two
+// planes have arrived, and the last apply and copy-out are one plane each:
+// a shorter fill and drain around the same steady state.
+static std::vector<int> slab_bounds(int nz, int nchunks) {
+  const int zper = (nz + nchunks - 1) / nchunks;
+  std::vector<int> zb{0};
+  int z = 0;
+  if (zper >= 3 && nchunks >= 4) {  // then nz >= 9
+    zb.push_back(1);
+    zb.push_back(2);
+    z = 2;
+    while (z < nz - 2) {
+      z = z + zper < nz - 2 ? z + zper : nz - 2;
+      zb.push_back(z);
+    }
+    zb.push_back(nz - 1);
+    zb.push_back(nz);
+  } else {
+    while (z < nz) {
+      z = z + zper < nz ? z + zper : nz;
+      zb.push_back(z);
+    }
+  }
+  return zb;
+}
+
+// Enqueues the copy pipeline over the slabs zb after the work already queued
+// on `origin`.
+static int enqueue_copy_pipeline(gbfem_operator_s* op, HostPipe* p, const void* u_host, void* w_host,
+                                 const std::vector<int>& zb, cudaStream_t origin) {
   const size_t es = op->precision == GBFEM_F64 ? 8 : 4;
-  const int nz = op->dg.grid.cells[2];
   const long long plane = (long long)op->dg.grid.cells[0] * op->dg.grid.cells[1];
   const size_t cell_bytes = size_t(op->nloc) * es;
-  auto first_cell = [&](int k) { return (long long)k * zper * plane; };
-  auto cell_count = [&](int k) {
-    const long long z1 = (long long)(k + 1) * zper < nz ? (long long)(k + 1) * zper : nz;
-    return (z1 - (long long)k * zper) * plane;
-  };
+  const int nchunks = int(zb.size()) - 1;
+  auto first_cell = [&](int k) { return (long long)zb[k] * plane; };
+  auto cell_count = [&](int k) { return (long long)(zb[k + 1] - zb[k]) * plane; };
   GBFEM_CUDA_TRY(cudaEventRecord(p->start, origin));
   GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->in, p->start, 0));
   GBFEM_CUDA_TRY(cudaStreamWaitEvent(p->comp, p->start, 0));
@@ -553,14 +580,14 @@ static int enqueue_copy_pipeline(gbfem_operator_s* op, HostPipe* p, const void* 
 // one launch then replaces the ~10 API calls and cross-stream waits per slab.
 // Every buffer the graph touches exists before the capture starts.
 static int capture_copy_pipeline(gbfem_operator_s* op, HostPipe* p, const void* u_host, void* w_host, int nchunks,
-                                 int zper) {
+                                 const std::vector<int>& zb) {
   drop_host_graph(p);
   if (op->coefficient_space) {
     void* tb = nullptr;
     GBFEM_TRY(trace_buffer(op, &tb));
   }
   GBFEM_CUDA_TRY(cudaStreamBeginCapture(p->in, cudaStreamCaptureModeThreadLocal));
-  int rc = enqueue_copy_pipeline(op, p, u_host, w_host, nchunks, zper, p->in);
+  int rc = enqueue_copy_pipeline(op, p, u_host, w_host, zb, p->in);
   if (rc == GBFEM_OK) {
     // join every forked stream back into the origin
     cudaStream_t forked[3] = {p->comp, p->out, op->coefficient_space ? p->tr : nullptr};
@@ -606,22 +633,21 @@ int dg_apply_host_pipelined(gbfem_operator_s* op, const void* u_host, void* w_ho
   }
   if (nchunks > nz) nchunks = nz;
   if (nchunks > 64) nchunks = 64;
-  const int zper = (nz + nchunks - 1) / nchunks;
-  nchunks = (nz + zper - 1) / zper;
+  const std::vector<int> zb = slab_bounds(nz, nchunks);
   HostPipe* p = nullptr;
-  GBFEM_TRY(host_pipe(op, nchunks, &p));
+  GBFEM_TRY(host_pipe(op, int(zb.size()) - 1, &p));
   // A graph needs page-locked buffers (asynchronous copies) and kernel
   // arguments that stay valid: the plain linear operators.  The graph is
-  // kept for the last pair of buffers.
+  // kept for the last pair of buffers (and slab count).
   if (pinned && !op->nonlinear && !op->jac_points) {
     if (!(p->gexec && p->g_u == u_host && p->g_w == w_host && p->g_chunks == nchunks))
-      GBFEM_TRY(capture_copy_pipeline(op, p, u_host, w_host, nchunks, zper));
+      GBFEM_TRY(capture_copy_pipeline(op, p, u_host, w_host, nchunks, zb));
     // on the legacy default stream: after the work already queued there
     GBFEM_CUDA_TRY(cudaGraphLaunch(p->gexec, 0));
     GBFEM_CUDA_TRY(cudaStreamSynchronize(0));
     return GBFEM_OK;
   }
-  const int rc = enqueue_copy_pipeline(op, p, u_host, w_host, nchunks, zper, 0);
+  const int rc = enqueue_copy_pipeline(op, p, u_host, w_host, zb, 0);
   // every slab's copy-out waited on its apply: the out stream ends last
   const cudaError_t e = cudaStreamSynchronize(p->out);
   GBFEM_TRY(rc);

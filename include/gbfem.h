@@ -135,7 +135,9 @@ int gbfem_operator_apply(gbfem_operator op, const void* u, void* w, void* stream
  * gbfem_operator_apply. */
 int gbfem_operator_apply_host(gbfem_operator op, const void* u_host, void* w_host);
 /* Number of slabs of the pipelined gbfem_operator_apply_host (0 = automatic:
- * up to 16, each >= 8192 cells; capped at the number of z-planes and 64). */
+ * up to 16, each >= 8192 cells; capped at the number of z-planes and 64).
+ * With three or more z-planes per slab the first two and the last two slabs
+ * become single planes (a shorter pipeline fill and drain). */
 int gbfem_operator_set_host_chunks(gbfem_operator op, int nchunks);
 /* How gbfem_operator_apply_host moves page-locked host buffers of the
  * constant-coefficient DG kernel: 0 (default) = the slab copy pipeline;

@@ -207,6 +207,35 @@ def test_pipelined_host_apply_is_bitwise_the_device_apply(gb, orc, algorithm, pe
     assert relmax(ref, prob.apply(u)) < TOL64
 
 
+@pytest.mark.parametrize("algorithm", [0, 1])
+@pytest.mark.parametrize("periodic_z", [0, 1])
+@pytest.mark.parametrize("pinned", [False, True])
+def test_host_apply_with_tapered_slabs(gb, orc, algorithm, periodic_z, pinned):
+    """With three or more z-planes per slab the pipeline makes its first two
+    and last two slabs single planes (13 planes in 4 slabs: 1, 1, 4, 4, 1, 1,
+    1): bit for bit the device apply, through the direct path (pageable
+    buffers) and the captured graph (page-locked buffers)."""
+    cells = (3, 4, 13)
+    kw = dict(mass=0.3, velocity=(0.2, -0.4, 0.7), periodic=(0, 1, periodic_z))
+    op = gb.DGOperator(cells, 2, algorithm=algorithm, **kw)
+    op.set_host_chunks(4)
+    u = np.random.default_rng(23).uniform(-1, 1, op.size)
+    w = gb.DeviceArray(op.size)
+    op(gb.DeviceArray.from_numpy(u), w)
+    ref = w.numpy()
+    if pinned:
+        torch = pytest.importorskip("torch")
+        keep = (torch.from_numpy(u).pin_memory(), torch.empty(op.size, dtype=torch.float64).pin_memory())
+        uh, wh = keep[0].numpy(), keep[1].numpy()
+    else:
+        uh, wh = u, np.empty(op.size)
+    for _ in range(2):
+        wh[:] = np.nan
+        op.apply_host(uh, wh)
+        assert np.array_equal(wh.view(np.uint64), ref.view(np.uint64))
+    assert relmax(ref, orc.DGProblem(cells, 2, **kw).apply(u)) < TOL64
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_kappa_point_cache_follows_update_coefficients(gb, orc, precision):
     """kappa is evaluated at the Gauss points when the operator is created; a
