@@ -393,26 +393,36 @@ void destroy_host_pipe(HostPipe* p) {
 
 static int host_pipe(gbfem_operator_s* op, int nchunks, HostPipe** out) {
   if (!op->pipe) {
-    op->pipe = new (std::nothrow) HostPipe();
-    if (!op->pipe) return set_error(GBFEM_ERR_INVALID, "out of host memory");
-    HostPipe* p = op->pipe;
-    GBFEM_CUDA_TRY(cudaStreamCreateWithFlags(&p->in, cudaStreamNonBlocking));
-    GBFEM_CUDA_TRY(cudaStreamCreateWithFlags(&p->comp, cudaStreamNonBlocking));
-    GBFEM_CUDA_TRY(cudaStreamCreateWithFlags(&p->out, cudaStreamNonBlocking));
-    GBFEM_CUDA_TRY(cudaStreamCreateWithFlags(&p->tr, cudaStreamNonBlocking));
-    GBFEM_CUDA_TRY(cudaEventCreateWithFlags(&p->start, cudaEventDisableTiming));
-    for (cudaEvent_t& e : p->join) GBFEM_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    // built in full before the operator keeps it
+    HostPipe* np = new (std::nothrow) HostPipe();
+    if (!np) return set_error(GBFEM_ERR_INVALID, "out of host memory");
+    cudaError_t e = cudaStreamCreateWithFlags(&np->in, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&np->comp, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&np->out, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&np->tr, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&np->start, cudaEventDisableTiming);
+    for (cudaEvent_t& j : np->join)
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      destroy_host_pipe(np);
+      return set_cuda_error(e, "gbfem_operator_apply_host: streams");
+    }
+    op->pipe = np;
   }
   HostPipe* p = op->pipe;
-  while (int(p->ev_in.size()) < nchunks) {
-    cudaEvent_t a = nullptr, b = nullptr;
-    GBFEM_CUDA_TRY(cudaEventCreateWithFlags(&a, cudaEventDisableTiming));
-    p->ev_in.push_back(a);
-    GBFEM_CUDA_TRY(cudaEventCreateWithFlags(&b, cudaEventDisableTiming));
-    p->ev_comp.push_back(b);
-    cudaEvent_t c = nullptr;
-    GBFEM_CUDA_TRY(cudaEventCreateWithFlags(&c, cudaEventDisableTiming));
-    p->ev_tr.push_back(c);
+  while (int(p->ev_in.size()) < nchunks) {  // the three lists grow together
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    cudaError_t e = cudaSuccess;
+    for (cudaEvent_t& x : ev)
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&x, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      for (cudaEvent_t x : ev)
+        if (x) cudaEventDestroy(x);
+      return set_cuda_error(e, "gbfem_operator_apply_host: events");
+    }
+    p->ev_in.push_back(ev[0]);
+    p->ev_comp.push_back(ev[1]);
+    p->ev_tr.push_back(ev[2]);
   }
   *out = p;
   return GBFEM_OK;
