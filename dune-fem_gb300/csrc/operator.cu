@@ -430,13 +430,15 @@ static int host_pipe(gbfem_operator_s* op, int nchunks, HostPipe** out) {
 
 // Host-buffer apply of a DG operator, pipelined over slabs of whole z-planes
 // (a slab is a contiguous range of cells and dofs): the host-to-device copy
-// of slab k+1, the apply of slab k and the device-to-host copy of slab k-1
-// run at the same time on three streams.  The apply of a slab needs its
-// z-neighbours' data (their traces for the closed-form kernel, their dofs for
-// the quadrature kernel), so it is issued once the next slab has arrived; with
-// periodic z, slab 0 also needs the last slab and is applied last.  Each cell
-// is computed by the same kernel code as the one-shot apply, so the result is
-// bitwise the same.
+// of slab k+1, the trace pass of slab k+1, the apply of slab k and the
+// device-to-host copy of slab k-1 run at the same time on four streams.  The
+// apply of a slab needs its z-neighbours' data (their traces for the
+// closed-form kernel, their dofs for the quadrature kernel), so it is issued
+// once the next slab's traces exist (or it has arrived); with periodic z,
+// slab 0 also needs the last slab and is applied last.  Each cell is computed
+// by the same kernel code as the one-shot apply, so the result is bitwise the
+// same.
+
 // The device address of page-locked (registered or cudaHostAlloc'ed) host
 // memory, or nullptr for anything else.  Only such memory is ever read or
 // written by a kernel.

@@ -188,7 +188,7 @@ def test_constant_coefficient_form_with_mass_advection_anisotropic(gb, orc, orde
 @pytest.mark.parametrize("periodic_z", [0, 1])
 @pytest.mark.parametrize("chunks", [1, 2, 3, 7, 0])
 def test_pipelined_host_apply_is_bitwise_the_device_apply(gb, orc, algorithm, periodic_z, chunks):
-    """The host-buffer apply runs over slabs of z-planes on three streams; every
+    """The host-buffer apply runs over slabs of z-planes on four streams; every
     slab count (uneven splits, periodic wrap-around in z) gives the device
     apply's result bit for bit."""
     cells = (3, 4, 7)
