@@ -77,3 +77,39 @@ def test_sipg_upwind_l2_order(orc, p):
     errs = [_solve(orc, N, p) for N in (4, 8)]
     eoc = np.log(errs[0] / errs[1]) / np.log(2.0)
     assert eoc >= p + 1 - 0.1, (errs, eoc)
+
+
+def _q1_solve_error(orc, N):
+    """Config 1's form: -Lap u + u = f on the unit square, continuous Q1,
+    u = sin(pi x) sin(pi y) (zero on the boundary), diagonal-preconditioned CG."""
+    h = 1.0 / N
+    xq, wq = _rule(3)
+    pts = (np.arange(N)[:, None] + xq[None, :]) * h           # [cell][point]
+    s = np.sin(np.pi * pts)
+    hat = np.stack([1 - xq, xq], 1)                            # [point][k]
+    I = h * np.einsum("ca,a,ak->ck", s, wq, hat)               # int sin(pi x) phi_k over each cell
+    S = np.zeros(N + 1)                                        # int sin(pi x) phi_v over [0, 1]
+    S[:-1] += I[:, 0]
+    S[1:] += I[:, 1]
+    b = (2 * np.pi ** 2 + 1) * np.outer(S, S).reshape(-1)      # vertex v = vy (N + 1) + vx
+    edge = np.zeros((N + 1, N + 1), bool)
+    edge[0, :] = edge[-1, :] = edge[:, 0] = edge[:, -1] = True
+    b[edge.reshape(-1)] = 0.0                                  # Dirichlet rows: u_D = g = 0
+    cells = (N, N)
+    diag = orc.q1_apply(cells, None, 1.0, 1.0, diag_only=True)
+    it, x, res = orc.cg(lambda v: orc.q1_apply(cells, v, 1.0, 1.0), b, prec=lambda r: r / diag,
+                        epsilon=1e-12, max_iter=5000)
+    assert it >= 0, "CG did not converge (residual %g)" % res
+    U = x.reshape(N + 1, N + 1)                                # [vy][vx]
+    # bilinear u_h at the Gauss points of every cell: [cy][cx][b][a]
+    vals = sum(np.einsum("yx,b,a->yxba", U[ky:ky + N, kx:kx + N], hat[:, ky], hat[:, kx])
+               for ky in (0, 1) for kx in (0, 1))
+    exact = np.einsum("yb,xa->yxba", s, s)
+    return np.sqrt(np.sum((vals - exact) ** 2 * np.outer(wq, wq)) * h * h)
+
+
+def test_q1_l2_order(orc):
+    """Measured: L2 EOC 2.00 between 16^2 and 32^2."""
+    errs = [_q1_solve_error(orc, N) for N in (16, 32)]
+    eoc = np.log(errs[0] / errs[1]) / np.log(2.0)
+    assert eoc >= 2 - 0.1, (errs, eoc)
