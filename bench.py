@@ -133,6 +133,19 @@ def allreduce_max(x, world, device="cuda"):
     return x
 
 
+def fma_peaks():
+    """FP64 and FP32 FMA-pipe peaks (TFLOP/s) of the current GPU, from the
+    benchmark-only microbenchmark library built beside libgbfem."""
+    import ctypes as C
+    L = C.CDLL(os.path.join(ROOT, "dune-fem_gb300", "lib", "libgbfem_bench.so"))
+    L.gbfem_bench_fma_peaks.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    a, b = C.c_double(), C.c_double()
+    rc = L.gbfem_bench_fma_peaks(C.byref(a), C.byref(b))
+    if rc != 0:
+        raise RuntimeError("FMA peak microbenchmark failed: CUDA error %d" % rc)
+    return a.value, b.value
+
+
 def cpu_sample_rate(prob, u, seconds, nthreads):
     """DoF/s of the oracle apply on a bounded sample: contiguous cell ranges
     (whole z-slabs) until `seconds` of CPU work have passed."""
@@ -268,7 +281,7 @@ def run_gpu(args, world, rank, local):
     ms_f32 = time_applies(op32, u32, w32, max(3, min(args.steps, 50)), stream)
     del opq, wq, op32, u32, w32
 
-    fp64_peak, fp32_peak = gbfem.measure_fma_peaks()
+    fp64_peak, fp32_peak = fma_peaks()
     achieved_gbs = BYTES_PER_DOF * n / (ms_step * 1e-3) / 1e9
     achieved_tflops = KERNEL_FLOP_PER_DOF * n / (ms_step * 1e-3) / 1e12
     traffic = None
@@ -284,7 +297,7 @@ def run_gpu(args, world, rank, local):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform[-1,1] dofs)",
-            "config": dict(CONFIG, parallelism="replicas" if world > 1 else "single GPU"),
+            "config": CONFIG,
             "gpu_launches": 2 * args.steps,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                     "steps": e2e_steps,

@@ -184,9 +184,9 @@ int gbfem_convert(int64_t n, int px, const void* x, int py, void* y, void* strea
 
 namespace gbfem {
 
-// Dot product over fixed chunks of `chunk` elements (one partial each),
-// launched on caller-provided scratch.  Used by the allocation-free entry
-// point; gbfem_dot keeps its own partition above.
+// Dot product over chunks of `chunk` elements (one partial each), launched
+// on caller-provided scratch.  Used by the allocation-free entry point, which
+// passes gbfem_dot's chunk wherever gbfem_dot's partition has <= 1024 chunks.
 int dot_device_fixed_chunks(int precision, long long n, long long chunk, const void* x, const void* y,
                             double* d_out, double* d_partial, cudaStream_t s) {
   const long long np = (n + chunk - 1) / chunk;

@@ -21,8 +21,12 @@
 
 namespace gbfem {
 
-// Each partial sum covers a fixed chunk of 8192 elements; at most 65536
-// partials, so n <= 65536 * 8192 = 536,870,912 elements.
+// One partial sum per chunk of at most 8192 elements: np = ceil(n / 8192)
+// partials of ceil(n / np) elements each.  Up to 1024 partials this is
+// exactly gbfem_dot's partition (dot_num_partials), so for n <= 1024 * 8192
+// the two entry points return bitwise the same sum; beyond that gbfem_dot
+// stops at 1024 longer chunks and this one keeps chunks of <= 8192.  At most
+// 65536 partials, so n <= 65536 * 8192 = 536,870,912 elements.
 constexpr long long kNoAllocChunk = 8192;
 constexpr long long kNoAllocMaxPartials = 65536;
 constexpr long long kNoAllocMaxN = kNoAllocChunk * kNoAllocMaxPartials;
@@ -36,7 +40,10 @@ static std::mutex g_noalloc_mu;
 static double* g_noalloc_ptr[kMaxDevices] = {};
 
 // Device address of the scratch array on the current device, looked up
-// once per device (with that device current).
+// once per device (with that device current).  The cached address belongs to
+// the device's current context: after cudaDeviceReset the library's module is
+// loaded again and the address must not be reused, so callers that reset a
+// device must not call this entry point afterwards in the same process.
 static int noalloc_scratch(double** out) {
   int dev = 0;
   GBFEM_CUDA_TRY(cudaGetDevice(&dev));
@@ -76,7 +83,9 @@ extern "C" int gbfem_dot_noalloc(int precision, int64_t n, const void* x, const 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // Pass 1 overwrites every partial it uses and pass 2 overwrites the result
   // slot, so nothing left by an earlier call needs clearing.
-  GBFEM_TRY(dot_device_fixed_chunks(precision, n, kNoAllocChunk, x, y, res, partial, s));
+  const long long np = (n + kNoAllocChunk - 1) / kNoAllocChunk;
+  const long long chunk = (n + np - 1) / np;
+  GBFEM_TRY(dot_device_fixed_chunks(precision, n, chunk, x, y, res, partial, s));
   GBFEM_CUDA_TRY(cudaMemcpyAsync(result, res, sizeof(double), cudaMemcpyDeviceToHost, s));
   GBFEM_CUDA_TRY(cudaStreamSynchronize(s));
   return GBFEM_OK;

@@ -113,7 +113,6 @@ def lib():
         L.gbfem_dg_operator_create.argtypes = [C.POINTER(DgDesc), C.POINTER(C.c_void_p)]
         L.gbfem_q1_operator_create.argtypes = [C.POINTER(GridDesc), C.c_int, C.c_double, C.c_double,
                                                C.POINTER(C.c_void_p)]
-        L.gbfem_measure_fma_peaks.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.gbfem_operator_assemble.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
         L.gbfem_fourier_modes.argtypes = [C.c_uint64, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double)]
         L.gbfem_dg_project.argtypes = [C.POINTER(GridDesc), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
@@ -439,12 +438,6 @@ def dot(x, y, stream=None):
 
 def axpy(alpha, x, y, stream=None):
     check(lib().gbfem_axpy(x.precision, x.n, alpha, x.ptr, y.ptr, stream))
-
-
-def measure_fma_peaks():
-    a, b = C.c_double(), C.c_double()
-    check(lib().gbfem_measure_fma_peaks(C.byref(a), C.byref(b)))
-    return a.value, b.value
 
 
 class Preconditioner:

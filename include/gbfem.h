@@ -486,22 +486,22 @@ int gbfem_convert(int64_t n, int precision_x, const void* x, int precision_y, vo
 /* Allocation-free dot product.  No counterpart in the reference: it exists
  * for callers that cannot let the library allocate device memory (a host
  * whose memory pool owns all of HBM, or a latency-critical loop that cannot
- * take cudaMalloc's implicit synchronisation).  Same FP64-accumulated
- * deterministic two-pass reduction as gbfem_dot, but its partial sums live
+ * take cudaMalloc's implicit synchronisation).  FP64-accumulated
+ * deterministic two-pass reduction like gbfem_dot, but its partial sums live
  * in a fixed file-scope device array (65536 partials + a result slot, about
  * 512 KB, held by every GPU that loads the library until exit), so it calls
- * no cudaMalloc/cudaFree.  n may be at most 536,870,912 (65536 chunks of
- * 8192); larger n returns GBFEM_ERR_INVALID.  The first call on a device looks
- * up the array's device address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  All calls share
- * the one array: calls that overlap on the GPU (other streams, other host
- * threads) race and must be serialised by the caller.  Synchronises `stream`
- * and writes the result to the host double *result. */
+ * no cudaMalloc/cudaFree.  For n <= 8,388,608 (1024 chunks of 8192) it uses
+ * gbfem_dot's partition and returns bitwise the same value; for larger n its
+ * chunks stay <= 8192 elements while gbfem_dot's grow, so the two agree to
+ * rounding only.  n may be at most 536,870,912 (65536 chunks of 8192); larger
+ * n returns GBFEM_ERR_INVALID; n <= 0 writes 0.0.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current and caches it; make that first call before any stream
+ * capture, and do not call it again after a cudaDeviceReset of that device.
+ * All calls share the one array: calls that overlap on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller.
+ * Synchronises `stream` and writes the result to the host double *result. */
 int gbfem_dot_noalloc(int precision, int64_t n, const void* x, const void* y, double* result, void* stream);
-
-/* ---- microbenchmarks ---------------------------------------------------- */
-/* FP64 and FP32 FMA-pipe peaks of the current device in TFLOP/s. */
-int gbfem_measure_fma_peaks(double* fp64_tflops, double* fp32_tflops);
 
 #ifdef __cplusplus
 }

@@ -576,6 +576,69 @@ int oracle_dg_rk3_step(const int* cells, const double* lower, const double* uppe
   return 0;
 }
 
+// One SSP-RK3 step as oracle_dg_rk3_step, evaluated only where the result on
+// the z-planes [z0, z1) depends on it (a bounded sample of a large step, for
+// comparing whole planes at full grid size).  Stage i's operator is applied
+// over the target planes widened by 3 - i planes (wrapping in z when the grid
+// is periodic there, clipped otherwise): every face of a cell in the planes
+// widened by 2 - i is then owned by a cell that is applied, so those rows are
+// complete.  Same stage formulas and operation order as the full step.  u is
+// full-size; only the target planes are updated.
+int oracle_dg_rk3_step_planes(const int* cells, const double* lower, const double* upper, const int* periodic,
+                              int order, int quad, double diffusion, double penalty, double mass,
+                              const double* velocity, int weak_dirichlet, const double* kappa, double* u, double dt,
+                              int z0, int z1, int nthreads) {
+  Desc d = make_desc(cells, lower, upper, periodic, order, quad, diffusion, penalty, mass, velocity, weak_dirichlet);
+  Space S(d);
+  const int nz = cells[2];
+  if (z0 < 0 || z1 > nz || z0 >= z1) return -1;
+  const long long nxy = (long long)cells[0] * cells[1];
+  const long long per = nxy * S.nloc;  // dofs per plane
+  const long long n = S.ncells * S.nloc;
+  // planes of the target range widened by h, each once
+  auto planes = [&](int h) {
+    std::vector<int> pl;
+    std::vector<char> seen(nz, 0);
+    for (int z = z0 - h; z < z1 + h; ++z) {
+      int zz = z;
+      if (zz < 0 || zz >= nz) {
+        if (!periodic[2]) continue;
+        zz = ((zz % nz) + nz) % nz;
+      }
+      if (!seen[zz]) { seen[zz] = 1; pl.push_back(zz); }
+    }
+    return pl;
+  };
+  static const double A[3][3] = {{0, 0, 0}, {1.0, 0, 0}, {0.25, 0.25, 0}};
+  static const double b[3] = {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0};
+  std::vector<std::vector<double>> k(3, std::vector<double>(n, 0.0));
+  std::vector<double> y(n, 0.0);
+  Lockset locks(4096);
+  // out = -A(in)/|K|, complete on the planes widened by h - 1
+  auto L = [&](const double* in, double* out, int h) {
+    for (int z : planes(h))
+      run_partitioned(nxy, nthreads, [&](long long bb, long long ee) {
+        dg_apply_range(S, in, kappa, out, z * nxy + bb, z * nxy + ee, locks, nthreads > 1);
+      });
+    for (int z : planes(h - 1))
+      for (long long i = z * per; i < (z + 1) * per; ++i) out[i] *= -1.0 / S.vol;  // applyInverseMass
+  };
+  L(u, k[0].data(), 3);
+  for (int i = 1; i < 3; ++i) {
+    for (int z : planes(3 - i))
+      for (long long t = z * per; t < (z + 1) * per; ++t) {
+        double v = u[t];
+        for (int j = 0; j < i; ++j) v += A[i][j] * dt * k[j][t];
+        y[t] = v;
+      }
+    L(y.data(), k[i].data(), 3 - i);
+  }
+  for (int j = 0; j < 3; ++j)
+    for (int z = z0; z < z1; ++z)
+      for (long long t = z * per; t < (z + 1) * per; ++t) u[t] += b[j] * dt * k[j][t];
+  return 0;
+}
+
 // ---------------------------------------------------------------- Krylov --
 typedef void (*oracle_op_fn)(void* ctx, const double* x, double* y);
 

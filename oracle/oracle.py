@@ -41,6 +41,7 @@ def lib():
         L.oracle_dg_apply_cells.argtypes = dg_args + [dp, dp, C.c_longlong, C.c_longlong, C.c_int]
         L.oracle_dg_project.argtypes = [ip, dp, dp, C.c_int, C.c_int, C.c_int, dp, dp, C.c_int, C.c_int, dp]
         L.oracle_dg_rk3_step.argtypes = dg_args + [dp, C.c_double, C.c_int]
+        L.oracle_dg_rk3_step_planes.argtypes = dg_args + [dp, C.c_double, C.c_int, C.c_int, C.c_int]
         L.oracle_q1_apply.argtypes = [ip, dp, dp, C.c_double, C.c_double, dp, dp, C.c_int]
         L.oracle_cg.argtypes = [C.c_longlong, OPFN, C.c_void_p, OPFN, C.c_void_p, dp, dp, C.c_double, C.c_int,
                                 C.c_int, dp]
@@ -109,6 +110,18 @@ class DGProblem:
     def apply_cells(self, u, w, c0, c1, kappa=None, nthreads=1):
         """Adds the contributions of cells [c0, c1) to w (a bounded sample of an apply)."""
         lib().oracle_dg_apply_cells(*self._args(kappa), _dp(u), _dp(w), int(c0), int(c1), nthreads)
+
+    def rk3_step_planes(self, u, dt, z0, z1, kappa=None, nthreads=1):
+        """One SSP-RK3 step evaluated only where the z-planes [z0, z1) depend
+        on it; returns a copy of u with those planes advanced (the other
+        planes unchanged)."""
+        u = np.array(u, dtype=np.float64)
+        if kappa is not None:
+            kappa = np.ascontiguousarray(kappa, dtype=np.float64)
+        rc = lib().oracle_dg_rk3_step_planes(*self._args(kappa), _dp(u), dt, int(z0), int(z1), nthreads)
+        if rc != 0:
+            raise ValueError("rk3_step_planes: bad plane range")
+        return u
 
     def rk3_step(self, u, dt, kappa=None, nthreads=1):
         """One SSP-RK3 step of u' = -A(u)/|K| (in place on a copy; returns it)."""

@@ -8,7 +8,11 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CPP = os.path.join(ROOT, "tests", "cpp")
 LIBDIR = os.path.join(ROOT, "dune-fem_gb300", "lib")
-REF = os.environ.get("GBFEM_REFERENCE_SRC", "/root/reference")
+
+
+def _reference_src():
+    r = subprocess.run(["sh", os.path.join(ROOT, "oracle", "ref_src.sh")], capture_output=True, text=True)
+    return r.stdout.strip() if r.returncode == 0 else None
 
 
 def _compile(src, out, extra=()):
@@ -20,7 +24,8 @@ def _compile(src, out, extra=()):
 
 
 def test_reference_krylov_templates_compile_against_gpu_types(gb, tmp_path):
-    if not os.path.isdir(os.path.join(REF, "dune", "fem", "solver", "linear")):
+    REF = _reference_src()
+    if REF is None:
         pytest.skip("dune-fem sources not present")
     src = os.path.join(CPP, "ref_templates_check.cpp")
     obj = str(tmp_path / "ref_templates_check.o")

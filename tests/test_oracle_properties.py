@@ -75,3 +75,45 @@ def test_smoother_oracle_converges_as_a_stationary_iteration():
     # one Gauss-Seidel sweep is the forward substitution with the lower triangle
     y = smoother_oracle.smoother_apply(A, b, "gauss-seidel", iterations=1)
     assert np.allclose(y, np.linalg.solve(np.tril(A), b), rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("zr", [(0, 2), (3, 5), (6, 8)])
+def test_rk3_step_on_planes_equals_full_step(orc, zr):
+    """The plane-restricted SSP-RK3 step (used to compare whole planes of a
+    large grid) against the full step: periodic in z, so the first and last
+    plane ranges wrap."""
+    kw = dict(diffusion=1e-2, velocity=(1.0, 0.5, 0.25), periodic=(1, 1, 1), weak_dirichlet=False)
+    prob = orc.DGProblem((3, 4, 8), 2, **kw)
+    u = np.random.default_rng(5).uniform(-1, 1, prob.ndofs)
+    dt = 1e-3
+    full = prob.rk3_step(u, dt)
+    part = prob.rk3_step_planes(u, dt, zr[0], zr[1], nthreads=3)
+    per = 3 * 4 * 27
+    sl = slice(zr[0] * per, zr[1] * per)
+    assert relmax(part[sl], full[sl]) < 1e-14
+    rest = np.ones(prob.ndofs, bool)
+    rest[sl] = False
+    assert np.array_equal(part[rest], u[rest])
+
+
+def test_rk3_step_on_planes_non_periodic(orc):
+    prob = orc.DGProblem((3, 3, 7), 1, diffusion=0.5, mass=0.2)
+    u = np.random.default_rng(6).uniform(-1, 1, prob.ndofs)
+    full = prob.rk3_step(u, 1e-3)
+    per = 9 * 8
+    for z0, z1 in ((0, 1), (3, 4), (5, 7)):
+        part = prob.rk3_step_planes(u, 1e-3, z0, z1)
+        assert relmax(part[z0 * per:z1 * per], full[z0 * per:z1 * per]) < 1e-14
+
+
+def test_apply_on_planes_with_neighbour_planes_equals_full_apply(orc):
+    """apply_cells over the planes [z0-1, z1+1) gives complete rows on
+    [z0, z1): the sampling rule of the full-size parity tests."""
+    prob = orc.DGProblem((4, 3, 6), 2, mass=0.3)
+    u = np.random.default_rng(8).uniform(-1, 1, prob.ndofs)
+    full = prob.apply(u)
+    nxy, per = 12, 12 * 27
+    for z0, z1 in ((0, 2), (2, 4), (4, 6)):
+        w = np.zeros(prob.ndofs)
+        prob.apply_cells(u, w, max(0, z0 - 1) * nxy, min(6, z1 + 1) * nxy, nthreads=2)
+        assert relmax(w[z0 * per:z1 * per], full[z0 * per:z1 * per]) < 1e-14
