@@ -22,6 +22,8 @@ int dg_const_launch_f64(const DgArgsT<double>&, const DgConstTablesT<double>&, i
                         double* ucopy = nullptr);
 int dg_const_launch_f32(const DgArgsT<float>&, const DgConstTablesT<float>&, int, float*, int, cudaStream_t,
                         float* ucopy = nullptr);
+int dg_cell_launch_f32(const DgArgsT<float>&, const DgConstTablesT<float>&, int, cudaStream_t);
+bool dg_cell_supported(int n);
 int dg_kappa_points_f64(const double*, double*, double*, long long, const DgTablesT<double>&, int, int, cudaStream_t);
 int dg_kappa_points_f32(const float*, float*, float*, long long, const DgTablesT<float>&, int, int, cudaStream_t);
 
@@ -243,6 +245,12 @@ static int dg_apply_linear(const gbfem_operator_s* op, const void* u, void* w, c
     if (unit_mode == 0 && op->coefficient_space) {
       DgConstTablesT<float> ct = op->ctab32;
       fill_line_operators(op, &ct);
+      // the whole grid in one kernel (no trace buffer) where the cell's dofs
+      // and results fit in registers; slabs of the host pipeline and p = 4
+      // take the two-kernel form
+      if (phase == 3 && cell_begin == 0 && (cell_count == 0 || cell_count == op->ncells) && !ucopy &&
+          dg_cell_supported(op->n) && !op->two_kernel_f32)
+        return dg_cell_launch_f32(a, ct, op->n, s);
       void* tb = nullptr;
       GBFEM_TRY(trace_buffer(op, &tb));
       return dg_const_launch_f32(a, ct, op->n, static_cast<float*>(tb), phase, s, static_cast<float*>(ucopy));
@@ -715,7 +723,12 @@ int gbfem_dg_operator_create(const gbfem_dg_desc* desc, gbfem_operator* out) {
       op->cD1[i * op->n + j] = double(ct.D1[i][j]);
     }
   // q >= p+1 always holds here, so the quadrature is exact for constant kappa
-  op->coefficient_space = desc->kappa == nullptr && desc->algorithm == GBFEM_ALGO_AUTO;
+  if (desc->algorithm < GBFEM_ALGO_AUTO || desc->algorithm > GBFEM_ALGO_TRACE_PASS) {
+    delete op;
+    return set_error(GBFEM_ERR_INVALID, "gbfem_dg_operator_create: unknown algorithm");
+  }
+  op->coefficient_space = desc->kappa == nullptr && desc->algorithm != GBFEM_ALGO_QUADRATURE;
+  op->two_kernel_f32 = desc->algorithm == GBFEM_ALGO_TRACE_PASS;
   const int rc = dg_kappa_cache(op);
   if (rc) {
     gbfem_operator_destroy(op);

@@ -51,6 +51,7 @@ struct gbfem_operator_s {
   gbfem::DgConstTablesT<double> ctab64{};
   gbfem::DgConstTablesT<float> ctab32{};
   bool coefficient_space = false;  // constant-coefficient closed form (exact quadrature)
+  bool two_kernel_f32 = false;     // FP32 closed form: trace pass + apply even where one kernel applies
   double cK1[gbfem::kDgMaxN * gbfem::kDgMaxN] = {};  // 1-D stiffness int L_i' L_j'
   double cD1[gbfem::kDgMaxN * gbfem::kDgMaxN] = {};  // 1-D advection int L_i' L_j
   gbfem::Q1Element q1{};

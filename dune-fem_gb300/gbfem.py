@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libgbfem.so")
 
 F64, F32 = 0, 1
 F16 = 2  # block-Jacobi storage only (scaled FP16 blocks, FP32 vectors)
-ALGO_AUTO, ALGO_QUADRATURE = 0, 1
+ALGO_AUTO, ALGO_QUADRATURE, ALGO_TRACE_PASS = 0, 1, 2
 _DTYPES = {F64: np.float64, F32: np.float32}
 
 

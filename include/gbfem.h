@@ -80,7 +80,7 @@ typedef struct {
   double velocity[3];   /* constant advection b, upwind flux; all zero = no advection */
   int weak_dirichlet;   /* 1 = Nitsche weak u=0 on non-periodic boundary faces, 0 = do-nothing */
   const void* kappa;    /* device DG coefficients of kappa (same layout/precision) or NULL = 1 */
-  int algorithm;        /* GBFEM_ALGO_AUTO or GBFEM_ALGO_QUADRATURE (see below) */
+  int algorithm;        /* GBFEM_ALGO_AUTO, GBFEM_ALGO_QUADRATURE or GBFEM_ALGO_TRACE_PASS (see below) */
   const void* kappa_cell; /* device array of one kappa per cell (same precision), or NULL; excludes
                              kappa and velocity.  A cellwise-constant coefficient: the closed form
                              applies it exactly (as a DG kappa field with only the mean) */
@@ -90,10 +90,15 @@ typedef struct {
  * same integrals (orthonormal basis, affine cells, exact Gauss quadrature:
  * 1-D stiffness/advection matrices along lines, identity tangential face
  * mass), which equals the quadrature result up to rounding; otherwise the
- * sum-factorised quadrature kernel.  GBFEM_ALGO_QUADRATURE always evaluates
- * at the q^3 volume / q^2 face Gauss points. */
+ * sum-factorised quadrature kernel.  The closed form runs as a trace pass
+ * into an operator-owned buffer followed by the apply, except FP32 with
+ * p <= 3 over the whole grid, which is one kernel without the buffer.
+ * GBFEM_ALGO_QUADRATURE always evaluates at the q^3 volume / q^2 face Gauss
+ * points.  GBFEM_ALGO_TRACE_PASS is the closed form always in its trace-pass
+ * form. */
 #define GBFEM_ALGO_AUTO 0
 #define GBFEM_ALGO_QUADRATURE 1
+#define GBFEM_ALGO_TRACE_PASS 2
 
 typedef struct gbfem_operator_s* gbfem_operator;
 
