@@ -576,13 +576,21 @@ static int cg(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_par
   double prev = 0.0, residual = 0.0;
   GBFEM_TRY(c.dot(p, q, &residual));
   double bb = 1.0;
-  if (prm.error_measure == GBFEM_TOL_RELATIVE) GBFEM_TRY(c.dot(b, b, &bb));
+  // GBFEM_TOL_RELATIVE_RESIDUAL (not in the reference): stop on the
+  // unpreconditioned residual ||b - A x|| <= eps ||b||, with p the recursively
+  // updated residual (one more dot product per iteration with a
+  // preconditioner); the iterates are those of the reference's loop.
+  const bool true_res = prm.error_measure == GBFEM_TOL_RELATIVE_RESIDUAL;
+  if (prm.error_measure == GBFEM_TOL_RELATIVE || true_res) GBFEM_TRY(c.dot(b, b, &bb));
   const double tolerance = prm.tolerance * prm.tolerance *
-                           (prm.error_measure == GBFEM_TOL_RELATIVE ? bb
+                           (prm.error_measure == GBFEM_TOL_RELATIVE || true_res ? bb
                             : prm.error_measure == GBFEM_TOL_RESIDUAL_REDUCTION ? residual : 1.0);
+  double rr = residual;
+  if (true_res && pc) GBFEM_TRY(c.dot(p, p, &rr));
   int it = 0;
   if (!finite(residual) || !finite(tolerance)) info->status = GBFEM_ERR_NONFINITE;
-  for (it = 0; info->status == GBFEM_OK && residual > tolerance && it < prm.max_iterations; ++it) {
+  for (it = 0; info->status == GBFEM_OK && (true_res ? rr : residual) > tolerance && it < prm.max_iterations;
+       ++it) {
     if (it > 0) {
       const double beta = residual / prev;
       if (pc) GBFEM_TRY(c.axpby(1.0, s, beta, q));   // q = beta q + s
@@ -604,10 +612,12 @@ static int cg(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_par
       prev = residual;
       GBFEM_TRY(c.dot(r, r, &residual));
     }
+    rr = residual;
+    if (true_res && pc) GBFEM_TRY(c.dot(p, p, &rr));
     if (prm.verbose) std::printf("gbfem CG it: %d : residual %.6e\n", it, std::sqrt(std::fabs(residual)));
   }
-  if (!finite(residual)) info->status = GBFEM_ERR_NONFINITE;  // a NaN ends the loop above as if converged
-  info->residual = std::sqrt(std::fabs(residual));
+  if (!finite(residual) || !finite(rr)) info->status = GBFEM_ERR_NONFINITE;  // a NaN ends the loop as if converged
+  info->residual = std::sqrt(std::fabs(true_res ? rr : residual));
   info->iterations = it < prm.max_iterations ? it : -it;
   info->converged = (it < prm.max_iterations && info->status == GBFEM_OK) ? 1 : 0;
   return GBFEM_OK;
@@ -1112,17 +1122,26 @@ int solve_impl(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_pa
   *info = gbfem_solver_info{};
   const auto t0 = std::chrono::steady_clock::now();
   int rc;
+  if (prm.error_measure < GBFEM_TOL_ABSOLUTE || prm.error_measure > GBFEM_TOL_RELATIVE_RESIDUAL)
+    return set_error(GBFEM_ERR_INVALID, "gbfem_solve: unknown error measure");
+  // the other methods already stop on the unpreconditioned residual
+  gbfem_solver_params pr = prm;
+  if (prm.method != GBFEM_SOLVER_CG && pr.error_measure == GBFEM_TOL_RELATIVE_RESIDUAL)
+    pr.error_measure = GBFEM_TOL_RELATIVE;
   switch (prm.method) {
     case GBFEM_SOLVER_CG:
       // device-resident loop unless the preconditioner is external (its apply
-      // may synchronise the host, which a graph capture cannot hold)
-      rc = (prm.graph_chunk > 0 && !(pc && pc->kind == PcKind::External)) ? cg_device(op, pc, prm, f, u, c, info)
-                                                                          : cg(op, pc, prm, f, u, c, info);
+      // may synchronise the host, which a graph capture cannot hold) or the
+      // stop is on the unpreconditioned residual (host loop)
+      rc = (pr.graph_chunk > 0 && !(pc && pc->kind == PcKind::External) &&
+            pr.error_measure != GBFEM_TOL_RELATIVE_RESIDUAL)
+               ? cg_device(op, pc, pr, f, u, c, info)
+               : cg(op, pc, pr, f, u, c, info);
       break;
-    case GBFEM_SOLVER_GMRES: rc = gmres(op, pc, prm, f, u, c, info, false); break;
-    case GBFEM_SOLVER_FGMRES: rc = gmres(op, pc, prm, f, u, c, info, true); break;
-    case GBFEM_SOLVER_BICGSTAB: rc = bicgstab(op, pc, prm, f, u, c, info); break;
-    case GBFEM_SOLVER_FCG: rc = fcg(op, pc, prm, f, u, c, info); break;
+    case GBFEM_SOLVER_GMRES: rc = gmres(op, pc, pr, f, u, c, info, false); break;
+    case GBFEM_SOLVER_FGMRES: rc = gmres(op, pc, pr, f, u, c, info, true); break;
+    case GBFEM_SOLVER_BICGSTAB: rc = bicgstab(op, pc, pr, f, u, c, info); break;
+    case GBFEM_SOLVER_FCG: rc = fcg(op, pc, pr, f, u, c, info); break;
     default: return set_error(GBFEM_ERR_INVALID, "gbfem_solve: unknown method " + std::to_string(prm.method));
   }
   GBFEM_CUDA_TRY(cudaStreamSynchronize(s));

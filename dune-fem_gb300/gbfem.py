@@ -77,7 +77,7 @@ NEWTON_FAILURES = {0: "Success", 1: "InvalidResidual", 4: "LineSearchFailed", 5:
                    6: "TooManyLinearIterations", 7: "LinearSolverFailed"}
 
 CG, GMRES, BICGSTAB, FCG, FGMRES = 0, 1, 2, 3, 4
-ABSOLUTE, RELATIVE, RESIDUAL_REDUCTION = 0, 1, 2
+ABSOLUTE, RELATIVE, RESIDUAL_REDUCTION, RELATIVE_RESIDUAL = 0, 1, 2, 3
 METHODS = {"cg": CG, "gmres": GMRES, "bicgstab": BICGSTAB, "fcg": FCG, "fgmres": FGMRES}
 
 _lib = None

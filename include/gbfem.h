@@ -227,10 +227,18 @@ int gbfem_preconditioner_destroy(gbfem_preconditioner pc);
 #define GBFEM_SOLVER_FCG 3
 #define GBFEM_SOLVER_FGMRES 4
 
-/* LinearSolver::ToleranceCriteria (solver/parameter.hh:14-17) */
+/* LinearSolver::ToleranceCriteria (solver/parameter.hh:14-17).  As in the
+ * reference, preconditioned CG measures the residual in the preconditioner's
+ * norm <r, B r> (solver/linear/cg.hh:62-67); GBFEM_TOL_RELATIVE_RESIDUAL (an
+ * addition, no counterpart in the reference) makes CG stop on the
+ * unpreconditioned ||b - A x|| <= tolerance ||b|| instead (one more dot
+ * product per iteration, same iterates; host loop).  The other methods
+ * measure the unpreconditioned residual already and treat it as
+ * GBFEM_TOL_RELATIVE. */
 #define GBFEM_TOL_ABSOLUTE 0
 #define GBFEM_TOL_RELATIVE 1
 #define GBFEM_TOL_RESIDUAL_REDUCTION 2
+#define GBFEM_TOL_RELATIVE_RESIDUAL 3
 
 typedef struct {
   int method;          /* GBFEM_SOLVER_* (fem.solver.method) */

@@ -368,3 +368,39 @@ def test_scaled_block_jacobi_for_cellwise_kappa(gb, orc, cells, periodic):
     gb.Preconditioner.scaled_block_jacobi(const)(gb.DeviceArray.from_numpy(r, gb.F32), z1)
     gb.Preconditioner.block_jacobi(const)(gb.DeviceArray.from_numpy(r, gb.F32), z2)
     assert relmax(z1.numpy(), z2.numpy()) < 2e-5
+
+
+def test_cg_true_residual_criterion(gb, orc):
+    """GBFEM_TOL_RELATIVE_RESIDUAL: block-Jacobi CG stops on the recursively
+    updated ||f - A u|| <= eps ||f|| (the reference's CG stops on <r, B r>);
+    the iterates are those of the reference's loop, so both criteria give
+    bitwise the same u after the same number of iterations."""
+    cells, order = (4, 4, 4), 2
+    nloc, ncell = (order + 1) ** 3, 64
+    rng = np.random.default_rng(5)
+    kappa = np.zeros(ncell * nloc)
+    kappa[::nloc] = np.exp(rng.uniform(-1.5, 1.5, ncell))  # positive cell means
+    kappa += 0.02 * rng.uniform(-1, 1, ncell * nloc)       # small variation inside the cells
+    op = gb.DGOperator(cells, order, kappa=gb.DeviceArray.from_numpy(kappa))
+    pc = gb.Preconditioner.block_jacobi(op)
+    f = np.random.default_rng(9).uniform(-1, 1, op.size)
+    info, u = _solve(gb, op, f, "cg", pc, tol=1e-10, error_measure=gb.RELATIVE_RESIDUAL)
+    assert info["converged"]
+    au = gb.DeviceArray(op.size)
+    op(gb.DeviceArray.from_numpy(u), au)
+    true_rel = np.linalg.norm(f - au.numpy()) / np.linalg.norm(f)
+    assert true_rel <= 1e-9  # the recursive residual may drift from f - A u by rounding
+    assert info["residual"] <= 1e-10 * np.linalg.norm(f)
+    i0, _ = _solve(gb, op, f, "cg", pc, tol=1e-10, error_measure=gb.RELATIVE)
+    assert i0["converged"] and 0 < i0["iterations"] <= info["iterations"]
+    k = max(1, info["iterations"] // 2)
+    i1, u1 = _solve(gb, op, f, "cg", pc, tol=1e-30, error_measure=gb.RELATIVE_RESIDUAL, max_iterations=k)
+    i2, u2 = _solve(gb, op, f, "cg", pc, tol=1e-30, error_measure=gb.RELATIVE, max_iterations=k)
+    assert i1["iterations"] == i2["iterations"] == -k
+    assert np.array_equal(u1.view(np.uint64), u2.view(np.uint64))
+
+
+def test_unknown_error_measure_is_rejected(gb, orc):
+    op, prob, f = _problem(gb, orc)
+    with pytest.raises(gb.GbfemError):
+        _solve(gb, op, f, "cg", error_measure=7)
