@@ -1,11 +1,13 @@
 #!/bin/sh
 # Compiles the reference's standalone-buildable sources for this path
 # (Gauss rules, Legendre tables, CG/GMRES/BiCGstab templates) with the driver
-# oracle/ref_driver.cpp into oracle/_ref/, runs it, and writes the golden
-# vectors tests/golden/ref_tables.json and tests/golden/ref_krylov.json.
+# oracle/ref_driver.cpp (with the oracle's operator, oracle.cpp) into
+# oracle/_ref/, runs it, and writes the golden vectors
+# tests/golden/ref_tables.json, ref_krylov.json and ref_krylov_sipg.json.
 # Needs the dune-fem source tree (located by ref_src.sh); without it this
-# recipe does nothing (the committed golden vectors stay as they are).  The
-# reference's own build system is not used.
+# recipe does nothing (the committed golden vectors stay as they are).  With
+# --compile-only it builds the driver and writes nothing.  The reference's
+# own build system is not used.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 if ! REF=$(sh "$HERE/ref_src.sh"); then
@@ -16,9 +18,14 @@ OUT="$HERE/_ref"
 GOLD="$HERE/../tests/golden"
 mkdir -p "$OUT" "$GOLD"
 CXX=${CXX:-g++}
-$CXX -O2 -std=c++17 -I"$HERE/shim" -I"$REF" \
-  "$HERE/ref_driver.cpp" "$REF/dune/fem/space/shapefunctionset/legendrepolynomials.cc" \
+$CXX -O2 -std=c++17 -pthread -I"$HERE/shim" -I"$REF" \
+  "$HERE/ref_driver.cpp" "$HERE/oracle.cpp" "$REF/dune/fem/space/shapefunctionset/legendrepolynomials.cc" \
   -o "$OUT/ref_driver"
+if [ "$1" = "--compile-only" ]; then
+  echo "built $OUT/ref_driver"
+  exit 0
+fi
 "$OUT/ref_driver" tables > "$GOLD/ref_tables.json"
 "$OUT/ref_driver" krylov > "$GOLD/ref_krylov.json"
-echo "wrote $GOLD/ref_tables.json $GOLD/ref_krylov.json"
+"$OUT/ref_driver" sipg > "$GOLD/ref_krylov_sipg.json"
+echo "wrote $GOLD/ref_tables.json $GOLD/ref_krylov.json $GOLD/ref_krylov_sipg.json"

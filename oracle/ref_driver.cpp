@@ -7,6 +7,8 @@
 //   dune/fem/quadrature/gausspoints.hh (+ _implementation.hh)  -> Gauss rules
 //   dune/fem/space/shapefunctionset/legendrepolynomials.{hh,cc} -> Legendre tables
 //   dune/fem/solver/linear/{cg,gmres,bicgstab}.hh               -> Krylov iterates
+// The "sipg" mode runs those Krylov templates over the oracle's DG SIPG
+// operator (oracle.cpp, linked in) on an 8^3 Q2 grid.
 // against the minimal shims in oracle/shim (visibility macros, FieldTraits,
 // ToleranceCriteria).  The vector type below provides the discrete-function
 // subset those templates call.
@@ -101,6 +103,111 @@ void print_vec(const char* name, const std::vector<double>& v, bool last = false
 
 }  // namespace refdrv
 
+// The oracle's DG operator (oracle.cpp, linked in): the SIPG systems on which
+// the reference's Krylov templates run in the "sipg" mode below.
+extern "C" int oracle_dg_apply(const int* cells, const double* lower, const double* upper, const int* periodic,
+                               int order, int quad, double diffusion, double penalty, double mass,
+                               const double* velocity, int weak_dirichlet, const double* kappa, const double* u,
+                               double* w, int nthreads);
+extern "C" int oracle_dg_block_diagonal(const int* cells, const double* lower, const double* upper,
+                                        const int* periodic, int order, int quad, double diffusion, double penalty,
+                                        double mass, const double* velocity, int weak_dirichlet, const double* kappa,
+                                        double* blocks, int nthreads);
+
+namespace refdrv {
+
+// 8^3 DG Q2 on the unit cube, q = p + 2, penalty 10 (p+1)^2, weak u = 0.
+struct SipgCase {
+  int cells[3] = {8, 8, 8};
+  double lower[3] = {0, 0, 0}, upper[3] = {1, 1, 1};
+  int periodic[3] = {0, 0, 0};
+  int order = 2, quad = 4;
+  double diffusion = 1.0, penalty = 90.0, mass = 0.0;
+  double velocity[3] = {0, 0, 0};
+  size_t ndofs() const { return size_t(cells[0]) * cells[1] * cells[2] * 27; }
+  void apply(const std::vector<double>& x, std::vector<double>& y) const {
+    oracle_dg_apply(cells, lower, upper, periodic, order, quad, diffusion, penalty, mass, velocity, 1, nullptr,
+                    x.data(), y.data(), 1);
+  }
+  std::vector<double> diagonal() const {
+    const size_t nc = size_t(cells[0]) * cells[1] * cells[2];
+    std::vector<double> blocks(nc * 27 * 27), d(nc * 27);
+    oracle_dg_block_diagonal(cells, lower, upper, periodic, order, quad, diffusion, penalty, mass, velocity, 1,
+                             nullptr, blocks.data(), 1);
+    for (size_t c = 0; c < nc; ++c)
+      for (int i = 0; i < 27; ++i) d[c * 27 + i] = blocks[(c * 27 + i) * 27 + i];
+    return d;
+  }
+};
+
+// Every 97th entry of x, its 2-norm and its sum: enough to pin an iterate of
+// 13,824 values in a small file.
+void print_sample(const char* name, const std::vector<double>& x, bool last = false) {
+  double n2 = 0, sm = 0;
+  for (double v : x) { n2 += v * v; sm += v; }
+  std::printf("  \"%s\": {\"norm2\": %.17g, \"sum\": %.17g, \"every97\": [", name, std::sqrt(n2), sm);
+  for (size_t i = 0; i < x.size(); i += 97) std::printf("%s%.17g", i ? ", " : "", x[i]);
+  std::printf("]}%s\n", last ? "" : ",");
+}
+
+int run_sipg() {
+  SipgCase sym;
+  SipgCase adv;
+  adv.diffusion = 0.1;
+  adv.mass = 1.0;
+  adv.velocity[0] = 1.0;
+  adv.velocity[1] = 0.5;
+  adv.velocity[2] = 0.25;
+  const size_t n = sym.ndofs();
+  SpaceT sp;
+  sp.aux.n = n;
+  Vec b(sp, n);
+  for (size_t i = 0; i < n; ++i) b.d[i] = std::sin(0.37 * double(i) + 0.2);
+  Op A{[&](const std::vector<double>& x, std::vector<double>& y) { sym.apply(x, y); }};
+  Op N{[&](const std::vector<double>& x, std::vector<double>& y) { adv.apply(x, y); }};
+  const std::vector<double> dg = sym.diagonal();
+  // the diagonal preconditioner (solver/diagonalpreconditioner.hh: 1/diag)
+  Op D{[&](const std::vector<double>& x, std::vector<double>& y) {
+    for (size_t i = 0; i < x.size(); ++i) y[i] = x[i] / dg[i];
+  }};
+  const int rel = Dune::Fem::LinearSolver::ToleranceCriteria::relative;
+  std::printf("{\n  \"problem\": \"8^3 DG Q2, q = 4, penalty 90, weak u = 0; b_i = sin(0.37 i + 0.2); "
+              "gmres, bicgstab: diffusion 0.1, mass 1, velocity (1, 0.5, 0.25)\",\n  \"n\": %zu,\n", n);
+  {
+    std::vector<Vec> tmp(3, Vec(sp, n));
+    Vec x(sp, n);
+    int it = Dune::Fem::LinearSolver::cg(A, (Op*)nullptr, tmp, x, b, 1e-10, 5000, rel);
+    std::printf("  \"cg_iterations\": %d,\n", it);
+    print_sample("cg_x", x.d);
+  }
+  {
+    std::vector<Vec> tmp(5, Vec(sp, n));
+    Vec x(sp, n);
+    int it = Dune::Fem::LinearSolver::cg(A, &D, tmp, x, b, 1e-10, 5000, rel);
+    std::printf("  \"diag_pcg_iterations\": %d,\n", it);
+    print_sample("diag_pcg_x", x.d);
+  }
+  {
+    const int m = 20;
+    std::vector<Vec> v(m + 1, Vec(sp, n));
+    Vec x(sp, n);
+    int it = Dune::Fem::LinearSolver::gmres(N, (Op*)nullptr, v, x, b, m, 1e-10, 5000, rel);
+    std::printf("  \"gmres_restart\": %d,\n  \"gmres_iterations\": %d,\n", m, it);
+    print_sample("gmres_x", x.d);
+  }
+  {
+    std::vector<Vec> v(5, Vec(sp, n));
+    Vec x(sp, n);
+    int it = Dune::Fem::LinearSolver::bicgstab(N, (Op*)nullptr, v, x, b, 1e-10, 5000, rel);
+    std::printf("  \"bicgstab_iterations\": %d,\n", it);
+    print_sample("bicgstab_x", x.d, true);
+  }
+  std::printf("}\n");
+  return 0;
+}
+
+}  // namespace refdrv
+
 int main(int argc, char** argv) {
   using namespace refdrv;
   const std::string what = argc > 1 ? argv[1] : "tables";
@@ -133,6 +240,7 @@ int main(int argc, char** argv) {
     std::printf("]\n  }\n}\n");
     return 0;
   }
+  if (what == "sipg") return run_sipg();
   // Krylov golden vectors
   const size_t n = 60;
   SpaceT sp;
