@@ -909,6 +909,32 @@ def workload_apply_kappa(args):
     return out
 
 
+def workload_apply_f32(args):
+    """The constant-coefficient FP32 apply (cells^3, Q_order) alone, --steps
+    times after 3 warm-up applies, with no other GPU work: the command the
+    kernel profiles under profiles/ are taken from.  --algorithm 0 is the
+    default (one kernel for p <= 3), 2 the two-kernel trace-pass form;
+    --kappa-cell uses a seeded kappa per cell."""
+    import gbfem
+    import torch
+    N, p = args.cells, args.order
+    cells = (N, N, N)
+    kc = None
+    if args.kappa_cell:
+        kc = gbfem.DeviceArray.from_numpy(
+            np.exp(np.random.default_rng(args.seed).uniform(-2, 2, N ** 3)).astype(np.float32))
+    op = gbfem.DGOperator(cells, p, precision=gbfem.F32, algorithm=args.algorithm, kappa_cell=kc)
+    u = gbfem.DeviceArray.from_numpy(np.random.default_rng(SEED).uniform(-1, 1, op.size).astype(np.float32))
+    w = gbfem.DeviceArray(op.size, gbfem.F32)
+    stream = torch.cuda.current_stream()
+    ms = time_applies(op, u, w, max(1, args.steps), stream)
+    return {"metric": "FP32 SIPG apply DoF/s", "unit": "DoF/s", "higher_is_better": True,
+            "value": op.size / (ms * 1e-3), "ms_per_step": ms, "dtype": "f32",
+            "hbm_frac_8B_per_dof": 8.0 * op.size / (ms * 1e-3) / 1e9 / load_peaks()[0]["hbm_gbs"],
+            "config": {"workload": "SIPG Q%d %d^3 FP32 apply, algorithm %d%s" %
+                                   (p, N, args.algorithm, ", kappa per cell" if kc is not None else "")}}
+
+
 def workload_newton(args):
     """Bratu problem -lap u = lambda e^u (lambda = 5, SIPG Q2, weak u = 0) on
     cells^3 by Newton with block-Jacobi CG for each Jacobian; with and without
@@ -966,7 +992,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gbfem", choices=["gbfem", "reference"])
     ap.add_argument("--workload", default="apply",
-                    choices=["apply", "q1cg", "rk3", "mixed", "learned", "kernels", "newton", "apply_kappa"])
+                    choices=["apply", "q1cg", "rk3", "mixed", "learned", "kernels", "newton", "apply_kappa",
+                             "apply_f32"])
     ap.add_argument("--rk-steps", type=int, default=100)
     ap.add_argument("--cells", type=int, default=96)
     ap.add_argument("--order", type=int, default=3)
@@ -990,11 +1017,13 @@ def main():
     ap.add_argument("--plain-max-iter", type=int, default=0)
     ap.add_argument("--verbose", action="store_true")
     ap.add_argument("--no-solve", action="store_true", help="skip the solve comparison of the headline line")
+    ap.add_argument("--algorithm", type=int, default=0)
+    ap.add_argument("--kappa-cell", action="store_true")
     args = ap.parse_args()
     if args.workload != "apply":
         fn = {"q1cg": workload_q1cg, "rk3": workload_rk3, "mixed": workload_mixed,
               "learned": workload_learned, "kernels": workload_kernels, "newton": workload_newton,
-              "apply_kappa": workload_apply_kappa}[args.workload]
+              "apply_kappa": workload_apply_kappa, "apply_f32": workload_apply_f32}[args.workload]
         line = fn(args)
         line.update({"n_gpus": 1, "data": "synthetic"})
         print(json.dumps(line), flush=True)
