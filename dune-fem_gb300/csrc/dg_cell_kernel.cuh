@@ -7,23 +7,27 @@
 // registers (n <= 4: 128 registers at Q3).  A face's numerical flux is
 // computed once and exchanged through shared memory, which holds one slot per
 // face of the brick ((8+1) 4 4 + 8 (4+1) 4 + 8 4 (4+1) = 464 slots of 2 n^2
-// values, 66.8 KB at Q3, three CTAs per SM):
+// values) plus one per face on the brick's lower boundary (80; 69.6 KB at Q3,
+// three CTAs per SM).  Slots are 128-byte rows whose 16-byte chunks are
+// XOR-swizzled by the slot index, so lanes at consecutive slots read
+// distinct banks without padding.
 //  0. every thread loads its cell's dofs (float4 loads where the cell's block
-//     is 16-byte aligned).  Halo items, spread over the threads: for each face
-//     on the brick's lower boundary, the flux from the cell below the brick
-//     (or the boundary terms) and the brick cell's dofs; for each face on the
-//     upper boundary, the lower-face traces of the cell above.  This is the
-//     only extra traffic: 2 (8*4 + 8*4 + 4*4) halo cells per 128, through L2;
+//     is 16-byte aligned).  Halo items, spread over the threads, load the
+//     brick's face neighbours outside it (2 (8*4 + 8*4 + 4*4) cells per 128,
+//     read through L2 -- the only traffic besides u and w) and write the
+//     trace of each one's face that touches the brick into that face's slot;
 //  1. every cell writes the two traces (v, P) of its lower face along each
-//     axis into that face's slot, unless the face is on the brick's lower
-//     boundary (that slot already holds the flux);
+//     axis into that face's slot, or, on the brick's lower boundary, into the
+//     boundary slot;
 //  2. every cell computes the flux of its upper face along each axis from its
-//     own traces and the slot (the upper neighbour's traces), and overwrites
-//     the slot with (Val, G) as seen from the face's lower cell.  The upper
-//     cell of a face reads the same numbers negated: the interior fluxes are
-//     odd in the two sides' traces (Val(-, +) = -Val(+, -), J likewise), which
-//     holds exactly in floating point because rounding is symmetric; a
-//     boundary face's terms are stored negated where the cell is the upper one;
+//     own traces and the slot (its upper neighbour's traces) and overwrites
+//     the slot with (Val, G) as seen from the face's lower cell; boundary items
+//     do the same for the brick's lower faces from the halo and boundary
+//     slots.  The upper cell of a face reads the numbers negated: the interior
+//     fluxes are odd in the two sides' traces (Val(-, +) = -Val(+, -), J
+//     likewise), which holds exactly in floating point because rounding is
+//     symmetric; a domain-boundary face's terms are stored negated where the
+//     cell is the upper one;
 //  3. one pass per axis over the cell's lines applies the 1-D line operator
 //     and the face expansion (the same formulas and summation order as
 //     dg_const_kernel's line pass), accumulating in registers;
@@ -44,12 +48,14 @@ template <int N>
 struct CellSlots {
   static constexpr int N2 = N * N;
   static constexpr int H = (N2 + 3) / 4 * 4;  // floats per half slot (v or Val | P or G), float4-aligned
-  static constexpr int STRIDE = 2 * H + 4;    // an odd number of float4s: lanes at consecutive slots hit
-                                              // distinct banks with 16-byte accesses
+  static constexpr int Q = H / 2;             // float4 chunks in use per slot
+  static constexpr int QS = Q <= 2 ? 2 : (Q <= 4 ? 4 : 8);  // chunks per slot (a power of two)
   static constexpr int NX = (kCellBX + 1) * kCellBY * kCellBZ;
   static constexpr int NY = kCellBX * (kCellBY + 1) * kCellBZ;
   static constexpr int NZ = kCellBX * kCellBY * (kCellBZ + 1);
-  static constexpr int FLOATS = (NX + NY + NZ) * STRIDE;
+  static constexpr int NFACE = NX + NY + NZ;
+  static constexpr int NBND = kCellBY * kCellBZ + kCellBX * kCellBZ + kCellBX * kCellBY;  // lower boundary
+  static constexpr int FLOATS = (NFACE + NBND) * QS * 4;
   static constexpr size_t BYTES = size_t(FLOATS) * sizeof(float);
 };
 
@@ -62,6 +68,22 @@ __device__ __forceinline__ int cell_slot(int d, int f, int la, int lb) {
   if (d == 0) return f + (kCellBX + 1) * (la + kCellBY * lb);
   if (d == 1) return S::NX + la + kCellBX * (f + (kCellBY + 1) * lb);
   return S::NX + S::NY + la + kCellBX * (lb + kCellBY * f);
+}
+
+// Boundary slot of the brick cell's lower face along d (its lower traces).
+template <int N>
+__device__ __forceinline__ int cell_bnd_slot(int d, int la, int lb) {
+  using S = CellSlots<N>;
+  if (d == 0) return S::NFACE + la + kCellBY * lb;
+  if (d == 1) return S::NFACE + kCellBY * kCellBZ + la + kCellBX * lb;
+  return S::NFACE + kCellBY * kCellBZ + kCellBX * kCellBZ + la + kCellBX * lb;
+}
+
+// Address of logical chunk q of slot s (XOR swizzle within the slot).
+template <int N>
+__device__ __forceinline__ float4* cell_chunk(float* slots, int s, int q) {
+  using S = CellSlots<N>;
+  return reinterpret_cast<float4*>(slots) + s * S::QS + (q ^ (s & (S::QS - 1)));
 }
 
 // Offset of value i of tangential line jk (= j n + k) along axis D within a
@@ -129,8 +151,8 @@ __device__ __forceinline__ void cell_interior_flux(const float (&vm)[N * N], con
 // the cell's own traces on it; stored negated when it is the cell's lower
 // face (the slot convention: as seen from the face's lower side).
 template <int N, bool ADV, bool KC, int D>
-__device__ __forceinline__ void cell_boundary_flux(bool upper, const float (&vo)[N * N], const float (&po)[N * N],
-                                                   float kc, const DgArgsT<float>& args,
+__device__ __forceinline__ void cell_boundary_flux(bool upper, const float (&vo)[N * N],
+                                                   const float (&po)[N * N], float kc, const DgArgsT<float>& args,
                                                    const DgConstTablesT<float>& tabs, float (&val)[N * N],
                                                    float (&G)[N * N]) {
   const float bn = upper ? args.b[D] : -args.b[D];
@@ -148,9 +170,10 @@ __device__ __forceinline__ void cell_boundary_flux(bool upper, const float (&vo)
   }
 }
 
-// Writes a[0..N2) and b[0..N2) into a slot (float4 stores, zero padding).
+// Writes a[0..N2) and b[0..N2) into slot s (float4 stores, zero padding).
 template <int N>
-__device__ __forceinline__ void cell_store_slot(float* slot, const float (&a)[N * N], const float (&b)[N * N]) {
+__device__ __forceinline__ void cell_store_slot(float* slots, int s, const float (&a)[N * N],
+                                                const float (&b)[N * N]) {
   constexpr int N2 = N * N, H = CellSlots<N>::H;
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
@@ -162,20 +185,20 @@ __device__ __forceinline__ void cell_store_slot(float* slot, const float (&a)[N 
       t.y = 4 * q + 1 < N2 ? src[4 * q + 1] : 0.f;
       t.z = 4 * q + 2 < N2 ? src[4 * q + 2] : 0.f;
       t.w = 4 * q + 3 < N2 ? src[4 * q + 3] : 0.f;
-      *reinterpret_cast<float4*>(slot + h * H + 4 * q) = t;
+      *cell_chunk<N>(slots, s, h * (H / 4) + q) = t;
     }
   }
 }
 
 template <int N>
-__device__ __forceinline__ void cell_load_slot(const float* slot, float (&a)[N * N], float (&b)[N * N]) {
+__device__ __forceinline__ void cell_load_slot(float* slots, int s, float (&a)[N * N], float (&b)[N * N]) {
   constexpr int N2 = N * N, H = CellSlots<N>::H;
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     float* dst = h ? b : a;
 #pragma unroll
     for (int q = 0; q < H / 4; ++q) {
-      const float4 t = *reinterpret_cast<const float4*>(slot + h * H + 4 * q);
+      const float4 t = *cell_chunk<N>(slots, s, h * (H / 4) + q);
       if (4 * q + 0 < N2) dst[4 * q + 0] = t.x;
       if (4 * q + 1 < N2) dst[4 * q + 1] = t.y;
       if (4 * q + 2 < N2) dst[4 * q + 2] = t.z;
@@ -212,56 +235,82 @@ struct CellBrick {
   long long stride[3];
 };
 
-// One halo item: the face at the brick's lower (upper = false) or upper
-// boundary normal to D, at brick-local coordinates (la, lb) of the other two
-// axes.  Lower: the flux (from the cell below, or the boundary terms) into
-// slot 0; upper: the traces of the cell above into slot e_D.
-template <int N, bool ADV, bool KC, int D>
-__device__ __forceinline__ void cell_halo_item(bool upper, int la, int lb, const CellBrick& B,
-                                               const DgArgsT<float>& args, const DgConstTablesT<float>& tabs,
-                                               float* slots) {
-  constexpr int N2 = N * N, N3 = N2 * N;
+// The face neighbour of brick-boundary position (D, la, lb) below (upper =
+// false) or above the brick; false where the domain ends there.
+template <int D>
+__device__ __forceinline__ bool cell_halo_neighbour(bool upper, int la, int lb, const CellBrick& B,
+                                                    const DgArgsT<float>& args, long long* hcell, long long* bcell) {
   constexpr int A = D == 0 ? 1 : 0, Bx = D == 2 ? 1 : 2;  // the other axes, increasing
-  int g = upper ? B.o[D] + B.e[D] : B.o[D] - 1;
-  bool has_nb = true;
-  if (g < 0 || g >= B.nc[D]) {
-    if (args.periodic[D]) g = (g + B.nc[D]) % B.nc[D];
-    else has_nb = false;
-  }
   const long long tang = (long long)(B.o[A] + la) * B.stride[A] + (long long)(B.o[Bx] + lb) * B.stride[Bx];
-  const long long hcell = tang + (long long)g * B.stride[D];
-  float* sl = slots + cell_slot<N>(D, upper ? B.e[D] : 0, la, lb) * CellSlots<N>::STRIDE;
-  float a[N2], b[N2];
-  if (upper) {
-    if (!has_nb) return;  // the brick cell below handles the boundary face
-    float x[N3];
-    cell_load_dofs<N>(args.u + hcell * N3, x);
-    cell_traces<N, KC, D>(x, false, tabs, a, b);
-    cell_store_slot<N>(sl, a, b);
-    return;
+  *bcell = tang + (long long)(upper ? B.o[D] + B.e[D] - 1 : B.o[D]) * B.stride[D];
+  int g = upper ? B.o[D] + B.e[D] : B.o[D] - 1;
+  if (g < 0 || g >= B.nc[D]) {
+    if (!args.periodic[D]) return false;
+    g = (g + B.nc[D]) % B.nc[D];
   }
-  // the brick cell on the lower boundary: its lower-face traces
-  const long long bcell = tang + (long long)B.o[D] * B.stride[D];
-  float vo[N2], po[N2];
-  {
-    float x[N3];
-    cell_load_dofs<N>(args.u + bcell * N3, x);
-    cell_traces<N, KC, D>(x, false, tabs, vo, po);
-  }
+  *hcell = tang + (long long)g * B.stride[D];
+  return true;
+}
+
+// Phase 0 item: the trace of the halo cell's face towards the brick (its
+// upper face below the brick, into slot 0; its lower face above, into slot
+// e_D).
+template <int N, bool KC, int D>
+__device__ __forceinline__ void cell_halo_traces(bool upper, int la, int lb, const CellBrick& B,
+                                                 const DgArgsT<float>& args, const DgConstTablesT<float>& tabs,
+                                                 float* slots) {
+  constexpr int N2 = N * N, N3 = N2 * N;
+  long long hcell, bcell;
+  if (!cell_halo_neighbour<D>(upper, la, lb, B, args, &hcell, &bcell)) return;
+  float x[N3], a[N2], b[N2];
+  cell_load_dofs<N>(args.u + hcell * N3, x);
+  cell_traces<N, KC, D>(x, !upper, tabs, a, b);
+  cell_store_slot<N>(slots, cell_slot<N>(D, upper ? B.e[D] : 0, la, lb), a, b);
+}
+
+// Phase 2 item: the flux through the brick's lower face at (D, la, lb) from
+// the halo cell's upper traces (slot 0) and the brick cell's lower traces
+// (its boundary slot), or the domain-boundary terms; into slot 0.
+template <int N, bool ADV, bool KC, int D>
+__device__ __forceinline__ void cell_lower_flux(int la, int lb, const CellBrick& B, const DgArgsT<float>& args,
+                                                const DgConstTablesT<float>& tabs, float* slots) {
+  constexpr int N2 = N * N;
+  long long hcell, bcell;
+  const bool has_nb = cell_halo_neighbour<D>(false, la, lb, B, args, &hcell, &bcell);
+  const int s0 = cell_slot<N>(D, 0, la, lb);
+  float vo[N2], po[N2], a[N2], b[N2];
+  cell_load_slot<N>(slots, cell_bnd_slot<N>(D, la, lb), vo, po);
   const float kb = KC ? __ldg(args.kcell + bcell) : 0.f;
   if (has_nb) {
     float vh[N2], ph[N2];
-    {
-      float x[N3];
-      cell_load_dofs<N>(args.u + hcell * N3, x);
-      cell_traces<N, KC, D>(x, true, tabs, vh, ph);
-    }
+    cell_load_slot<N>(slots, s0, vh, ph);
     const float kh = KC ? __ldg(args.kcell + hcell) : 0.f;
     cell_interior_flux<N, ADV, KC, D>(vh, ph, vo, po, kh, kb, args, tabs, a, b);
   } else {
     cell_boundary_flux<N, ADV, KC, D>(false, vo, po, kb, args, tabs, a, b);
   }
-  cell_store_slot<N>(sl, a, b);
+  cell_store_slot<N>(slots, s0, a, b);
+}
+
+// The r-th face on the brick's lower (or upper) boundary: its axis D and
+// brick-local coordinates (la, lb); c0, c1 are the counts of the x and y
+// faces.
+__device__ __forceinline__ int cell_boundary_face(int r, int c0, int c1, const CellBrick& B, int* la, int* lb) {
+  if (r < c0) {
+    *la = r % B.e[1];
+    *lb = r / B.e[1];
+    return 0;
+  }
+  if (r < c0 + c1) {
+    r -= c0;
+    *la = r % B.e[0];
+    *lb = r / B.e[0];
+    return 1;
+  }
+  r -= c0 + c1;
+  *la = r % B.e[0];
+  *lb = r / B.e[0];
+  return 2;
 }
 
 template <int N, bool ADV, bool KC>
@@ -290,6 +339,10 @@ __global__ void __launch_bounds__(kCellThreads, 3) dg_cell_kernel(const __grid_c
   const int l[3] = {tid % kCellBX, (tid / kCellBX) % kCellBY, tid / (kCellBX * kCellBY)};
   const bool valid = l[0] < B.e[0] && l[1] < B.e[1] && l[2] < B.e[2];
   const long long cell = (B.o[0] + l[0]) + B.stride[1] * (B.o[1] + l[1]) + B.stride[2] * (B.o[2] + l[2]);
+  // faces on the brick's lower (and upper) boundary: c0 normal to x, c1 to
+  // y, c2 to z; nb <= 80
+  const int c0 = B.e[1] * B.e[2], c1 = B.e[0] * B.e[2], c2 = B.e[0] * B.e[1];
+  const int nb = c0 + c1 + c2;
 
   // ---- 0. own dofs -------------------------------------------------------------
   float u[N3];
@@ -300,55 +353,35 @@ __global__ void __launch_bounds__(kCellThreads, 3) dg_cell_kernel(const __grid_c
     for (int q = 0; q < N3; ++q) u[q] = 0.f;
   }
 
-  // ---- 0. halo items: lower-boundary faces (two cells each) on threads
-  // [0, nlow), upper-boundary faces (one cell each) on the rest ---------------------
-  {
-    const int c0 = B.e[1] * B.e[2], c1 = B.e[0] * B.e[2], c2 = B.e[0] * B.e[1];
-    const int nlow = c0 + c1 + c2;  // <= 80 < kCellThreads
-    const int nup = nlow;
-    auto item = [&](bool upper, int r) {
-      if (r < c0) {
-        cell_halo_item<N, ADV, KC, 0>(upper, r % B.e[1], r / B.e[1], B, args, tabs, slots);
-      } else if (r < c0 + c1) {
-        r -= c0;
-        cell_halo_item<N, ADV, KC, 1>(upper, r % B.e[0], r / B.e[0], B, args, tabs, slots);
-      } else {
-        r -= c0 + c1;
-        cell_halo_item<N, ADV, KC, 2>(upper, r % B.e[0], r / B.e[0], B, args, tabs, slots);
-      }
-    };
-    if (tid < nlow) {
-      item(false, tid);
-    } else {
-      for (int r = tid - nlow; r < nup; r += kCellThreads - nlow) item(true, r);
-    }
+  // ---- 0. halo items: one cell each, lower side then upper side -----------------
+  for (int item = tid; item < 2 * nb; item += kCellThreads) {
+    const bool upper = item >= nb;
+    int la, lb;
+    const int D = cell_boundary_face(upper ? item - nb : item, c0, c1, B, &la, &lb);
+    if (D == 0) cell_halo_traces<N, KC, 0>(upper, la, lb, B, args, tabs, slots);
+    else if (D == 1) cell_halo_traces<N, KC, 1>(upper, la, lb, B, args, tabs, slots);
+    else cell_halo_traces<N, KC, 2>(upper, la, lb, B, args, tabs, slots);
   }
 
-  // ---- 1. own lower-face traces (faces inside the brick) -----------------------
+  // ---- 1. own lower-face traces --------------------------------------------------
   if (valid) {
     float a[N2], b[N2];
-    if (l[0] > 0) {
-      cell_traces<N, KC, 0>(u, false, tabs, a, b);
-      cell_store_slot<N>(slots + cell_slot<N>(0, l[0], l[1], l[2]) * S::STRIDE, a, b);
-    }
-    if (l[1] > 0) {
-      cell_traces<N, KC, 1>(u, false, tabs, a, b);
-      cell_store_slot<N>(slots + cell_slot<N>(1, l[1], l[0], l[2]) * S::STRIDE, a, b);
-    }
-    if (l[2] > 0) {
-      cell_traces<N, KC, 2>(u, false, tabs, a, b);
-      cell_store_slot<N>(slots + cell_slot<N>(2, l[2], l[0], l[1]) * S::STRIDE, a, b);
-    }
+    cell_traces<N, KC, 0>(u, false, tabs, a, b);
+    cell_store_slot<N>(slots, l[0] > 0 ? cell_slot<N>(0, l[0], l[1], l[2]) : cell_bnd_slot<N>(0, l[1], l[2]), a, b);
+    cell_traces<N, KC, 1>(u, false, tabs, a, b);
+    cell_store_slot<N>(slots, l[1] > 0 ? cell_slot<N>(1, l[1], l[0], l[2]) : cell_bnd_slot<N>(1, l[0], l[2]), a, b);
+    cell_traces<N, KC, 2>(u, false, tabs, a, b);
+    cell_store_slot<N>(slots, l[2] > 0 ? cell_slot<N>(2, l[2], l[0], l[1]) : cell_bnd_slot<N>(2, l[0], l[1]), a, b);
   }
   __syncthreads();
 
-  // ---- 2. fluxes of the upper faces ---------------------------------------------
+  // ---- 2. fluxes of the upper faces, and of the brick's lower faces ---------------
   const float kc = KC && valid ? __ldg(args.kcell + cell) : 0.f;
   if (valid) {
     auto upper_face = [&](auto dc) {
       constexpr int D = decltype(dc)::value;
       const int la = l[D == 0 ? 1 : 0], lb = l[D == 2 ? 1 : 2];
-      float* sl = slots + cell_slot<N>(D, l[D] + 1, la, lb) * S::STRIDE;
+      const int sl = cell_slot<N>(D, l[D] + 1, la, lb);
       const int cd = B.o[D] + l[D];
       int nd = cd + 1;
       bool has_nb = true;
@@ -360,17 +393,28 @@ __global__ void __launch_bounds__(kCellThreads, 3) dg_cell_kernel(const __grid_c
       cell_traces<N, KC, D>(u, true, tabs, vo, po);
       if (has_nb) {
         float vn[N2], pn[N2];
-        cell_load_slot<N>(sl, vn, pn);
+        cell_load_slot<N>(slots, sl, vn, pn);
         const float kn = KC ? __ldg(args.kcell + cell + (long long)(nd - cd) * B.stride[D]) : 0.f;
         cell_interior_flux<N, ADV, KC, D>(vo, po, vn, pn, kc, kn, args, tabs, a, b);
       } else {
         cell_boundary_flux<N, ADV, KC, D>(true, vo, po, kc, args, tabs, a, b);
       }
-      cell_store_slot<N>(sl, a, b);
+      cell_store_slot<N>(slots, sl, a, b);
     };
     upper_face(std::integral_constant<int, 0>());
     upper_face(std::integral_constant<int, 1>());
     upper_face(std::integral_constant<int, 2>());
+  }
+  // the lower-boundary faces on the threads that had one halo item in phase 0
+  {
+    const int first = 2 * nb > kCellThreads ? 2 * nb - kCellThreads : 0;
+    for (int r = tid - first; r >= 0 && r < nb; r += kCellThreads) {
+      int la, lb;
+      const int D = cell_boundary_face(r, c0, c1, B, &la, &lb);
+      if (D == 0) cell_lower_flux<N, ADV, KC, 0>(la, lb, B, args, tabs, slots);
+      else if (D == 1) cell_lower_flux<N, ADV, KC, 1>(la, lb, B, args, tabs, slots);
+      else cell_lower_flux<N, ADV, KC, 2>(la, lb, B, args, tabs, slots);
+    }
   }
   __syncthreads();
   if (!valid) return;
@@ -382,15 +426,15 @@ __global__ void __launch_bounds__(kCellThreads, 3) dg_cell_kernel(const __grid_c
   auto line_pass = [&](auto dc) {
     constexpr int D = decltype(dc)::value;
     const int la = l[D == 0 ? 1 : 0], lb = l[D == 2 ? 1 : 2];
-    const float* s0 = slots + cell_slot<N>(D, l[D], la, lb) * S::STRIDE;      // lower face
-    const float* s1 = slots + cell_slot<N>(D, l[D] + 1, la, lb) * S::STRIDE;  // upper face
+    const int s0 = cell_slot<N>(D, l[D], la, lb);      // lower face
+    const int s1 = cell_slot<N>(D, l[D] + 1, la, lb);  // upper face
     const float gscale = KC ? -tabs.A2[D] * kc : 1.f;
 #pragma unroll
     for (int q = 0; q < S::H / 4; ++q) {
-      const float4 V0 = *reinterpret_cast<const float4*>(s0 + 4 * q);
-      const float4 G0 = *reinterpret_cast<const float4*>(s0 + S::H + 4 * q);
-      const float4 V1 = *reinterpret_cast<const float4*>(s1 + 4 * q);
-      const float4 G1 = *reinterpret_cast<const float4*>(s1 + S::H + 4 * q);
+      const float4 V0 = *cell_chunk<N>(slots, s0, q);
+      const float4 G0 = *cell_chunk<N>(slots, s0, S::H / 4 + q);
+      const float4 V1 = *cell_chunk<N>(slots, s1, q);
+      const float4 G1 = *cell_chunk<N>(slots, s1, S::H / 4 + q);
       const float v0a[4] = {V0.x, V0.y, V0.z, V0.w}, g0a[4] = {G0.x, G0.y, G0.z, G0.w};
       const float v1a[4] = {V1.x, V1.y, V1.z, V1.w}, g1a[4] = {G1.x, G1.y, G1.z, G1.w};
 #pragma unroll
