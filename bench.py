@@ -936,6 +936,35 @@ def workload_apply_f32(args):
                                    (p, N, args.algorithm, ", kappa per cell" if kc is not None else "")}}
 
 
+def workload_scaled_bj(args):
+    """The scaled shared-block Jacobi apply of the cellwise-kappa FP32
+    operator (cells^3, Q_order, seeded kappa per cell) on both engines of its
+    tile products: tcgen05 tensor cores (3xTF32) and FP32 FMA; --steps applies
+    after 3 warm-up applies, CUDA events."""
+    import gbfem
+    import torch
+    N, p = args.cells, args.order
+    nc = N ** 3
+    kc = gbfem.DeviceArray.from_numpy(np.exp(np.random.default_rng(args.seed).uniform(-2, 2, nc)).astype(np.float32))
+    op = gbfem.DGOperator((N, N, N), p, precision=gbfem.F32, kappa_cell=kc)
+    r = gbfem.DeviceArray.from_numpy(np.random.default_rng(SEED).uniform(-1, 1, op.size).astype(np.float32))
+    z = gbfem.DeviceArray(op.size, gbfem.F32)
+    stream = torch.cuda.current_stream()
+    out = {"metric": "scaled block-Jacobi apply", "unit": "ms", "higher_is_better": False, "dtype": "f32",
+           "config": {"workload": "scaled shared-block Jacobi, SIPG Q%d %d^3 (%d dofs), kappa per cell" % (p, N, op.size)}}
+    res = {}
+    for engine in ("tensor", "fma"):
+        pc = gbfem.Preconditioner.scaled_block_jacobi(op, engine=engine)
+        ms = time_applies(pc, r, z, max(1, args.steps), stream)
+        res[engine] = z.numpy()
+        out[engine] = {"ms": ms, "hbm_frac_8B_per_dof": 8.0 * op.size / (ms * 1e-3) / 1e9 / load_peaks()[0]["hbm_gbs"],
+                       "status": pc.status() if engine == "tensor" else 0}
+        del pc
+    out["value"] = out["tensor"]["ms"]
+    out["tensor_vs_fma_rel_max_diff"] = float(np.max(np.abs(res["tensor"] - res["fma"])) / np.max(np.abs(res["fma"])))
+    return out
+
+
 def workload_newton(args):
     """Bratu problem -lap u = lambda e^u (lambda = 5, SIPG Q2, weak u = 0) on
     cells^3 by Newton with block-Jacobi CG for each Jacobian; with and without
@@ -994,7 +1023,7 @@ def main():
     ap.add_argument("--impl", default="gbfem", choices=["gbfem", "reference"])
     ap.add_argument("--workload", default="apply",
                     choices=["apply", "q1cg", "rk3", "mixed", "learned", "kernels", "newton", "apply_kappa",
-                             "apply_f32"])
+                             "apply_f32", "scaled_bj"])
     ap.add_argument("--rk-steps", type=int, default=100)
     ap.add_argument("--cells", type=int, default=96)
     ap.add_argument("--order", type=int, default=3)
@@ -1024,7 +1053,8 @@ def main():
     if args.workload != "apply":
         fn = {"q1cg": workload_q1cg, "rk3": workload_rk3, "mixed": workload_mixed,
               "learned": workload_learned, "kernels": workload_kernels, "newton": workload_newton,
-              "apply_kappa": workload_apply_kappa, "apply_f32": workload_apply_f32}[args.workload]
+              "apply_kappa": workload_apply_kappa, "apply_f32": workload_apply_f32,
+              "scaled_bj": workload_scaled_bj}[args.workload]
         line = fn(args)
         line.update({"n_gpus": 1, "data": "synthetic"})
         print(json.dumps(line), flush=True)

@@ -521,7 +521,9 @@ int precond_apply(const gbfem_preconditioner_s* pc, const void* r, void* z, cuda
         g.nc[d] = pc->sor_op->dg.grid.cells[d];
         g.per[d] = pc->sor_op->dg.grid.periodic[d];
       }
-      if (pc->sb_tiles) {
+      if (pc->sb_engine == GBFEM_SB_ENGINE_TENSOR && pc->sb_tc_tiles) {
+        return sb_tc_apply(pc, (const float*)pc->sor_op->dg.kappa_cell, (const float*)r, (float*)z, s);
+      } else if (pc->sb_tiles) {
         // one CTA per SM over a contiguous range of quads: the inverse and
         // two residual tiles per group, 192 KB at nb = 125
         const size_t sm = size_t(nb) * (128 + 2 * kSbGroups * kSbTile) * 4;
@@ -1285,8 +1287,24 @@ int gbfem_preconditioner_block_jacobi_create(gbfem_operator op, int precision, g
 }
 
 int gbfem_preconditioner_scaled_block_jacobi_create(gbfem_operator op, gbfem_preconditioner* out) {
+  return gbfem_preconditioner_scaled_block_jacobi_create_engine(op, GBFEM_SB_ENGINE_TENSOR, out);
+}
+
+int gbfem_preconditioner_status(gbfem_preconditioner pc, int* status) {
+  if (!pc || !status) return set_error(GBFEM_ERR_INVALID, "gbfem_preconditioner_status: null argument");
+  *status = 0;
+  if (pc->sb_tc_status) {
+    GBFEM_CUDA_TRY(cudaDeviceSynchronize());
+    GBFEM_CUDA_TRY(cudaMemcpy(status, pc->sb_tc_status, sizeof(int), cudaMemcpyDeviceToHost));
+  }
+  return GBFEM_OK;
+}
+
+int gbfem_preconditioner_scaled_block_jacobi_create_engine(gbfem_operator op, int engine, gbfem_preconditioner* out) {
   if (!op || !out) return set_error(GBFEM_ERR_INVALID, "gbfem_preconditioner_scaled_block_jacobi_create: null argument");
   *out = nullptr;
+  if (engine != GBFEM_SB_ENGINE_TENSOR && engine != GBFEM_SB_ENGINE_FMA)
+    return set_error(GBFEM_ERR_INVALID, "scaled block Jacobi: unknown engine");
   const gbfem_dg_desc& d = op->dg;
   if (op->kind != OpKind::DG || !d.kappa_cell || op->precision != GBFEM_F32 || d.mass != 0.0 || op->nonlinear)
     return set_error(GBFEM_ERR_INVALID,
@@ -1315,6 +1333,7 @@ int gbfem_preconditioner_scaled_block_jacobi_create(gbfem_operator op, gbfem_pre
     return set_error(GBFEM_ERR_INVALID, "out of host memory");
   }
   pc->kind = PcKind::ScaledBlock;
+  pc->sb_engine = engine;
   pc->precision = GBFEM_F32;
   pc->n = op->ndofs;
   pc->nloc = op->nloc;
@@ -1368,6 +1387,13 @@ int gbfem_preconditioner_scaled_block_jacobi_create(gbfem_operator op, gbfem_pre
       return set_cuda_error(e, "scaled block Jacobi: tiles");
     }
     pc->sb_ntiles = (long long)(tiles.size() / 3);
+    if (engine == GBFEM_SB_ENGINE_TENSOR) {
+      const int rc = sb_tc_setup(pc, tiles, op->nloc, 0);
+      if (rc) {
+        gbfem_preconditioner_destroy(pc);
+        return rc;
+      }
+    }
   }
   *out = pc;
   return GBFEM_OK;
@@ -1390,6 +1416,9 @@ int gbfem_preconditioner_destroy(gbfem_preconditioner pc) {
   if (pc->scales) cudaFree(pc->scales);
   if (pc->sor_cells) cudaFree(pc->sor_cells);
   if (pc->sb_tiles) cudaFree(pc->sb_tiles);
+  if (pc->sb_tc_tiles) cudaFree(pc->sb_tc_tiles);
+  if (pc->sb_tc_img) cudaFree(pc->sb_tc_img);
+  if (pc->sb_tc_status) cudaFree(pc->sb_tc_status);
   if (pc->sor_tmp) cudaFree(pc->sor_tmp);
   if (pc->ext_destroy) pc->ext_destroy(pc->ext_ctx);
   delete pc;

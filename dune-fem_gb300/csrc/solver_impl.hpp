@@ -13,6 +13,11 @@ enum class PcKind { Diagonal = 1, BlockJacobi = 2, External = 3, Sor = 4, Scaled
 int precond_apply(const struct ::gbfem_preconditioner_s* pc, const void* r, void* z, cudaStream_t s);
 // Jacobi / Gauss-Seidel / SOR / SSOR sweeps over an assembled operator (sor.cu)
 int sor_apply(const struct ::gbfem_preconditioner_s* pc, const void* r, void* z, cudaStream_t s);
+// scaled block Jacobi on the tensor cores (sb_tc.cu): set-up from the
+// (type, start, count) tiles, and the apply
+int sb_tc_setup(struct ::gbfem_preconditioner_s* pc, const std::vector<int>& tiles3, int nb, cudaStream_t s);
+int sb_tc_apply(const struct ::gbfem_preconditioner_s* pc, const float* kcell, const float* r, float* z,
+                cudaStream_t s);
 
 }  // namespace gbfem
 
@@ -45,4 +50,11 @@ struct gbfem_preconditioner_s {
   // (type, start, count) into it
   int* sb_tiles = nullptr;
   long long sb_ntiles = 0;
+  // ScaledBlock on the tensor cores: tiles without padding, A_hi | A_lo
+  // images per type, the kernel's status word (1 = a wait timed out)
+  int sb_engine = GBFEM_SB_ENGINE_TENSOR;
+  int* sb_tc_tiles = nullptr;
+  int sb_tc_ntiles = 0;
+  void* sb_tc_img = nullptr;
+  int* sb_tc_status = nullptr;
 };

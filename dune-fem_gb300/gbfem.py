@@ -148,6 +148,9 @@ def lib():
         L.gbfem_preconditioner_sor_create.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double,
                                                       C.POINTER(C.c_void_p)]
         L.gbfem_preconditioner_scaled_block_jacobi_create.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+        L.gbfem_preconditioner_scaled_block_jacobi_create_engine.argtypes = [C.c_void_p, C.c_int,
+                                                                             C.POINTER(C.c_void_p)]
+        L.gbfem_preconditioner_status.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
         L.gbfem_preconditioner_destroy.argtypes = [C.c_void_p]
         L.gbfem_solver_params_default.argtypes = [C.POINTER(SolverParams)]
         L.gbfem_solve.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(SolverParams), C.c_void_p, C.c_void_p,
@@ -462,12 +465,20 @@ class Preconditioner:
         return cls(h, F32 if precision == F16 else precision, op)
 
     @classmethod
-    def scaled_block_jacobi(cls, op):
+    def scaled_block_jacobi(cls, op, engine="tensor"):
         """For an FP32 operator with kappa_cell (no mass): z_c = H_t^-1 r_c / kappa_c
-        with the shared kappa = 1 blocks H_t of the cell's boundary type."""
+        with the shared kappa = 1 blocks H_t of the cell's boundary type.
+        engine: "tensor" (tcgen05, 3xTF32) or "fma" for the tile products."""
         h = C.c_void_p()
-        check(lib().gbfem_preconditioner_scaled_block_jacobi_create(op.handle, C.byref(h)))
+        eng = {"tensor": 0, "fma": 1}[engine]
+        check(lib().gbfem_preconditioner_scaled_block_jacobi_create_engine(op.handle, eng, C.byref(h)))
         return cls(h, F32, op)
+
+    def status(self):
+        """0, or 1 if a bounded wait in the tensor-core kernel gave up."""
+        st = C.c_int()
+        check(lib().gbfem_preconditioner_status(self.handle, C.byref(st)))
+        return st.value
 
     SMOOTHERS = {"ssor": 2, "sor": 3, "gauss-seidel": 5, "jacobi": 6}
 

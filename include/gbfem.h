@@ -209,6 +209,19 @@ int gbfem_preconditioner_sor_create(gbfem_operator assembled, int method, int it
  * approximates it (the penalty's face average) elsewhere.  No counterpart in
  * the reference.  op must outlive pc. */
 int gbfem_preconditioner_scaled_block_jacobi_create(gbfem_operator op, gbfem_preconditioner* pc);
+/* The same with the engine of the tile product chosen: for blocks of 33 to
+ * 128 dofs (p = 3, 4) the cells are cut into tiles of <= 32 cells of one
+ * boundary type and each tile is the dense product H_t^{-1} R_tile.
+ * GBFEM_SB_ENGINE_TENSOR (the default of the create call above): tcgen05
+ * tensor cores, TF32 with the 3xTF32 split (FP32 accuracy), the inverse
+ * staged by TMA; GBFEM_SB_ENGINE_FMA: FP32 FMA in registers. */
+#define GBFEM_SB_ENGINE_TENSOR 0
+#define GBFEM_SB_ENGINE_FMA 1
+int gbfem_preconditioner_scaled_block_jacobi_create_engine(gbfem_operator op, int engine, gbfem_preconditioner* pc);
+/* Device-side status of a preconditioner's kernels: 0, or 1 if a bounded
+ * wait inside the tensor-core kernel gave up (its result is then invalid).
+ * Synchronises the device. */
+int gbfem_preconditioner_status(gbfem_preconditioner pc, int* status);
 int gbfem_preconditioner_apply(gbfem_preconditioner pc, const void* r, void* z, void* stream);
 int gbfem_preconditioner_precision(gbfem_preconditioner pc, int* precision);
 int gbfem_preconditioner_destroy(gbfem_preconditioner pc);

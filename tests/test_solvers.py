@@ -404,3 +404,45 @@ def test_unknown_error_measure_is_rejected(gb, orc):
     op, prob, f = _problem(gb, orc)
     with pytest.raises(gb.GbfemError):
         _solve(gb, op, f, "cg", error_measure=7)
+
+
+@pytest.mark.parametrize("order", [3, 4])
+@pytest.mark.parametrize("cells,periodic", [((5, 4, 3), (0, 0, 0)), ((9, 7, 6), (1, 0, 0)), ((20, 18, 16), (0, 1, 1))])
+def test_scaled_block_jacobi_tensor_cores(gb, orc, order, cells, periodic):
+    """The tile products on the tcgen05 tensor cores (TF32 with the 3xTF32
+    split) against the oracle's kappa = 1 blocks and against the FP32-FMA
+    engine; many tiles and type changes per CTA on the largest grid; the
+    kernel's bounded waits all completed (status 0); two applies in a row
+    give bitwise the same result."""
+    ncell = int(np.prod(cells))
+    nloc = (order + 1) ** 3
+    rng = np.random.default_rng(ncell + order)
+    kc = rng.uniform(0.5, 2.0, ncell).astype(np.float32)
+    op = gb.DGOperator(cells, order, precision=gb.F32, periodic=periodic,
+                       kappa_cell=gb.DeviceArray.from_numpy(kc, gb.F32))
+    r = gb.DeviceArray.from_numpy(rng.uniform(-1, 1, ncell * nloc).astype(np.float32), gb.F32)
+    out = {}
+    for engine in ("tensor", "fma"):
+        pc = gb.Preconditioner.scaled_block_jacobi(op, engine=engine)
+        z = gb.DeviceArray(ncell * nloc, gb.F32)
+        pc(r, z)
+        out[engine] = z.numpy()
+        if engine == "tensor":
+            z2 = gb.DeviceArray(ncell * nloc, gb.F32)
+            pc(r, z2)
+            assert np.array_equal(out[engine].view(np.uint32), z2.numpy().view(np.uint32))
+            assert pc.status() == 0
+    assert relmax(out["tensor"], out["fma"]) < 2e-5
+    if ncell <= 200:
+        prob = orc.DGProblem(cells, order, periodic=periodic)
+        hinv = np.linalg.inv(prob.block_diagonal())  # kappa = 1
+        ref = np.einsum("cij,cj->ci", hinv, r.numpy().astype(np.float64).reshape(-1, nloc))
+        ref /= kc[:, None].astype(np.float64)
+        assert relmax(out["tensor"], ref.ravel()) < 2e-5
+
+
+def test_scaled_block_jacobi_rejects_unknown_engine(gb):
+    op = gb.DGOperator((2, 2, 2), 3, precision=gb.F32,
+                       kappa_cell=gb.DeviceArray.from_numpy(np.ones(8, np.float32), gb.F32))
+    with pytest.raises((gb.GbfemError, KeyError)):
+        gb.Preconditioner.scaled_block_jacobi(op, engine="nope")
