@@ -773,11 +773,16 @@ def workload_learned(args):
     evaluated on args.eval_seeds held-out seeds against FP64 CG."""
     import gbfem
     import learned
-    N, p = args.cells, 3
+    N, p = args.cells, args.order
     net = gbfem.CNN(p, N, seed=2026)
     log = (lambda m: print(m, file=sys.stderr, flush=True)) if args.verbose else None
     t0 = time.perf_counter()
-    if args.loss == "anorm":
+    if args.loss == "projected":
+        args.form = "twolevel"
+        net.scale = 1.0
+        losses = learned.train_projected(net, N, p, list(range(args.train_seeds)), steps_per_pair=args.train_steps,
+                                         lr=args.lr, log=log)
+    elif args.loss == "anorm":
         losses = learned.train_anorm(net, N, p, list(range(args.train_seeds)), steps_per_pair=args.train_steps,
                                      lr=args.lr, log=log, form=args.form)
     else:
@@ -793,11 +798,11 @@ def workload_learned(args):
     def mean(key, field):
         v = [e[key][field] for e in evals if key in e]
         return float(np.mean(v)) if v else None
-    out = {"metric": "SIPG Q3 variable-kappa solve time to 1e-10: learned/mixed vs plain FP64 CG", "unit": "s",
+    out = {"metric": "SIPG Q%d variable-kappa solve time to 1e-10: learned/mixed vs plain FP64 CG" % p, "unit": "s",
            "higher_is_better": False, "dtype": "f64 outer / f32 inner / bf16 network",
-           "config": {"workload": "SIPG Q3 %d^3 (%d dofs), -div(kappa grad u) = 1, log kappa ~ 256 Fourier modes; "
-                                  "%d training seeds, %d held-out seeds" % (N, N ** 3 * 64, args.train_seeds,
-                                                                          args.eval_seeds)},
+           "config": {"workload": "SIPG Q%d %d^3 (%d dofs), -div(kappa grad u) = 1, log kappa ~ 256 Fourier modes; "
+                                  "%d training seeds, %d held-out seeds" % (p, N, N ** 3 * (p + 1) ** 3,
+                                                                          args.train_seeds, args.eval_seeds)},
            "value": mean("mixed_learned", "time_s"),
            "train_s": t_train, "train_steps": len(losses), "loss_first": losses[0], "loss_last": losses[-1],
            "loss_last_mean20": float(np.mean(losses[-20:])), "form": args.form, "loss": args.loss,
@@ -1043,7 +1048,7 @@ def main():
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--save-net", default="")
     ap.add_argument("--form", default="additive", choices=["additive", "twolevel"])
-    ap.add_argument("--loss", default="anorm", choices=["anorm", "mse"])
+    ap.add_argument("--loss", default="projected", choices=["projected", "anorm", "mse"])
     ap.add_argument("--plain-max-iter", type=int, default=0)
     ap.add_argument("--verbose", action="store_true")
     ap.add_argument("--no-solve", action="store_true", help="skip the solve comparison of the headline line")

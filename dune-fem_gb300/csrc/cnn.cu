@@ -101,6 +101,25 @@ __global__ void assemble_input_kernel(const T* __restrict__ r, const float* __re
   }
 }
 
+// out[0] = sum_p r[p*nloc]^2: the coarse mode's normalisation (the cell
+// means of r only), one CTA of 256 threads, fixed summation order
+template <typename T>
+__global__ void coarse_sumsq_kernel(const T* __restrict__ r, int nloc, long long P, double* __restrict__ out) {
+  __shared__ double part[256];
+  double s = 0.0;
+  for (long long p = threadIdx.x; p < P; p += 256) {
+    const double v = double(r[p * nloc]);
+    s = fma(v, v, s);
+  }
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = part[0];
+}
+
 // z[p*nloc+l] (+)= S * rms(r) * y[p][l]
 template <typename T>
 __global__ void emit_output_kernel(const float* __restrict__ y, const double* __restrict__ rr, long long n, int nloc,
@@ -115,20 +134,22 @@ __global__ void emit_output_kernel(const float* __restrict__ y, const double* __
   }
 }
 
-// diff[p][l] = y[p][l] - t[p*nloc+l] / (S rms) (0 on padded channels); dy = 2 diff / (P*nloc)
+// diff[p][l] = y[p][l] - t[p*nloc+l] / (S rms) (0 on padded channels, and in
+// coarse mode on every channel but the cell mean); dy = 2 diff / (P*nloc)
+// (coarse: 2 diff / P)
 template <typename T>
 __global__ void loss_grad_kernel(const float* __restrict__ y, const T* __restrict__ t, const double* __restrict__ rr,
-                                 long long n, int nloc, int cout, long long P, float S, float* __restrict__ diff,
-                                 bf16* __restrict__ dy) {
+                                 long long n, int nloc, int cout, long long P, float S, int coarse,
+                                 float* __restrict__ diff, bf16* __restrict__ dy) {
   const double rms = sqrt(rr[0] / double(n));
   const double inv = rms > 0.0 ? 1.0 / (double(S) * rms) : 0.0;
   const long long total = P * cout;
-  const float scale = 2.f / float(P * nloc);
+  const float scale = 2.f / float(coarse ? P : P * nloc);
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
     const int c = int(e % cout);
     const long long p = e / cout;
     float d = 0.f;
-    if (c < nloc) d = float(double(y[e]) - double(t[p * nloc + c]) * inv);
+    if (c < (coarse ? 1 : nloc)) d = float(double(y[e]) - double(t[p * nloc + c]) * inv);
     diff[e] = d;
     dy[e] = __float2bfloat16_rn(scale * d);
   }
@@ -350,11 +371,18 @@ static int refresh_bf16(gbfem_cnn_s* c, cudaStream_t s) {
   return GBFEM_OK;
 }
 
+// Values the normalisation rms(r) = sqrt(rr / nnorm) is taken over: every
+// dof, or in coarse mode the cell means only.
+static long long cnn_nnorm(const gbfem_cnn_s* c) { return c->coarse ? c->P[0] : c->ndofs; }
+
 template <typename T>
 static int cnn_input(gbfem_cnn_s* c, const void* r, cudaStream_t s) {
-  GBFEM_TRY(dot_device(sizeof(T) == 8 ? GBFEM_F64 : GBFEM_F32, c->ndofs, r, r, c->d_rr, c->d_partial, s));
+  if (c->coarse)
+    coarse_sumsq_kernel<T><<<1, 256, 0, s>>>(static_cast<const T*>(r), c->nloc, c->P[0], c->d_rr);
+  else
+    GBFEM_TRY(dot_device(sizeof(T) == 8 ? GBFEM_F64 : GBFEM_F32, c->ndofs, r, r, c->d_rr, c->d_partial, s));
   assemble_input_kernel<T><<<grid1(c->P[0] * c->cin0), 256, 0, s>>>(static_cast<const T*>(r), c->logk, c->d_rr,
-                                                                    c->ndofs, c->nloc, c->cin0, c->P[0], c->coarse,
+                                                                    cnn_nnorm(c), c->nloc, c->cin0, c->P[0], c->coarse,
                                                                     c->x0);
   GBFEM_CUDA_TRY(cudaGetLastError());
   return GBFEM_OK;
@@ -365,10 +393,10 @@ static int cnn_apply(gbfem_cnn_s* c, int precision, const void* r, void* z, int 
   else GBFEM_TRY(cnn_input<float>(c, r, s));
   GBFEM_TRY(cnn_forward(c, s));
   if (precision == GBFEM_F64)
-    emit_output_kernel<double><<<grid1(c->ndofs), 256, 0, s>>>(c->y, c->d_rr, c->ndofs, c->nloc, c->cout0, c->P[0],
+    emit_output_kernel<double><<<grid1(c->ndofs), 256, 0, s>>>(c->y, c->d_rr, cnn_nnorm(c), c->nloc, c->cout0, c->P[0],
                                                                c->S, accumulate, c->coarse, static_cast<double*>(z));
   else
-    emit_output_kernel<float><<<grid1(c->ndofs), 256, 0, s>>>(c->y, c->d_rr, c->ndofs, c->nloc, c->cout0, c->P[0],
+    emit_output_kernel<float><<<grid1(c->ndofs), 256, 0, s>>>(c->y, c->d_rr, cnn_nnorm(c), c->nloc, c->cout0, c->P[0],
                                                               c->S, accumulate, c->coarse, static_cast<float*>(z));
   GBFEM_CUDA_TRY(cudaGetLastError());
   return GBFEM_OK;
@@ -382,18 +410,20 @@ static int cnn_loss_grad(gbfem_cnn_s* c, int precision, const void* r, const voi
   GBFEM_TRY(cnn_forward(c, s));
   const long long ny = c->P[0] * c->cout0;
   if (precision == GBFEM_F64)
-    loss_grad_kernel<double><<<grid1(ny), 256, 0, s>>>(c->y, static_cast<const double*>(target), c->d_rr, c->ndofs,
-                                                       c->nloc, c->cout0, c->P[0], c->S, c->diff, c->dy);
+    loss_grad_kernel<double><<<grid1(ny), 256, 0, s>>>(c->y, static_cast<const double*>(target), c->d_rr,
+                                                       cnn_nnorm(c), c->nloc, c->cout0, c->P[0], c->S, c->coarse,
+                                                       c->diff, c->dy);
   else
-    loss_grad_kernel<float><<<grid1(ny), 256, 0, s>>>(c->y, static_cast<const float*>(target), c->d_rr, c->ndofs,
-                                                      c->nloc, c->cout0, c->P[0], c->S, c->diff, c->dy);
+    loss_grad_kernel<float><<<grid1(ny), 256, 0, s>>>(c->y, static_cast<const float*>(target), c->d_rr,
+                                                      cnn_nnorm(c), c->nloc, c->cout0, c->P[0], c->S, c->coarse,
+                                                      c->diff, c->dy);
   GBFEM_CUDA_TRY(cudaGetLastError());
   GBFEM_TRY(cnn_backward(c, s));
   if (loss) {
     GBFEM_TRY(dot_device(GBFEM_F32, ny, c->diff, c->diff, c->d_loss, c->d_partial, s));
     GBFEM_CUDA_TRY(cudaMemcpyAsync(c->h_loss, c->d_loss, sizeof(double), cudaMemcpyDeviceToHost, s));
     GBFEM_CUDA_TRY(cudaStreamSynchronize(s));
-    *loss = c->h_loss[0] / double(c->P[0] * c->nloc);
+    *loss = c->h_loss[0] / double(c->coarse ? c->P[0] : c->P[0] * c->nloc);
   }
   return GBFEM_OK;
 }
@@ -404,27 +434,42 @@ struct LearnedCtx {
   gbfem_operator op;        // not owned; NULL = additive form
   void* t = nullptr;        // work vectors of the two-level form
   void* at = nullptr;
+  double* dots = nullptr;   // n.r, n.An (device)
+  double* partial = nullptr;
   ~LearnedCtx() {
     if (t) cudaFree(t);
     if (at) cudaFree(at);
+    if (dots) cudaFree(dots);
+    if (partial) cudaFree(partial);
   }
 };
 
-template <typename T>
-__global__ void learned_residual_kernel(long long n, const T* __restrict__ r, const T* __restrict__ az,
-                                        T* __restrict__ t) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    t[i] = r[i] - az[i];
-}
 template <typename T>
 __global__ void learned_add_kernel(long long n, const T* __restrict__ a, T* __restrict__ z) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     z[i] += a[i];
 }
 
+// z *= alpha, t = r - alpha az with alpha = (n.r) / (n.An), or 0 where n.An
+// is not positive (every thread computes alpha from the two device dots)
+template <typename T>
+__global__ void learned_scale_kernel(long long n, const double* __restrict__ dots, const T* __restrict__ r,
+                                     const T* __restrict__ az, T* __restrict__ z, T* __restrict__ t) {
+  const double b = dots[1];
+  const double alpha = (b > 0.0 && isfinite(b) && isfinite(dots[0])) ? dots[0] / b : 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    z[i] = T(alpha * double(z[i]));
+    t[i] = T(double(r[i]) - alpha * double(az[i]));
+  }
+}
+
 // Additive:   z = BJ(r) + NN(r)
-// Two-level:  z = NN(r);  z += BJ(r - A z)   (the network as the coarse
-//             correction, one block-Jacobi smoothing step after it)
+// Two-level:  n = NN(r) (coarse mode: the shape of the error's cell means),
+//             z = alpha n with the Galerkin-optimal alpha = n.r / n.An (the
+//             A-norm projection of the error onto span{n}), then one
+//             block-Jacobi smoothing step z += BJ(r - A z).  A network whose
+//             output does not correlate with the error gives alpha ~ 0, i.e.
+//             block Jacobi.
 static int ext_learned_apply(void* ctx, const void* r, void* z, cudaStream_t s) {
   LearnedCtx* lc = static_cast<LearnedCtx*>(ctx);
   gbfem_cnn_s* c = lc->cnn;
@@ -437,10 +482,14 @@ static int ext_learned_apply(void* ctx, const void* r, void* z, cudaStream_t s) 
   GBFEM_TRY(cnn_apply(c, prec, r, z, 0, s));
   GBFEM_TRY(gbfem_operator_apply(lc->op, z, lc->at, s));
   const long long n = c->ndofs;
+  GBFEM_TRY(dot_device(prec, n, z, r, lc->dots, lc->partial, s));
+  GBFEM_TRY(dot_device(prec, n, z, lc->at, lc->dots + 1, lc->partial, s));
   if (prec == GBFEM_F64) {
-    learned_residual_kernel<double><<<grid1(n), 256, 0, s>>>(n, (const double*)r, (const double*)lc->at, (double*)lc->t);
+    learned_scale_kernel<double><<<grid1(n), 256, 0, s>>>(n, lc->dots, (const double*)r, (const double*)lc->at,
+                                                          (double*)z, (double*)lc->t);
   } else {
-    learned_residual_kernel<float><<<grid1(n), 256, 0, s>>>(n, (const float*)r, (const float*)lc->at, (float*)lc->t);
+    learned_scale_kernel<float><<<grid1(n), 256, 0, s>>>(n, lc->dots, (const float*)r, (const float*)lc->at,
+                                                         (float*)z, (float*)lc->t);
   }
   GBFEM_TRY(precond_apply(lc->bj, lc->t, lc->at, s));
   if (prec == GBFEM_F64) learned_add_kernel<double><<<grid1(n), 256, 0, s>>>(n, (const double*)lc->at, (double*)z);
@@ -627,10 +676,10 @@ int gbfem_cnn_train_step_grad(gbfem_cnn c, int precision, const void* r, const v
   GBFEM_TRY(cnn_forward(c, s));
   const long long ny = c->P[0] * c->cout0;
   if (precision == GBFEM_F64)
-    grad_from_dofs_kernel<double><<<grid1(ny), 256, 0, s>>>(static_cast<const double*>(grad_z), c->d_rr, c->ndofs,
+    grad_from_dofs_kernel<double><<<grid1(ny), 256, 0, s>>>(static_cast<const double*>(grad_z), c->d_rr, cnn_nnorm(c),
                                                             c->nloc, c->cout0, c->P[0], c->S, c->coarse, c->dy);
   else
-    grad_from_dofs_kernel<float><<<grid1(ny), 256, 0, s>>>(static_cast<const float*>(grad_z), c->d_rr, c->ndofs,
+    grad_from_dofs_kernel<float><<<grid1(ny), 256, 0, s>>>(static_cast<const float*>(grad_z), c->d_rr, cnn_nnorm(c),
                                                            c->nloc, c->cout0, c->P[0], c->S, c->coarse, c->dy);
   GBFEM_CUDA_TRY(cudaGetLastError());
   GBFEM_TRY(cnn_backward(c, s));
@@ -734,6 +783,8 @@ int gbfem_preconditioner_learned_create(gbfem_cnn c, gbfem_preconditioner bj, gb
     const size_t bytes = size_t(c->ndofs) * (bj->precision == GBFEM_F64 ? 8 : 4);
     cudaError_t e = cudaMalloc(&lc->t, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&lc->at, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&lc->dots, 2 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&lc->partial, sizeof(double) * (dot_num_partials(c->ndofs) + 8));
     if (e != cudaSuccess) {
       delete lc;
       delete pc;

@@ -137,11 +137,59 @@ def train_anorm(cnn, cells, order, seeds, ks=(0, 10, 40, 120, 400, 1000), steps_
     return losses
 
 
+def train_projected(cnn, cells, order, seeds, ks=(0, 10, 40, 120, 400, 1000), steps_per_pair=4, lr=1e-3, log=None):
+    """Training for the two-level form with the Galerkin-scaled coarse
+    correction (the network in coarse mode proposes the shape n of the
+    error's cell means; the preconditioner uses alpha n, alpha = n.r / n.An):
+    on the solver's own pairs (r_k, e_k), minimise
+        L = 1 - (n.A e)^2 / ((n.A n)(e.A e)),
+    the fraction of the A-norm error that the best multiple of n leaves.  L
+    is invariant to the scale of n, so the network only has to learn where
+    the smooth error is, not its size.  With a = n.r (= n.A e), b = n.A n:
+        dL/dn = 2 a / (b E) (a / b A n - r),  E = e.A e.
+    Returns the per-step losses."""
+    losses = []
+    t0 = time.perf_counter()
+    cnn.set_coarse(True)
+    for i, seed in enumerate(seeds):
+        op64, op32, k64, k32, f = sipg_problem(cells, order, seed)
+        del op64
+        pairs, _ = make_pairs(cells, order, seed, ks, form="twolevel")   # (r, e) in FP32
+        cnn.set_kappa(k32)
+        n = op32.size
+        z = gbfem.DeviceArray(n, gbfem.F32)
+        az = gbfem.DeviceArray(n, gbfem.F32)
+        ae = gbfem.DeviceArray(n, gbfem.F32)
+        g = gbfem.DeviceArray(n, gbfem.F32)
+        for _ in range(steps_per_pair):
+            for r, e in pairs:
+                op32(e, ae)
+                E = gbfem.dot(e, ae)
+                cnn.forward(r, z)                 # n = NN(r)
+                op32(z, az)
+                a, b = gbfem.dot(z, r), gbfem.dot(z, az)
+                if not (b > 0.0 and E > 0.0):
+                    continue
+                losses.append(1.0 - a * a / (b * E))
+                # g = 2 a / (b E) * (a / b * A n - r)
+                g.clear()
+                gbfem.axpy(a / b, az, g)
+                gbfem.axpy(-1.0, r, g)
+                gbfem.check(gbfem.lib().gbfem_scal(gbfem.F32, n, 2.0 * a / (b * E), g.ptr, None))
+                cnn.train_step_grad(r, g, lr)
+        if log:
+            log("seed %d (%d/%d): projected loss %.4e  (%.1f s)" % (seed, i + 1, len(seeds), losses[-1] if losses
+                                                                      else float("nan"), time.perf_counter() - t0))
+    return losses
+
+
 def evaluate(cnn, cells, order, seed, tol=1e-10, max_iterations=20000, plain=True, form="additive",
-             plain_max_iterations=None):
+             plain_max_iterations=None, restart=20):
     """Iterations and times on one held-out seed: FP64 flexible CG with the
     learned preconditioner vs FP64 block-Jacobi PCG (and unpreconditioned CG),
-    plus the mixed FP32/FP64 solve with the learned preconditioner inside."""
+    plus the mixed FP32/FP64 solve with the learned preconditioner inside.
+    restart: directions the flexible CG keeps (the learned preconditioner is
+    nonlinear, so a longer memory keeps more of CG's Krylov optimality)."""
     op64, op32, k64, k32, f = sipg_problem(cells, order, seed)
     out = {"seed": seed}
     bj64 = gbfem.Preconditioner.block_jacobi(op64)
@@ -155,7 +203,7 @@ def evaluate(cnn, cells, order, seed, tol=1e-10, max_iterations=20000, plain=Tru
         runs.insert(0, ("plain_cg", "cg", None))
     for name, method, pc in runs:
         cap = plain_max_iterations if (name == "plain_cg" and plain_max_iterations) else max_iterations
-        inv = gbfem.KrylovInverseOperator(method, tolerance=tol, max_iterations=cap, restart=4)
+        inv = gbfem.KrylovInverseOperator(method, tolerance=tol, max_iterations=cap, restart=restart)
         inv.bind(op64, pc)
         u.clear()
         t0 = time.perf_counter()
@@ -169,7 +217,7 @@ def evaluate(cnn, cells, order, seed, tol=1e-10, max_iterations=20000, plain=Tru
         u.clear()
         t0 = time.perf_counter()
         info = gbfem.solve_mixed(op64, op32, pc, f, u, tolerance=tol, inner_method=method, inner_tolerance=1e-3,
-                                 inner_restart=4)
+                                 inner_restart=restart)
         out[name] = {"iterations": info.iterations, "time_s": time.perf_counter() - t0,
                      "converged": bool(info.converged), "rel_residual": info.residual}
     return out
