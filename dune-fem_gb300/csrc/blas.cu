@@ -82,6 +82,87 @@ int dot_partial_device(int precision, long long n, const void* x, const void* y,
   return GBFEM_OK;
 }
 
+struct DotPairs {
+  const void* x[kMaxDotPairs];
+  const void* y[kMaxDotPairs];
+};
+
+// dot_partial_kernel for pair blockIdx.y: the same chunk, thread order and
+// block reduction, so partial[l np + b] is bitwise the single dot's partial b
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) multi_dot_partial_kernel(const __grid_constant__ DotPairs pr, long long n,
+                                                                        long long chunk, int np, double* partial) {
+  const T* __restrict__ x = static_cast<const T*>(pr.x[blockIdx.y]);
+  const T* __restrict__ y = static_cast<const T*>(pr.y[blockIdx.y]);
+  const long long b0 = (long long)blockIdx.x * chunk;
+  long long b1 = b0 + chunk;
+  if (b1 > n) b1 = n;
+  double s = 0.0;
+  for (long long i = b0 + threadIdx.x; i < b1; i += kRedThreads) s = fma(double(x[i]), double(y[i]), s);
+  s = block_sum(s);
+  if (threadIdx.x == 0) partial[(long long)blockIdx.y * np + blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kRedThreads) multi_dot_final_kernel(const double* __restrict__ partial, int np,
+                                                                      double* out) {
+  const double s = dot_final_sum(partial + (long long)blockIdx.x * np, np);
+  if (threadIdx.x == 0) out[blockIdx.x] = s;
+}
+
+struct AxpyTerms {
+  double a[kMaxDotPairs];
+  const void* x[kMaxDotPairs];
+};
+
+// y = a_0 x_0 + 1 y, then a_1 x_1 + 1 y, ...: the arithmetic of k
+// successive y = a x + b y updates with b = 1, in one pass over y
+template <typename T>
+__global__ void multi_axpy_kernel(long long n, int k, const __grid_constant__ AxpyTerms t, T* __restrict__ y) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    T acc = y[i];
+    for (int l = 0; l < k; ++l) acc = T(t.a[l]) * static_cast<const T*>(t.x[l])[i] + T(1.0) * acc;
+    y[i] = acc;
+  }
+}
+
+int multi_dot_device(int precision, long long n, int k, const void* const* xs, const void* const* ys, double* d_out,
+                     double* d_partial, cudaStream_t s) {
+  if (k <= 0) return GBFEM_OK;
+  if (k > kMaxDotPairs) return set_error(GBFEM_ERR_INVALID, "multi_dot: too many pairs");
+  const int np = dot_num_partials(n);
+  const long long chunk = (n + np - 1) / np;
+  DotPairs pr{};
+  for (int l = 0; l < k; ++l) {
+    pr.x[l] = xs[l];
+    pr.y[l] = ys[l];
+  }
+  const dim3 grid{unsigned(np), unsigned(k), 1u};
+  if (precision == GBFEM_F64)
+    multi_dot_partial_kernel<double><<<grid, kRedThreads, 0, s>>>(pr, n, chunk, np, d_partial);
+  else
+    multi_dot_partial_kernel<float><<<grid, kRedThreads, 0, s>>>(pr, n, chunk, np, d_partial);
+  multi_dot_final_kernel<<<unsigned(k), kRedThreads, 0, s>>>(d_partial, np, d_out);
+  GBFEM_CUDA_TRY(cudaGetLastError());
+  return GBFEM_OK;
+}
+
+int multi_axpy_device(int precision, long long n, int k, const double* a, const void* const* xs, void* y,
+                      cudaStream_t s) {
+  if (k <= 0) return GBFEM_OK;
+  if (k > kMaxDotPairs) return set_error(GBFEM_ERR_INVALID, "multi_axpy: too many terms");
+  AxpyTerms t{};
+  for (int l = 0; l < k; ++l) {
+    t.a[l] = a[l];
+    t.x[l] = xs[l];
+  }
+  if (precision == GBFEM_F64)
+    multi_axpy_kernel<double><<<stream_grid(n), 256, 0, s>>>(n, k, t, static_cast<double*>(y));
+  else
+    multi_axpy_kernel<float><<<stream_grid(n), 256, 0, s>>>(n, k, t, static_cast<float*>(y));
+  GBFEM_CUDA_TRY(cudaGetLastError());
+  return GBFEM_OK;
+}
+
 int dot_device(int precision, long long n, const void* x, const void* y, double* d_out, double* d_partial,
                cudaStream_t s) {
   const int np = dot_num_partials(n);

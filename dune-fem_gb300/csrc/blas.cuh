@@ -55,6 +55,16 @@ int dot_device(int precision, long long n, const void* x, const void* y, double*
 // scratch (ceil(n/chunk) partials).
 int dot_device_fixed_chunks(int precision, long long n, long long chunk, const void* x, const void* y,
                             double* d_out, double* d_partial, cudaStream_t s);
+// Up to kMaxDotPairs dot products x_l . y_l in one pass 1 (a 2-D grid:
+// chunks x pairs) and one pass 2, each with exactly gbfem_dot's partition and
+// summation order, so every result is bitwise the single dot's.  d_partial
+// must hold k * dot_num_partials(n) doubles, d_out k doubles.
+constexpr int kMaxDotPairs = 32;
+int multi_dot_device(int precision, long long n, int k, const void* const* xs, const void* const* ys, double* d_out,
+                     double* d_partial, cudaStream_t s);
+// y = y + sum_l a_l x_l (l = 0..k-1 in order, k <= kMaxDotPairs), one pass.
+int multi_axpy_device(int precision, long long n, int k, const double* a, const void* const* xs, void* y,
+                      cudaStream_t s);
 // The library's per-device scratch (allocated on first use).
 int library_scratch(double** partial, double** result);
 // Grid size of the grid-stride streaming kernels.

@@ -409,9 +409,29 @@ struct Ctx {
     prec = precision;
     n = nn;
     s = st;
-    GBFEM_CUDA_TRY(cudaMalloc(&d_partial, sizeof(double) * (dot_num_partials(n) + 8)));
-    GBFEM_CUDA_TRY(cudaMalloc(&d_res, sizeof(double) * 8));
-    GBFEM_CUDA_TRY(cudaMallocHost(&h_res, sizeof(double) * 8));
+    GBFEM_CUDA_TRY(cudaMalloc(&d_partial, sizeof(double) * (size_t(kMaxDotPairs) * dot_num_partials(n) + 8)));
+    GBFEM_CUDA_TRY(cudaMalloc(&d_res, sizeof(double) * kMaxDotPairs));
+    GBFEM_CUDA_TRY(cudaMallocHost(&h_res, sizeof(double) * kMaxDotPairs));
+    return GBFEM_OK;
+  }
+  // out[l] = xs[l] . ys[l] for l < k, one pass and one host synchronisation
+  // per kMaxDotPairs pairs; each bitwise equal to dot(xs[l], ys[l])
+  int multi_dot(int k, const void* const* xs, const void* const* ys, double* out) {
+    for (int l0 = 0; l0 < k; l0 += kMaxDotPairs) {
+      const int kk = k - l0 < kMaxDotPairs ? k - l0 : kMaxDotPairs;
+      GBFEM_TRY(multi_dot_device(prec, n, kk, xs + l0, ys + l0, d_res, d_partial, s));
+      GBFEM_CUDA_TRY(cudaMemcpyAsync(h_res, d_res, sizeof(double) * kk, cudaMemcpyDeviceToHost, s));
+      GBFEM_CUDA_TRY(cudaStreamSynchronize(s));
+      for (int l = 0; l < kk; ++l) out[l0 + l] = h_res[l];
+    }
+    return GBFEM_OK;
+  }
+  // y += sum_l a[l] xs[l], in order
+  int multi_axpy(int k, const double* a, const void* const* xs, void* y) {
+    for (int l0 = 0; l0 < k; l0 += kMaxDotPairs) {
+      const int kk = k - l0 < kMaxDotPairs ? k - l0 : kMaxDotPairs;
+      GBFEM_TRY(multi_axpy_device(prec, n, kk, a + l0, xs + l0, y, s));
+    }
     return GBFEM_OK;
   }
   ~Ctx() {
@@ -905,9 +925,16 @@ static int gmres(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_
       } else {
         GBFEM_TRY(op_apply(op, vj, vjp, c));
       }
-      for (int l = 0; l <= j; ++l) GBFEM_TRY(c.dot(vjp, v[l], &gd[l]));
+      // classical Gram-Schmidt: the j+1 products with the same vector in one
+      // pass and one host read (the reference sums them in one comm.sum,
+      // gmres.hh:91), then one fused update
+      std::vector<const void*> xs(j + 1, vjp), vs(j + 1);
+      for (int l = 0; l <= j; ++l) vs[l] = v[l];
+      GBFEM_TRY(c.multi_dot(j + 1, xs.data(), vs.data(), gd.data()));
       for (int i = 0; i <= j; ++i) Hm(i, j) = gd[i];
-      for (int l = 0; l <= j; ++l) GBFEM_TRY(c.axpby(-gd[l], v[l], 1.0, vjp));
+      std::vector<double> neg(j + 1);
+      for (int l = 0; l <= j; ++l) neg[l] = -gd[l];
+      GBFEM_TRY(c.multi_axpy(j + 1, neg.data(), vs.data(), vjp));
       double nn;
       GBFEM_TRY(c.dot(vjp, vjp, &nn));
       Hm(j + 1, j) = std::sqrt(nn);
@@ -1003,11 +1030,12 @@ static int bicgstab(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solv
     } else {
       GBFEM_TRY(op_apply(op, s, r, c));
     }
-    GBFEM_TRY(c.dot(r, s, &gdot[0]));
-    GBFEM_TRY(c.dot(r, r, &gdot[1]));
-    GBFEM_TRY(c.dot(s, s, &gdot[2]));
-    GBFEM_TRY(c.dot(s, rs, &gdot[3]));
-    GBFEM_TRY(c.dot(r, rs, &gdot[4]));
+    {
+      // the five products of this step in one pass and one host read
+      const void* xs[5] = {r, r, s, s, r};
+      const void* ys[5] = {s, r, s, rs, rs};
+      GBFEM_TRY(c.multi_dot(5, xs, ys, gdot));
+    }
     const double omega = gdot[0] / gdot[1];
     res = std::sqrt(gdot[2] - omega * (2.0 * gdot[0] - omega * gdot[1]));
     const double beta = (gdot[3] - omega * gdot[4]) * alpha / (omega * nu);
