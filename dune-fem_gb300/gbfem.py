@@ -206,6 +206,20 @@ class DeviceArray:
     def clear(self):
         check(lib().gbfem_memset(self.ptr, 0, self.n * self.itemsize))
 
+    @property
+    def __cuda_array_interface__(self):
+        """Zero-copy view of the dofs for GPU array libraries (the CUDA Array
+        Interface, version 3): torch.as_tensor(a, device="cuda"), cupy, numba
+        see the same device memory, no copy.  (numpy() copies to the host.)"""
+        return {"shape": (self.n,), "typestr": "<f8" if self.precision == F64 else "<f4",
+                "data": (int(self.ptr.value or 0), False), "version": 3, "strides": None}
+
+    def as_tensor(self):
+        """The dofs as a torch tensor on the GPU sharing this memory (no copy);
+        the DeviceArray must outlive it."""
+        import torch
+        return torch.as_tensor(self, device="cuda")
+
     def free(self):
         if self.ptr:
             lib().gbfem_free(self.ptr)
@@ -421,6 +435,128 @@ class NewtonInverseOperator:
         return {"converged": bool(i.converged), "iterations": i.iterations, "linear_iterations": i.linear_iterations,
                 "residual": i.residual, "failure": NEWTON_FAILURES.get(i.failure, str(i.failure)),
                 "time_ms": i.time_ms}
+
+
+class Space:
+    """The discrete space a scheme acts on: its size and precision, and the
+    zero vector (scheme.space.zero)."""
+
+    def __init__(self, size, precision):
+        self.size = size
+        self.precision = precision
+
+    @property
+    def zero(self):
+        z = DeviceArray(self.size, self.precision)
+        z.clear()
+        return z
+
+    def function(self, name=None):
+        """A new discrete function (dof vector) of this space, set to zero."""
+        return self.zero
+
+
+_PRECONDITIONING = ("none", "jacobi", "blockjacobi", "sor", "ssor", "gauss-seidel")
+
+
+class Scheme:
+    """A Galerkin scheme over one of the library's operators, in the shape of
+    dune.fem's schemes (python/dune/fem/scheme/__init__.py:17-45,
+    dune/fempy/py/scheme.hh:112-190): scheme(u, w) applies the operator,
+    scheme.solve(target, rightHandSide=...) solves S(target) = rightHandSide
+    from the initial guess in target and returns the info dictionary
+    {converged, iterations, linear_iterations, timing}.
+
+    parameters: the fem.solver keys without the prefix, as dune.fem takes
+    them: "linear.method" (cg, gmres, bicgstab, fcg, fgmres),
+    "linear.tolerance", "linear.errormeasure" (absolute, relative,
+    residualreduction), "linear.maxiterations", "linear.gmres.restart",
+    "linear.preconditioning.method" (none, jacobi, blockjacobi, sor, ssor,
+    gauss-seidel), "linear.verbose"; for a nonlinear operator
+    "nonlinear.tolerance", "nonlinear.maxiterations",
+    "nonlinear.linesearch" (none, simple), "nonlinear.forcing" (none,
+    eisenstatwalker).  The deprecated "newton." prefix is accepted, as in
+    dune.fem."""
+
+    _MEASURES = {"absolute": ABSOLUTE, "relative": RELATIVE, "residualreduction": RESIDUAL_REDUCTION}
+
+    def __init__(self, op, parameters=None):
+        self.op = op
+        self.space = Space(op.size, op.precision)
+        prm = {}
+        for k, v in (parameters or {}).items():
+            prm[k[len("newton."):] if k.startswith("newton.") else k] = v
+        self.parameters = prm
+        pre = prm.get("linear.preconditioning.method", "none")
+        if pre not in _PRECONDITIONING:
+            raise GbfemError(-1, "Scheme: unknown preconditioning method %r" % (pre,))
+        self._pc = None
+
+    def __call__(self, u, w):
+        """w = S(u): the operator's apply (GalerkinOperator::operator())."""
+        self.op(u, w)
+
+    def linear(self):
+        """The linear operator of a linear scheme, the Jacobian at 0 of a nonlinear one."""
+        if not self.op.nonlinear():
+            return self.op
+        return self.op.jacobian(self.space.zero)
+
+    def _preconditioner(self, op):
+        pre = self.parameters.get("linear.preconditioning.method", "none")
+        if pre == "none":
+            return None
+        if pre == "jacobi":
+            return Preconditioner.diagonal(op)
+        if pre == "blockjacobi":
+            return Preconditioner.block_jacobi(op)
+        return Preconditioner.sor(op.assemble(), method=pre,
+                                  iterations=int(self.parameters.get("linear.preconditioning.iterations", 1)),
+                                  relaxation=float(self.parameters.get("linear.preconditioning.relaxation", 1.0)))
+
+    def inverseLinearOperator(self, parameters=None):
+        """A KrylovInverseOperator bound to the linear operator, with this
+        scheme's parameters (updated by `parameters`)."""
+        prm = dict(self.parameters)
+        prm.update(parameters or {})
+        inv = KrylovInverseOperator(prm.get("linear.method", "cg"), tolerance=float(prm.get("linear.tolerance", 1e-8)),
+                                    error_measure=self._MEASURES[prm.get("linear.errormeasure", "absolute")],
+                                    max_iterations=prm.get("linear.maxiterations"),
+                                    restart=int(prm.get("linear.gmres.restart", 20)),
+                                    verbose=bool(prm.get("linear.verbose", False)))
+        op = self.linear()
+        inv.bind(op, self._preconditioner(op))
+        return inv
+
+    def solve(self, target, rightHandSide=None):
+        """target = S^{-1}(rightHandSide) (rightHandSide None: zero), target
+        on entry the initial guess.  Linear: the Krylov inverse operator;
+        nonlinear: Newton with that linear solver."""
+        rhs = rightHandSide if rightHandSide is not None else self.space.zero
+        prm = self.parameters
+        if not self.op.nonlinear():
+            inv = self.inverseLinearOperator()
+            inv(rhs, target)
+            i = inv.info()
+            return {"converged": i["converged"], "iterations": 0, "linear_iterations": i["iterations"],
+                    "timing": [i["time_ms"] * 1e-3]}
+        pre = prm.get("linear.preconditioning.method", "none")
+        pcs = {"none": PC_NONE, "jacobi": PC_DIAGONAL, "blockjacobi": PC_BLOCK_JACOBI}
+        if pre not in pcs:
+            raise GbfemError(-1, "Scheme: a nonlinear scheme takes none, jacobi or blockjacobi preconditioning")
+        newton = NewtonInverseOperator(
+            tolerance=float(prm.get("nonlinear.tolerance", 1e-6)), max_iterations=prm.get("nonlinear.maxiterations"),
+            line_search=prm.get("nonlinear.linesearch", "none"), forcing=prm.get("nonlinear.forcing", "none"),
+            preconditioner=pcs[pre], linear_method=prm.get("linear.method", "cg"),
+            linear_tolerance=float(prm.get("linear.tolerance", 1e-8)),
+            linear_error_measure=self._MEASURES[prm.get("linear.errormeasure", "relative")],
+            linear_max_iterations=prm.get("linear.maxiterations"),
+            linear_restart=int(prm.get("linear.gmres.restart", 20)))
+        newton.bind(self.op)
+        newton(rhs, target)
+        i = newton.info()
+        return {"converged": i["converged"], "iterations": i["iterations"], "linear_iterations": i["linear_iterations"],
+                "timing": [i["time_ms"] * 1e-3]}
 
 
 class Q1Operator(Operator):
