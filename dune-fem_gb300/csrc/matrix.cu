@@ -123,6 +123,9 @@ extern "C" int gbfem_operator_assemble(gbfem_operator op, gbfem_operator* out) {
   a->owns_kcache = false;
   a->jit_lib = a->jit_kernel = nullptr;
   a->owns_kfield = false;
+  a->form = a->form_jacobian = 0;  // the matrix of a form's Jacobian is a plain matrix
+  a->form_u0 = nullptr;
+  a->owns_form_u0 = false;
   a->bsr_blocks = nullptr;
   a->bsr_col = nullptr;
   a->trace_buf = nullptr;

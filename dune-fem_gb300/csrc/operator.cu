@@ -201,6 +201,7 @@ int dg_apply(const gbfem_operator_s* op, const void* u, void* w, cudaStream_t s,
              void* blocks, long long cell_begin, long long cell_count, int phase, void* ucopy) {
   if (op->nonlinear && unit_mode != 0)
     return set_error(GBFEM_ERR_INVALID, "nonlinear operator: diagonal and blocks belong to its Jacobian");
+  if (op->form) return form_apply(op, u, w, s, unit_mode, blocks, cell_begin, cell_count);
   GBFEM_TRY(dg_apply_linear(op, u, w, s, unit_mode, blocks, cell_begin, cell_count, phase, ucopy));
   const long long count = cell_count > 0 ? cell_count : op->ncells - cell_begin;
   if (unit_mode == 0 && (phase & 2)) {
@@ -778,6 +779,7 @@ int gbfem_operator_destroy(gbfem_operator op) {
     if (op->kf_cache) cudaFree(op->kf_cache);
   }
   if (op->jit_lib) cudaLibraryUnload(static_cast<cudaLibrary_t>(op->jit_lib));
+  if (op->owns_form_u0 && op->form_u0) cudaFree(op->form_u0);
   if (op->owns_kfield && op->kappa_field) cudaFree(op->kappa_field);
   if (op->host_u) cudaFree(op->host_u);
   if (op->host_w) cudaFree(op->host_w);
@@ -816,7 +818,7 @@ int gbfem_operator_apply_host(gbfem_operator op, const void* u_host, void* w_hos
     GBFEM_CUDA_TRY(cudaMalloc(&op->host_u, bytes));
     GBFEM_CUDA_TRY(cudaMalloc(&op->host_w, bytes));
   }
-  if (op->kind == OpKind::DG) return dg_apply_host_pipelined(op, u_host, w_host);
+  if (op->kind == OpKind::DG && !op->form) return dg_apply_host_pipelined(op, u_host, w_host);
   GBFEM_CUDA_TRY(cudaMemcpyAsync(op->host_u, u_host, bytes, cudaMemcpyHostToDevice, 0));
   GBFEM_TRY(gbfem_operator_apply(op, op->host_u, op->host_w, nullptr));
   GBFEM_CUDA_TRY(cudaMemcpyAsync(w_host, op->host_w, bytes, cudaMemcpyDeviceToHost, 0));

@@ -31,6 +31,10 @@ int bsr_apply(const struct ::gbfem_operator_s* op, const void* x, void* y, cudaS
 // R'(u0) u; blocks_mode 1/2 add the linearised cell blocks / their diagonal.
 int reaction_launch(const struct ::gbfem_operator_s* op, int mode, const void* u, void* w, void* pts,
                     long long cell_begin, long long count, int blocks_mode, cudaStream_t s);
+// general form operators (form.cu): unit_mode as dg_apply; a form's Jacobian
+// applies S'(u0) in unit mode 0
+int form_apply(const struct ::gbfem_operator_s* op, const void* u, void* w, cudaStream_t s, int unit_mode,
+               void* blocks, long long cell_begin, long long cell_count);
 struct HostPipe;
 void destroy_host_pipe(HostPipe* p);
 int dg_apply_host_pipelined(struct ::gbfem_operator_s* op, const void* u_host, void* w_host);
@@ -72,5 +76,13 @@ struct gbfem_operator_s {
   bool owns_kfield = false;
   void* jit_lib = nullptr;     // run-time compiled reaction (cudaLibrary_t), owned by the operator
   void* jit_kernel = nullptr;  // its kernel (cudaKernel_t): modes 0 and 1 of the reaction
+  // run-time compiled general form (form.cu): kind DG, nonlinear, M components
+  int form = 0;
+  int form_m = 1;
+  void* form_val = nullptr;    // cudaKernel_t: w = S(u)
+  void* form_lin = nullptr;    // cudaKernel_t: the dual-number linearisation (Jacobian modes)
+  int form_jacobian = 0;       // this operator is S'(form_u0) of a form
+  void* form_u0 = nullptr;     // its linearisation point (owned by the Jacobian)
+  bool owns_form_u0 = false;
   gbfem::HostPipe* pipe = nullptr;  // its streams and events
 };

@@ -177,7 +177,20 @@ int gbfem_operator_jacobian_create(gbfem_operator op, gbfem_operator* jac) {
   j->owns_kcache = false;  // shares the operator's kappa point caches
   j->jit_lib = j->jit_kernel = nullptr;  // the Jacobian applies the stored linearisation only
   j->owns_kfield = false;
-  if (op->nonlinear) {
+  j->owns_form_u0 = false;
+  if (op->form && op->nonlinear) {
+    // a form's Jacobian: the dual-number kernel at a stored point (the form's
+    // kernels stay owned by the form)
+    const size_t bytes = size_t(op->ndofs) * (op->precision == GBFEM_F64 ? 8 : 4);
+    const cudaError_t e = cudaMalloc(&j->form_u0, bytes);
+    if (e != cudaSuccess) {
+      delete j;
+      return set_cuda_error(e, "gbfem_operator_jacobian_create");
+    }
+    cudaMemset(j->form_u0, 0, bytes);
+    j->owns_form_u0 = true;
+    j->form_jacobian = 1;
+  } else if (op->nonlinear) {
     const size_t bytes = size_t(op->ncells) * op->q * op->q * op->q * (op->precision == GBFEM_F64 ? 8 : 4);
     const cudaError_t e = cudaMalloc(&j->jac_points, bytes);
     if (e != cudaSuccess) {
@@ -192,9 +205,17 @@ int gbfem_operator_jacobian_create(gbfem_operator op, gbfem_operator* jac) {
 
 int gbfem_operator_jacobian(gbfem_operator op, const void* u, gbfem_operator jac, void* stream) {
   if (!op || !u || !jac) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_jacobian: null argument");
-  if (jac->ncells != op->ncells || jac->q != op->q || jac->n != op->n || jac->precision != op->precision)
+  if (jac->ncells != op->ncells || jac->q != op->q || jac->n != op->n || jac->precision != op->precision ||
+      jac->nloc != op->nloc)
     return set_error(GBFEM_ERR_INVALID, "gbfem_operator_jacobian: jacobian was created for another operator");
   if (!op->nonlinear) return GBFEM_OK;  // the Jacobian of a linear operator is the operator
+  if (op->form) {
+    if (!jac->form_jacobian || !jac->form_u0)
+      return set_error(GBFEM_ERR_INVALID, "gbfem_operator_jacobian: jacobian was created for another operator");
+    const size_t bytes = size_t(op->ndofs) * (op->precision == GBFEM_F64 ? 8 : 4);
+    GBFEM_CUDA_TRY(cudaMemcpyAsync(jac->form_u0, u, bytes, cudaMemcpyDeviceToDevice, static_cast<cudaStream_t>(stream)));
+    return GBFEM_OK;
+  }
   if (!jac->jac_points) return set_error(GBFEM_ERR_INVALID, "gbfem_operator_jacobian: jacobian has no linearisation storage");
   jac->react[0] = op->react[0];
   jac->react[1] = op->react[1];

@@ -330,6 +330,30 @@ int gbfem_dg_nonlinear_operator_create(const gbfem_dg_desc* desc, const gbfem_re
  * GalerkinOperator over UFL-generated integrands (python/dune/models/
  * integrands/ufl.py). */
 int gbfem_dg_nonlinear_operator_create_jit(const gbfem_dg_desc* desc, const char* cubin_path, gbfem_operator* op);
+/* A general DG form compiled at run time: S(u) = sum_K int_K s.v + F:grad v
+ * + sum_F int_F (own side) s.v + F:grad v + boundary terms, for `components`
+ * (1..4) solution components, with the user's pointwise interior / skeleton /
+ * boundary functions of (x, u, grad u) (both sides' traces on a face).
+ * cubin_path holds the kernels gbfem_form_<f64|f32>_n<p+1>_q<q>_m<M>_val and
+ * _lin (the dual-number linearisation), which the Python package's
+ * integrands module generates and compiles.  desc supplies the grid, order,
+ * quadrature, precision and penalty (sigma = penalty / h_F is handed to the
+ * face functions); its diffusion, mass, velocity and weak_dirichlet fields
+ * are not used, kappa and kappa_cell must be NULL.  Dof layout
+ * dof = cell * M (p+1)^3 + i * M + m (i the scalar Legendre index, m the
+ * component), the reference's vector-valued DG layout
+ * (space/basisfunctionset/vectorial.hh:139-165).  The operator is nonlinear:
+ * gbfem_operator_jacobian gives S'(u) exactly (forward-mode dual numbers
+ * through the same kernel) with apply, diagonal, block diagonal and assembly;
+ * Newton, the Krylov solvers, the preconditioners and the explicit
+ * Runge-Kutta solver take it like the other DG operators.  ≙ GalerkinOperator
+ * over UFL-generated integrands (schemes/galerkin.hh:332-537, 1383-1504,
+ * 1548-1643; python/dune/models/integrands/ufl.py:197-348).  A Jacobian must
+ * not outlive its form. */
+int gbfem_form_operator_create(const gbfem_dg_desc* desc, int components, const char* cubin_path,
+                               gbfem_operator* op);
+/* Solution components of an operator (1 except for general forms). */
+int gbfem_operator_components(gbfem_operator op, int* components);
 /* ≙ Operator::nonlinear() (operator/common/operator.hh:64). */
 int gbfem_operator_nonlinear(gbfem_operator op, int* nonlinear);
 /* A Jacobian operator for op (storage for the linearisation; initially at u = 0
