@@ -1,8 +1,10 @@
 """CPU (numpy, float64) restatement of the learned preconditioner's network,
 forward and backward, for checking the GPU kernels' outputs and gradients.
 
-TEST INFRASTRUCTURE ONLY.  The forward rounds its stored activations to BF16
-at the points where the GPU stores BF16; the backward is exact float64.
+TEST INFRASTRUCTURE ONLY.  Forward and backward round every stored
+activation and activation gradient to BF16 at the points where the GPU
+stores BF16 (csrc/cnn.cu cnn_forward/cnn_backward); sums and products are
+float64 in between, where the GPU accumulates in FP32.
 
 Layer order and weight layout ([taps][cout][cin], tap t = (dz+1)*9 +
 (dy+1)*3 + (dx+1)) follow the GPU network: in-proj 1x1 + relu, then
@@ -145,24 +147,27 @@ def loss_grad(Ws, r, target, logk, N, nloc, S):
     diff = y - t
     diff[:, nloc:] = 0.0
     loss = np.sum(diff ** 2) / (P * nloc)
-    dy = 2.0 * diff / (P * nloc)
+    dy = bf16(2.0 * diff / (P * nloc))
     Wb, L = c["Wb"], c["L"]
     g = [None] * 9
     dd1, g[8] = conv_bwd(c["d1"], Wb[8], dy, L[0])
-    dd1 = dd1 * (c["d1"] > 0)
+    dd1 = bf16(dd1) * (c["d1"] > 0)
     du1, g[7] = conv_bwd(c["u1"], Wb[7], dd1, L[0])
-    dd2 = up_bwd(du1, L[0]) * (c["d2"] > 0)
+    du1 = bf16(du1)
+    dd2 = bf16(up_bwd(du1, L[0]) * (c["d2"] > 0))
     du2, g[6] = conv_bwd(c["u2"], Wb[6], dd2, L[1])
-    dd3 = up_bwd(du2, L[1]) * (c["d3"] > 0)
+    du2 = bf16(du2)
+    dd3 = bf16(up_bwd(du2, L[1]) * (c["d3"] > 0))
     du3, g[5] = conv_bwd(c["u3"], Wb[5], dd3, L[2])
-    db4 = up_bwd(du3, L[2]) * (c["b4"] > 0)
+    du3 = bf16(du3)
+    db4 = bf16(up_bwd(du3, L[2]) * (c["b4"] > 0))
     dp3, g[4] = conv_bwd(c["p3"], Wb[4], db4, L[3])
-    ds3 = (du3 + pool_bwd(dp3, L[2])) * (c["s3"] > 0)
+    ds3 = bf16((du3 + pool_bwd(bf16(dp3), L[2])) * (c["s3"] > 0))
     dp2, g[3] = conv_bwd(c["p2"], Wb[3], ds3, L[2])
-    ds2 = (du2 + pool_bwd(dp2, L[1])) * (c["s2"] > 0)
+    ds2 = bf16((du2 + pool_bwd(bf16(dp2), L[1])) * (c["s2"] > 0))
     dp1, g[2] = conv_bwd(c["p1"], Wb[2], ds2, L[1])
-    ds1 = (du1 + pool_bwd(dp1, L[0])) * (c["s1"] > 0)
+    ds1 = bf16((du1 + pool_bwd(bf16(dp1), L[0])) * (c["s1"] > 0))
     da0, g[1] = conv_bwd(c["a0"], Wb[1], ds1, L[0])
-    da0 = da0 * (c["a0"] > 0)
+    da0 = bf16(da0) * (c["a0"] > 0)
     _, g[0] = conv_bwd(c["x0"], Wb[0], da0, L[0])
     return loss, g, y

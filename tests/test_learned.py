@@ -35,14 +35,66 @@ def test_forward_and_gradients_match_cpu_oracle(gb, order):
     loss_ref, g_ref, y = co.loss_grad(Ws, r, t, logk, N, nloc, 0.7)
     rms = np.sqrt(np.mean(r ** 2))
     z_ref = (0.7 * rms * y[:, :nloc]).ravel()
-    assert _rel(z.numpy(), z_ref) < 2e-2
+    # random weights: BF16 rounding of near-ties differs between the FP32
+    # accumulation and the float64 oracle and propagates; measured worst over
+    # orders 1-3 and two seeds: output 3e-3, loss 2e-6, 1 - cos 4e-4
+    assert _rel(z.numpy(), z_ref) < 1e-2
     loss = net.loss_grad(dr, dt)
-    assert abs(loss - loss_ref) < 2e-2 * loss_ref
+    assert abs(loss - loss_ref) < 1e-4 * loss_ref
     g = co.unflatten(net.grads(), nloc)
     for i, (a, b) in enumerate(zip(g, g_ref)):
         cos = np.sum(a * b) / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-300)
-        assert cos > 0.995, (i, cos)
+        assert cos > 0.998, (i, cos)
         assert _rel(a, b) < 0.1, (i, _rel(a, b))
+
+
+@pytest.mark.parametrize("order", [1, 3])
+def test_exact_arithmetic_network_matches_oracle_bitwise(gb, order):
+    """With one tap per 3x3x3 layer and a scaled permutation as its channel
+    matrix, weights in {1/2, 1, 2}, inputs +-1 (rms 1), kappa 1 and dyadic
+    targets, every product and sum the kernels form is exact in FP32, so the
+    GPU and the oracle round the same values to BF16: the output must agree
+    bitwise and the weight gradients to FP32 accumulation order.  A wrong tap
+    offset, flip or channel index anywhere in forward, backward-data or
+    weight-gradient kernels shows as a mismatch."""
+    import cnn_oracle as co
+    N = 8
+    nloc = (order + 1) ** 3
+    net = gb.CNN(order, N, seed=1)
+    rng = np.random.default_rng(10 + order)
+    shapes, cin0, cout0 = co.layer_shapes(nloc)
+    Ws = []
+    for li, (taps, cout, cin) in enumerate(shapes):
+        W = np.zeros((taps, cout, cin))
+        t = int(rng.integers(taps))
+        src = rng.permutation(cin)[:cout] if cout <= cin else rng.integers(cin, size=cout)
+        if li == 0:  # read the residual channels where there are enough of them
+            src = rng.permutation(min(nloc, cin))[:cout] if nloc >= cout else src
+        W[t, np.arange(cout), src] = rng.choice([0.5, 1.0, 2.0], size=cout)
+        Ws.append(W)
+    net.set_params(np.concatenate([W.ravel() for W in Ws]).astype(np.float32))
+    n = N ** 3 * nloc
+    kappa = np.zeros(n)
+    kappa[::nloc] = 1.0
+    net.set_kappa(gb.DeviceArray.from_numpy(kappa))
+    net.scale = 1.0
+    r = rng.choice([-1.0, 1.0], size=n)
+    t = rng.integers(-8, 9, size=n) * 0.25
+    dr, dt = gb.DeviceArray.from_numpy(r), gb.DeviceArray.from_numpy(t)
+    z = gb.DeviceArray(n)
+    net.forward(dr, z)
+    loss_ref, g_ref, y = co.loss_grad(Ws, r, t, np.zeros(N ** 3), N, nloc, 1.0)
+    z_ref = y[:, :nloc].ravel()
+    assert np.max(np.abs(z_ref)) > 0
+    assert np.array_equal(z.numpy(), z_ref)
+    loss = net.loss_grad(dr, dt)
+    assert abs(loss - loss_ref) <= 1e-6 * loss_ref
+    g = co.unflatten(net.grads(), nloc)
+    nonzero = 0
+    for i, (a, b) in enumerate(zip(g, g_ref)):
+        nonzero += int(np.count_nonzero(b))
+        assert np.max(np.abs(a - b)) <= 1e-5 * max(np.max(np.abs(b)), 1e-30), (i, _rel(a, b))
+    assert nonzero > 0
 
 
 def test_training_reduces_the_loss_and_is_reproducible(gb):
