@@ -970,6 +970,52 @@ def workload_scaled_bj(args):
     return out
 
 
+def workload_cnn(args):
+    """The learned preconditioner's network on cells^3 DG Q_order: forward
+    (z = S rms NN(r/rms)) and forward + loss + backward, each --steps times
+    after 3 warm-ups, CUDA events, on both engines of the 3x3x3 convolutions
+    (tcgen05 with TMA loads, and mma.sync); the command the convolution
+    profiles under profiles/ are taken from."""
+    import gbfem
+    import torch
+    N, p = args.cells, args.order
+    nloc = (p + 1) ** 3
+    n = N ** 3 * nloc
+    rng = np.random.default_rng(args.seed)
+    kappa = np.zeros(n)
+    kappa[::nloc] = np.exp(rng.normal(0, 1, N ** 3))
+    r = gbfem.DeviceArray.from_numpy(rng.uniform(-1, 1, n))
+    t = gbfem.DeviceArray.from_numpy(rng.uniform(-1, 1, n))
+    z = gbfem.DeviceArray(n)
+    stream = torch.cuda.current_stream()
+    out = {"metric": "learned-preconditioner network time", "unit": "ms", "higher_is_better": False, "dtype": "bf16",
+           "config": {"workload": "4-level 3-D U-net, 32 channels, DG Q%d %d^3 (%d dofs)" % (p, N, n)}}
+    steps = max(1, args.steps)
+    for engine in ("tensor", "mma"):
+        net = gbfem.CNN(p, N, seed=1)
+        net.set_conv_engine(engine)
+        net.set_kappa(gbfem.DeviceArray.from_numpy(kappa))
+        res = {}
+        for name, fn in (("forward", lambda: net.forward(r, z)),
+                         ("forward_backward", lambda: gbfem.check(gbfem.lib().gbfem_cnn_loss_grad(
+                             net.handle, gbfem.F64, r.ptr, t.ptr, None, None)))):
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            res[name + "_ms"] = e0.elapsed_time(e1) / steps
+        res["status"] = net.status()
+        out[engine] = res
+        del net
+    out["value"] = out["tensor"]["forward_ms"]
+    return out
+
+
 def workload_newton(args):
     """Bratu problem -lap u = lambda e^u (lambda = 5, SIPG Q2, weak u = 0) on
     cells^3 by Newton with block-Jacobi CG for each Jacobian; with and without
@@ -1028,7 +1074,7 @@ def main():
     ap.add_argument("--impl", default="gbfem", choices=["gbfem", "reference"])
     ap.add_argument("--workload", default="apply",
                     choices=["apply", "q1cg", "rk3", "mixed", "learned", "kernels", "newton", "apply_kappa",
-                             "apply_f32", "scaled_bj"])
+                             "apply_f32", "scaled_bj", "cnn"])
     ap.add_argument("--rk-steps", type=int, default=100)
     ap.add_argument("--cells", type=int, default=96)
     ap.add_argument("--order", type=int, default=3)
@@ -1059,7 +1105,7 @@ def main():
         fn = {"q1cg": workload_q1cg, "rk3": workload_rk3, "mixed": workload_mixed,
               "learned": workload_learned, "kernels": workload_kernels, "newton": workload_newton,
               "apply_kappa": workload_apply_kappa, "apply_f32": workload_apply_f32,
-              "scaled_bj": workload_scaled_bj}[args.workload]
+              "scaled_bj": workload_scaled_bj, "cnn": workload_cnn}[args.workload]
         line = fn(args)
         line.update({"n_gpus": 1, "data": "synthetic"})
         print(json.dumps(line), flush=True)

@@ -17,6 +17,7 @@
 //   d2 -up+s1-> u1 -[3^3]-> d1 -[1x1, 32->COUT0]-> y
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -26,6 +27,8 @@
 
 #include "blas.cuh"
 #include "cnn_kernels.cuh"
+#include "cnn_tc.cuh"
+#include "convert.cuh"
 #include "gbfem_internal.cuh"
 #include "operator_impl.hpp"
 #include "solver_impl.hpp"
@@ -83,21 +86,28 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g, 
   }
 }
 
-// x0[p][c]: c < nloc: r[p*nloc+c] / rms(r); c == nloc: log kappa_mean[p]; else 0
+// x0[p][c]: c < nloc: r[p*nloc+c] / rms(r); c == nloc: log kappa_mean[p]; else 0.
+// One thread per channel pair; the dof values are rounded to FP32 in integer
+// arithmetic (convert.cuh), the product is FP32.
 template <typename T>
 __global__ void assemble_input_kernel(const T* __restrict__ r, const float* __restrict__ logk,
                                       const double* __restrict__ rr, long long n, int nloc, int cin,
                                       long long P, int coarse, bf16* __restrict__ x0) {
   const double ms = rr[0] / double(n);
   const float inv = ms > 0.0 ? float(1.0 / sqrt(ms)) : 0.f;
-  const long long total = P * cin;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-    const int c = int(e % cin);
-    const long long p = e / cin;
-    float v = 0.f;
-    if (c < nloc) v = (coarse && c > 0) ? 0.f : float(r[p * nloc + c]) * inv;
-    else if (c == nloc) v = logk[p];
-    x0[e] = __float2bfloat16_rn(v);
+  const unsigned half = unsigned(cin) / 2u, total = unsigned(P) * half, nl = unsigned(nloc);
+  __nv_bfloat162* x2 = reinterpret_cast<__nv_bfloat162*>(x0);
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const unsigned p = e / half, c = 2u * (e - p * half);
+    float v[2];
+#pragma unroll
+    for (unsigned j = 0; j < 2; ++j) {
+      const unsigned cc = c + j;
+      v[j] = 0.f;
+      if (cc < nl) v[j] = (coarse && cc > 0) ? 0.f : to_f32(r[p * nl + cc]) * inv;
+      else if (cc == nl) v[j] = logk[p];
+    }
+    x2[e] = __floats2bfloat162_rn(v[0], v[1]);
   }
 }
 
@@ -120,36 +130,36 @@ __global__ void coarse_sumsq_kernel(const T* __restrict__ r, int nloc, long long
   if (threadIdx.x == 0) out[0] = part[0];
 }
 
-// z[p*nloc+l] (+)= S * rms(r) * y[p][l]
+// z[p*nloc+l] (+)= S * rms(r) * y[p][l]: the scale and the product in FP32,
+// widened to T in integer arithmetic (an FP64 add only when accumulating)
 template <typename T>
 __global__ void emit_output_kernel(const float* __restrict__ y, const double* __restrict__ rr, long long n, int nloc,
                                    int cout, long long P, float S, int accumulate, int coarse, T* __restrict__ z) {
-  const double rms = sqrt(rr[0] / double(n));
-  const long long total = P * nloc;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-    const int l = int(e % nloc);
-    const long long p = e / nloc;
-    const double v = (coarse && l > 0) ? 0.0 : double(S) * rms * double(y[p * cout + l]);
-    z[e] = accumulate ? T(double(z[e]) + v) : T(v);
+  const float sc = float(double(S) * sqrt(rr[0] / double(n)));
+  const unsigned nl = unsigned(nloc), total = unsigned(P) * nl, co = unsigned(cout);
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const unsigned p = e / nl, l = e - p * nl;
+    const float v = (coarse && l > 0) ? 0.f : sc * y[p * co + l];
+    z[e] = accumulate ? T(z[e] + from_f32<T>(v)) : from_f32<T>(v);
   }
 }
 
 // diff[p][l] = y[p][l] - t[p*nloc+l] / (S rms) (0 on padded channels, and in
 // coarse mode on every channel but the cell mean); dy = 2 diff / (P*nloc)
-// (coarse: 2 diff / P)
+// (coarse: 2 diff / P); FP32 arithmetic
 template <typename T>
 __global__ void loss_grad_kernel(const float* __restrict__ y, const T* __restrict__ t, const double* __restrict__ rr,
                                  long long n, int nloc, int cout, long long P, float S, int coarse,
                                  float* __restrict__ diff, bf16* __restrict__ dy) {
   const double rms = sqrt(rr[0] / double(n));
-  const double inv = rms > 0.0 ? 1.0 / (double(S) * rms) : 0.0;
-  const long long total = P * cout;
+  const float inv = rms > 0.0 ? float(1.0 / (double(S) * rms)) : 0.f;
+  const unsigned co = unsigned(cout), nl = unsigned(nloc), total = unsigned(P) * co;
+  const unsigned lim = coarse ? 1u : nl;
   const float scale = 2.f / float(coarse ? P : P * nloc);
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-    const int c = int(e % cout);
-    const long long p = e / cout;
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const unsigned p = e / co, c = e - p * co;
     float d = 0.f;
-    if (c < (coarse ? 1 : nloc)) d = float(double(y[e]) - double(t[p * nloc + c]) * inv);
+    if (c < lim) d = y[e] - to_f32(t[p * nl + c]) * inv;
     diff[e] = d;
     dy[e] = __float2bfloat16_rn(scale * d);
   }
@@ -159,13 +169,12 @@ __global__ void loss_grad_kernel(const float* __restrict__ y, const T* __restric
 template <typename T>
 __global__ void grad_from_dofs_kernel(const T* __restrict__ g, const double* __restrict__ rr, long long n, int nloc,
                                       int cout, long long P, float S, int coarse, bf16* __restrict__ dy) {
-  const double rms = sqrt(rr[0] / double(n));
-  const long long total = P * cout;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-    const int c = int(e % cout);
-    const long long p = e / cout;
-    const double v = (c < nloc && !(coarse && c > 0)) ? double(S) * rms * double(g[p * nloc + c]) : 0.0;
-    dy[e] = __float2bfloat16_rn(float(v));
+  const float sc = float(double(S) * sqrt(rr[0] / double(n)));
+  const unsigned co = unsigned(cout), nl = unsigned(nloc), total = unsigned(P) * co;
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const unsigned p = e / co, c = e - p * co;
+    const float v = (c < nl && !(coarse && c > 0)) ? sc * to_f32(g[p * nl + c]) : 0.f;
+    dy[e] = __float2bfloat16_rn(v);
   }
 }
 
@@ -209,6 +218,14 @@ struct gbfem_cnn_s {
   double* d_loss = nullptr;
   double* d_partial = nullptr;
   double* h_loss = nullptr;
+  int* status = nullptr;     // set by a tensor-core convolution whose wait ran out
+  struct ConvMap {
+    CUtensorMap map;         // 4-D [z][y][x][32 channels] BF16, box of 128 positions, 64-byte swizzle
+    const bf16* ptr;
+    int N;
+  };
+  std::vector<ConvMap> conv_maps;  // the inputs of the 3x3x3 convolutions
+  int conv_engine = GBFEM_CNN_CONV_TENSOR_CORE;
   std::vector<void*> allocs;
 };
 
@@ -227,6 +244,75 @@ static int launch_conv(const bf16* in, const bf16* w, TOUT* out, int N, cudaStre
   const long long P = (long long)N * N * N;
   const unsigned blocks = unsigned((P + 63) / 64);
   k<<<blocks, 128, sm, s>>>(in, w, out, N);
+  GBFEM_CUDA_TRY(cudaGetLastError());
+  return GBFEM_OK;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// dependency on the driver library); null if unavailable
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+static bool tma_conv_level(int N) { return N >= 8 && N <= 256 && (N & (N - 1)) == 0; }
+
+// tensor map of an activation buffer of an N^3 grid for conv_tma_kernel
+static int conv_map(gbfem_cnn_s* c, const bf16* ptr, int N) {
+  if (!tma_conv_level(N)) return GBFEM_OK;
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return GBFEM_OK;  // the mma.sync engine serves
+  gbfem_cnn_s::ConvMap m{};
+  m.ptr = ptr;
+  m.N = N;
+  const cuuint64_t dims[4] = {cuuint64_t(C), cuuint64_t(N), cuuint64_t(N), cuuint64_t(N)};
+  const cuuint64_t strides[3] = {cuuint64_t(C) * 2, cuuint64_t(C) * 2 * N, cuuint64_t(C) * 2 * N * N};
+  const cuuint32_t bx = N < kCtM ? N : kCtM;
+  const cuuint32_t by = (kCtM / bx) < cuuint32_t(N) ? (kCtM / bx) : cuuint32_t(N);
+  const cuuint32_t box[4] = {cuuint32_t(C), bx, by, cuuint32_t(kCtM) / (bx * by)};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUresult r = enc(&m.map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(ptr), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(GBFEM_ERR_CUDA, "gbfem_cnn: tensor map of a convolution input");
+  c->conv_maps.push_back(m);
+  return GBFEM_OK;
+}
+
+// The 3x3x3 32 -> 32 convolution (forward: RELU; backward-data: the
+// flipped weights, no RELU) on the engine the network is set to: TMA +
+// tcgen05 where the level allows it (N a power of two >= 8), else mma.sync.
+template <bool RELU>
+static int launch_conv27(gbfem_cnn_s* c, const bf16* in, const bf16* w, bf16* out, int N, cudaStream_t s) {
+  const CUtensorMap* map = nullptr;
+  if (c->conv_engine == GBFEM_CNN_CONV_TENSOR_CORE)
+    for (const auto& m : c->conv_maps)
+      if (m.ptr == in && m.N == N) map = &m.map;
+  if (!map) return launch_conv<C, C, 27, RELU, bf16>(in, w, out, N, s);
+  static_assert(C == kCtN, "the tensor-core convolution is 32 -> 32 channels");
+  GBFEM_CUDA_TRY(cudaFuncSetAttribute(conv_tma_kernel<RELU>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kCtSmem)));
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) ==
+                                                  cudaSuccess && v > 0)
+      sms = v;
+    else
+      sms = 152;
+  }
+  const long long P = (long long)N * N * N;
+  const long long ntiles = P / kCtM;
+  const long long grid = ntiles < sms ? ntiles : sms;
+  conv_tma_kernel<RELU><<<unsigned(grid), kCtThreads, kCtSmem, s>>>(*map, w, out, N, c->status);
   GBFEM_CUDA_TRY(cudaGetLastError());
   return GBFEM_OK;
 }
@@ -275,19 +361,19 @@ static int conv_out_fwd(gbfem_cnn_s* c, cudaStream_t s) {
 static int cnn_forward(gbfem_cnn_s* c, cudaStream_t s) {
   const int* N = c->N;
   GBFEM_TRY(conv_in_fwd(c, s));
-  GBFEM_TRY((launch_conv<C, C, 27, true, bf16>(c->a0, c->L[1].wb, c->s1, N[0], s)));
+  GBFEM_TRY((launch_conv27<true>(c, c->a0, c->L[1].wb, c->s1, N[0], s)));
   pool_fwd_kernel<<<grid1(c->P[1] * C), 256, 0, s>>>(c->s1, c->p1, N[0], C);
-  GBFEM_TRY((launch_conv<C, C, 27, true, bf16>(c->p1, c->L[2].wb, c->s2, N[1], s)));
+  GBFEM_TRY((launch_conv27<true>(c, c->p1, c->L[2].wb, c->s2, N[1], s)));
   pool_fwd_kernel<<<grid1(c->P[2] * C), 256, 0, s>>>(c->s2, c->p2, N[1], C);
-  GBFEM_TRY((launch_conv<C, C, 27, true, bf16>(c->p2, c->L[3].wb, c->s3, N[2], s)));
+  GBFEM_TRY((launch_conv27<true>(c, c->p2, c->L[3].wb, c->s3, N[2], s)));
   pool_fwd_kernel<<<grid1(c->P[3] * C), 256, 0, s>>>(c->s3, c->p3, N[2], C);
-  GBFEM_TRY((launch_conv<C, C, 27, true, bf16>(c->p3, c->L[4].wb, c->b4, N[3], s)));
+  GBFEM_TRY((launch_conv27<true>(c, c->p3, c->L[4].wb, c->b4, N[3], s)));
   up_add_kernel<<<grid1(c->P[2] * C), 256, 0, s>>>(c->b4, c->s3, c->u3, N[2], C);
-  GBFEM_TRY((launch_conv<C, C, 27, true, bf16>(c->u3, c->L[5].wb, c->d3, N[2], s)));
+  GBFEM_TRY((launch_conv27<true>(c, c->u3, c->L[5].wb, c->d3, N[2], s)));
   up_add_kernel<<<grid1(c->P[1] * C), 256, 0, s>>>(c->d3, c->s2, c->u2, N[1], C);
-  GBFEM_TRY((launch_conv<C, C, 27, true, bf16>(c->u2, c->L[6].wb, c->d2, N[1], s)));
+  GBFEM_TRY((launch_conv27<true>(c, c->u2, c->L[6].wb, c->d2, N[1], s)));
   up_add_kernel<<<grid1(c->P[0] * C), 256, 0, s>>>(c->d2, c->s1, c->u1, N[0], C);
-  GBFEM_TRY((launch_conv<C, C, 27, true, bf16>(c->u1, c->L[7].wb, c->d1, N[0], s)));
+  GBFEM_TRY((launch_conv27<true>(c, c->u1, c->L[7].wb, c->d1, N[0], s)));
   GBFEM_TRY(conv_out_fwd(c, s));
   GBFEM_CUDA_TRY(cudaGetLastError());
   return GBFEM_OK;
@@ -319,37 +405,37 @@ static int cnn_backward(gbfem_cnn_s* c, cudaStream_t s) {
   relu_mask_kernel<<<grid1(P[0] * C), 256, 0, s>>>(G00, c->d1, P[0] * C);
   // d1 = relu(W7 * u1) [0]:  dW7;  G01 = du1 = W7^T * G00
   GBFEM_TRY((launch_wgrad<C, C, 27>(c, c->u1, G00, c->L[7].g, N[0], s)));
-  GBFEM_TRY((launch_conv<C, C, 27, false, bf16>(G00, c->L[7].wbt, G01, N[0], s)));
+  GBFEM_TRY((launch_conv27<false>(c, G00, c->L[7].wbt, G01, N[0], s)));
   // u1 = up(d2) + s1:  G10 = dd2 = downsum(du1) * (d2 > 0) [1]
   up_bwd_mask_kernel<<<grid1(P[1] * C), 256, 0, s>>>(G01, c->d2, G10, N[0], C);
   // d2 = relu(W6 * u2) [1]:  dW6;  G11 = du2
   GBFEM_TRY((launch_wgrad<C, C, 27>(c, c->u2, G10, c->L[6].g, N[1], s)));
-  GBFEM_TRY((launch_conv<C, C, 27, false, bf16>(G10, c->L[6].wbt, G11, N[1], s)));
+  GBFEM_TRY((launch_conv27<false>(c, G10, c->L[6].wbt, G11, N[1], s)));
   // u2 = up(d3) + s2:  G20 = dd3 [2]
   up_bwd_mask_kernel<<<grid1(P[2] * C), 256, 0, s>>>(G11, c->d3, G20, N[1], C);
   // d3 = relu(W5 * u3) [2]:  dW5;  G21 = du3
   GBFEM_TRY((launch_wgrad<C, C, 27>(c, c->u3, G20, c->L[5].g, N[2], s)));
-  GBFEM_TRY((launch_conv<C, C, 27, false, bf16>(G20, c->L[5].wbt, G21, N[2], s)));
+  GBFEM_TRY((launch_conv27<false>(c, G20, c->L[5].wbt, G21, N[2], s)));
   // u3 = up(b4) + s3:  G30 = db4 [3]
   up_bwd_mask_kernel<<<grid1(P[3] * C), 256, 0, s>>>(G21, c->b4, G30, N[2], C);
   // b4 = relu(W4 * p3) [3]:  dW4;  G31 = dp3
   GBFEM_TRY((launch_wgrad<C, C, 27>(c, c->p3, G30, c->L[4].g, N[3], s)));
-  GBFEM_TRY((launch_conv<C, C, 27, false, bf16>(G30, c->L[4].wbt, G31, N[3], s)));
+  GBFEM_TRY((launch_conv27<false>(c, G30, c->L[4].wbt, G31, N[3], s)));
   // p3 = pool(s3):  G20 = ds3 = (du3 + pool_back(dp3)) * (s3 > 0) [2]
   pool_bwd_add_mask_kernel<<<grid1(P[2] * C), 256, 0, s>>>(G21, G31, c->s3, G20, N[2], C);
   // s3 = relu(W3 * p2) [2]:  dW3;  G21 = dp2
   GBFEM_TRY((launch_wgrad<C, C, 27>(c, c->p2, G20, c->L[3].g, N[2], s)));
-  GBFEM_TRY((launch_conv<C, C, 27, false, bf16>(G20, c->L[3].wbt, G21, N[2], s)));
+  GBFEM_TRY((launch_conv27<false>(c, G20, c->L[3].wbt, G21, N[2], s)));
   // p2 = pool(s2):  G10 = ds2 = (du2 + pool_back(dp2)) * (s2 > 0) [1]
   pool_bwd_add_mask_kernel<<<grid1(P[1] * C), 256, 0, s>>>(G11, G21, c->s2, G10, N[1], C);
   // s2 = relu(W2 * p1) [1]:  dW2;  G11 = dp1
   GBFEM_TRY((launch_wgrad<C, C, 27>(c, c->p1, G10, c->L[2].g, N[1], s)));
-  GBFEM_TRY((launch_conv<C, C, 27, false, bf16>(G10, c->L[2].wbt, G11, N[1], s)));
+  GBFEM_TRY((launch_conv27<false>(c, G10, c->L[2].wbt, G11, N[1], s)));
   // p1 = pool(s1):  G00 = ds1 = (du1 + pool_back(dp1)) * (s1 > 0) [0]
   pool_bwd_add_mask_kernel<<<grid1(P[0] * C), 256, 0, s>>>(G01, G11, c->s1, G00, N[0], C);
   // s1 = relu(W1 * a0) [0]:  dW1;  G01 = da0 = (W1^T * ds1) * (a0 > 0)
   GBFEM_TRY((launch_wgrad<C, C, 27>(c, c->a0, G00, c->L[1].g, N[0], s)));
-  GBFEM_TRY((launch_conv<C, C, 27, false, bf16>(G00, c->L[1].wbt, G01, N[0], s)));
+  GBFEM_TRY((launch_conv27<false>(c, G00, c->L[1].wbt, G01, N[0], s)));
   relu_mask_kernel<<<grid1(P[0] * C), 256, 0, s>>>(G01, c->a0, P[0] * C);
   // a0 = relu(W0 x0) [0]:  dW0
   switch (c->cin0) {
@@ -381,7 +467,7 @@ static int cnn_input(gbfem_cnn_s* c, const void* r, cudaStream_t s) {
     coarse_sumsq_kernel<T><<<1, 256, 0, s>>>(static_cast<const T*>(r), c->nloc, c->P[0], c->d_rr);
   else
     GBFEM_TRY(dot_device(sizeof(T) == 8 ? GBFEM_F64 : GBFEM_F32, c->ndofs, r, r, c->d_rr, c->d_partial, s));
-  assemble_input_kernel<T><<<grid1(c->P[0] * c->cin0), 256, 0, s>>>(static_cast<const T*>(r), c->logk, c->d_rr,
+  assemble_input_kernel<T><<<grid1(c->P[0] * c->cin0 / 2), 256, 0, s>>>(static_cast<const T*>(r), c->logk, c->d_rr,
                                                                     cnn_nnorm(c), c->nloc, c->cin0, c->P[0], c->coarse,
                                                                     c->x0);
   GBFEM_CUDA_TRY(cudaGetLastError());
@@ -507,6 +593,8 @@ int gbfem_cnn_create(int order, int cells, uint64_t seed, gbfem_cnn* out) {
   *out = nullptr;
   if (order < 1 || order > 4) return set_error(GBFEM_ERR_INVALID, "gbfem_cnn_create: order 1..4");
   if (cells < 8 || cells % 8) return set_error(GBFEM_ERR_INVALID, "gbfem_cnn_create: cells must be a multiple of 8");
+  if (cells > 256)  // the elementwise kernels index with 32 bits
+    return set_error(GBFEM_ERR_NOT_IMPLEMENTED, "gbfem_cnn_create: at most 256 cells per direction");
   auto* c = new (std::nothrow) gbfem_cnn_s();
   if (!c) return set_error(GBFEM_ERR_INVALID, "out of host memory");
   const int n = order + 1;
@@ -561,6 +649,7 @@ int gbfem_cnn_create(int order, int cells, uint64_t seed, gbfem_cnn* out) {
   A((void**)&c->logk, c->P[0] * 4);
   A((void**)&c->d_rr, 64);
   A((void**)&c->d_loss, 64);
+  A((void**)&c->status, 64);
   A((void**)&c->d_partial, sizeof(double) * (dot_num_partials(std::max(c->ndofs, c->P[0] * c->cout0)) + 8));
   if (rc == GBFEM_OK) {
     cudaError_t e = cudaMallocHost(&c->h_loss, 64);
@@ -591,6 +680,16 @@ int gbfem_cnn_create(int order, int cells, uint64_t seed, gbfem_cnn* out) {
     if (e != cudaSuccess) rc = set_cuda_error(e, "gbfem_cnn_create: init");
   }
   if (rc == GBFEM_OK) {
+    cudaError_t e = cudaMemset(c->status, 0, sizeof(int));
+    if (e != cudaSuccess) rc = set_cuda_error(e, "gbfem_cnn_create");
+  }
+  // tensor maps of the 3x3x3 convolutions' inputs (forward, backward-data)
+  {
+    const bf16* in[] = {c->a0, c->p1, c->p2, c->p3, c->u3, c->u2, c->u1, c->G[0][0], c->G[1][0], c->G[2][0], c->G[3][0]};
+    const int lv[] = {0, 1, 2, 3, 2, 1, 0, 0, 1, 2, 3};
+    for (int k = 0; k < 11 && rc == GBFEM_OK; ++k) rc = conv_map(c, in[k], c->N[lv[k]]);
+  }
+  if (rc == GBFEM_OK) {
     logkappa_kernel<double><<<grid1(c->P[0]), 256>>>(nullptr, c->nloc, c->P[0], c->logk);
     rc = refresh_bf16(c, nullptr);
   }
@@ -619,6 +718,19 @@ int gbfem_cnn_set_kappa(gbfem_cnn c, int precision, const void* kappa, void* str
   else
     logkappa_kernel<float><<<grid1(c->P[0]), 256, 0, s>>>(static_cast<const float*>(kappa), c->nloc, c->P[0], c->logk);
   GBFEM_CUDA_TRY(cudaGetLastError());
+  return GBFEM_OK;
+}
+
+int gbfem_cnn_set_conv_engine(gbfem_cnn c, int engine) {
+  if (!c || (engine != GBFEM_CNN_CONV_TENSOR_CORE && engine != GBFEM_CNN_CONV_MMA_SYNC))
+    return set_error(GBFEM_ERR_INVALID, "gbfem_cnn_set_conv_engine: invalid argument");
+  c->conv_engine = engine;
+  return GBFEM_OK;
+}
+
+int gbfem_cnn_status(gbfem_cnn c, int* status) {
+  if (!c || !status) return set_error(GBFEM_ERR_INVALID, "gbfem_cnn_status: null argument");
+  GBFEM_CUDA_TRY(cudaMemcpy(status, c->status, sizeof(int), cudaMemcpyDeviceToHost));
   return GBFEM_OK;
 }
 

@@ -207,76 +207,113 @@ __global__ void wgrad_reduce_kernel(const float* __restrict__ part, float* __res
 }
 
 // ------------------------------------------------------------ elementwise --
-// 2x2x2 average pooling: out[P/8][C] from in[P][C] (grid N -> N/2)
+// 32 channels per position, handled as 16 BF16 pairs; 32-bit indices (the
+// network's grids hold fewer than 2^31 values, checked at creation).
+constexpr int kEwC = 32, kEwPairs = kEwC / 2;
+typedef __nv_bfloat162 bf162;
+
+__device__ __forceinline__ unsigned ew_coarse(unsigned x, unsigned y, unsigned z, unsigned Nc) {
+  return (x >> 1) + Nc * ((y >> 1) + Nc * (z >> 1));
+}
+
+// 2x2x2 average pooling: out[P/8][32] from in[P][32] (grid N -> N/2)
 __global__ void pool_fwd_kernel(const bf16* __restrict__ in, bf16* __restrict__ out, int N, int C) {
-  const int Nc = N / 2;
-  const long long total = (long long)Nc * Nc * Nc * C;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-    const int c = int(e % C);
-    const long long pc = e / C;
-    const int x = int(pc % Nc), y = int((pc / Nc) % Nc), z = int(pc / ((long long)Nc * Nc));
-    float s = 0.f;
+  const unsigned Nc = unsigned(N) / 2u, total = Nc * Nc * Nc * kEwPairs;
+  const bf162* in2 = reinterpret_cast<const bf162*>(in);
+  bf162* out2 = reinterpret_cast<bf162*>(out);
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const unsigned c2 = e % kEwPairs, pc = e / kEwPairs;
+    const unsigned x = pc % Nc, y = (pc / Nc) % Nc, z = pc / (Nc * Nc);
+    float s0 = 0.f, s1 = 0.f;
+#pragma unroll
     for (int k = 0; k < 8; ++k) {
-      const long long pf = (2 * x + (k & 1)) + (long long)N * ((2 * y + ((k >> 1) & 1)) + (long long)N * (2 * z + (k >> 2)));
-      s += __bfloat162float(in[pf * C + c]);
+      const unsigned pf = (2u * x + (k & 1)) + unsigned(N) * ((2u * y + ((k >> 1) & 1)) + unsigned(N) * (2u * z + (k >> 2)));
+      const float2 v = __bfloat1622float2(in2[pf * kEwPairs + c2]);
+      s0 += v.x;
+      s1 += v.y;
     }
-    out[e] = __float2bfloat16_rn(0.125f * s);
+    out2[e] = __floats2bfloat162_rn(0.125f * s0, 0.125f * s1);
   }
+  (void)C;
 }
 
 // d_fine = (d_skip + pool_backward(d_coarse)) * (act > 0), fine grid N
 __global__ void pool_bwd_add_mask_kernel(const bf16* __restrict__ dskip, const bf16* __restrict__ dcoarse,
                                          const bf16* __restrict__ act, bf16* __restrict__ dfine, int N, int C) {
-  const long long total = (long long)N * N * N * C;
-  const int Nc = N / 2;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-    const int c = int(e % C);
-    const long long p = e / C;
-    const int x = int(p % N), y = int((p / N) % N), z = int(p / ((long long)N * N));
-    const long long pc = (x / 2) + (long long)Nc * ((y / 2) + (long long)Nc * (z / 2));
-    float v = __bfloat162float(dskip[e]) + 0.125f * __bfloat162float(dcoarse[pc * C + c]);
-    if (!(__bfloat162float(act[e]) > 0.f)) v = 0.f;
-    dfine[e] = __float2bfloat16_rn(v);
+  const unsigned Nn = unsigned(N), Nc = Nn / 2u, total = Nn * Nn * Nn * kEwPairs;
+  const bf162* ds = reinterpret_cast<const bf162*>(dskip);
+  const bf162* dc = reinterpret_cast<const bf162*>(dcoarse);
+  const bf162* ac = reinterpret_cast<const bf162*>(act);
+  bf162* df = reinterpret_cast<bf162*>(dfine);
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const unsigned c2 = e % kEwPairs, p = e / kEwPairs;
+    const unsigned x = p % Nn, y = (p / Nn) % Nn, z = p / (Nn * Nn);
+    const float2 a = __bfloat1622float2(ds[e]);
+    const float2 b = __bfloat1622float2(dc[ew_coarse(x, y, z, Nc) * kEwPairs + c2]);
+    const float2 m = __bfloat1622float2(ac[e]);
+    float v0 = a.x + 0.125f * b.x, v1 = a.y + 0.125f * b.y;
+    if (!(m.x > 0.f)) v0 = 0.f;
+    if (!(m.y > 0.f)) v1 = 0.f;
+    df[e] = __floats2bfloat162_rn(v0, v1);
   }
+  (void)C;
 }
 
 // out_fine = upsample_nearest(coarse) + skip
 __global__ void up_add_kernel(const bf16* __restrict__ coarse, const bf16* __restrict__ skip, bf16* __restrict__ out,
                               int N, int C) {
-  const long long total = (long long)N * N * N * C;
-  const int Nc = N / 2;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-    const int c = int(e % C);
-    const long long p = e / C;
-    const int x = int(p % N), y = int((p / N) % N), z = int(p / ((long long)N * N));
-    const long long pc = (x / 2) + (long long)Nc * ((y / 2) + (long long)Nc * (z / 2));
-    out[e] = __float2bfloat16_rn(__bfloat162float(coarse[pc * C + c]) + __bfloat162float(skip[e]));
+  const unsigned Nn = unsigned(N), Nc = Nn / 2u, total = Nn * Nn * Nn * kEwPairs;
+  const bf162* co = reinterpret_cast<const bf162*>(coarse);
+  const bf162* sk = reinterpret_cast<const bf162*>(skip);
+  bf162* o = reinterpret_cast<bf162*>(out);
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const unsigned c2 = e % kEwPairs, p = e / kEwPairs;
+    const unsigned x = p % Nn, y = (p / Nn) % Nn, z = p / (Nn * Nn);
+    const float2 a = __bfloat1622float2(co[ew_coarse(x, y, z, Nc) * kEwPairs + c2]);
+    const float2 b = __bfloat1622float2(sk[e]);
+    o[e] = __floats2bfloat162_rn(a.x + b.x, a.y + b.y);
   }
+  (void)C;
 }
 
 // d_coarse = (sum of the 8 children of d_fine) * (act_coarse > 0)
 __global__ void up_bwd_mask_kernel(const bf16* __restrict__ dfine, const bf16* __restrict__ act,
                                    bf16* __restrict__ dcoarse, int N, int C) {
-  const int Nc = N / 2;
-  const long long total = (long long)Nc * Nc * Nc * C;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
-    const int c = int(e % C);
-    const long long pc = e / C;
-    const int x = int(pc % Nc), y = int((pc / Nc) % Nc), z = int(pc / ((long long)Nc * Nc));
-    float s = 0.f;
+  const unsigned Nc = unsigned(N) / 2u, total = Nc * Nc * Nc * kEwPairs;
+  const bf162* df = reinterpret_cast<const bf162*>(dfine);
+  const bf162* ac = reinterpret_cast<const bf162*>(act);
+  bf162* dc = reinterpret_cast<bf162*>(dcoarse);
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const unsigned c2 = e % kEwPairs, pc = e / kEwPairs;
+    const unsigned x = pc % Nc, y = (pc / Nc) % Nc, z = pc / (Nc * Nc);
+    float s0 = 0.f, s1 = 0.f;
+#pragma unroll
     for (int k = 0; k < 8; ++k) {
-      const long long pf = (2 * x + (k & 1)) + (long long)N * ((2 * y + ((k >> 1) & 1)) + (long long)N * (2 * z + (k >> 2)));
-      s += __bfloat162float(dfine[pf * C + c]);
+      const unsigned pf = (2u * x + (k & 1)) + unsigned(N) * ((2u * y + ((k >> 1) & 1)) + unsigned(N) * (2u * z + (k >> 2)));
+      const float2 v = __bfloat1622float2(df[pf * kEwPairs + c2]);
+      s0 += v.x;
+      s1 += v.y;
     }
-    if (!(__bfloat162float(act[e]) > 0.f)) s = 0.f;
-    dcoarse[e] = __float2bfloat16_rn(s);
+    const float2 m = __bfloat1622float2(ac[e]);
+    if (!(m.x > 0.f)) s0 = 0.f;
+    if (!(m.y > 0.f)) s1 = 0.f;
+    dc[e] = __floats2bfloat162_rn(s0, s1);
   }
+  (void)C;
 }
 
-// x *= (act > 0)
+// x *= (act > 0), n values (even)
 __global__ void relu_mask_kernel(bf16* __restrict__ x, const bf16* __restrict__ act, long long n) {
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
-    if (!(__bfloat162float(act[e]) > 0.f)) x[e] = __float2bfloat16_rn(0.f);
+  bf162* x2 = reinterpret_cast<bf162*>(x);
+  const bf162* a2 = reinterpret_cast<const bf162*>(act);
+  const unsigned total = unsigned(n / 2);
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const float2 m = __bfloat1622float2(a2[e]);
+    float2 v = __bfloat1622float2(x2[e]);
+    if (!(m.x > 0.f)) v.x = 0.f;
+    if (!(m.y > 0.f)) v.y = 0.f;
+    x2[e] = __floats2bfloat162_rn(v.x, v.y);
+  }
 }
 
 }  // namespace cnn

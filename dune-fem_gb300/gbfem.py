@@ -954,6 +954,17 @@ class CNN:
     def scale(self, v):
         check(lib().gbfem_cnn_set_output_scale(self.handle, float(v)))
 
+    def set_conv_engine(self, engine):
+        """"tensor" (default): the 3x3x3 convolutions as tcgen05 implicit
+        GEMMs; "mma": warp-level mma.sync."""
+        check(lib().gbfem_cnn_set_conv_engine(self.handle, {"tensor": 0, "mma": 1}[engine]))
+
+    def status(self):
+        """0, or 1 if a tensor-core convolution gave up on a bounded wait."""
+        v = C.c_int()
+        check(lib().gbfem_cnn_status(self.handle, C.byref(v)))
+        return v.value
+
     def set_coarse(self, coarse=True):
         """Learned coarse-grid correction: cell means in, cell means out."""
         check(lib().gbfem_cnn_set_coarse(self.handle, 1 if coarse else 0))

@@ -490,6 +490,21 @@ int gbfem_cnn_set_kappa(gbfem_cnn cnn, int precision, const void* kappa, void* s
  * and log kappa, and writes only the cell means of z: a learned coarse-grid
  * correction for the two-level form of the learned preconditioner. */
 int gbfem_cnn_set_coarse(gbfem_cnn cnn, int coarse);
+/* The engine of the 3x3x3 convolutions (forward and backward-data):
+ * GBFEM_CNN_CONV_TENSOR_CORE (default) runs them as implicit GEMMs on the
+ * tcgen05 tensor cores (BF16 operands, FP32 accumulators in tensor memory);
+ * GBFEM_CNN_CONV_MMA_SYNC on warp-level mma.sync. */
+#define GBFEM_CNN_CONV_TENSOR_CORE 0
+#define GBFEM_CNN_CONV_MMA_SYNC 1
+int gbfem_cnn_set_conv_engine(gbfem_cnn cnn, int engine);
+/* 0, or 1 once a tensor-core convolution gave up on a bounded wait (its
+ * output is then incomplete).  Synchronises with the device. */
+int gbfem_cnn_status(gbfem_cnn cnn, int* status);
+/* Self-test: the float <-> double conversions the elementwise kernels do in
+ * integer arithmetic against the hardware's, on n random bit patterns
+ * (including values near the binary32 range limits and rounding ties);
+ * mismatches is 0 when they agree everywhere. */
+int gbfem_selftest_conversions(uint64_t n, uint64_t seed, uint64_t* mismatches);
 int gbfem_cnn_set_output_scale(gbfem_cnn cnn, double scale);
 int gbfem_cnn_get_output_scale(gbfem_cnn cnn, double* scale);
 /* z = S rms(r) NN(r/rms(r)) (accumulate = 1: z += ...). */

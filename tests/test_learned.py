@@ -13,12 +13,13 @@ def _rel(a, b):
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
-@pytest.mark.parametrize("order", [1, 3])
-def test_forward_and_gradients_match_cpu_oracle(gb, order):
+@pytest.mark.parametrize("order,engine", [(1, "tensor"), (3, "tensor"), (3, "mma")])
+def test_forward_and_gradients_match_cpu_oracle(gb, order, engine):
     import cnn_oracle as co
     N = 8
     nloc = (order + 1) ** 3
     net = gb.CNN(order, N, seed=3)
+    net.set_conv_engine(engine)
     rng = np.random.default_rng(order)
     n = N ** 3 * nloc
     kappa = np.zeros(n)
@@ -46,10 +47,11 @@ def test_forward_and_gradients_match_cpu_oracle(gb, order):
         cos = np.sum(a * b) / (np.linalg.norm(a) * np.linalg.norm(b) + 1e-300)
         assert cos > 0.998, (i, cos)
         assert _rel(a, b) < 0.1, (i, _rel(a, b))
+    assert net.status() == 0
 
 
-@pytest.mark.parametrize("order", [1, 3])
-def test_exact_arithmetic_network_matches_oracle_bitwise(gb, order):
+@pytest.mark.parametrize("order,engine,N", [(1, "tensor", 8), (3, "tensor", 8), (3, "mma", 8), (1, "tensor", 16)])
+def test_exact_arithmetic_network_matches_oracle_bitwise(gb, order, engine, N):
     """With one tap per 3x3x3 layer and a scaled permutation as its channel
     matrix, weights in {1/2, 1, 2}, inputs +-1 (rms 1), kappa 1 and dyadic
     targets, every product and sum the kernels form is exact in FP32, so the
@@ -58,9 +60,9 @@ def test_exact_arithmetic_network_matches_oracle_bitwise(gb, order):
     offset, flip or channel index anywhere in forward, backward-data or
     weight-gradient kernels shows as a mismatch."""
     import cnn_oracle as co
-    N = 8
     nloc = (order + 1) ** 3
     net = gb.CNN(order, N, seed=1)
+    net.set_conv_engine(engine)
     rng = np.random.default_rng(10 + order)
     shapes, cin0, cout0 = co.layer_shapes(nloc)
     Ws = []
@@ -95,6 +97,35 @@ def test_exact_arithmetic_network_matches_oracle_bitwise(gb, order):
         nonzero += int(np.count_nonzero(b))
         assert np.max(np.abs(a - b)) <= 1e-5 * max(np.max(np.abs(b)), 1e-30), (i, _rel(a, b))
     assert nonzero > 0
+    assert net.status() == 0
+
+
+def test_tensor_core_and_mma_convolutions_agree(gb):
+    """Both engines on a 32^3 grid (256 tiles of 128 positions, two CTAs per
+    SM): the outputs agree to the BF16 rounding of FP32 sums taken in a
+    different order, and the training step's gradients likewise."""
+    N, order = 32, 2
+    nloc = 27
+    n = N ** 3 * nloc
+    rng = np.random.default_rng(5)
+    kappa = np.zeros(n)
+    kappa[::nloc] = np.exp(rng.normal(0, 1, N ** 3))
+    r = gb.DeviceArray.from_numpy(rng.uniform(-1, 1, n))
+    t = gb.DeviceArray.from_numpy(rng.uniform(-1, 1, n))
+    outs, grads = [], []
+    for engine in ("tensor", "mma"):
+        net = gb.CNN(order, N, seed=7)
+        net.set_conv_engine(engine)
+        net.set_kappa(gb.DeviceArray.from_numpy(kappa))
+        z = gb.DeviceArray(n)
+        net.forward(r, z)
+        net.loss_grad(r, t)
+        outs.append(z.numpy())
+        grads.append(net.grads())
+        assert net.status() == 0
+    assert _rel(outs[0], outs[1]) < 2e-2
+    cos = np.dot(grads[0], grads[1]) / (np.linalg.norm(grads[0]) * np.linalg.norm(grads[1]))
+    assert cos > 0.999
 
 
 def test_training_reduces_the_loss_and_is_reproducible(gb):
@@ -238,3 +269,14 @@ def test_trained_network_gains_over_block_jacobi_on_held_out_kappa(gb):
     op64(u, au)
     ff = f.numpy()
     assert np.linalg.norm(ff - au.numpy()) <= 1.01e-10 * np.linalg.norm(ff)
+
+
+def test_integer_float_double_conversions_match_the_hardware(gb):
+    """The elementwise kernels convert between binary32 and binary64 in
+    integer arithmetic (csrc/convert.cuh); on 16M bit patterns, including
+    values near the binary32 limits and rounding ties, the results equal the
+    hardware's conversions bit for bit."""
+    import ctypes as C
+    bad = C.c_uint64(1)
+    gb.check(gb.lib().gbfem_selftest_conversions(C.c_uint64(1 << 24), C.c_uint64(12345), C.byref(bad)))
+    assert bad.value == 0
