@@ -1,0 +1,389 @@
+"""A UFL-shaped front end for the run-time compiled DG forms.
+
+dune-fem writes schemes in UFL (python/dune/models/integrands/ufl.py lowers
+a UFL form to the C++ of an integrands class).  This module accepts forms
+written the same way over the structured-grid DG spaces of this package,
+for example
+
+    u, v, x = TrialFunction(1), TestFunction(1), SpatialCoordinate()
+    a = inner((1 + u[0]**2) * grad(u)[0, :], grad(v)[0, :]) * dx \
+        + (u[0]**3 - sin(x[0])) * v[0] * dx
+    form = to_form(a, dirichlet=[x[0] * x[1]])
+
+and lowers them to the pointwise pieces of integrands.Form: the coefficient
+of grad v in the dx terms becomes the diffusive flux F(x, u, grad u), the
+coefficient of v the source s(x, u, grad u), and the DG face terms are the
+interior-penalty ones Form builds from F (with A = dF/d grad u by dual
+numbers).  A convective flux with its wave speed and Dirichlet data are
+given as expressions too.
+
+What is supported: the trial function u (components u[m]), its gradient
+grad(u)[m, k], the spatial coordinate x[k], numbers and Constant, + - * /
+and ** (numeric or integer exponents), exp, log, sqrt, sin, cos, tan, tanh,
+sinh, cosh, atan, abs, max_value / min_value, conditional(cond, a, b) with
+lt / gt / le / ge, inner / dot over component lists, and the facet normal
+n[k] in a wave speed.  The form must be
+linear in the test function v, with every term integrated over dx.
+Interior facet (dS) and boundary (ds) measures, jump and avg are not
+supported: the face terms are generated.
+"""
+import numbers
+
+import integrands
+
+
+class Expr:
+    """A scalar expression tree; cpp() is its CUDA C++ text in the form
+    kernels' names (u[m], g[m][k], x[k])."""
+
+    def __add__(self, o):
+        return _bin("+", self, o)
+
+    def __radd__(self, o):
+        return _bin("+", o, self)
+
+    def __sub__(self, o):
+        return _bin("-", self, o)
+
+    def __rsub__(self, o):
+        return _bin("-", o, self)
+
+    def __mul__(self, o):
+        if isinstance(o, (VLinear, Vector)):
+            return o.__rmul__(self)
+        return _bin("*", self, o)
+
+    def __rmul__(self, o):
+        return _bin("*", o, self)
+
+    def __truediv__(self, o):
+        return _bin("/", self, o)
+
+    def __rtruediv__(self, o):
+        return _bin("/", o, self)
+
+    def __neg__(self):
+        return Op("-", (self,))
+
+    def __abs__(self):
+        return Op("fabs", (self,))
+
+    def __pow__(self, p):
+        if isinstance(p, numbers.Integral) and 1 <= p <= 16:
+            return Op("ipow%d" % p, (self,))
+        return Op("pow", (self, _wrap(p)))
+
+    def __lt__(self, o):
+        return Cond("<", self, _wrap(o))
+
+    def __gt__(self, o):
+        return Cond(">", self, _wrap(o))
+
+    def __le__(self, o):
+        return Cond("<=", self, _wrap(o))
+
+    def __ge__(self, o):
+        return Cond(">=", self, _wrap(o))
+
+
+class Num(Expr):
+    def __init__(self, v):
+        self.v = float(v)
+
+    def cpp(self):
+        return repr(self.v)
+
+
+class Constant(Num):
+    """A named constant (its value is compiled into the kernel)."""
+
+    def __init__(self, v, name=None):
+        super().__init__(v)
+        self.name = name
+
+
+class Leaf(Expr):
+    def __init__(self, text):
+        self.text = text
+
+    def cpp(self):
+        return self.text
+
+
+class Op(Expr):
+    _FN = {"exp", "log", "sqrt", "sin", "cos", "tan", "tanh", "sinh", "cosh", "atan", "fabs", "pow", "max", "min"}
+
+    def __init__(self, op, args):
+        self.op, self.args = op, args
+
+    def cpp(self):
+        a = [x.cpp() for x in self.args]
+        if self.op in "+-*/" and len(a) == 2:
+            return "(%s %s %s)" % (a[0], self.op, a[1])
+        if self.op == "-":
+            return "(-%s)" % a[0]
+        if self.op.startswith("ipow"):
+            return "ipow<%s>(D(%s))" % (self.op[4:], a[0])
+        if self.op in ("max", "min"):
+            return "%s(D(%s), D(%s))" % (self.op, a[0], a[1])
+        if self.op == "pow":
+            return "pow(D(%s), %s)" % (a[0], a[1])
+        return "%s(%s)" % (self.op, ", ".join(a))
+
+
+class Cond(Expr):
+    def __init__(self, op, a, b):
+        self.op, self.a, self.b = op, a, b
+
+    def cpp(self):
+        return "(%s %s %s)" % (self.a.cpp(), self.op, self.b.cpp())
+
+
+class Conditional(Expr):
+    def __init__(self, c, a, b):
+        self.c, self.a, self.b = c, a, b
+
+    def cpp(self):
+        return "(%s ? D(%s) : D(%s))" % (self.c.cpp(), self.a.cpp(), self.b.cpp())
+
+
+def _wrap(v):
+    if isinstance(v, Expr):
+        return v
+    if isinstance(v, numbers.Real):
+        return Num(v)
+    raise TypeError("ufl: cannot use %r in an expression" % (v,))
+
+
+def _is(e, v):
+    return isinstance(e, Num) and not isinstance(e, Constant) and e.v == v
+
+
+def _bin(op, a, b):
+    a, b = _wrap(a), _wrap(b)
+    if op == "*" and _is(b, 1.0):
+        return a
+    if op == "*" and _is(a, 1.0):
+        return b
+    return Op(op, (a, b))
+
+
+def _fn(name):
+    def f(a):
+        return Op(name, (_wrap(a),))
+    return f
+
+
+exp, log, sqrt, sin, cos, tan = _fn("exp"), _fn("log"), _fn("sqrt"), _fn("sin"), _fn("cos"), _fn("tan")
+tanh, sinh, cosh, atan = _fn("tanh"), _fn("sinh"), _fn("cosh"), _fn("atan")
+
+
+def max_value(a, b):
+    return Op("max", (_wrap(a), _wrap(b)))
+
+
+def min_value(a, b):
+    return Op("min", (_wrap(a), _wrap(b)))
+
+
+def conditional(c, a, b):
+    if not isinstance(c, Cond):
+        raise TypeError("ufl: conditional needs a comparison (lt, gt, le, ge or <, >, <=, >=)")
+    return Conditional(c, _wrap(a), _wrap(b))
+
+
+def lt(a, b):
+    return Cond("<", _wrap(a), _wrap(b))
+
+
+def gt(a, b):
+    return Cond(">", _wrap(a), _wrap(b))
+
+
+def le(a, b):
+    return Cond("<=", _wrap(a), _wrap(b))
+
+
+def ge(a, b):
+    return Cond(">=", _wrap(a), _wrap(b))
+
+
+class Vector:
+    """A list of expressions (a gradient row, a coefficient vector)."""
+
+    def __init__(self, items):
+        self.items = list(items)
+
+    def __len__(self):
+        return len(self.items)
+
+    def __getitem__(self, k):
+        return self.items[k]
+
+    def __mul__(self, s):
+        return Vector([e * s for e in self.items])
+
+    def __rmul__(self, s):
+        return Vector([s * e for e in self.items])
+
+    def __add__(self, o):
+        return Vector([a + b for a, b in zip(self.items, o.items)])
+
+    def __sub__(self, o):
+        return Vector([a - b for a, b in zip(self.items, o.items)])
+
+    def __neg__(self):
+        return Vector([-a for a in self.items])
+
+
+def as_vector(items):
+    return Vector([_wrap(e) if not isinstance(e, VLinear) else e for e in items])
+
+
+# ---- the test function and forms linear in it ---------------------------------
+
+class VLinear:
+    """sum_m c_v[m] v_m + sum_{m,k} c_g[m][k] dv_m/dx_k (c: expressions)."""
+
+    def __init__(self, terms=None):
+        self.terms = dict(terms or {})  # ("v", m) or ("g", m, k) -> Expr
+
+    def _scale(self, s):
+        return VLinear({k: _wrap(s) * c for k, c in self.terms.items()})
+
+    def __mul__(self, s):
+        if isinstance(s, (VLinear, Vector)):
+            raise ValueError("ufl: the form is not linear in the test function")
+        if isinstance(s, Measure):
+            return s.__rmul__(self)
+        return self._scale(s)
+
+    __rmul__ = _scale
+
+    def __truediv__(self, s):
+        return self._scale(1.0 / _wrap(s) if not isinstance(s, numbers.Real) else 1.0 / s)
+
+    def __add__(self, o):
+        if not isinstance(o, VLinear):
+            raise ValueError("ufl: a sum of terms linear and not linear in the test function")
+        t = dict(self.terms)
+        for k, c in o.terms.items():
+            t[k] = t[k] + c if k in t else c
+        return VLinear(t)
+
+    def __sub__(self, o):
+        return self + (-1.0) * o
+
+    def __neg__(self):
+        return self._scale(-1.0)
+
+
+class TestFunction:
+    """v of the DG space with `components` components: v[m]."""
+
+    def __init__(self, components=1):
+        self.components = components
+
+    def __getitem__(self, m):
+        return VLinear({("v", m): Num(1.0)})
+
+
+class TrialFunction:
+    """u, the unknown of a (possibly nonlinear) form: u[m]."""
+
+    def __init__(self, components=1):
+        self.components = components
+
+    def __getitem__(self, m):
+        return Leaf("u[%d]" % m)
+
+
+class SpatialCoordinate:
+    def __getitem__(self, k):
+        return Leaf("x[%d]" % k)
+
+
+class _Grad:
+    def __init__(self, f):
+        self.f = f
+
+    def __getitem__(self, idx):
+        m, k = idx
+        if isinstance(self.f, TestFunction):
+            if isinstance(k, slice):
+                return Vector([VLinear({("g", m, kk): Num(1.0)}) for kk in range(3)])
+            return VLinear({("g", m, k): Num(1.0)})
+        if isinstance(k, slice):
+            return Vector([Leaf("g[%d][%d]" % (m, kk)) for kk in range(3)])
+        return Leaf("g[%d][%d]" % (m, k))
+
+
+def grad(f):
+    """grad(u)[m, k] = du_m/dx_k (grad(u)[m, :] is the row as a vector)."""
+    if not isinstance(f, (TestFunction, TrialFunction)):
+        raise TypeError("ufl: grad of a test or trial function only")
+    return _Grad(f)
+
+
+def inner(a, b):
+    if isinstance(a, Vector) and isinstance(b, Vector):
+        if len(a) != len(b):
+            raise ValueError("ufl: inner of vectors of different lengths")
+        s = a[0] * b[0]
+        for i in range(1, len(a)):
+            s = s + a[i] * b[i]
+        return s
+    return a * b
+
+
+dot = inner
+
+
+class Measure:
+    def __init__(self, name):
+        self.name = name
+
+    def __rmul__(self, integrand):
+        if self.name != "dx":
+            raise NotImplementedError("ufl: only dx; the face terms are generated (interior penalty)")
+        if not isinstance(integrand, VLinear):
+            raise ValueError("ufl: the integrand must be linear in the test function")
+        return integrand
+
+
+dx = Measure("dx")
+ds = Measure("ds")
+dS = Measure("dS")
+
+
+def to_form(a, components=1, advection=None, wavespeed=None, dirichlet=None, symmetry=1):
+    """integrands.Form of the dx form `a` (linear in the test function):
+    flux F[m][k] = coefficient of dv_m/dx_k, source s[m] = coefficient of
+    v_m.  advection: per component a list of three expressions (Fa[m][k]),
+    wavespeed: an expression (may use n[k]), dirichlet: one expression of x
+    per component (None: natural boundary)."""
+    if not isinstance(a, VLinear):
+        raise ValueError("ufl: a must be a form (an integrand linear in v times dx)")
+    flux, source = [], []
+    for key, c in sorted(a.terms.items(), key=lambda kv: repr(kv[0])):
+        if key[0] == "g":
+            flux.append("F[%d][%d] = F[%d][%d] + D(%s);" % (key[1], key[2], key[1], key[2], c.cpp()))
+        else:
+            source.append("s[%d] = s[%d] + D(%s);" % (key[1], key[1], c.cpp()))
+    adv = None
+    if advection is not None:
+        adv = "\n".join("Fa[%d][%d] = D(%s);" % (m, k, _wrap(e).cpp())
+                        for m, row in enumerate(advection) for k, e in enumerate(row) if row is not None)
+    ws = _wrap(wavespeed).cpp() if wavespeed is not None else None
+    dirich = None
+    if dirichlet is not None:
+        dirich = "using D = R;\n" + "\n".join("gD[%d] = R(%s);" % (m, _wrap(e).cpp()) for m, e in enumerate(dirichlet))
+    return integrands.Form(components=components, flux="\n".join(flux) or None, source="\n".join(source) or None,
+                           advection=adv, wavespeed=ws, dirichlet=dirich, symmetry=symmetry)
+
+
+class FacetNormal:
+    """n[k] of the face, for the wave speed of a convective flux."""
+
+    def __getitem__(self, k):
+        return Leaf("n[%d]" % k)

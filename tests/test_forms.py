@@ -332,3 +332,77 @@ def test_rk3_steps_a_generated_form(gb):
         ra.step(ua, 1e-3)
         rb.step(ub, 1e-3)
     assert relmax(ua.numpy(), ub.numpy()) < 1e-12
+
+
+# ---- the UFL-shaped front end ------------------------------------------------------
+
+
+def _ufl_scalar():
+    from ufl_forms import (TestFunction, TrialFunction, SpatialCoordinate, grad, inner, dx, sin, to_form,
+                           as_vector)
+    u, v, x = TrialFunction(1), TestFunction(1), SpatialCoordinate()
+    gu = grad(u)[0, :]
+    a = (1 + u[0] ** 2)
+    F = as_vector([a * gu[0] + 0.3 * u[0] * gu[1], a * gu[1] - 0.3 * u[0] * gu[0], a * gu[2]])
+    form = inner(F, grad(v)[0, :]) * dx + (u[0] ** 3 - sin(x[0]) * x[1]) * v[0] * dx
+    return to_form(form, dirichlet=[x[0] * x[1] + 0.5])
+
+
+def _ufl_system():
+    from ufl_forms import (TestFunction, TrialFunction, SpatialCoordinate, FacetNormal, grad, inner, dx, cos,
+                           to_form)
+    u, v, x, n = TrialFunction(2), TestFunction(2), SpatialCoordinate(), FacetNormal()
+    F0 = grad(u)[0, :] + 0.2 * u[1] * grad(u)[1, :]
+    F1 = (1.0 + u[0] ** 2) * grad(u)[1, :]
+    form = (inner(F0, grad(v)[0, :]) + inner(F1, grad(v)[1, :]) + u[0] * u[1] * v[0]
+            + (-u[0] + cos(x[2])) * v[1]) * dx
+    b = _B
+    bn = b[0] * n[0] + b[1] * n[1] + b[2] * n[2]
+    return to_form(form, components=2, advection=[[0.0, 0.0, 0.0], [0.5 * u[1] ** 2 * bk for bk in b]],
+                   wavespeed=abs(bn * u[1]), dirichlet=[0.0, x[1]])
+
+
+def test_ufl_front_end_lowers_and_compiles(gb):
+    import ufl_forms as U
+    f = _ufl_scalar()
+    assert "F[0][0]" in f.pieces["flux"] and "s[0]" in f.pieces["source"] and "gD[0]" in f.pieces["dirichlet"]
+    g = _ufl_system()
+    assert g.components == 2 and "Fa[1][2]" in g.pieces["advection"] and "fabs" in g.pieces["wavespeed"]
+    u, v = U.TrialFunction(1), U.TestFunction(1)
+    with pytest.raises(ValueError):
+        (v[0] * v[0]) * U.dx  # not linear in v
+    with pytest.raises(NotImplementedError):
+        (u[0] * v[0]) * U.ds
+    with pytest.raises(TypeError):
+        U.grad(3.0)
+    if shutil.which("nvcc") is None and not __import__("os").path.exists("/usr/local/cuda/bin/nvcc"):
+        pytest.skip("no nvcc")
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        assert g.compile(gb.F64, 1, cache_dir=d).endswith(".cubin")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("system", [False, True])
+def test_ufl_forms_against_oracle(gb, system):
+    """The UFL-written forms equal the oracle of the same forms (and so the
+    hand-written pieces of the tests above)."""
+    import form_oracle as fo
+    import integrands
+    if system:
+        cells, order, periodic, M, form, orc = (4, 2, 2), 2, (1, 0, 0), 2, _ufl_system(), _sys_oracle(fo)
+    else:
+        cells, order, periodic, M, form, orc = (3, 2, 2), 2, (0, 0, 0), 1, _ufl_scalar(), _nl_oracle(fo)
+    lo, up = ((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)) if system else ((0.0, -0.4, 0.2), (1.2, 0.6, 1.0))
+    op = integrands.FormOperator(form, cells, order, periodic=periodic, lower=lo, upper=up)
+    spec = fo.FormSpec(cells, order, M, *orc, periodic=periodic, lower=lo, upper=up)
+    u = _rand(op.size, 21, 0.7)
+    w = gb.DeviceArray(op.size)
+    op(gb.DeviceArray.from_numpy(u), w)
+    assert relmax(w.numpy(), fo.residual(spec, u)) < 1e-12
+    du = _rand(op.size, 22)
+    if not system:  # smooth: the Jacobian against differences of the oracle
+        jac = op.jacobian(gb.DeviceArray.from_numpy(u))
+        y = gb.DeviceArray(op.size)
+        jac(gb.DeviceArray.from_numpy(du), y)
+        assert relmax(y.numpy(), fo.linearize(spec, u, du)) < 1e-9
