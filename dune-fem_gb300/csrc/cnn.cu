@@ -87,8 +87,10 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g, 
 }
 
 // x0[p][c]: c < nloc: r[p*nloc+c] / rms(r); c == nloc: log kappa_mean[p]; else 0.
-// One thread per channel pair; the dof values are rounded to FP32 in integer
-// arithmetic (convert.cuh), the product is FP32.
+// Channel pairs; each thread handles kEwUnroll of them per iteration and
+// issues all their loads first.  The dof values are rounded to FP32 in
+// integer arithmetic (convert.cuh), the product is FP32.
+constexpr int kEwUnroll = 4;
 template <typename T>
 __global__ void assemble_input_kernel(const T* __restrict__ r, const float* __restrict__ logk,
                                       const double* __restrict__ rr, long long n, int nloc, int cin,
@@ -97,18 +99,83 @@ __global__ void assemble_input_kernel(const T* __restrict__ r, const float* __re
   const float inv = ms > 0.0 ? float(1.0 / sqrt(ms)) : 0.f;
   const unsigned half = unsigned(cin) / 2u, total = unsigned(P) * half, nl = unsigned(nloc);
   __nv_bfloat162* x2 = reinterpret_cast<__nv_bfloat162*>(x0);
-  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-    const unsigned p = e / half, c = 2u * (e - p * half);
-    float v[2];
+  const unsigned stride = gridDim.x * blockDim.x;
+  for (unsigned e0 = blockIdx.x * blockDim.x * kEwUnroll + threadIdx.x; e0 < total; e0 += stride * kEwUnroll) {
+    T a[kEwUnroll][2];
+    float lk[kEwUnroll];
+    unsigned cs[kEwUnroll];
 #pragma unroll
-    for (unsigned j = 0; j < 2; ++j) {
-      const unsigned cc = c + j;
-      v[j] = 0.f;
-      if (cc < nl) v[j] = (coarse && cc > 0) ? 0.f : to_f32(r[p * nl + cc]) * inv;
-      else if (cc == nl) v[j] = logk[p];
+    for (int u = 0; u < kEwUnroll; ++u) {
+      const unsigned e = e0 + u * blockDim.x;
+      const unsigned p = e / half, c = 2u * (e - p * half);
+      cs[u] = c;
+      a[u][0] = a[u][1] = T(0);
+      lk[u] = 0.f;
+      if (e < total) {
+        if (c < nl) a[u][0] = r[p * nl + c];
+        if (c + 1 < nl) a[u][1] = r[p * nl + c + 1];
+        if (c <= nl && nl <= c + 1) lk[u] = logk[p];
+      }
     }
-    x2[e] = __floats2bfloat162_rn(v[0], v[1]);
+#pragma unroll
+    for (int u = 0; u < kEwUnroll; ++u) {
+      const unsigned e = e0 + u * blockDim.x;
+      if (e >= total) continue;
+      float v[2];
+#pragma unroll
+      for (unsigned j = 0; j < 2; ++j) {
+        const unsigned cc = cs[u] + j;
+        v[j] = 0.f;
+        if (cc < nl) v[j] = (coarse && cc > 0) ? 0.f : to_f32(a[u][j]) * inv;
+        else if (cc == nl) v[j] = lk[u];
+      }
+      x2[e] = __floats2bfloat162_rn(v[0], v[1]);
+    }
   }
+}
+
+// Partial sums of r_i^2 in FP32 (values rounded to FP32 in integer
+// arithmetic): one per block, fixed order; the normalisation rms(r) needs no
+// more precision, and an FP64 product per dof would bind on the FP64 pipe.
+template <typename T>
+__global__ void sumsq_partial_kernel(const T* __restrict__ r, unsigned n, double* __restrict__ part) {
+  __shared__ float red[256];
+  float acc[kEwUnroll] = {0.f, 0.f, 0.f, 0.f};
+  const unsigned stride = gridDim.x * blockDim.x;
+  for (unsigned e0 = blockIdx.x * blockDim.x * kEwUnroll + threadIdx.x; e0 < n; e0 += stride * kEwUnroll) {
+    T a[kEwUnroll];
+#pragma unroll
+    for (int u = 0; u < kEwUnroll; ++u) {
+      const unsigned e = e0 + u * blockDim.x;
+      a[u] = e < n ? r[e] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < kEwUnroll; ++u) {
+      const float v = to_f32(a[u]);
+      acc[u] = fmaf(v, v, acc[u]);
+    }
+  }
+  red[threadIdx.x] = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (int(threadIdx.x) < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = double(red[0]);
+}
+
+// out[0] = sum of the partials in block order
+__global__ void sum_partials_kernel(const double* __restrict__ part, int np, double* __restrict__ out) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < np; i += 256) s += part[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (int(threadIdx.x) < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = red[0];
 }
 
 // out[0] = sum_p r[p*nloc]^2: the coarse mode's normalisation (the cell
@@ -131,16 +198,33 @@ __global__ void coarse_sumsq_kernel(const T* __restrict__ r, int nloc, long long
 }
 
 // z[p*nloc+l] (+)= S * rms(r) * y[p][l]: the scale and the product in FP32,
-// widened to T in integer arithmetic (an FP64 add only when accumulating)
+// widened to T in integer arithmetic (an FP64 add only when accumulating);
+// kEwUnroll values per thread and iteration, loads first
 template <typename T>
 __global__ void emit_output_kernel(const float* __restrict__ y, const double* __restrict__ rr, long long n, int nloc,
                                    int cout, long long P, float S, int accumulate, int coarse, T* __restrict__ z) {
   const float sc = float(double(S) * sqrt(rr[0] / double(n)));
   const unsigned nl = unsigned(nloc), total = unsigned(P) * nl, co = unsigned(cout);
-  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-    const unsigned p = e / nl, l = e - p * nl;
-    const float v = (coarse && l > 0) ? 0.f : sc * y[p * co + l];
-    z[e] = accumulate ? T(z[e] + from_f32<T>(v)) : from_f32<T>(v);
+  const unsigned stride = gridDim.x * blockDim.x;
+  for (unsigned e0 = blockIdx.x * blockDim.x * kEwUnroll + threadIdx.x; e0 < total; e0 += stride * kEwUnroll) {
+    float yv[kEwUnroll];
+    T zv[kEwUnroll];
+#pragma unroll
+    for (int u = 0; u < kEwUnroll; ++u) {
+      const unsigned e = e0 + u * blockDim.x;
+      yv[u] = 0.f;
+      zv[u] = T(0);
+      if (e < total) {
+        const unsigned p = e / nl, l = e - p * nl;
+        if (!(coarse && l > 0)) yv[u] = y[p * co + l];
+        if (accumulate) zv[u] = z[e];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kEwUnroll; ++u) {
+      const unsigned e = e0 + u * blockDim.x;
+      if (e < total) z[e] = accumulate ? T(zv[u] + from_f32<T>(sc * yv[u])) : from_f32<T>(sc * yv[u]);
+    }
   }
 }
 
@@ -299,7 +383,6 @@ static int launch_conv27(gbfem_cnn_s* c, const bf16* in, const bf16* w, bf16* ou
       if (m.ptr == in && m.N == N) map = &m.map;
   if (!map) return launch_conv<C, C, 27, RELU, bf16>(in, w, out, N, s);
   static_assert(C == kCtN, "the tensor-core convolution is 32 -> 32 channels");
-  GBFEM_CUDA_TRY(cudaFuncSetAttribute(conv_tma_kernel<RELU>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kCtSmem)));
   static int sms = 0;
   if (sms == 0) {
     int dev = 0, v = 0;
@@ -312,6 +395,7 @@ static int launch_conv27(gbfem_cnn_s* c, const bf16* in, const bf16* w, bf16* ou
   const long long P = (long long)N * N * N;
   const long long ntiles = P / kCtM;
   const long long grid = ntiles < sms ? ntiles : sms;
+  GBFEM_CUDA_TRY(cudaFuncSetAttribute(conv_tma_kernel<RELU>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kCtSmem)));
   conv_tma_kernel<RELU><<<unsigned(grid), kCtThreads, kCtSmem, s>>>(*map, w, out, N, c->status);
   GBFEM_CUDA_TRY(cudaGetLastError());
   return GBFEM_OK;
@@ -466,8 +550,12 @@ static int cnn_input(gbfem_cnn_s* c, const void* r, cudaStream_t s) {
   if (c->coarse)
     coarse_sumsq_kernel<T><<<1, 256, 0, s>>>(static_cast<const T*>(r), c->nloc, c->P[0], c->d_rr);
   else
-    GBFEM_TRY(dot_device(sizeof(T) == 8 ? GBFEM_F64 : GBFEM_F32, c->ndofs, r, r, c->d_rr, c->d_partial, s));
-  assemble_input_kernel<T><<<grid1(c->P[0] * c->cin0 / 2), 256, 0, s>>>(static_cast<const T*>(r), c->logk, c->d_rr,
+  {
+    const int np = grid1(c->ndofs / kEwUnroll);
+    sumsq_partial_kernel<T><<<np, 256, 0, s>>>(static_cast<const T*>(r), unsigned(c->ndofs), c->d_partial);
+    sum_partials_kernel<<<1, 256, 0, s>>>(c->d_partial, np, c->d_rr);
+  }
+  assemble_input_kernel<T><<<grid1(c->P[0] * c->cin0 / 2 / kEwUnroll), 256, 0, s>>>(static_cast<const T*>(r), c->logk, c->d_rr,
                                                                     cnn_nnorm(c), c->nloc, c->cin0, c->P[0], c->coarse,
                                                                     c->x0);
   GBFEM_CUDA_TRY(cudaGetLastError());
@@ -479,10 +567,10 @@ static int cnn_apply(gbfem_cnn_s* c, int precision, const void* r, void* z, int 
   else GBFEM_TRY(cnn_input<float>(c, r, s));
   GBFEM_TRY(cnn_forward(c, s));
   if (precision == GBFEM_F64)
-    emit_output_kernel<double><<<grid1(c->ndofs), 256, 0, s>>>(c->y, c->d_rr, cnn_nnorm(c), c->nloc, c->cout0, c->P[0],
+    emit_output_kernel<double><<<grid1(c->ndofs / kEwUnroll), 256, 0, s>>>(c->y, c->d_rr, cnn_nnorm(c), c->nloc, c->cout0, c->P[0],
                                                                c->S, accumulate, c->coarse, static_cast<double*>(z));
   else
-    emit_output_kernel<float><<<grid1(c->ndofs), 256, 0, s>>>(c->y, c->d_rr, cnn_nnorm(c), c->nloc, c->cout0, c->P[0],
+    emit_output_kernel<float><<<grid1(c->ndofs / kEwUnroll), 256, 0, s>>>(c->y, c->d_rr, cnn_nnorm(c), c->nloc, c->cout0, c->P[0],
                                                               c->S, accumulate, c->coarse, static_cast<float*>(z));
   GBFEM_CUDA_TRY(cudaGetLastError());
   return GBFEM_OK;
@@ -650,7 +738,10 @@ int gbfem_cnn_create(int order, int cells, uint64_t seed, gbfem_cnn* out) {
   A((void**)&c->d_rr, 64);
   A((void**)&c->d_loss, 64);
   A((void**)&c->status, 64);
-  A((void**)&c->d_partial, sizeof(double) * (dot_num_partials(std::max(c->ndofs, c->P[0] * c->cout0)) + 8));
+  // partials of the loss reduction (gbfem's dot) and of the input's sum of
+  // squares (one per block of sumsq_partial_kernel, at most stream_grid(ndofs))
+  A((void**)&c->d_partial, sizeof(double) * (std::max<long long>(dot_num_partials(std::max(c->ndofs, c->P[0] * c->cout0)),
+                                                                  stream_grid(c->ndofs)) + 8));
   if (rc == GBFEM_OK) {
     cudaError_t e = cudaMallocHost(&c->h_loss, 64);
     if (e != cudaSuccess) rc = set_cuda_error(e, "gbfem_cnn_create");

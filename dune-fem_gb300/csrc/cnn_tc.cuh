@@ -13,11 +13,14 @@
 //    the 128 rows of the box are the tile's positions in order, and the
 //    zero fill of the tensor map outside the grid is the convolution's
 //    zero padding.  The box lands in the 64-byte-swizzled K-major layout
-//    (rows of 64 bytes).  16 stages of 8 KB.
+//    (rows of 64 bytes).  A pipeline stage holds the nine (x, y) shifts of
+//    one z shift (nine boxes, 72 KB): one barrier round trip and one commit
+//    per nine taps, two stages.
 //  - The weights (B, 32 x 27*32) are written once per CTA into shared memory
 //    in the 128-byte-swizzled K-major layout (56 KB).
 //  - Warp 4 (one lane) issues the TMA loads, warp 5 (one lane) the MMAs
-//    (two K = 16 instructions per tap) and their commits, warps 0-3 read the
+//    (two K = 16 instructions per tap, six per stage) and their commits,
+//    warps 0-3 read the
 //    accumulator back (warp w owns TMEM lanes 32w..32w+31 = its rows),
 //    rectify (forward), round to BF16 and store 64 contiguous bytes per
 //    position.  Full / empty mbarriers between loads and MMAs, two
@@ -36,9 +39,17 @@ namespace gbfem {
 namespace cnn {
 
 constexpr int kCtThreads = 192;
-constexpr int kCtM = 128, kCtN = 32, kCtTaps = 27, kCtStages = 16;
+constexpr int kCtM = 128, kCtN = 32, kCtTaps = 27;
+constexpr int kCtTapBytes = kCtM * 64;           // 8 KB: 128 rows of 32 BF16
+// A stage holds the nine (x, y) shifts of one z shift.  Measured at 64^3 Q3
+// (forward pass): one tap per stage (16 stages) 0.568 ms, three (6 stages)
+// 0.463 ms, nine (2 stages) 0.438 ms: the cost is the barrier round trip
+// and commit per stage, not the loads.
+constexpr int kCtTapsPerStage = 9;
+constexpr int kCtStepsPerTile = kCtTaps / kCtTapsPerStage;
+constexpr int kCtStages = 2;
 constexpr uint32_t kCtBBytes = 14 * kCtN * 128;  // 56 KB: 14 atoms of 64 BF16 (taps 2a, 2a+1)
-constexpr uint32_t kCtStageBytes = kCtM * 64;    // 8 KB: 128 rows of 32 BF16
+constexpr uint32_t kCtStageBytes = kCtTapsPerStage * kCtTapBytes;  // 24 KB
 constexpr size_t kCtSmem = size_t(kCtBBytes) + kCtStages * size_t(kCtStageBytes) + 1024;
 constexpr uint32_t kCtWaitLimit = 1u << 24;
 constexpr uint32_t kCtCols = 64;  // two 32-column FP32 accumulators
@@ -136,7 +147,7 @@ __global__ void __launch_bounds__(kCtThreads, 1)
       for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         const long long p0 = tile * kCtM;
         const int x0 = int(p0 % N), y0 = int((p0 / N) % N), z0 = int(p0 / ((long long)N * N));
-        for (int t = 0; t < kCtTaps; ++t, ++g) {
+        for (int j = 0; j < kCtStepsPerTile; ++j, ++g) {
           const uint32_t s = g % kCtStages;
           if (g >= kCtStages && !ct_wait(&empty[s], ((g / kCtStages) - 1) & 1u)) {
             ok = false;
@@ -149,12 +160,17 @@ __global__ void __launch_bounds__(kCtThreads, 1)
           asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ct_smem(&full[s])),
                        "r"(kCtStageBytes)
                        : "memory");
-          const int xx = x0 + t % 3 - 1, yy = y0 + (t / 3) % 3 - 1, zz = z0 + t / 9 - 1;
-          asm volatile(
-              "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-              "[%6];" ::"r"(ct_smem(sA + s * kCtStageBytes)),
-              "l"(&map), "r"(0), "r"(xx), "r"(yy), "r"(zz), "r"(ct_smem(&full[s]))
-              : "memory");
+          // tap t = kCtTapsPerStage j + k: shifts t % 3 - 1, (t / 3) % 3 - 1, t / 9 - 1
+#pragma unroll
+          for (int k = 0; k < kCtTapsPerStage; ++k) {
+            const int t = kCtTapsPerStage * j + k;
+            asm volatile(
+                "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+                "%5}], [%6];" ::"r"(ct_smem(sA + s * kCtStageBytes + k * kCtTapBytes)),
+                "l"(&map), "r"(0), "r"(x0 + t % 3 - 1), "r"(y0 + (t / 3) % 3 - 1), "r"(z0 + t / 9 - 1),
+                "r"(ct_smem(&full[s]))
+                : "memory");
+          }
         }
       }
       if (!ok) abort_flag = 1;
@@ -176,23 +192,27 @@ __global__ void __launch_bounds__(kCtThreads, 1)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        for (int t = 0; t < kCtTaps; ++t, ++g) {
+        for (int j = 0; j < kCtStepsPerTile; ++j, ++g) {
           const uint32_t s = g % kCtStages;
           if (!ct_wait(&full[s], (g / kCtStages) & 1u) || abort_flag) {
             ok = false;
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const uint64_t ad = adesc0 + (uint64_t(s * kCtStageBytes) >> 4);
-          const uint64_t bd = bdesc0 + (uint64_t((t >> 1) * (kCtN * 128) + (t & 1) * 64) >> 4);
 #pragma unroll
-          for (int kk = 0; kk < 2; ++kk) {
-            const uint32_t acc = (t > 0 || kk > 0) ? 1u : 0u;
-            asm volatile(
-                "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem + b * kCtN),
-                "l"(ad + uint64_t(2 * kk)), "l"(bd + uint64_t(2 * kk)), "r"(kCtIdesc), "r"(acc)
-                : "memory");
+          for (int k = 0; k < kCtTapsPerStage; ++k) {
+            const int t = kCtTapsPerStage * j + k;
+            const uint64_t ad = adesc0 + (uint64_t(s * kCtStageBytes + k * kCtTapBytes) >> 4);
+            const uint64_t bd = bdesc0 + (uint64_t((t >> 1) * (kCtN * 128) + (t & 1) * 64) >> 4);
+#pragma unroll
+            for (int kk = 0; kk < 2; ++kk) {
+              const uint32_t acc = (t > 0 || kk > 0) ? 1u : 0u;
+              asm volatile(
+                  "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem + b * kCtN),
+                  "l"(ad + uint64_t(2 * kk)), "l"(bd + uint64_t(2 * kk)), "r"(kCtIdesc), "r"(acc)
+                  : "memory");
+            }
           }
           asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                            ct_smem(&empty[s]))

@@ -956,7 +956,7 @@ class CNN:
 
     def set_conv_engine(self, engine):
         """"tensor" (default): the 3x3x3 convolutions as tcgen05 implicit
-        GEMMs; "mma": warp-level mma.sync."""
+        GEMMs with TMA loads; "mma": warp-level mma.sync."""
         check(lib().gbfem_cnn_set_conv_engine(self.handle, {"tensor": 0, "mma": 1}[engine]))
 
     def status(self):

@@ -492,8 +492,10 @@ int gbfem_cnn_set_kappa(gbfem_cnn cnn, int precision, const void* kappa, void* s
 int gbfem_cnn_set_coarse(gbfem_cnn cnn, int coarse);
 /* The engine of the 3x3x3 convolutions (forward and backward-data):
  * GBFEM_CNN_CONV_TENSOR_CORE (default) runs them as implicit GEMMs on the
- * tcgen05 tensor cores (BF16 operands, FP32 accumulators in tensor memory);
- * GBFEM_CNN_CONV_MMA_SYNC on warp-level mma.sync. */
+ * tcgen05 tensor cores (TMA tensor loads, BF16 operands, FP32 accumulators
+ * in tensor memory) on grid levels with a power-of-two size >= 8, and
+ * mma.sync on the others; GBFEM_CNN_CONV_MMA_SYNC on warp-level mma.sync
+ * everywhere. */
 #define GBFEM_CNN_CONV_TENSOR_CORE 0
 #define GBFEM_CNN_CONV_MMA_SYNC 1
 int gbfem_cnn_set_conv_engine(gbfem_cnn cnn, int engine);
