@@ -1016,6 +1016,70 @@ def workload_cnn(args):
     return out
 
 
+def workload_forms(args):
+    """The general-form path against the built-in operator on the same
+    problem: Bratu -lap u = 5 e^u (SIPG Q2, weak u = 0) on cells^3 as
+    NonlinearDGOperator (hand-written reaction kernel) and as a run-time
+    compiled Form (flux g, source -5 e^u, dual-number Jacobian): apply and
+    Jacobian-apply times (CUDA events, --steps after 3 warm-ups), their
+    relative difference, and the Newton solve (Eisenstat-Walker, GMRES,
+    block Jacobi of each Jacobian) matrix-free and with each Jacobian
+    assembled into the block-sparse matrix."""
+    import gbfem
+    import integrands
+    import torch
+    N, p = args.cells, 2
+    cells = (N, N, N)
+    builtin = gbfem.NonlinearDGOperator(cells, p, reaction=(0.0, 0.0, -5.0))
+    form = integrands.Form(flux="for (int k = 0; k < 3; ++k) F[0][k] = g[0][k];", source="s[0] = -5.0 * exp(u[0]);",
+                           dirichlet="")
+    generated = integrands.FormOperator(form, cells, p)
+    n = builtin.size
+    rng = np.random.default_rng(SEED)
+    u = gbfem.DeviceArray.from_numpy(0.3 * rng.uniform(-1, 1, n))
+    du = gbfem.DeviceArray.from_numpy(rng.uniform(-1, 1, n))
+    w = gbfem.DeviceArray(n)
+    stream = torch.cuda.current_stream()
+    steps = max(1, args.steps)
+    out = {"metric": "Bratu on a generated form vs the built-in operator", "unit": "ms", "higher_is_better": False,
+           "dtype": "f64", "config": {"workload": "Bratu -lap u = 5 e^u, SIPG Q2 %d^3 (%d dofs), u = 0 weak" % (N, n)}}
+    res = {}
+    for name, op in (("builtin", builtin), ("form", generated)):
+        jac = op.jacobian(u)
+        r = {"apply_ms": time_applies(op, u, w, steps, stream)}
+        res[name] = w.numpy()
+        r["jacobian_apply_ms"] = time_applies(jac, du, w, steps, stream)
+        res[name + "_j"] = w.numpy()
+        for assembled in (False, True):
+            newton = gbfem.NewtonInverseOperator(tolerance=1e-9, forcing="eisenstatwalker", linear_tolerance=1e-10,
+                                                 linear_method="gmres", linear_restart=50, max_iterations=100,
+                                                 preconditioner=gbfem.PC_BLOCK_JACOBI, assembled=assembled)
+            newton.bind(op)
+            rhs = gbfem.DeviceArray(n)
+            rhs.clear()
+            x = gbfem.DeviceArray(n)
+            x.clear()
+            newton(rhs, x)  # warm-up
+            x.clear()
+            _, t = _timed(lambda: newton(rhs, x))
+            info = newton.info()
+            key = "newton_assembled" if assembled else "newton_matrix_free"
+            r[key] = {"s": t, "newton_iterations": info["iterations"], "linear_iterations": info["linear_iterations"],
+                      "converged": info["converged"]}
+            res[name + "_x" + ("a" if assembled else "")] = x.numpy()
+            del newton
+        out[name] = r
+        del jac
+    def rel(a, b):
+        return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+    out["apply_rel_diff"] = rel(res["form"], res["builtin"])
+    out["jacobian_rel_diff"] = rel(res["form_j"], res["builtin_j"])
+    out["solution_rel_diff"] = rel(res["form_x"], res["builtin_x"])
+    out["assembled_vs_matrix_free_rel_diff"] = rel(res["form_xa"], res["form_x"])
+    out["value"] = out["form"]["apply_ms"]
+    return out
+
+
 def workload_newton(args):
     """Bratu problem -lap u = lambda e^u (lambda = 5, SIPG Q2, weak u = 0) on
     cells^3 by Newton with block-Jacobi CG for each Jacobian; with and without
@@ -1074,7 +1138,7 @@ def main():
     ap.add_argument("--impl", default="gbfem", choices=["gbfem", "reference"])
     ap.add_argument("--workload", default="apply",
                     choices=["apply", "q1cg", "rk3", "mixed", "learned", "kernels", "newton", "apply_kappa",
-                             "apply_f32", "scaled_bj", "cnn"])
+                             "apply_f32", "scaled_bj", "cnn", "forms"])
     ap.add_argument("--rk-steps", type=int, default=100)
     ap.add_argument("--cells", type=int, default=96)
     ap.add_argument("--order", type=int, default=3)
@@ -1105,7 +1169,7 @@ def main():
         fn = {"q1cg": workload_q1cg, "rk3": workload_rk3, "mixed": workload_mixed,
               "learned": workload_learned, "kernels": workload_kernels, "newton": workload_newton,
               "apply_kappa": workload_apply_kappa, "apply_f32": workload_apply_f32,
-              "scaled_bj": workload_scaled_bj, "cnn": workload_cnn}[args.workload]
+              "scaled_bj": workload_scaled_bj, "cnn": workload_cnn, "forms": workload_forms}[args.workload]
         line = fn(args)
         line.update({"n_gpus": 1, "data": "synthetic"})
         print(json.dumps(line), flush=True)

@@ -136,6 +136,7 @@ int gbfem_form_operator_create(const gbfem_dg_desc* desc, int components, const 
   const std::string base = std::string("gbfem_form_") + (op->precision == GBFEM_F64 ? "f64" : "f32") + "_n" +
                            std::to_string(op->n) + "_q" + std::to_string(op->q) + "_m" + std::to_string(components);
   auto fail = [&](int rc) {
+    (void)cudaGetLastError();  // the failed runtime call must not surface at the next launch check
     gbfem_operator_destroy(op);
     *out = nullptr;
     return rc;

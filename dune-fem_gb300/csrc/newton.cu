@@ -151,6 +151,7 @@ int gbfem_newton_params_default(gbfem_newton_params* prm) {
   prm->simplified = 0;
   prm->preconditioner = GBFEM_PC_NONE;
   prm->verbose = 0;
+  prm->assembled = 0;
   GBFEM_TRY(gbfem_solver_params_default(&prm->linear));
   return GBFEM_OK;
 }
@@ -183,6 +184,7 @@ int gbfem_newton_solve(gbfem_operator op, const gbfem_newton_params* prm_in, con
   bool compute_jacobian = true;
   int idle_solves = 0;  // consecutive linear solves that made no iteration
   PcHolder pc;
+  OpHolder mat;  // the assembled Jacobian (assembled = 1)
   if (nt.prm.verbose) std::printf("Start Newton: tol = %.3e\nNewton iteration 0: |residual| = %.6e\n", nt.prm.tolerance, nt.delta);
   while (true) {
     if (compute_jacobian) {
@@ -192,16 +194,24 @@ int gbfem_newton_solve(gbfem_operator op, const gbfem_newton_params* prm_in, con
         gbfem_preconditioner_destroy(pc.pc);
         pc.pc = nullptr;
       }
-      if (nt.prm.preconditioner == GBFEM_PC_DIAGONAL) GBFEM_TRY(gbfem_preconditioner_diagonal_create(jac.op, &pc.pc));
+      if (nt.prm.assembled) {
+        if (mat.op) {
+          gbfem_operator_destroy(mat.op);
+          mat.op = nullptr;
+        }
+        GBFEM_TRY(gbfem_operator_assemble(jac.op, &mat.op));
+      }
+      gbfem_operator J = nt.prm.assembled ? mat.op : jac.op;
+      if (nt.prm.preconditioner == GBFEM_PC_DIAGONAL) GBFEM_TRY(gbfem_preconditioner_diagonal_create(J, &pc.pc));
       else if (nt.prm.preconditioner == GBFEM_PC_BLOCK_JACOBI)
-        GBFEM_TRY(gbfem_preconditioner_block_jacobi_create(jac.op, nt.prec, &pc.pc));
+        GBFEM_TRY(gbfem_preconditioner_block_jacobi_create(J, nt.prec, &pc.pc));
     }
     if (nt.prm.max_linear_iterations - nt.linear_iterations <= 0) break;
     gbfem_solver_params lp = nt.prm.linear;
     lp.max_iterations = nt.prm.max_linear_iterations - nt.linear_iterations;
     GBFEM_CUDA_TRY(cudaMemset(dw.p, 0, bytes));
     gbfem_solver_info li{};
-    GBFEM_TRY(gbfem_solve(jac.op, pc.pc, &lp, nt.residual, dw.p, &li));
+    GBFEM_TRY(gbfem_solve(nt.prm.assembled ? mat.op : jac.op, pc.pc, &lp, nt.residual, dw.p, &li));
     if (li.iterations < 0) {
       nt.linear_iterations = li.iterations;
       break;

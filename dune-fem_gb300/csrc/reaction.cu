@@ -135,6 +135,7 @@ int gbfem_dg_nonlinear_operator_create_jit(const gbfem_dg_desc* desc, const char
   cudaLibrary_t lib = nullptr;
   cudaError_t e = cudaLibraryLoadFromFile(&lib, cubin_path, nullptr, nullptr, 0, nullptr, nullptr, 0);
   if (e != cudaSuccess) {
+    (void)cudaGetLastError();  // the failed runtime call must not surface at the next launch check
     gbfem_operator_destroy(op);
     *out = nullptr;
     return set_cuda_error(e, (std::string("gbfem_dg_nonlinear_operator_create_jit: loading ") + cubin_path).c_str());
@@ -142,6 +143,7 @@ int gbfem_dg_nonlinear_operator_create_jit(const gbfem_dg_desc* desc, const char
   cudaKernel_t k = nullptr;
   e = cudaLibraryGetKernel(&k, lib, name.c_str());
   if (e != cudaSuccess) {
+    (void)cudaGetLastError();
     cudaLibraryUnload(lib);
     gbfem_operator_destroy(op);
     *out = nullptr;

@@ -64,7 +64,7 @@ class NewtonParams(C.Structure):
     _fields_ = [("tolerance", C.c_double), ("max_iterations", C.c_int), ("max_linear_iterations", C.c_int),
                 ("max_line_search_iterations", C.c_int), ("line_search", C.c_int), ("forcing", C.c_int),
                 ("eta_max", C.c_double), ("gamma", C.c_double), ("simplified", C.c_int),
-                ("preconditioner", C.c_int), ("verbose", C.c_int), ("linear", SolverParams)]
+                ("preconditioner", C.c_int), ("verbose", C.c_int), ("linear", SolverParams), ("assembled", C.c_int)]
 
 
 class NewtonInfo(C.Structure):
@@ -386,12 +386,15 @@ class NewtonInverseOperator:
 
     linear: a KrylovInverseOperator-style parameter set (method, tolerance,
     error_measure, max_iterations, restart); preconditioner: PC_* of each
-    Jacobian; line_search "none" | "simple"; forcing "none" | "eisenstatwalker"."""
+    Jacobian; line_search "none" | "simple"; forcing "none" | "eisenstatwalker";
+    assembled: solve with each Jacobian assembled into the block-sparse matrix
+    (the reference's matrix-based Newton) instead of matrix-free."""
 
     def __init__(self, tolerance=1e-6, max_iterations=None, max_linear_iterations=None, line_search="none",
                  forcing="none", eta_max=0.99, gamma=0.1, simplified=False, preconditioner=PC_BLOCK_JACOBI,
                  linear_method="cg", linear_tolerance=1e-8, linear_error_measure=RELATIVE,
-                 linear_max_iterations=None, linear_restart=20, max_line_search_iterations=None, verbose=False):
+                 linear_max_iterations=None, linear_restart=20, max_line_search_iterations=None, verbose=False,
+                 assembled=False):
         p = NewtonParams()
         check(lib().gbfem_newton_params_default(C.byref(p)))
         p.tolerance = tolerance
@@ -405,6 +408,7 @@ class NewtonInverseOperator:
         p.simplified = 1 if simplified else 0
         p.preconditioner = preconditioner
         p.verbose = 1 if verbose else 0
+        p.assembled = 1 if assembled else 0
         p.linear = solver_params(linear_method, linear_tolerance, linear_error_measure, linear_max_iterations,
                                  linear_restart)
         p.max_linear_iterations = p.linear.max_iterations if max_linear_iterations is None else max_linear_iterations

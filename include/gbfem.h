@@ -391,6 +391,10 @@ typedef struct {
   int preconditioner;           /* GBFEM_PC_* of each Jacobian */
   int verbose;
   gbfem_solver_params linear;   /* the linear solver (its tolerance is replaced under forcing) */
+  int assembled;                /* 1: assemble each Jacobian into the block-sparse matrix
+                                   (gbfem_operator_assemble) and solve and precondition with it, as the
+                                   reference's Newton does with its sparse-matrix Jacobian; 0 (default):
+                                   matrix-free */
 } gbfem_newton_params;
 /* NewtonFailure (solver/newtoninverseoperator.hh:389-400) */
 #define GBFEM_NEWTON_SUCCESS 0

@@ -312,6 +312,15 @@ def test_newton_and_scheme_on_generated_form(gb):
             z = scheme.space.zero
             assert scheme.solve(target=z)["converged"]
             assert relmax(z.numpy(), w.numpy()) < 1e-8
+            # Newton on each Jacobian assembled into the block-sparse matrix: the same steps
+            na = gb.NewtonInverseOperator(tolerance=1e-10, linear_method="gmres", linear_tolerance=1e-12,
+                                          preconditioner=gb.PC_BLOCK_JACOBI, assembled=True)
+            na.bind(op)
+            wa = gb.DeviceArray(op.size)
+            wa.clear()
+            na(rhs, wa)
+            assert na.info()["converged"] and na.info()["iterations"] == info["iterations"]
+            assert relmax(wa.numpy(), w.numpy()) < 1e-8
     assert errs[1] < errs[0] / 5.0, errs
 
 
@@ -406,3 +415,31 @@ def test_ufl_forms_against_oracle(gb, system):
         y = gb.DeviceArray(op.size)
         jac(gb.DeviceArray.from_numpy(du), y)
         assert relmax(y.numpy(), fo.linearize(spec, u, du)) < 1e-9
+
+
+@pytest.mark.gpu
+def test_form_operator_rejects_mismatched_cubins_and_arguments(gb):
+    """A cubin compiled for another order (or component count) is refused
+    with an error naming the missing kernels; 5 components and a kappa are
+    refused; nothing is created."""
+    import ctypes as C
+    import integrands
+    L = gb.lib()
+    L.gbfem_form_operator_create.argtypes = [C.POINTER(gb.DgDesc), C.c_int, C.c_char_p, C.POINTER(C.c_void_p)]
+    cub = integrands.Form(flux="for (int k = 0; k < 3; ++k) F[0][k] = g[0][k];").compile(gb.F64, 1)
+    d = gb.DgDesc()
+    d.grid = gb.grid_desc((2, 2, 2))
+    d.order, d.quad_points, d.precision, d.penalty = 2, 4, gb.F64, 90.0
+    for comps in (1, 2, 5):  # order 2 against an order-1 cubin; 2 components; 5 components
+        h = C.c_void_p()
+        assert L.gbfem_form_operator_create(C.byref(d), comps, cub.encode(), C.byref(h)) != 0
+        assert not h.value
+    d.order, d.quad_points = 1, 3
+    h = C.c_void_p()
+    assert L.gbfem_form_operator_create(C.byref(d), 1, b"/nonexistent/form.cubin", C.byref(h)) != 0
+    assert L.gbfem_form_operator_create(C.byref(d), 1, cub.encode(), C.byref(h)) == 0 and h.value
+    L.gbfem_operator_destroy(h)
+    # the refused loads leave no error behind for the next launch
+    op = gb.DGOperator((2, 2, 2), 1)
+    x, y = gb.DeviceArray.from_numpy(np.ones(op.size)), gb.DeviceArray(op.size)
+    op(x, y)
