@@ -32,9 +32,9 @@ __global__ void __launch_bounds__(kRedThreads) dot_partial_kernel(const T* __res
   const long long b0 = (long long)blockIdx.x * chunk;
   long long b1 = b0 + chunk;
   if (b1 > n) b1 = n;
-  double s = 0.0;
-  for (long long i = b0 + threadIdx.x; i < b1; i += kRedThreads) s = fma(double(x[i]), double(y[i]), s);
-  s = block_sum(s);
+  DotAcc<T> acc;
+  for (long long i = b0 + threadIdx.x; i < b1; i += kRedThreads) acc.add(x[i], y[i]);
+  const double s = block_sum(acc.value());
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
@@ -97,9 +97,9 @@ __global__ void __launch_bounds__(kRedThreads) multi_dot_partial_kernel(const __
   const long long b0 = (long long)blockIdx.x * chunk;
   long long b1 = b0 + chunk;
   if (b1 > n) b1 = n;
-  double s = 0.0;
-  for (long long i = b0 + threadIdx.x; i < b1; i += kRedThreads) s = fma(double(x[i]), double(y[i]), s);
-  s = block_sum(s);
+  DotAcc<T> acc;
+  for (long long i = b0 + threadIdx.x; i < b1; i += kRedThreads) acc.add(x[i], y[i]);
+  const double s = block_sum(acc.value());
   if (threadIdx.x == 0) partial[(long long)blockIdx.y * np + blockIdx.x] = s;
 }
 

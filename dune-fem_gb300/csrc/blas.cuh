@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "convert.cuh"
+
 namespace gbfem {
 
 // Number of FP64 partial sums pass 1 of a dot product of length n writes.
@@ -17,6 +19,33 @@ __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
 }
+
+// A thread's share of a dot product, sum of x_i y_i in its fixed order.
+// FP64 vectors: FP64 fma.  FP32 vectors: each product is formed exactly as
+// p + e (p = x y rounded, e = fma(x, y, -p)) and the terms are summed in
+// float-float (Knuth's two-sum for p, the errors and e into a second float),
+// all on the FP32 pipe -- an FP64 product per element would bind on this
+// GPU's narrow FP64 pipe -- and widened to FP64 once per thread.  The sum
+// carries about 48 significant bits per thread share; the products keep
+// the FP32 exponent range.
+template <typename T> struct DotAcc;
+template <> struct DotAcc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <> struct DotAcc<float> {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float a, float b) {
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);
+    const float t = s + p;
+    const float bp = t - s;
+    c += ((s - (t - bp)) + (p - bp)) + e;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return f32_to_f64(s) + f32_to_f64(c); }
+};
 
 // Fixed-shape block reduction of one value per thread (kRedThreads threads);
 // the result is valid in thread 0.

@@ -706,7 +706,7 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_update_dot(long long n, long
   const long long b0 = (long long)blockIdx.x * chunk;
   long long b1 = b0 + chunk;
   if (b1 > n) b1 = n;
-  double acc = 0.0;
+  DotAcc<T> acc;  // the order and arithmetic of dot_partial_kernel
   for (long long i = b0 + threadIdx.x; i < b1; i += kRedThreads) {
     T vi = v[i];
     if (active) {
@@ -717,13 +717,13 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_update_dot(long long n, long
     if (PC == 1) {
       const T si = vi * dinv[i];
       sz[i] = si;
-      acc = fma(double(vi), double(si), acc);
+      acc.add(vi, si);
     } else {
-      acc = fma(double(vi), double(vi), acc);
+      acc.add(vi, vi);
     }
   }
-  acc = block_sum(acc);
-  if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+  const double sum = block_sum(acc.value());
+  if (threadIdx.x == 0) partial[blockIdx.x] = sum;
 }
 // x += alpha q; p -= alpha h, if active (a general preconditioner follows):
 // grid-stride, since no dot-product partition has to be kept

@@ -282,7 +282,7 @@ typedef struct {
  * iterations INT_MAX, restart 20 (solver/parameter.hh:91-201). */
 int gbfem_solver_params_default(gbfem_solver_params* prm);
 /* u = op^{-1}(f) with optional preconditioner pc (NULL = none).  All vectors
- * in the operator's precision; dot products accumulate in FP64. */
+ * in the operator's precision; dot products are summed into FP64 (see gbfem_dot). */
 int gbfem_solve(gbfem_operator op, gbfem_preconditioner pc, const gbfem_solver_params* prm, const void* f,
                 void* u, gbfem_solver_info* info);
 
@@ -547,6 +547,11 @@ int gbfem_preconditioner_learned_create(gbfem_cnn cnn, gbfem_preconditioner bj, 
 /* ---- BLAS-1 on dof vectors (function/common/discretefunction.hh:781-901,
  *      function/common/scalarproducts.hh:101-127).  Reductions are
  *      deterministic: fixed-order two-pass, independent of launch shape. -- */
+/* x . y into *result (FP64).  FP64 vectors: FP64 products and sums.  FP32
+ * vectors: every product exact (FMA two-product), each thread's share summed
+ * in float-float (about 48 significant bits) and the shares in FP64 -- all
+ * on the FP32 pipe but for one FP64 add per thread; products keep the FP32
+ * exponent range. */
 int gbfem_dot(int precision, int64_t n, const void* x, const void* y, double* result, void* stream);
 int gbfem_axpy(int precision, int64_t n, double alpha, const void* x, void* y, void* stream);
 int gbfem_scal(int precision, int64_t n, double alpha, void* x, void* stream);
@@ -557,8 +562,8 @@ int gbfem_convert(int64_t n, int precision_x, const void* x, int precision_y, vo
 /* Allocation-free dot product.  No counterpart in the reference: it exists
  * for callers that cannot let the library allocate device memory (a host
  * whose memory pool owns all of HBM, or a latency-critical loop that cannot
- * take cudaMalloc's implicit synchronisation).  FP64-accumulated
- * deterministic two-pass reduction like gbfem_dot, but its partial sums live
+ * take cudaMalloc's implicit synchronisation).  The deterministic two-pass
+ * reduction of gbfem_dot, but its partial sums live
  * in a fixed file-scope device array (65536 partials + a result slot, about
  * 512 KB, held by every GPU that loads the library until exit), so it calls
  * no cudaMalloc/cudaFree.  For n <= 8,388,608 (1024 chunks of 8192) it uses
