@@ -55,6 +55,7 @@ struct gbfem_preconditioner_s {
   int sb_engine = GBFEM_SB_ENGINE_TENSOR;
   int* sb_tc_tiles = nullptr;
   int sb_tc_ntiles = 0;
+  int sb_tc_wide = 0;  // 64-cell tiles with K = 64 (blocks of up to 64 dofs)
   void* sb_tc_img = nullptr;
   int* sb_tc_status = nullptr;
 };
