@@ -407,13 +407,15 @@ def test_unknown_error_measure_is_rejected(gb, orc):
 
 
 @pytest.mark.parametrize("order", [3, 4])
-@pytest.mark.parametrize("cells,periodic", [((5, 4, 3), (0, 0, 0)), ((9, 7, 6), (1, 0, 0)), ((20, 18, 16), (0, 1, 1))])
+@pytest.mark.parametrize("cells,periodic", [((5, 4, 3), (0, 0, 0)), ((9, 7, 6), (1, 0, 0)), ((20, 18, 16), (0, 1, 1)),
+                                            ((40, 36, 32), (0, 0, 1))])
 def test_scaled_block_jacobi_tensor_cores(gb, orc, order, cells, periodic):
     """The tile products on the tcgen05 tensor cores (TF32 with the 3xTF32
     split) against the oracle's kappa = 1 blocks and against the FP32-FMA
-    engine; many tiles and type changes per CTA on the largest grid; the
-    kernel's bounded waits all completed (status 0); two applies in a row
-    give bitwise the same result."""
+    engine; type changes per CTA, and on the largest grid several full tiles
+    per CTA through the software pipeline (720 tiles of 64 cells at Q3,
+    1440 of 32 at Q4); the kernel's bounded waits all completed (status 0);
+    two applies in a row give bitwise the same result."""
     ncell = int(np.prod(cells))
     nloc = (order + 1) ** 3
     rng = np.random.default_rng(ncell + order)
