@@ -1080,6 +1080,40 @@ def workload_forms(args):
     return out
 
 
+def workload_mixed_solve(args):
+    """The mixed arm of the headline line's solve object alone (64^3 Q3,
+    kappa seed 1, f = 1, to ||f - A u|| / ||f|| <= 1e-10): FP64 FGMRES(30) on
+    the full kappa around the FP32 inner CG (device-resident, graph chunks of
+    16) on the cellwise-kappa one-kernel apply with the tcgen05 scaled block
+    Jacobi.  --max-outer bounds the outer iterations (a short window for
+    kernel launch lists)."""
+    import gbfem
+    import torch
+    N, p = SOLVE_CELLS, SOLVE_ORDER
+    cells = (N, N, N)
+    modes = gbfem.fourier_modes(SOLVE_SEED, 256, 0.1, 1.0)
+    k64 = gbfem.project(cells, p, gbfem.FN_EXP_FOURIER, modes=modes)
+    k32 = gbfem.project(cells, p, gbfem.FN_EXP_FOURIER, modes=modes, precision=gbfem.F32)
+    f = gbfem.project(cells, p, gbfem.FN_CONSTANT, params=(1.0,), scale_by_volume=True)
+    op64 = gbfem.DGOperator(cells, p, kappa=k64)
+    op32c = gbfem.DGOperator(cells, p, precision=gbfem.F32, kappa_cell=gbfem.cell_means(k32, p))
+    u = gbfem.DeviceArray(op64.size)
+    u.clear()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pcs = gbfem.Preconditioner.scaled_block_jacobi(op32c)
+    info = gbfem.solve_mixed(op64, op32c, pcs, f, u, tolerance=1e-10, inner_tolerance=1e-2,
+                             max_outer=args.max_outer, outer="fgmres", outer_restart=30, graph_chunk=16)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    inner = abs(info.iterations)
+    return {"metric": "mixed solve time to relative residual 1e-10", "unit": "s", "higher_is_better": False,
+            "value": t, "dtype": "f64/f32", "outer_iterations": info.outer_iterations, "inner_iterations": inner,
+            "converged": bool(info.converged), "ms_per_inner_iteration": t / max(1, inner) * 1e3,
+            "config": {"workload": "SIPG Q3 %d^3 (%d dofs), variable kappa (seed %d), mixed FGMRES arm; max outer %d"
+                                   % (N, op64.size, SOLVE_SEED, args.max_outer)}}
+
+
 def workload_newton(args):
     """Bratu problem -lap u = lambda e^u (lambda = 5, SIPG Q2, weak u = 0) on
     cells^3 by Newton with block-Jacobi CG for each Jacobian; with and without
@@ -1138,7 +1172,7 @@ def main():
     ap.add_argument("--impl", default="gbfem", choices=["gbfem", "reference"])
     ap.add_argument("--workload", default="apply",
                     choices=["apply", "q1cg", "rk3", "mixed", "learned", "kernels", "newton", "apply_kappa",
-                             "apply_f32", "scaled_bj", "cnn", "forms"])
+                             "apply_f32", "scaled_bj", "cnn", "forms", "mixed_solve"])
     ap.add_argument("--rk-steps", type=int, default=100)
     ap.add_argument("--cells", type=int, default=96)
     ap.add_argument("--order", type=int, default=3)
@@ -1164,12 +1198,14 @@ def main():
     ap.add_argument("--no-solve", action="store_true", help="skip the solve comparison of the headline line")
     ap.add_argument("--algorithm", type=int, default=0)
     ap.add_argument("--kappa-cell", action="store_true")
+    ap.add_argument("--max-outer", type=int, default=300)
     args = ap.parse_args()
     if args.workload != "apply":
         fn = {"q1cg": workload_q1cg, "rk3": workload_rk3, "mixed": workload_mixed,
               "learned": workload_learned, "kernels": workload_kernels, "newton": workload_newton,
               "apply_kappa": workload_apply_kappa, "apply_f32": workload_apply_f32,
-              "scaled_bj": workload_scaled_bj, "cnn": workload_cnn, "forms": workload_forms}[args.workload]
+              "scaled_bj": workload_scaled_bj, "cnn": workload_cnn, "forms": workload_forms,
+              "mixed_solve": workload_mixed_solve}[args.workload]
         line = fn(args)
         line.update({"n_gpus": 1, "data": "synthetic"})
         print(json.dumps(line), flush=True)
