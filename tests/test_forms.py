@@ -443,3 +443,32 @@ def test_form_operator_rejects_mismatched_cubins_and_arguments(gb):
     op = gb.DGOperator((2, 2, 2), 1)
     x, y = gb.DeviceArray.from_numpy(np.ones(op.size)), gb.DeviceArray(op.size)
     op(x, y)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_form_oracle_natural_boundary_equals_dg_oracle(orc, order):
+    """Without Dirichlet data the interior-penalty form has no boundary terms
+    for a pure diffusion: the DG oracle's do-nothing boundary."""
+    import form_oracle as fo
+    cells, eps, c = (3, 2, 2), 1.3, 0.2
+    prob = orc.DGProblem(cells, order, diffusion=eps, mass=c, weak_dirichlet=False)
+    I, S, Bd = fo.sipg(1, flux=lambda x, u, g: eps * g, source=lambda x, u, g: c * u)
+    spec = fo.FormSpec(cells, order, 1, I, S, Bd, penalty=eps * prob.penalty)
+    u = np.random.default_rng(7 + order).uniform(-1, 1, prob.ndofs)
+    assert relmax(fo.residual(spec, u), prob.apply(u)) < 1e-14
+
+
+def test_form_oracle_linearisation_is_consistent():
+    """The oracle's Richardson-difference linearisation is linear in the
+    direction and matches a small central difference (a check of the
+    checker used by the GPU Jacobian tests)."""
+    import form_oracle as fo
+    I, S, Bd = _nl_oracle(fo)
+    spec = fo.FormSpec((2, 2, 1), 1, 1, I, S, Bd)
+    rng = np.random.default_rng(3)
+    u, a, b = (rng.uniform(-0.5, 0.5, spec.ndofs) for _ in range(3))
+    ja, jb, jab = fo.linearize(spec, u, a), fo.linearize(spec, u, b), fo.linearize(spec, u, 2.0 * a - b)
+    assert relmax(jab, 2.0 * ja - jb) < 1e-9
+    h = 1e-6
+    cd = (fo.residual(spec, u + h * a) - fo.residual(spec, u - h * a)) / (2 * h)
+    assert relmax(ja, cd) < 1e-7
