@@ -472,3 +472,29 @@ def test_form_oracle_linearisation_is_consistent():
     h = 1e-6
     cd = (fo.residual(spec, u + h * a) - fo.residual(spec, u - h * a)) / (2 * h)
     assert relmax(ja, cd) < 1e-7
+
+
+@pytest.mark.parametrize("components,order,prec", [(3, 3, 0), (4, 1, 1), (1, 4, 1), (2, 4, 0)])
+def test_form_kernels_compile_for_more_shapes(gb, components, order, prec):
+    """Kernel shapes beyond those the GPU tests run: 3 and 4 components,
+    order 4 (q = 6), FP32 duals; each stays within the shared memory of one
+    CTA (form_smem_bytes)."""
+    import integrands
+    if shutil.which("nvcc") is None and not __import__("os").path.exists("/usr/local/cuda/bin/nvcc"):
+        pytest.skip("no nvcc")
+    M = components
+    flux = "for (int m = 0; m < %d; ++m) for (int k = 0; k < 3; ++k) F[m][k] = (1.0 + u[0] * u[0]) * g[m][k];" % M
+    src = "for (int m = 0; m < %d; ++m) s[m] = u[m] * u[(m + 1) %% %d] - sin(x[m %% 3]);" % (M, M)
+    adv = "for (int k = 0; k < 3; ++k) Fa[0][k] = 0.5 * u[0] * u[0];"
+    form = integrands.Form(components=M, flux=flux, source=src, advection=adv,
+                           wavespeed="fabs(u[0] * (n[0] + n[1] + n[2]))", dirichlet="gD[0] = x[0];")
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        assert form.compile(gb.F64 if prec == 0 else gb.F32, order, cache_dir=d).endswith(".cubin")
+    q, n = order + 2, order + 1
+    cpb = 1 if q ** 3 * M >= 128 else (2 if 2 * q ** 3 * M >= 128 else 4)
+    vol = cpb * M * (q * n * n + q * q * n + 4 * q ** 3)
+    face = cpb * M * 8 * (n * n + q * n + 3 * q * q)
+    rb = 8 if prec == 0 else 4
+    smem = ((7 * 5 + 49 + 7 + 20) * rb + 15) // 16 * 16 + (2 * cpb * M * n ** 3 + max(vol, face)) * 2 * rb
+    assert smem <= 227 * 1024
