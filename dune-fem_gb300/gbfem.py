@@ -318,6 +318,17 @@ class Operator:
             pass
 
 
+def weak_dirichlet_flag(weak_dirichlet):
+    """The descriptor's weak_dirichlet field: 1 for the symmetric interior-
+    penalty boundary (the full -u kappa grad v . n term), 0 for none.  The
+    boundary of dune-fem's DGEllipticOperator, which halves that term, is a
+    different form; it is available as an integrands.Form, not here."""
+    if weak_dirichlet in (True, False, 0, 1):
+        return 1 if weak_dirichlet else 0
+    raise ValueError("weak_dirichlet must be True or False (got %r); write other boundary forms "
+                     "with integrands.Form" % (weak_dirichlet,))
+
+
 class DGOperator(Operator):
     """SIPG / upwind / mass DG operator on a structured hexahedral grid."""
 
@@ -336,7 +347,7 @@ class DGOperator(Operator):
         d.mass = mass
         for k in range(3):
             d.velocity[k] = velocity[k]
-        d.weak_dirichlet = 1 if weak_dirichlet else 0
+        d.weak_dirichlet = weak_dirichlet_flag(weak_dirichlet)
         self.kappa = kappa  # keep the device array alive
         d.kappa = kappa.ptr if kappa is not None else None
         d.algorithm = algorithm
@@ -365,7 +376,7 @@ class NonlinearDGOperator(DGOperator):
         d.mass = mass
         for k in range(3):
             d.velocity[k] = velocity[k]
-        d.weak_dirichlet = 1 if weak_dirichlet else 0
+        d.weak_dirichlet = weak_dirichlet_flag(weak_dirichlet)
         self.kappa = kappa
         d.kappa = kappa.ptr if kappa is not None else None
         d.algorithm = algorithm

@@ -111,7 +111,7 @@ class UserNonlinearDGOperator(gbfem.DGOperator):
         d.mass = mass
         for k in range(3):
             d.velocity[k] = velocity[k]
-        d.weak_dirichlet = 1 if weak_dirichlet else 0
+        d.weak_dirichlet = gbfem.weak_dirichlet_flag(weak_dirichlet)
         self.kappa = kappa
         d.kappa = kappa.ptr if kappa is not None else None
         d.algorithm = algorithm

@@ -2,8 +2,11 @@
 # Compiles the reference's standalone-buildable sources for this path
 # (Gauss rules, Legendre tables, CG/GMRES/BiCGstab templates) with the driver
 # oracle/ref_driver.cpp (with the oracle's operator, oracle.cpp) into
-# oracle/_ref/, runs it, and writes the golden vectors
-# tests/golden/ref_tables.json, ref_krylov.json and ref_krylov_sipg.json.
+# oracle/_ref/, and the reference's DG elliptic operator (dgelliptic.hh over
+# legendre.hh) with oracle/ref_dgelliptic.cpp against the grid shim in
+# oracle/shim_dg; runs them, and writes the golden vectors
+# tests/golden/ref_tables.json, ref_krylov.json, ref_krylov_sipg.json and
+# ref_dgelliptic.json.
 # Needs the dune-fem source tree (located by ref_src.sh); without it this
 # recipe does nothing (the committed golden vectors stay as they are).  With
 # --compile-only it builds the driver and writes nothing.  The reference's
@@ -21,11 +24,15 @@ CXX=${CXX:-g++}
 $CXX -O2 -std=c++17 -pthread -I"$HERE/shim" -I"$REF" \
   "$HERE/ref_driver.cpp" "$HERE/oracle.cpp" "$REF/dune/fem/space/shapefunctionset/legendrepolynomials.cc" \
   -o "$OUT/ref_driver"
+$CXX -O2 -std=c++17 -I"$HERE/shim_dg" -I"$HERE/shim" -I"$REF" \
+  "$HERE/ref_dgelliptic.cpp" "$REF/dune/fem/space/shapefunctionset/legendrepolynomials.cc" \
+  -o "$OUT/ref_dgelliptic"
 if [ "$1" = "--compile-only" ]; then
-  echo "built $OUT/ref_driver"
+  echo "built $OUT/ref_driver $OUT/ref_dgelliptic"
   exit 0
 fi
 "$OUT/ref_driver" tables > "$GOLD/ref_tables.json"
 "$OUT/ref_driver" krylov > "$GOLD/ref_krylov.json"
 "$OUT/ref_driver" sipg > "$GOLD/ref_krylov_sipg.json"
-echo "wrote $GOLD/ref_tables.json $GOLD/ref_krylov.json $GOLD/ref_krylov_sipg.json"
+"$OUT/ref_dgelliptic" > "$GOLD/ref_dgelliptic.json"
+echo "wrote $GOLD/ref_tables.json $GOLD/ref_krylov.json $GOLD/ref_krylov_sipg.json $GOLD/ref_dgelliptic.json"

@@ -319,8 +319,12 @@ void dg_apply_range(const Space& S, const double* u, const double* kappa, double
           for (int l = 0; l < nloc; ++l) w[o * nloc + l] += wo[l];
         }
       } else {
-        // boundary integral (galerkin.hh:414-435): weak homogeneous Dirichlet
+        // boundary integral (galerkin.hh:414-435): weak homogeneous Dirichlet.
+        // weak_dirichlet 1: symmetric SIPG (-u kappa grad v . n in full);
+        // weak_dirichlet 2: the boundary of dune-fem's DGEllipticOperator,
+        // which weights that symmetry term by 1/2 (dgelliptic.hh:426-431)
         const double hB = S.vol / area;
+        const double sym = d.weak_dirichlet == 2 ? 0.5 : 1.0;
         const double sigma = d.penalty / hB;
         for (int iq = 0; iq < nf; ++iq) {
           double vi, gi[3], ki = 1, gk[3];
@@ -332,7 +336,7 @@ void dg_apply_range(const Space& S, const double* u, const double* kappa, double
           double val = 0, gn = 0;
           if (d.weak_dirichlet) {
             val = d.diffusion * (sigma * ki * vi - ki * dn);
-            gn = d.diffusion * (-ki * vi);
+            gn = d.diffusion * (-sym * ki * vi);
           }
           if (adv && bn > 0) val += bn * vi;
           axpy_face(S, f, iq, W * val, W * gn, n, wl.data());

@@ -89,7 +89,9 @@ class DGProblem:
         self.penalty = 10.0 * (order + 1) ** 2 if penalty is None else penalty
         self.mass = mass
         self.velocity = np.array(velocity, dtype=np.float64)
-        self.weak_dirichlet = 1 if weak_dirichlet else 0
+        # True: symmetric SIPG on the boundary; "dgelliptic": the boundary of
+        # dune-fem's DGEllipticOperator (symmetry term weighted by 1/2)
+        self.weak_dirichlet = 2 if weak_dirichlet == "dgelliptic" else (1 if weak_dirichlet else 0)
         self.nloc = (order + 1) ** 3
         self.ncells = int(np.prod(self.cells))
         self.ndofs = self.ncells * self.nloc

@@ -1,0 +1,151 @@
+// Runs dune-fem's own DG elliptic operator -- DGEllipticOperator::apply and
+// DefaultPenalty from dune/fem/schemes/dgelliptic.hh, over the reference's
+// LegendreShapeFunctionSet (legendre.hh), LegendrePolynomials
+// (legendrepolynomials.{hh,cc}) and GaussPts (gausspoints.hh), all compiled
+// unmodified -- on small Cartesian grids provided by the shim layer in
+// oracle/shim_dg, and prints the results as JSON golden vectors.  Built and
+// run only by oracle/make_ref_golden.sh where the dune-fem sources are
+// present; test infrastructure, never part of the product.
+//
+// The model below is the SIPG diffusion + mass problem of this path:
+//   source(u)   = mass * u,
+//   flux(du)    = diffusion * kappa(x) * du,
+//   penalty     = diffusion * kappa(x)   (averaged over the two sides by the
+//                                         operator, dgelliptic.hh:364-368),
+// with kappa an optional Q_p field in the same Legendre basis.  Boundary
+// faces are either do-nothing (no Dirichlet components, dgelliptic.hh:
+// 438-443) or weak homogeneous Dirichlet (g = 0, dgelliptic.hh:393-446), or
+// absent on fully periodic grids.
+//
+// Inputs are generated by integer formulas whose conversion to double is
+// exact, so a test can rebuild them bit for bit:
+//   u[i]             = ((i * 7919 + 13) % 2003 - 1001) / 1000
+//   kappa[c*nl + 0]  = 1 + ((c * 31 + 7) % 11) / 10
+//   kappa[c*nl + l]  = (((c*nl + l) * 37 + 5) % 9 - 4) / 1000   (l > 0)
+#include <config.h>
+
+#include <array>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "dgspace.hh"
+#include <dune/fem/schemes/dgelliptic.hh>
+
+namespace refdg {
+
+using Dune::Fem::Cell;
+using Dune::Fem::ConstLocalFunction;
+using Dune::Fem::DGFunction;
+using Dune::Fem::Face;
+using Dune::Fem::LegendreDGSpace;
+
+struct SipgMassModel {
+  typedef LegendreDGSpace::RangeType RangeType;
+  typedef LegendreDGSpace::JacobianRangeType JacobianRangeType;
+
+  SipgMassModel(const DGFunction* kappa, double diffusion, double mass, bool dirichlet)
+      : diffusion_(diffusion), mass_(mass), dirichlet_(dirichlet), kappa_(kappa) {
+    if (kappa_) klf_.reset(new ConstLocalFunction<DGFunction>(*kappa_));
+  }
+  bool init(const Cell& e) const {
+    if (klf_) klf_->bind(e);
+    return true;
+  }
+  template <class Point>
+  double coefficient(const Point& x) const {
+    if (!klf_) return diffusion_;
+    RangeType k;
+    klf_->evaluate(x, k);
+    return diffusion_ * k[0];
+  }
+  template <class Point>
+  void source(const Point&, const RangeType& u, const JacobianRangeType&, RangeType& s) const {
+    s[0] = mass_ * u[0];
+  }
+  template <class Point>
+  void flux(const Point& x, const RangeType&, const JacobianRangeType& du, JacobianRangeType& f) const {
+    const double k = coefficient(x);
+    for (int d = 0; d < 3; ++d) f[0][d] = k * du[0][d];
+  }
+  template <class Point>
+  RangeType penalty(const Point& x, const RangeType&) const {
+    return RangeType(coefficient(x));
+  }
+  void isDirichletIntersection(const Face&, std::array<int, 1>& components) const { components[0] = dirichlet_ ? 1 : 0; }
+  template <class Point>
+  void dirichlet(int, const Point&, RangeType& g) const { g = RangeType(0.0); }
+
+ private:
+  double diffusion_, mass_;
+  bool dirichlet_;
+  const DGFunction* kappa_;
+  std::unique_ptr<ConstLocalFunction<DGFunction>> klf_;
+};
+
+struct Case {
+  const char* name;
+  int cells[3];
+  double upper[3];
+  int periodic[3];
+  int order;
+  int reported_order;  // quadrature from order() of u plus order() of w
+  bool kappa_field;
+  bool dirichlet;
+  double diffusion, mass, penalty;
+};
+
+void run_case(const Case& k, bool last) {
+  Dune::Fem::CartesianGrid g;
+  for (int d = 0; d < 3; ++d) {
+    g.N[d] = k.cells[d];
+    g.lower[d] = 0.0;
+    g.h[d] = k.upper[d] / k.cells[d];
+    g.periodic[d] = k.periodic[d];
+  }
+  LegendreDGSpace space(g, k.order, k.reported_order);
+  const long long nl = (long long)space.localSize();
+  DGFunction u(space), w(space), kappa(space);
+  for (long long i = 0; i < (long long)space.size(); ++i) u.dofs()[i] = double((i * 7919 + 13) % 2003 - 1001) / 1000.0;
+  for (long long c = 0; c < g.ncells(); ++c) {
+    kappa.dofs()[c * nl] = 1.0 + double((c * 31 + 7) % 11) / 10.0;
+    for (long long l = 1; l < nl; ++l) kappa.dofs()[c * nl + l] = double(((c * nl + l) * 37 + 5) % 9 - 4) / 1000.0;
+  }
+  SipgMassModel model(k.kappa_field ? &kappa : nullptr, k.diffusion, k.mass, k.dirichlet);
+  Dune::Fem::ParameterReader params;
+  params.set("penalty", k.penalty);
+  DGEllipticOperator<DGFunction, SipgMassModel> op(space, model, params);
+  op(u, w);
+
+  const int m = Dune::Fem::gauss_points_for_order(2 * k.reported_order);
+  std::printf("  {\"name\": \"%s\", \"cells\": [%d, %d, %d], \"upper\": [%.17g, %.17g, %.17g], "
+              "\"periodic\": [%d, %d, %d], \"order\": %d, \"quad_points\": %d, \"kappa_field\": %s, \"dirichlet\": %s, "
+              "\"diffusion\": %.17g, \"mass\": %.17g, \"penalty\": %.17g,\n   \"w\": [",
+              k.name, k.cells[0], k.cells[1], k.cells[2], k.upper[0], k.upper[1], k.upper[2], k.periodic[0],
+              k.periodic[1], k.periodic[2], k.order, m, k.kappa_field ? "true" : "false", k.dirichlet ? "true" : "false", k.diffusion, k.mass,
+              k.penalty);
+  for (std::size_t i = 0; i < w.dofs().size(); ++i) std::printf("%s%.17g", i ? ", " : "", w.dofs()[i]);
+  std::printf("]}%s\n", last ? "" : ",");
+}
+
+}  // namespace refdg
+
+int main() {
+  using refdg::Case;
+  const Case cases[] = {
+      {"q1_periodic_aniso_kappa_mass", {3, 2, 2}, {1.5, 1.0, 0.5}, {1, 1, 1}, 1, 1, true, false, 1.0, 0.7, 40.0},
+      {"q2_periodic_kappa_qp2", {2, 3, 2}, {1.0, 1.0, 1.0}, {1, 1, 1}, 2, 3, true, false, 1.0, 0.0, 90.0},
+      {"q3_periodic_const_mass", {2, 2, 2}, {1.0, 0.75, 1.25}, {1, 1, 1}, 3, 3, false, false, 0.5, 1.3, 160.0},
+      {"q2_open_z_kappa", {3, 2, 2}, {1.0, 1.0, 1.0}, {1, 1, 0}, 2, 2, true, false, 1.0, 0.0, 90.0},
+      {"q4_periodic_kappa_qp2", {2, 2, 2}, {1.0, 1.0, 1.0}, {1, 1, 1}, 4, 5, true, false, 1.0, 0.2, 250.0},
+      {"q3_open_const_qp2", {2, 2, 2}, {1.0, 1.0, 1.0}, {0, 0, 0}, 3, 4, false, false, 1.0, 0.0, 160.0},
+      {"q2_dirichlet_kappa", {3, 2, 2}, {1.0, 1.0, 1.0}, {0, 0, 0}, 2, 2, true, true, 1.0, 0.0, 90.0},
+      {"q3_dirichlet_aniso_qp2", {2, 2, 2}, {1.0, 0.5, 2.0}, {0, 1, 0}, 3, 4, false, true, 0.8, 0.4, 160.0},
+  };
+  const int n = int(sizeof(cases) / sizeof(cases[0]));
+  std::printf("{\"source\": \"dune-fem DGEllipticOperator (dune/fem/schemes/dgelliptic.hh) over LegendreShapeFunctionSet "
+              "and GaussPts, compiled unmodified against oracle/shim_dg\",\n \"cases\": [\n");
+  for (int i = 0; i < n; ++i) refdg::run_case(cases[i], i == n - 1);
+  std::printf(" ]}\n");
+  return 0;
+}

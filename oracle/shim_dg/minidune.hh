@@ -1,0 +1,406 @@
+// A minimal grid / discrete-function-space layer of our own, just large
+// enough to compile dune-fem's DGEllipticOperator (dune/fem/schemes/
+// dgelliptic.hh) and LegendreShapeFunctionSet (dune/fem/space/
+// shapefunctionset/legendre.hh) unmodified, standing in for dune-common,
+// dune-geometry and dune-grid, which are absent here.  Test infrastructure
+// only: built by oracle/make_ref_golden.sh into oracle/_ref/, never used by
+// the product.
+//
+// What it provides, and the reference behaviour each piece restates:
+//  - FieldVector / FieldMatrix with the dense operations the two headers call
+//    (umv, mmv, usmv, mv, mtv, two_norm, scalar assignment);
+//  - an axis-aligned Cartesian grid of N0 x N1 x N2 cells on a box, cells
+//    numbered x fastest (YaspGrid's lexicographic order), optionally periodic
+//    per direction; a periodic boundary face is a neighbour intersection, as
+//    in YaspGrid; intersections of a cell in the order -x,+x,-y,+y,-z,+z;
+//  - affine cell geometry: integrationElement = |K|, J^{-T} = diag(1/h);
+//  - intersection geometry: |F| as volume and integration element, and
+//    integrationOuterNormal = |F| n (face reference element [0,1]^2, whose
+//    two coordinates are the cell's other two axes in increasing order);
+//  - tensor Gauss quadratures built from the reference's compiled GaussPts:
+//    m = the first rule whose order reaches the requested one (order <= 0
+//    taken as 1), point index with the first coordinate fastest
+//    (quadrature/femquadratures_inline.hh:33-90);
+//  - local functions over the Legendre set: values sum dof * phi, gradients
+//    are summed in reference coordinates and then mapped by J^{-T}, and axpy
+//    adds value * phi + (J^{-1} * factor) . grad_ref phi
+//    (space/basisfunctionset/default.hh:225-246, 451-459).
+#ifndef GBFEM_SHIM_DG_MINIDUNE_HH
+#define GBFEM_SHIM_DG_MINIDUNE_HH
+
+#include <array>
+#include <cmath>
+#include <cstddef>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <dune/fem/quadrature/gausspoints.hh>
+
+namespace Dune {
+
+template <class K, int n>
+class FieldVector {
+ public:
+  typedef K value_type;
+  typedef K field_type;
+  static constexpr int dimension = n;
+  FieldVector() { for (int i = 0; i < n; ++i) d_[i] = K(0); }
+  FieldVector(const K& v) { for (int i = 0; i < n; ++i) d_[i] = v; }
+  K& operator[](int i) { return d_[i]; }
+  const K& operator[](int i) const { return d_[i]; }
+  static constexpr int size() { return n; }
+  FieldVector& operator+=(const FieldVector& o) { for (int i = 0; i < n; ++i) d_[i] += o.d_[i]; return *this; }
+  FieldVector& operator-=(const FieldVector& o) { for (int i = 0; i < n; ++i) d_[i] -= o.d_[i]; return *this; }
+  FieldVector& operator*=(const K& s) { for (int i = 0; i < n; ++i) d_[i] *= s; return *this; }
+  FieldVector& operator/=(const K& s) { for (int i = 0; i < n; ++i) d_[i] /= s; return *this; }
+  FieldVector operator+(const FieldVector& o) const { FieldVector r(*this); r += o; return r; }
+  FieldVector operator-(const FieldVector& o) const { FieldVector r(*this); r -= o; return r; }
+  FieldVector operator-() const { FieldVector r(*this); r *= K(-1); return r; }
+  FieldVector& axpy(const K& a, const FieldVector& y) { for (int i = 0; i < n; ++i) d_[i] += a * y.d_[i]; return *this; }
+  K operator*(const FieldVector& o) const { K s(0); for (int i = 0; i < n; ++i) s += d_[i] * o.d_[i]; return s; }
+  K two_norm() const { K s(0); for (int i = 0; i < n; ++i) s += d_[i] * d_[i]; return std::sqrt(s); }
+
+ private:
+  K d_[n];
+};
+
+template <class K, int r, int c>
+class FieldMatrix {
+ public:
+  typedef FieldVector<K, c> row_type;
+  typedef row_type value_type;
+  typedef K field_type;
+  static constexpr int rows = r;
+  static constexpr int cols = c;
+  FieldMatrix() {}
+  FieldMatrix(const K& v) { for (int i = 0; i < r; ++i) m_[i] = row_type(v); }
+  row_type& operator[](int i) { return m_[i]; }
+  const row_type& operator[](int i) const { return m_[i]; }
+  FieldMatrix& operator+=(const FieldMatrix& o) { for (int i = 0; i < r; ++i) m_[i] += o.m_[i]; return *this; }
+  FieldMatrix& operator-=(const FieldMatrix& o) { for (int i = 0; i < r; ++i) m_[i] -= o.m_[i]; return *this; }
+  FieldMatrix& operator*=(const K& s) { for (int i = 0; i < r; ++i) m_[i] *= s; return *this; }
+  // y = A x
+  template <class X, class Y>
+  void mv(const X& x, Y& y) const { for (int i = 0; i < r; ++i) { y[i] = K(0); for (int j = 0; j < c; ++j) y[i] += m_[i][j] * x[j]; } }
+  // y = A^T x
+  template <class X, class Y>
+  void mtv(const X& x, Y& y) const { for (int j = 0; j < c; ++j) { y[j] = K(0); for (int i = 0; i < r; ++i) y[j] += m_[i][j] * x[i]; } }
+  // y += A x
+  template <class X, class Y>
+  void umv(const X& x, Y& y) const { for (int i = 0; i < r; ++i) for (int j = 0; j < c; ++j) y[i] += m_[i][j] * x[j]; }
+  // y -= A x
+  template <class X, class Y>
+  void mmv(const X& x, Y& y) const { for (int i = 0; i < r; ++i) for (int j = 0; j < c; ++j) y[i] -= m_[i][j] * x[j]; }
+  // y += alpha A x
+  template <class X, class Y>
+  void usmv(const K& alpha, const X& x, Y& y) const { for (int i = 0; i < r; ++i) for (int j = 0; j < c; ++j) y[i] += alpha * m_[i][j] * x[j]; }
+
+ private:
+  row_type m_[r];
+};
+
+namespace Fem {
+
+// -- parameters ------------------------------------------------------------
+class ParameterReader {
+ public:
+  template <class T>
+  T getValue(const std::string& key, const T& fallback) const {
+    auto it = values_.find(key);
+    return it == values_.end() ? fallback : T(it->second);
+  }
+  void set(const std::string& key, double v) { values_[key] = v; }
+
+ private:
+  std::map<std::string, double> values_;
+};
+struct Parameter {
+  static ParameterReader& container() { static ParameterReader r; return r; }
+};
+
+// -- operator interfaces (operator/common/operator.hh:55,
+//    differentiableoperator.hh:54) ------------------------------------------
+template <class DomainFunction, class RangeFunction = DomainFunction>
+struct Operator {
+  virtual ~Operator() {}
+  virtual void operator()(const DomainFunction& u, RangeFunction& w) const = 0;
+};
+template <class JacobianOperator>
+struct DifferentiableOperator
+    : public Operator<typename JacobianOperator::DomainFunctionType, typename JacobianOperator::RangeFunctionType> {};
+
+// Declared so that the Jacobian-assembly template of dgelliptic.hh parses;
+// the apply driver never instantiates it.
+template <class DomainSpace, class RangeSpace>
+class TemporaryLocalMatrix;
+template <class DomainSpace, class RangeSpace>
+class DiagonalAndNeighborStencil;
+
+// -- function space --------------------------------------------------------
+struct ScalarFunctionSpace3 {
+  static const int dimDomain = 3;
+  static const int dimRange = 1;
+  typedef double DomainFieldType;
+  typedef double RangeFieldType;
+  typedef FieldVector<double, 3> DomainType;
+  typedef FieldVector<double, 1> RangeType;
+  typedef FieldMatrix<double, 1, 3> JacobianRangeType;
+  typedef FieldVector<FieldMatrix<double, 3, 3>, 1> HessianRangeType;
+};
+
+// -- grid ------------------------------------------------------------------
+struct CartesianGrid {
+  int N[3];
+  double lower[3], h[3];
+  int periodic[3];
+  long long ncells() const { return (long long)N[0] * N[1] * N[2]; }
+  void coords(long long c, int* x) const {
+    x[0] = int(c % N[0]);
+    x[1] = int((c / N[0]) % N[1]);
+    x[2] = int(c / ((long long)N[0] * N[1]));
+  }
+  long long index(const int* x) const { return x[0] + (long long)N[0] * (x[1] + (long long)N[1] * x[2]); }
+  // neighbour of cell c through face f (-x,+x,-y,+y,-z,+z); -1 on a domain boundary
+  long long neighbour(long long c, int f) const {
+    int x[3];
+    coords(c, x);
+    const int dir = f / 2;
+    x[dir] += (f % 2) ? 1 : -1;
+    if (x[dir] < 0 || x[dir] >= N[dir]) {
+      if (!periodic[dir]) return -1;
+      x[dir] = (x[dir] + N[dir]) % N[dir];
+    }
+    return index(x);
+  }
+  double volume() const { return h[0] * h[1] * h[2]; }
+};
+
+class CellGeometry {
+ public:
+  typedef FieldMatrix<double, 3, 3> JacobianInverseTransposed;
+  explicit CellGeometry(const CartesianGrid* g) : g_(g) {}
+  double volume() const { return g_->volume(); }
+  template <class X>
+  double integrationElement(const X&) const { return g_->volume(); }
+  template <class X>
+  JacobianInverseTransposed jacobianInverseTransposed(const X&) const {
+    JacobianInverseTransposed j(0.0);
+    for (int k = 0; k < 3; ++k) j[k][k] = 1.0 / g_->h[k];
+    return j;
+  }
+
+ private:
+  const CartesianGrid* g_;
+};
+
+class Cell {
+ public:
+  typedef CellGeometry Geometry;
+  Cell() : g_(nullptr), idx_(-1) {}
+  Cell(const CartesianGrid* g, long long idx) : g_(g), idx_(idx) {}
+  Geometry geometry() const { return Geometry(g_); }
+  long long index() const { return idx_; }
+  const CartesianGrid* grid() const { return g_; }
+
+ private:
+  const CartesianGrid* g_;
+  long long idx_;
+};
+
+class FaceGeometry {
+ public:
+  FaceGeometry(const CartesianGrid* g, int dir) : area_(g->volume() / g->h[dir]) {}
+  double volume() const { return area_; }
+  template <class X>
+  double integrationElement(const X&) const { return area_; }
+
+ private:
+  double area_;
+};
+
+class Face {
+ public:
+  typedef FaceGeometry Geometry;
+  Face(const CartesianGrid* g, long long in, int f) : g_(g), in_(in), f_(f), out_(g->neighbour(in, f)) {}
+  bool neighbor() const { return out_ >= 0; }
+  bool boundary() const {
+    // YaspGrid: a face on the domain boundary is a boundary intersection,
+    // periodic or not
+    int x[3];
+    g_->coords(in_, x);
+    const int dir = f_ / 2;
+    return (f_ % 2) ? x[dir] == g_->N[dir] - 1 : x[dir] == 0;
+  }
+  Cell inside() const { return Cell(g_, in_); }
+  Cell outside() const { return Cell(g_, out_); }
+  Geometry geometry() const { return Geometry(g_, f_ / 2); }
+  int indexInInside() const { return f_; }
+  int indexInOutside() const { return f_ ^ 1; }
+  template <class X>
+  FieldVector<double, 3> unitOuterNormal(const X&) const {
+    FieldVector<double, 3> n(0.0);
+    n[f_ / 2] = (f_ % 2) ? 1.0 : -1.0;
+    return n;
+  }
+  template <class X>
+  FieldVector<double, 3> integrationOuterNormal(const X& x) const {
+    FieldVector<double, 3> n = unitOuterNormal(x);
+    n *= geometry().volume();
+    return n;
+  }
+  const CartesianGrid* grid() const { return g_; }
+
+ private:
+  const CartesianGrid* g_;
+  long long in_;
+  int f_;
+  long long out_;
+};
+
+class FaceIterator {
+ public:
+  typedef Face Intersection;
+  FaceIterator(const CartesianGrid* g, long long c, int f) : g_(g), c_(c), f_(f) {}
+  Face operator*() const { return Face(g_, c_, f_); }
+  FaceIterator& operator++() { ++f_; return *this; }
+  bool operator!=(const FaceIterator& o) const { return f_ != o.f_ || c_ != o.c_; }
+  bool operator==(const FaceIterator& o) const { return !(*this != o); }
+
+ private:
+  const CartesianGrid* g_;
+  long long c_;
+  int f_;
+};
+
+class CellIterator {
+ public:
+  typedef Cell Entity;
+  CellIterator(const CartesianGrid* g, long long c) : g_(g), c_(c) {}
+  Cell operator*() const { return Cell(g_, c_); }
+  CellIterator& operator++() { ++c_; return *this; }
+  bool operator!=(const CellIterator& o) const { return c_ != o.c_; }
+  bool operator==(const CellIterator& o) const { return c_ == o.c_; }
+
+ private:
+  const CartesianGrid* g_;
+  long long c_;
+};
+
+class GridPart {
+ public:
+  typedef FaceIterator IntersectionIteratorType;
+  typedef Face IntersectionType;
+  explicit GridPart(const CartesianGrid* g) : g_(g) {}
+  FaceIterator ibegin(const Cell& e) const { return FaceIterator(g_, e.index(), 0); }
+  FaceIterator iend(const Cell& e) const { return FaceIterator(g_, e.index(), 6); }
+  const CartesianGrid* grid() const { return g_; }
+
+ private:
+  const CartesianGrid* g_;
+};
+
+// -- quadratures -----------------------------------------------------------
+// A quadrature point as handed to local functions and models: the position
+// in the reference cell of the element it is evaluated on.
+struct ElementPoint {
+  FieldVector<double, 3> x;
+};
+inline const FieldVector<double, 3>& coordinate(const ElementPoint& p) { return p.x; }
+inline const FieldVector<double, 3>& coordinate(const FieldVector<double, 3>& x) { return x; }
+
+inline int gauss_points_for_order(int order) {
+  static const GaussPts gp;
+  if (order <= 0) order = 1;
+  for (int i = 0; i <= GaussPts::MAXP; ++i)
+    if (gp.order(i) >= order) return i;
+  return -1;
+}
+inline const GaussPts& gauss_rules() {
+  static const GaussPts gp;
+  return gp;
+}
+
+template <class GridPartT, int codim>
+class CachingQuadrature;
+
+template <class GridPartT>
+class CachingQuadrature<GridPartT, 0> {
+ public:
+  typedef FieldVector<double, 3> CoordinateType;
+  typedef ElementPoint QuadraturePointWrapperType;
+  CachingQuadrature(const Cell&, int order) {
+    const int m = gauss_points_for_order(order);
+    const GaussPts& gp = gauss_rules();
+    for (int i = 0; i < m * m * m; ++i) {
+      int z = i;
+      ElementPoint p;
+      double w = 1.0;
+      for (int k = 0; k < 3; ++k) {
+        const int xk = z % m;
+        z /= m;
+        p.x[k] = gp.point(m, xk);
+        w *= gp.weight(m, xk);
+      }
+      pts_.push_back(p);
+      wts_.push_back(w);
+    }
+  }
+  std::size_t nop() const { return pts_.size(); }
+  const CoordinateType& point(std::size_t i) const { return pts_[i].x; }
+  double weight(std::size_t i) const { return wts_[i]; }
+  const ElementPoint& operator[](std::size_t i) const { return pts_[i]; }
+
+ private:
+  std::vector<ElementPoint> pts_;
+  std::vector<double> wts_;
+};
+
+template <class GridPartT, int codim>
+class ElementQuadrature;
+
+template <class GridPartT>
+class ElementQuadrature<GridPartT, 1> {
+ public:
+  enum Side { INSIDE, OUTSIDE };
+  typedef FieldVector<double, 2> LocalCoordinateType;
+  typedef FieldVector<double, 3> CoordinateType;
+  ElementQuadrature(const GridPartT&, const Face& face, int order, Side side) {
+    const int m = gauss_points_for_order(order);
+    const GaussPts& gp = gauss_rules();
+    const int f = side == INSIDE ? face.indexInInside() : face.indexInOutside();
+    const int dir = f / 2;
+    int axes[2], a = 0;
+    for (int k = 0; k < 3; ++k)
+      if (k != dir) axes[a++] = k;
+    for (int i = 0; i < m * m; ++i) {
+      const int s = i % m, t = i / m;
+      LocalCoordinateType xl;
+      xl[0] = gp.point(m, s);
+      xl[1] = gp.point(m, t);
+      ElementPoint p;
+      p.x[dir] = (f % 2) ? 1.0 : 0.0;
+      p.x[axes[0]] = xl[0];
+      p.x[axes[1]] = xl[1];
+      local_.push_back(xl);
+      pts_.push_back(p);
+      wts_.push_back(gp.weight(m, s) * gp.weight(m, t));
+    }
+  }
+  std::size_t nop() const { return pts_.size(); }
+  const LocalCoordinateType& localPoint(std::size_t i) const { return local_[i]; }
+  const CoordinateType& point(std::size_t i) const { return pts_[i].x; }
+  double weight(std::size_t i) const { return wts_[i]; }
+  const ElementPoint& operator[](std::size_t i) const { return pts_[i]; }
+
+ private:
+  std::vector<LocalCoordinateType> local_;
+  std::vector<ElementPoint> pts_;
+  std::vector<double> wts_;
+};
+
+}  // namespace Fem
+}  // namespace Dune
+
+#endif
