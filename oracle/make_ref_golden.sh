@@ -2,11 +2,13 @@
 # Compiles the reference's standalone-buildable sources for this path
 # (Gauss rules, Legendre tables, CG/GMRES/BiCGstab templates) with the driver
 # oracle/ref_driver.cpp (with the oracle's operator, oracle.cpp) into
-# oracle/_ref/, and the reference's DG elliptic operator (dgelliptic.hh over
-# legendre.hh) with oracle/ref_dgelliptic.cpp against the grid shim in
+# oracle/_ref/, the reference's DG elliptic operator (dgelliptic.hh over
+# legendre.hh) with oracle/ref_dgelliptic.cpp, and its explicit time loop
+# (timeprovider.hh, rungekutta/explicit.hh, butchertable.cc) over that
+# operator with oracle/ref_timeloop.cpp, both against the grid shim in
 # oracle/shim_dg; runs them, and writes the golden vectors
-# tests/golden/ref_tables.json, ref_krylov.json, ref_krylov_sipg.json and
-# ref_dgelliptic.json.
+# tests/golden/ref_tables.json, ref_krylov.json, ref_krylov_sipg.json,
+# ref_dgelliptic.json and ref_timeloop.json.
 # Needs the dune-fem source tree (located by ref_src.sh); without it this
 # recipe does nothing (the committed golden vectors stay as they are).  With
 # --compile-only it builds the driver and writes nothing.  The reference's
@@ -27,12 +29,17 @@ $CXX -O2 -std=c++17 -pthread -I"$HERE/shim" -I"$REF" \
 $CXX -O2 -std=c++17 -I"$HERE/shim_dg" -I"$HERE/shim" -I"$REF" \
   "$HERE/ref_dgelliptic.cpp" "$REF/dune/fem/space/shapefunctionset/legendrepolynomials.cc" \
   -o "$OUT/ref_dgelliptic"
+$CXX -O2 -std=c++17 -I"$HERE/shim_dg" -I"$HERE/shim" -I"$REF" \
+  "$HERE/ref_timeloop.cpp" "$REF/dune/fem/space/shapefunctionset/legendrepolynomials.cc" \
+  "$REF/dune/fem/solver/rungekutta/butchertable.cc" -o "$OUT/ref_timeloop"
 if [ "$1" = "--compile-only" ]; then
-  echo "built $OUT/ref_driver $OUT/ref_dgelliptic"
+  echo "built $OUT/ref_driver $OUT/ref_dgelliptic $OUT/ref_timeloop"
   exit 0
 fi
 "$OUT/ref_driver" tables > "$GOLD/ref_tables.json"
 "$OUT/ref_driver" krylov > "$GOLD/ref_krylov.json"
 "$OUT/ref_driver" sipg > "$GOLD/ref_krylov_sipg.json"
 "$OUT/ref_dgelliptic" > "$GOLD/ref_dgelliptic.json"
-echo "wrote $GOLD/ref_tables.json $GOLD/ref_krylov.json $GOLD/ref_krylov_sipg.json $GOLD/ref_dgelliptic.json"
+"$OUT/ref_timeloop" > "$GOLD/ref_timeloop.json"
+echo "wrote $GOLD/ref_tables.json $GOLD/ref_krylov.json $GOLD/ref_krylov_sipg.json $GOLD/ref_dgelliptic.json" \
+  "$GOLD/ref_timeloop.json"

@@ -7,6 +7,7 @@
 #define GBFEM_SHIM_DG_DGSPACE_HH
 
 #include <algorithm>
+#include <string>
 #include <vector>
 
 #include "minidune.hh"
@@ -62,8 +63,13 @@ class DGFunction {
   typedef LocalFunctionTraits LocalFunctionType;
   typedef double DofType;
   explicit DGFunction(const LegendreDGSpace& s) : space_(&s), dofs_(s.size(), 0.0) {}
+  DGFunction(const std::string&, const LegendreDGSpace& s) : DGFunction(s) {}
   const LegendreDGSpace& space() const { return *space_; }
   void clear() { std::fill(dofs_.begin(), dofs_.end(), 0.0); }
+  void assign(const DGFunction& o) { dofs_ = o.dofs_; }
+  void axpy(double a, const DGFunction& x) {
+    for (std::size_t i = 0; i < dofs_.size(); ++i) dofs_[i] += a * x.dofs_[i];
+  }
   void communicate() {}
   std::vector<double>& dofs() { return dofs_; }
   const std::vector<double>& dofs() const { return dofs_; }

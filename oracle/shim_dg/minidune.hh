@@ -1,12 +1,18 @@
 // A minimal grid / discrete-function-space layer of our own, just large
 // enough to compile dune-fem's DGEllipticOperator (dune/fem/schemes/
-// dgelliptic.hh) and LegendreShapeFunctionSet (dune/fem/space/
-// shapefunctionset/legendre.hh) unmodified, standing in for dune-common,
-// dune-geometry and dune-grid, which are absent here.  Test infrastructure
-// only: built by oracle/make_ref_golden.sh into oracle/_ref/, never used by
-// the product.
+// dgelliptic.hh), LegendreShapeFunctionSet (dune/fem/space/shapefunctionset/
+// legendre.hh), TimeProvider (solver/timeprovider.hh) and
+// ExplicitRungeKuttaSolver (solver/rungekutta/explicit.hh) unmodified,
+// standing in for dune-common, dune-geometry and dune-grid and the parts of
+// dune-fem those headers pull in, which are absent here.  Test
+// infrastructure only: built by oracle/make_ref_golden.sh into oracle/_ref/,
+// never used by the product.
 //
 // What it provides, and the reference behaviour each piece restates:
+//  - DUNE_THROW and the exception types; DynamicVector / DynamicMatrix;
+//    a serial MPIManager; no-op persistence hooks; a numeric ParameterReader;
+//    the SpaceOperatorInterface the Runge-Kutta solver calls (operator(),
+//    space(), setTime(), timeStepEstimate());
 //  - FieldVector / FieldMatrix with the dense operations the two headers call
 //    (umv, mmv, usmv, mv, mtv, two_norm, scalar assignment);
 //  - an axis-aligned Cartesian grid of N0 x N1 x N2 cells on a box, cells
@@ -31,14 +37,66 @@
 #include <array>
 #include <cmath>
 #include <cstddef>
+#include <limits>
 #include <map>
 #include <memory>
+#include <sstream>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
 #include <dune/fem/quadrature/gausspoints.hh>
 
+// exceptions (dune/common/exceptions.hh)
+#define DUNE_THROW(E, m)                 \
+  do {                                   \
+    std::ostringstream dune_throw_msg_;  \
+    dune_throw_msg_ << m;                \
+    throw E(dune_throw_msg_.str());      \
+  } while (0)
+
 namespace Dune {
+
+struct Exception : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct InvalidStateException : Exception {
+  using Exception::Exception;
+};
+struct NotImplemented : Exception {
+  using Exception::Exception;
+};
+
+// dense containers of run-time size (dune/common/dynvector.hh, dynmatrix.hh)
+template <class K>
+class DynamicVector {
+ public:
+  DynamicVector() {}
+  explicit DynamicVector(std::size_t n, const K& v = K(0)) : d_(n, v) {}
+  K& operator[](std::size_t i) { return d_[i]; }
+  const K& operator[](std::size_t i) const { return d_[i]; }
+  std::size_t size() const { return d_.size(); }
+  typename std::vector<K>::iterator begin() { return d_.begin(); }
+  typename std::vector<K>::iterator end() { return d_.end(); }
+  typename std::vector<K>::const_iterator begin() const { return d_.begin(); }
+  typename std::vector<K>::const_iterator end() const { return d_.end(); }
+
+ private:
+  std::vector<K> d_;
+};
+
+template <class K>
+class DynamicMatrix {
+ public:
+  DynamicMatrix() {}
+  DynamicMatrix(std::size_t m, std::size_t n, const K& v = K(0)) : rows_(m, DynamicVector<K>(n, v)) {}
+  DynamicVector<K>& operator[](std::size_t i) { return rows_[i]; }
+  const DynamicVector<K>& operator[](std::size_t i) const { return rows_[i]; }
+  std::size_t rows() const { return rows_.size(); }
+
+ private:
+  std::vector<DynamicVector<K>> rows_;
+};
 
 template <class K, int n>
 class FieldVector {
@@ -103,13 +161,27 @@ class FieldMatrix {
 
 namespace Fem {
 
-// -- parameters ------------------------------------------------------------
+// parameters (dune/fem/io/parameter.hh): numeric values by key
 class ParameterReader {
  public:
   template <class T>
   T getValue(const std::string& key, const T& fallback) const {
     auto it = values_.find(key);
     return it == values_.end() ? fallback : T(it->second);
+  }
+  template <class T, class Validator>
+  T getValidValue(const std::string& key, const T& fallback, const Validator& valid) const {
+    const T v = getValue<T>(key, fallback);
+    if (!valid(v)) throw std::invalid_argument("invalid value for parameter " + key);
+    return v;
+  }
+  template <class T, class Validator>
+  T getValidValue(const std::string& key, const Validator& valid) const {
+    auto it = values_.find(key);
+    if (it == values_.end()) throw std::invalid_argument("missing parameter " + key);
+    const T v = T(it->second);
+    if (!valid(v)) throw std::invalid_argument("invalid value for parameter " + key);
+    return v;
   }
   void set(const std::string& key, double v) { values_[key] = v; }
 
@@ -118,6 +190,48 @@ class ParameterReader {
 };
 struct Parameter {
   static ParameterReader& container() { static ParameterReader r; return r; }
+};
+
+// a serial run (dune/fem/misc/mpimanager.hh)
+struct SerialCommunication {
+  template <class T>
+  T min(const T& x) const { return x; }
+  template <class T>
+  T max(const T& x) const { return x; }
+  template <class T>
+  T sum(const T& x) const { return x; }
+};
+struct MPIManager {
+  typedef SerialCommunication Communication;
+  static const Communication& comm() { static Communication c; return c; }
+};
+
+// checkpointing hooks (dune/fem/io/file/persistencemanager.hh): no-ops here
+struct AutoPersistentObject {
+  virtual ~AutoPersistentObject() {}
+  virtual void backup() const {}
+  virtual void restore() {}
+};
+struct PersistenceManager {
+  template <class T>
+  static void backupValue(const std::string&, const T&) {}
+  template <class T>
+  static void restoreValue(const std::string&, T&) {}
+};
+
+template <class Grid>
+class DofManager;
+
+// the right-hand side of an ODE u' = L(u) (operator/common/spaceoperatorif.hh)
+template <class DestinationImp>
+struct SpaceOperatorInterface {
+  typedef DestinationImp DestinationType;
+  typedef typename DestinationImp::DiscreteFunctionSpaceType SpaceType;
+  virtual ~SpaceOperatorInterface() {}
+  virtual void operator()(const DestinationType& u, DestinationType& w) const = 0;
+  virtual const SpaceType& space() const = 0;
+  virtual void setTime(const double) {}
+  virtual double timeStepEstimate() const { return std::numeric_limits<double>::max(); }
 };
 
 // -- operator interfaces (operator/common/operator.hh:55,
