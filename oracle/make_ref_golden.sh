@@ -2,13 +2,14 @@
 # Compiles the reference's standalone-buildable sources for this path
 # (Gauss rules, Legendre tables, CG/GMRES/BiCGstab templates) with the driver
 # oracle/ref_driver.cpp (with the oracle's operator, oracle.cpp) into
-# oracle/_ref/, the reference's DG elliptic operator (dgelliptic.hh over
-# legendre.hh) with oracle/ref_dgelliptic.cpp, and its explicit time loop
+# oracle/_ref/, the reference's DG elliptic operator and its assembled
+# Jacobian (dgelliptic.hh over legendre.hh) with oracle/ref_dgelliptic.cpp,
+# and its explicit time loop
 # (timeprovider.hh, rungekutta/explicit.hh, butchertable.cc) over that
 # operator with oracle/ref_timeloop.cpp, both against the grid shim in
 # oracle/shim_dg; runs them, and writes the golden vectors
 # tests/golden/ref_tables.json, ref_krylov.json, ref_krylov_sipg.json,
-# ref_dgelliptic.json and ref_timeloop.json.
+# ref_dgelliptic.json, ref_dgelliptic_jacobian.json and ref_timeloop.json.
 # Needs the dune-fem source tree (located by ref_src.sh); without it this
 # recipe does nothing (the committed golden vectors stay as they are).  With
 # --compile-only it builds the driver and writes nothing.  The reference's
@@ -40,6 +41,7 @@ fi
 "$OUT/ref_driver" krylov > "$GOLD/ref_krylov.json"
 "$OUT/ref_driver" sipg > "$GOLD/ref_krylov_sipg.json"
 "$OUT/ref_dgelliptic" > "$GOLD/ref_dgelliptic.json"
+"$OUT/ref_dgelliptic" jacobian > "$GOLD/ref_dgelliptic_jacobian.json"
 "$OUT/ref_timeloop" > "$GOLD/ref_timeloop.json"
 echo "wrote $GOLD/ref_tables.json $GOLD/ref_krylov.json $GOLD/ref_krylov_sipg.json $GOLD/ref_dgelliptic.json" \
-  "$GOLD/ref_timeloop.json"
+  "$GOLD/ref_dgelliptic_jacobian.json $GOLD/ref_timeloop.json"

@@ -16,6 +16,33 @@
 namespace Dune {
 namespace Fem {
 
+class LegendreDGSpace;
+
+// The basis of one cell (DefaultBasisFunctionSet): values and gradients of
+// all shape functions at a point, gradients mapped by J^{-T}
+// (space/basisfunctionset/default.hh:276-330, 361-372).
+class LegendreBasisFunctionSet {
+ public:
+  typedef ScalarFunctionSpace3::RangeType RangeType;
+  typedef ScalarFunctionSpace3::JacobianRangeType JacobianRangeType;
+  LegendreBasisFunctionSet() : space_(nullptr) {}
+  LegendreBasisFunctionSet(const LegendreDGSpace* s, const Cell& c) : space_(s), cell_(c) {}
+  inline std::size_t size() const;
+  template <class Point>
+  void evaluateAll(const Point& x, std::vector<RangeType>& phi) const;
+  template <class Point>
+  void jacobianAll(const Point& x, std::vector<JacobianRangeType>& dphi) const;
+
+ private:
+  const LegendreDGSpace* space_;
+  Cell cell_;
+};
+
+struct BlockMapper {
+  std::size_t n;
+  std::size_t maxNumDofs() const { return n; }
+};
+
 class LegendreDGSpace {
  public:
   typedef ScalarFunctionSpace3 FunctionSpaceType;
@@ -25,6 +52,8 @@ class LegendreDGSpace {
   typedef GridPart GridPartType;
   typedef CellIterator IteratorType;
   typedef LegendreShapeFunctionSet<FunctionSpaceType, false> ShapeFunctionSetType;
+  typedef LegendreBasisFunctionSet BasisFunctionSetType;
+  static const int localBlockSize = 1;
 
   // reported_order: the polynomial order that local functions report to the
   // operator, which chooses its quadrature from it (order() of u plus order()
@@ -40,6 +69,8 @@ class LegendreDGSpace {
   std::size_t localSize() const { return shapes_.size(); }
   std::size_t size() const { return shapes_.size() * grid_.ncells(); }
   const ShapeFunctionSetType& shapeFunctionSet() const { return shapes_; }
+  BasisFunctionSetType basisFunctionSet(const Cell& c) const { return BasisFunctionSetType(this, c); }
+  BlockMapper blockMapper() const { return BlockMapper{shapes_.size()}; }
   const CartesianGrid& grid() const { return grid_; }
 
  private:
@@ -48,6 +79,19 @@ class LegendreDGSpace {
   ShapeFunctionSetType shapes_;
   int order_, reported_;
 };
+
+inline std::size_t LegendreBasisFunctionSet::size() const { return space_->localSize(); }
+template <class Point>
+void LegendreBasisFunctionSet::evaluateAll(const Point& x, std::vector<RangeType>& phi) const {
+  space_->shapeFunctionSet().evaluateEach(x, [&](std::size_t i, const RangeType& v) { phi[i] = v; });
+}
+template <class Point>
+void LegendreBasisFunctionSet::jacobianAll(const Point& x, std::vector<JacobianRangeType>& dphi) const {
+  const auto jit = cell_.geometry().jacobianInverseTransposed(coordinate(x));
+  space_->shapeFunctionSet().jacobianEach(x, [&](std::size_t i, const JacobianRangeType& d) {
+    jit.mv(d[0], dphi[i][0]);
+  });
+}
 
 struct LocalFunctionTraits {
   typedef LegendreDGSpace::RangeType RangeType;
@@ -150,6 +194,88 @@ class AddLocalContribution {
   DF* f_;
   Cell cell_;
   std::vector<double> local_;
+};
+
+// A dense local matrix between the basis of a domain cell (columns) and of a
+// range cell (rows), with the column axpy of operator/common/localmatrix.hh:
+// 545-566: a_ij += weight (factor phi_i + jacobianFactor : dphi_i).
+template <class DomainSpace, class RangeSpace>
+class TemporaryLocalMatrix {
+ public:
+  class Column {
+   public:
+    Column(TemporaryLocalMatrix* m, int c) : m_(m), c_(c) {}
+    template <class RangeVector, class JacobianVector, class R, class J>
+    void axpy(const RangeVector& phi, const JacobianVector& dphi, const R& factor, const J& jacobianFactor,
+              double weight) {
+      for (int row = 0; row < m_->rows(); ++row) {
+        double value = factor * phi[row];
+        for (int k = 0; k < J::rows; ++k) value += jacobianFactor[k] * dphi[row][k];
+        m_->a_[std::size_t(row) * m_->cols() + c_] += weight * value;
+      }
+    }
+
+   private:
+    TemporaryLocalMatrix* m_;
+    int c_;
+  };
+  TemporaryLocalMatrix(const DomainSpace& d, const RangeSpace& r) : domain_(&d), range_(&r) {}
+  void bind(const Cell& domainEntity, const Cell& rangeEntity) {
+    de_ = domainEntity;
+    re_ = rangeEntity;
+    a_.assign(std::size_t(rows()) * cols(), 0.0);
+  }
+  void unbind() {}
+  void clear() { std::fill(a_.begin(), a_.end(), 0.0); }
+  int rows() const { return int(range_->localSize()); }
+  int cols() const { return int(domain_->localSize()); }
+  double get(int i, int j) const { return a_[std::size_t(i) * cols() + j]; }
+  LegendreBasisFunctionSet domainBasisFunctionSet() const { return domain_->basisFunctionSet(de_); }
+  LegendreBasisFunctionSet rangeBasisFunctionSet() const { return range_->basisFunctionSet(re_); }
+  Column column(int c) { return Column(this, c); }
+  const Cell& domainEntity() const { return de_; }
+  const Cell& rangeEntity() const { return re_; }
+
+ private:
+  const DomainSpace* domain_;
+  const RangeSpace* range_;
+  Cell de_, re_;
+  std::vector<double> a_;
+};
+
+template <class DomainSpace, class RangeSpace>
+class DiagonalAndNeighborStencil {
+ public:
+  DiagonalAndNeighborStencil(const DomainSpace&, const RangeSpace&) {}
+};
+
+// The assembled Jacobian as a dense matrix (rows: range dofs, columns: domain
+// dofs), filled by addLocalMatrix like the reference's sparse-row operator.
+class DenseLinearOperator {
+ public:
+  typedef DGFunction DomainFunctionType;
+  typedef DGFunction RangeFunctionType;
+  explicit DenseLinearOperator(const LegendreDGSpace& s) : space_(&s), n_(s.size()), a_(n_ * n_, 0.0) {}
+  const LegendreDGSpace& domainSpace() const { return *space_; }
+  const LegendreDGSpace& rangeSpace() const { return *space_; }
+  template <class Stencil>
+  void reserve(const Stencil&) {}
+  void clear() { std::fill(a_.begin(), a_.end(), 0.0); }
+  template <class Local>
+  void addLocalMatrix(const Cell& domainEntity, const Cell& rangeEntity, const Local& m) {
+    const std::size_t nl = space_->localSize();
+    for (int i = 0; i < m.rows(); ++i)
+      for (int j = 0; j < m.cols(); ++j)
+        a_[(rangeEntity.index() * nl + i) * n_ + domainEntity.index() * nl + j] += m.get(i, j);
+  }
+  void flushAssembly() {}
+  double operator()(std::size_t i, std::size_t j) const { return a_[i * n_ + j]; }
+  std::size_t size() const { return n_; }
+
+ private:
+  const LegendreDGSpace* space_;
+  std::size_t n_;
+  std::vector<double> a_;
 };
 
 template <class LF>

@@ -243,10 +243,10 @@ struct Operator {
 };
 template <class JacobianOperator>
 struct DifferentiableOperator
-    : public Operator<typename JacobianOperator::DomainFunctionType, typename JacobianOperator::RangeFunctionType> {};
+    : public virtual Operator<typename JacobianOperator::DomainFunctionType,
+                              typename JacobianOperator::RangeFunctionType> {};
 
-// Declared so that the Jacobian-assembly template of dgelliptic.hh parses;
-// the apply driver never instantiates it.
+// defined in dgspace.hh
 template <class DomainSpace, class RangeSpace>
 class TemporaryLocalMatrix;
 template <class DomainSpace, class RangeSpace>

@@ -27,6 +27,11 @@ from conftest import relmax
 GOLD = os.path.join(os.path.dirname(__file__), "golden", "ref_dgelliptic.json")
 with open(GOLD) as _f:
     CASES = {c["name"]: c for c in json.load(_f)["cases"]}
+# the same operator's assembled Jacobian (DifferentiableDGEllipticOperator::
+# jacobian, dgelliptic.hh:456-766): J v, its diagonal, some diagonal blocks
+# and the Frobenius norms of all nonzero cell blocks
+with open(os.path.join(os.path.dirname(__file__), "golden", "ref_dgelliptic_jacobian.json")) as _f:
+    JAC = {c["name"]: c for c in json.load(_f)["cases"]}
 
 
 def inputs(case):
@@ -45,6 +50,12 @@ def inputs(case):
         kappa[:, 0] = 1.0 + ((c * 31 + 7) % 11) / 10.0
         kappa = kappa.reshape(-1)
     return u, kappa
+
+
+def probe(n):
+    """The second probe vector of the Jacobian golden (exact, as u)."""
+    i = np.arange(n, dtype=np.int64)
+    return ((i * 4243 + 7) % 1999 - 999) / 1000.0
 
 
 def problem_kw(case):
@@ -89,6 +100,30 @@ def test_gpu_operator_rejects_the_half_symmetry_boundary(gb):
     reference operator's variant is an error, not a silent substitution."""
     with pytest.raises(ValueError):
         gb.DGOperator((2, 2, 2), 2, weak_dirichlet="dgelliptic")
+
+
+@pytest.mark.parametrize("name", sorted(JAC))
+def test_oracle_matrix_equals_reference_jacobian(orc, name):
+    """The oracle's operator, assembled column by column, is the reference's
+    assembled Jacobian: the same nonzero cell blocks with the same norms,
+    products, diagonal and diagonal blocks."""
+    case = JAC[name]
+    _, kappa = inputs(case)
+    prob = orc.DGProblem(tuple(case["cells"]), case["order"],
+                         weak_dirichlet="dgelliptic" if case["dirichlet"] else False, **problem_kw(case))
+    n, nl = prob.ndofs, prob.nloc
+    A = np.stack([prob.apply(e, kappa=kappa) for e in np.eye(n)], axis=1)
+    assert relmax(A @ probe(n), case["Jv"]) < 1e-13
+    assert relmax(np.diag(A), case["diag"]) < 1e-13
+    ref_norms = {(r, c): f for r, c, f in case["block_norms"]}
+    blocks = A.reshape(prob.ncells, nl, prob.ncells, nl)
+    norms = np.linalg.norm(blocks, axis=(1, 3))
+    assert set(zip(*np.nonzero(norms))) == set(ref_norms)
+    assert max(abs(norms[k] - f) / f for k, f in ref_norms.items()) < 1e-13
+    bd = prob.block_diagonal(kappa=kappa)
+    cells = case["block_cells"]
+    if cells:
+        assert relmax(bd[cells], np.array(case["blocks"]).reshape(len(cells), nl, nl)) < 1e-13
 
 
 # ---- the reference operator's integrands as a raw form ------------------------------
@@ -188,3 +223,27 @@ def test_gpu_raw_form_equals_reference_dgelliptic(gb, name):
     w = gb.DeviceArray(u.size)
     op(gb.DeviceArray.from_numpy(u), w)
     assert relmax(w.numpy(), case["w"]) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(n for n, c in JAC.items() if not c["dirichlet"]))
+def test_gpu_jacobian_equals_reference_jacobian(gb, name):
+    """The block diagonal, the diagonal and the assembled block-sparse matrix
+    of DGOperator against the reference's assembled Jacobian."""
+    case = JAC[name]
+    _, kappa = inputs(case)
+    op = gb.DGOperator(tuple(case["cells"]), case["order"], weak_dirichlet=False,
+                       kappa=None if kappa is None else gb.DeviceArray.from_numpy(kappa), **problem_kw(case))
+    nl = (case["order"] + 1) ** 3
+    ncells = int(np.prod(case["cells"]))
+    assert relmax(op.diagonal().numpy(), case["diag"]) < 1e-12
+    cells = case["block_cells"]
+    if cells:
+        bd = op.block_diagonal(nl).numpy().reshape(ncells, nl, nl)
+        assert relmax(bd[cells], np.array(case["blocks"]).reshape(len(cells), nl, nl)) < 1e-12
+    A = op.assemble()
+    v = probe(ncells * nl)
+    y = gb.DeviceArray(v.size)
+    A(gb.DeviceArray.from_numpy(v), y)
+    assert relmax(y.numpy(), case["Jv"]) < 1e-12
+    assert relmax(A.diagonal().numpy(), case["diag"]) < 1e-12
