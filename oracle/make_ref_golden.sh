@@ -9,7 +9,8 @@
 # operator with oracle/ref_timeloop.cpp, both against the grid shim in
 # oracle/shim_dg; runs them, and writes the golden vectors
 # tests/golden/ref_tables.json, ref_krylov.json, ref_krylov_sipg.json,
-# ref_dgelliptic.json, ref_dgelliptic_jacobian.json and ref_timeloop.json.
+# ref_dgelliptic.json, ref_dgelliptic_jacobian.json, ref_legendre_order.json
+# (the hierarchical shape-function order) and ref_timeloop.json.
 # Needs the dune-fem source tree (located by ref_src.sh); without it this
 # recipe does nothing (the committed golden vectors stay as they are).  With
 # --compile-only it builds the driver and writes nothing.  The reference's
@@ -42,6 +43,7 @@ fi
 "$OUT/ref_driver" sipg > "$GOLD/ref_krylov_sipg.json"
 "$OUT/ref_dgelliptic" > "$GOLD/ref_dgelliptic.json"
 "$OUT/ref_dgelliptic" jacobian > "$GOLD/ref_dgelliptic_jacobian.json"
+"$OUT/ref_dgelliptic" hierarchical > "$GOLD/ref_legendre_order.json"
 "$OUT/ref_timeloop" > "$GOLD/ref_timeloop.json"
 echo "wrote $GOLD/ref_tables.json $GOLD/ref_krylov.json $GOLD/ref_krylov_sipg.json $GOLD/ref_dgelliptic.json" \
-  "$GOLD/ref_dgelliptic_jacobian.json $GOLD/ref_timeloop.json"
+  "$GOLD/ref_dgelliptic_jacobian.json $GOLD/ref_legendre_order.json $GOLD/ref_timeloop.json"

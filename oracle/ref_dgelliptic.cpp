@@ -7,7 +7,10 @@
 // argument "jacobian" it assembles the operator's Jacobian instead
 // (DifferentiableDGEllipticOperator::jacobian, dgelliptic.hh:456-766) and
 // prints it through products, its diagonal, some diagonal blocks and the
-// norms of all its nonzero cell blocks.  Built and run only by
+// norms of all its nonzero cell blocks.  With "hierarchical" it prints the
+// order of the hierarchically sorted LegendreShapeFunctionSet (legendre.hh:
+// 236-249) as indices into the default (non-hierarchical) set, for 1-3
+// dimensions and orders 0-4.  Built and run only by
 // oracle/make_ref_golden.sh where the dune-fem sources are present; test
 // infrastructure, never part of the product.
 //
@@ -31,6 +34,7 @@
 #include <array>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -213,10 +217,54 @@ void run_jacobian(const Case& k, const std::vector<long long>& block_cells, bool
   std::printf("]}%s\n", last ? "" : ",");
 }
 
+// perm[h] = index in the non-hierarchical set of the h-th function of the
+// hierarchical set, found by matching values at a generic point (the values
+// of the (p+1)^dim functions there are distinct; checked).
+template <int dim>
+std::vector<int> hierarchical_order(int order) {
+  typedef Dune::Fem::ScalarFunctionSpace<dim> FS;
+  Dune::Fem::LegendreShapeFunctionSet<FS, false> plain(order);
+  Dune::Fem::LegendreShapeFunctionSet<FS, true> hier(order);
+  typename FS::DomainType x;
+  const double at[3] = {0.2137, 0.6183, 0.4471};
+  for (int d = 0; d < dim; ++d) x[d] = at[d];
+  std::vector<double> vp(plain.size()), vh(hier.size());
+  plain.evaluateEach(x, [&](std::size_t i, const typename FS::RangeType& v) { vp[i] = v[0]; });
+  hier.evaluateEach(x, [&](std::size_t i, const typename FS::RangeType& v) { vh[i] = v[0]; });
+  std::vector<int> perm;
+  for (double v : vh) {
+    int found = -1, count = 0;
+    for (std::size_t i = 0; i < vp.size(); ++i)
+      if (vp[i] == v) { found = int(i); ++count; }
+    if (count != 1) { std::fprintf(stderr, "hierarchical_order: ambiguous value\n"); std::exit(1); }
+    perm.push_back(found);
+  }
+  return perm;
+}
+
+template <int dim>
+void print_orders(bool last) {
+  for (int p = 0; p <= 4; ++p) {
+    const std::vector<int> perm = hierarchical_order<dim>(p);
+    std::printf("  {\"dim\": %d, \"order\": %d, \"perm\": [", dim, p);
+    for (std::size_t i = 0; i < perm.size(); ++i) std::printf("%s%d", i ? ", " : "", perm[i]);
+    std::printf("]}%s\n", last && p == 4 ? "" : ",");
+  }
+}
+
 }  // namespace refdg
 
 int main(int argc, char** argv) {
   using refdg::Case;
+  if (argc > 1 && std::string(argv[1]) == "hierarchical") {
+    std::printf("{\"source\": \"dune-fem LegendreShapeFunctionSet<FS, true> (legendre.hh) against the default "
+                "ordering, compiled unmodified\",\n \"orders\": [\n");
+    refdg::print_orders<1>(false);
+    refdg::print_orders<2>(false);
+    refdg::print_orders<3>(true);
+    std::printf(" ]}\n");
+    return 0;
+  }
   if (argc > 1 && std::string(argv[1]) == "jacobian") {
     const Case cases[] = {
         {"q1_periodic_aniso_kappa_mass", {3, 2, 2}, {1.5, 1.0, 0.5}, {1, 1, 1}, 1, 1, true, false, 1.0, 0.7, 40.0},

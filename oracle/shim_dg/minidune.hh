@@ -252,17 +252,19 @@ class TemporaryLocalMatrix;
 template <class DomainSpace, class RangeSpace>
 class DiagonalAndNeighborStencil;
 
-// -- function space --------------------------------------------------------
-struct ScalarFunctionSpace3 {
-  static const int dimDomain = 3;
+// -- function spaces -------------------------------------------------------
+template <int dim>
+struct ScalarFunctionSpace {
+  static const int dimDomain = dim;
   static const int dimRange = 1;
   typedef double DomainFieldType;
   typedef double RangeFieldType;
-  typedef FieldVector<double, 3> DomainType;
+  typedef FieldVector<double, dim> DomainType;
   typedef FieldVector<double, 1> RangeType;
-  typedef FieldMatrix<double, 1, 3> JacobianRangeType;
-  typedef FieldVector<FieldMatrix<double, 3, 3>, 1> HessianRangeType;
+  typedef FieldMatrix<double, 1, dim> JacobianRangeType;
+  typedef FieldVector<FieldMatrix<double, dim, dim>, 1> HessianRangeType;
 };
+typedef ScalarFunctionSpace<3> ScalarFunctionSpace3;
 
 // -- grid ------------------------------------------------------------------
 struct CartesianGrid {
@@ -422,7 +424,8 @@ struct ElementPoint {
   FieldVector<double, 3> x;
 };
 inline const FieldVector<double, 3>& coordinate(const ElementPoint& p) { return p.x; }
-inline const FieldVector<double, 3>& coordinate(const FieldVector<double, 3>& x) { return x; }
+template <class K, int d>
+inline const FieldVector<K, d>& coordinate(const FieldVector<K, d>& x) { return x; }
 
 inline int gauss_points_for_order(int order) {
   static const GaussPts gp;

@@ -57,6 +57,19 @@ def _reference_hierarchical_order(order, dim):
     return sorted(range(len(idx)), key=lambda l: (max(idx[l]), idx[l]))
 
 
+def test_hierarchical_permutation_equals_the_compiled_reference_set(gb):
+    """tests/golden/ref_legendre_order.json: the order of dune-fem's own
+    LegendreShapeFunctionSet<FS, true> (legendre.hh, compiled unmodified by
+    oracle/make_ref_golden.sh) as indices into the default set, dims 1-3,
+    orders 0-4."""
+    import json
+    with open(os.path.join(os.path.dirname(__file__), "golden", "ref_legendre_order.json")) as f:
+        orders = json.load(f)["orders"]
+    assert len(orders) == 15
+    for o in orders:
+        assert list(gb.hierarchical_permutation(o["order"], o["dim"])) == o["perm"]
+
+
 @pytest.mark.parametrize("order", [0, 1, 2, 3, 4])
 @pytest.mark.parametrize("dim", [1, 2, 3])
 def test_hierarchical_permutation_matches_the_reference_sort(gb, order, dim):
