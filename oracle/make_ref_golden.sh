@@ -4,16 +4,18 @@
 # oracle/ref_driver.cpp (with the oracle's operator, oracle.cpp) into
 # oracle/_ref/, the reference's DG elliptic operator and its assembled
 # Jacobian (dgelliptic.hh over legendre.hh) with oracle/ref_dgelliptic.cpp,
-# and its explicit time loop
+# its explicit time loop
 # (timeprovider.hh, rungekutta/explicit.hh, butchertable.cc) over that
-# operator with oracle/ref_timeloop.cpp, both against the grid shim in
-# oracle/shim_dg; runs them, and writes the golden vectors
+# operator with oracle/ref_timeloop.cpp, and its Newton solver
+# (newtoninverseoperator.hh) with oracle/ref_newton.cpp, all against the grid
+# shim in oracle/shim_dg; runs them, and writes the golden vectors
 # tests/golden/ref_tables.json, ref_krylov.json, ref_krylov_sipg.json,
 # ref_dgelliptic.json, ref_dgelliptic_jacobian.json, ref_legendre_order.json
-# (the hierarchical shape-function order) and ref_timeloop.json.
+# (the hierarchical shape-function order), ref_timeloop.json and
+# ref_newton.json.
 # Needs the dune-fem source tree (located by ref_src.sh); without it this
 # recipe does nothing (the committed golden vectors stay as they are).  With
-# --compile-only it builds the driver and writes nothing.  The reference's
+# --compile-only it builds the drivers and writes nothing.  The reference's
 # own build system is not used.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -25,17 +27,30 @@ OUT="$HERE/_ref"
 GOLD="$HERE/../tests/golden"
 mkdir -p "$OUT" "$GOLD"
 CXX=${CXX:-g++}
+LEG="$REF/dune/fem/space/shapefunctionset/legendrepolynomials.cc"
+# the four drivers compile in parallel; each failure is reported
 $CXX -O2 -std=c++17 -pthread -I"$HERE/shim" -I"$REF" \
-  "$HERE/ref_driver.cpp" "$HERE/oracle.cpp" "$REF/dune/fem/space/shapefunctionset/legendrepolynomials.cc" \
-  -o "$OUT/ref_driver"
+  "$HERE/ref_driver.cpp" "$HERE/oracle.cpp" "$LEG" -o "$OUT/ref_driver" &
+P1=$!
 $CXX -O2 -std=c++17 -I"$HERE/shim_dg" -I"$HERE/shim" -I"$REF" \
-  "$HERE/ref_dgelliptic.cpp" "$REF/dune/fem/space/shapefunctionset/legendrepolynomials.cc" \
-  -o "$OUT/ref_dgelliptic"
+  "$HERE/ref_dgelliptic.cpp" "$LEG" -o "$OUT/ref_dgelliptic" &
+P2=$!
 $CXX -O2 -std=c++17 -I"$HERE/shim_dg" -I"$HERE/shim" -I"$REF" \
-  "$HERE/ref_timeloop.cpp" "$REF/dune/fem/space/shapefunctionset/legendrepolynomials.cc" \
-  "$REF/dune/fem/solver/rungekutta/butchertable.cc" -o "$OUT/ref_timeloop"
+  "$HERE/ref_timeloop.cpp" "$LEG" "$REF/dune/fem/solver/rungekutta/butchertable.cc" -o "$OUT/ref_timeloop" &
+P3=$!
+$CXX -O2 -std=c++17 -I"$HERE/shim_dg" -I"$HERE/shim" -I"$REF" \
+  "$HERE/ref_newton.cpp" "$LEG" -o "$OUT/ref_newton" &
+P4=$!
+FAIL=0
+for P in $P1 $P2 $P3 $P4; do
+  wait "$P" || FAIL=1
+done
+if [ "$FAIL" != 0 ]; then
+  echo "make_ref_golden.sh: a reference driver did not compile" >&2
+  exit 1
+fi
 if [ "$1" = "--compile-only" ]; then
-  echo "built $OUT/ref_driver $OUT/ref_dgelliptic $OUT/ref_timeloop"
+  echo "built $OUT/ref_driver $OUT/ref_dgelliptic $OUT/ref_timeloop $OUT/ref_newton"
   exit 0
 fi
 "$OUT/ref_driver" tables > "$GOLD/ref_tables.json"
@@ -45,5 +60,7 @@ fi
 "$OUT/ref_dgelliptic" jacobian > "$GOLD/ref_dgelliptic_jacobian.json"
 "$OUT/ref_dgelliptic" hierarchical > "$GOLD/ref_legendre_order.json"
 "$OUT/ref_timeloop" > "$GOLD/ref_timeloop.json"
+"$OUT/ref_newton" > "$GOLD/ref_newton.json"
 echo "wrote $GOLD/ref_tables.json $GOLD/ref_krylov.json $GOLD/ref_krylov_sipg.json $GOLD/ref_dgelliptic.json" \
-  "$GOLD/ref_dgelliptic_jacobian.json $GOLD/ref_legendre_order.json $GOLD/ref_timeloop.json"
+  "$GOLD/ref_dgelliptic_jacobian.json $GOLD/ref_legendre_order.json $GOLD/ref_timeloop.json" \
+  "$GOLD/ref_newton.json"

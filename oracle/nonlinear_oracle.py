@@ -95,7 +95,7 @@ def newton(S, jacobian_solve, rhs, w, tolerance=1e-6, max_iterations=2 ** 31 - 1
     Returns (w, info dict) with the reference's counters and failure code."""
     w = np.array(w, dtype=np.float64)
     st = {"it": 0, "lin": 0, "done": True, "delta": 0.0, "prev_eta": -1.0, "prev_res": -1.0, "lin_tol": None,
-          "halvings": 0}
+          "halvings": 0, "history": []}
 
     def failed():
         d = st["delta"]
@@ -174,7 +174,9 @@ def newton(S, jacobian_solve, rhs, w, tolerance=1e-6, max_iterations=2 ** 31 - 1
         st["done"] = ls >= 0
         update_linear_tolerance()
         st["it"] += 1
+        st["history"].append(st["delta"])
         if st["delta"] < tolerance or failed() != SUCCESS:
             break
     return w, {"iterations": st["it"], "linear_iterations": st["lin"], "residual": st["delta"],
-               "failure": failed(), "converged": failed() == SUCCESS, "line_search_halvings": st["halvings"]}
+               "failure": failed(), "converged": failed() == SUCCESS, "line_search_halvings": st["halvings"],
+               "residuals": st["history"]}

@@ -111,6 +111,15 @@ class DGFunction {
   const LegendreDGSpace& space() const { return *space_; }
   void clear() { std::fill(dofs_.begin(), dofs_.end(), 0.0); }
   void assign(const DGFunction& o) { dofs_ = o.dofs_; }
+  DGFunction& operator-=(const DGFunction& o) {
+    for (std::size_t i = 0; i < dofs_.size(); ++i) dofs_[i] -= o.dofs_[i];
+    return *this;
+  }
+  double scalarProductDofs(const DGFunction& o) const {
+    double s = 0.0;
+    for (std::size_t i = 0; i < dofs_.size(); ++i) s += dofs_[i] * o.dofs_[i];
+    return s;
+  }
   void axpy(double a, const DGFunction& x) {
     for (std::size_t i = 0; i < dofs_.size(); ++i) dofs_[i] += a * x.dofs_[i];
   }
@@ -256,6 +265,9 @@ class DenseLinearOperator {
   typedef DGFunction DomainFunctionType;
   typedef DGFunction RangeFunctionType;
   explicit DenseLinearOperator(const LegendreDGSpace& s) : space_(&s), n_(s.size()), a_(n_ * n_, 0.0) {}
+  template <class SolverParam>
+  DenseLinearOperator(const std::string&, const LegendreDGSpace& domain, const LegendreDGSpace&, const SolverParam&)
+      : DenseLinearOperator(domain) {}
   const LegendreDGSpace& domainSpace() const { return *space_; }
   const LegendreDGSpace& rangeSpace() const { return *space_; }
   template <class Stencil>

@@ -10,7 +10,8 @@
 //
 // What it provides, and the reference behaviour each piece restates:
 //  - DUNE_THROW and the exception types; DynamicVector / DynamicMatrix;
-//    a serial MPIManager; no-op persistence hooks; a numeric ParameterReader;
+//    a serial MPIManager; no-op persistence hooks; a ParameterReader over
+//    string values with getEnum, and LocalParameter;
 //    the SpaceOperatorInterface the Runge-Kutta solver calls (operator(),
 //    space(), setTime(), timeStepEstimate());
 //  - FieldVector / FieldMatrix with the dense operations the two headers call
@@ -43,6 +44,7 @@
 #include <sstream>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include <dune/fem/quadrature/gausspoints.hh>
@@ -161,13 +163,21 @@ class FieldMatrix {
 
 namespace Fem {
 
-// parameters (dune/fem/io/parameter.hh): numeric values by key
+// parameters (dune/fem/io/parameter.hh): string values by key, converted on
+// read; getEnum returns the position of the value in a table of names
 class ParameterReader {
  public:
+  bool exists(const std::string& key) const { return values_.count(key) != 0; }
   template <class T>
   T getValue(const std::string& key, const T& fallback) const {
     auto it = values_.find(key);
-    return it == values_.end() ? fallback : T(it->second);
+    return it == values_.end() ? fallback : convert<T>(it->second);
+  }
+  template <class T>
+  T getValue(const std::string& key) const {
+    auto it = values_.find(key);
+    if (it == values_.end()) throw std::invalid_argument("missing parameter " + key);
+    return convert<T>(it->second);
   }
   template <class T, class Validator>
   T getValidValue(const std::string& key, const T& fallback, const Validator& valid) const {
@@ -177,19 +187,57 @@ class ParameterReader {
   }
   template <class T, class Validator>
   T getValidValue(const std::string& key, const Validator& valid) const {
-    auto it = values_.find(key);
-    if (it == values_.end()) throw std::invalid_argument("missing parameter " + key);
-    const T v = T(it->second);
+    const T v = getValue<T>(key);
     if (!valid(v)) throw std::invalid_argument("invalid value for parameter " + key);
     return v;
   }
-  void set(const std::string& key, double v) { values_[key] = v; }
+  template <class Names>
+  int getEnum(const std::string& key, const Names& names, int fallback) const {
+    auto it = values_.find(key);
+    if (it == values_.end()) return fallback;
+    for (std::size_t i = 0; i < names.size(); ++i)
+      if (names[i] == it->second) return int(i);
+    throw std::invalid_argument("parameter " + key + ": unknown value " + it->second);
+  }
+  void set(const std::string& key, double v) {
+    std::ostringstream os;
+    os.precision(17);
+    os << v;
+    values_[key] = os.str();
+  }
+  void set(const std::string& key, const std::string& v) { values_[key] = v; }
 
  private:
-  std::map<std::string, double> values_;
+  template <class T>
+  static T convert(const std::string& s) {
+    if (std::is_same<T, bool>::value) return T(s == "true" || s == "1");
+    std::istringstream is(s);
+    double v = 0;
+    is >> v;
+    return T(v);
+  }
+  std::map<std::string, std::string> values_;
 };
 struct Parameter {
+  static const int solverStatistics = 1;
+  static const int extendedStatistics = 2;
   static ParameterReader& container() { static ParameterReader r; return r; }
+  static void append(const std::string& key, const std::string& value, bool = false) { container().set(key, value); }
+  static bool verbose(int = 0) { return false; }
+};
+
+// parameter classes with a clone() (dune/fem/io/parameter.hh: LocalParameter)
+template <class ParamDefault, class ParamImpl>
+struct LocalParameter : public ParamDefault {
+  virtual ~LocalParameter() {}
+  virtual ParamDefault* clone() const { return new ParamImpl(static_cast<const ParamImpl&>(*this)); }
+  template <class... Args>
+  LocalParameter(Args... args) : ParamDefault(args...) {}
+};
+template <class ParamDefault>
+struct LocalParameter<ParamDefault, ParamDefault> {
+  virtual ~LocalParameter() {}
+  virtual ParamDefault* clone() const { return new ParamDefault(static_cast<const ParamDefault&>(*this)); }
 };
 
 // a serial run (dune/fem/misc/mpimanager.hh)
@@ -238,13 +286,20 @@ struct SpaceOperatorInterface {
 //    differentiableoperator.hh:54) ------------------------------------------
 template <class DomainFunction, class RangeFunction = DomainFunction>
 struct Operator {
+  typedef DomainFunction DomainFunctionType;
+  typedef RangeFunction RangeFunctionType;
+  typedef double DomainFieldType;
+  typedef double RangeFieldType;
   virtual ~Operator() {}
   virtual void operator()(const DomainFunction& u, RangeFunction& w) const = 0;
+  virtual bool nonlinear() const { return true; }
 };
 template <class JacobianOperator>
 struct DifferentiableOperator
     : public virtual Operator<typename JacobianOperator::DomainFunctionType,
-                              typename JacobianOperator::RangeFunctionType> {};
+                              typename JacobianOperator::RangeFunctionType> {
+  virtual void jacobian(const typename JacobianOperator::DomainFunctionType& u, JacobianOperator& jOp) const = 0;
+};
 
 // defined in dgspace.hh
 template <class DomainSpace, class RangeSpace>
