@@ -4,7 +4,8 @@
 // (dgelliptic.hh) with a nonlinear source and its Jacobian comes from
 // DifferentiableDGEllipticOperator::jacobian, on the shim grid of
 // oracle/shim_dg; prints, per case, the residual norm after every Newton
-// step, the iteration counts and the solution as JSON golden vectors.
+// step, the tolerance set for every linear solve, the iteration counts and
+// the solution as JSON golden vectors.
 // The linear inverse operator is an exact dense LU solve of our own (one
 // "linear iteration" per Newton step), so the golden vectors record the
 // Newton loop itself.  Built and run only by oracle/make_ref_golden.sh
@@ -82,7 +83,9 @@ struct ReactionDiffusionModel {
 };
 
 // The linear inverse operator handed to the Newton solver: an exact solve of
-// the dense Jacobian by Gaussian elimination with partial pivoting.
+// the dense Jacobian by Gaussian elimination with partial pivoting.  It
+// records the tolerance the Newton loop set for each solve (the
+// Eisenstat-Walker forcing terms, when that forcing is on).
 class DenseLUInverse {
  public:
   typedef Dune::Fem::SolverParameter SolverParameterType;
@@ -92,7 +95,9 @@ class DenseLUInverse {
   void setMaxIterations(int) {}
   int iterations() const { return iterations_; }
   SolverParameterType& parameter() const { return param_; }
+  const std::vector<double>& tolerances() const { return tolerances_; }
   void operator()(const DGFunction& f, DGFunction& x) const {
+    tolerances_.push_back(param_.tolerance());
     const std::size_t n = op_->size();
     std::vector<double> a(n * n), b(f.dofs());
     for (std::size_t i = 0; i < n; ++i)
@@ -123,10 +128,18 @@ class DenseLUInverse {
   const DenseLinearOperator* op_ = nullptr;
   mutable SolverParameterType param_;
   mutable int iterations_ = 0;
+  mutable std::vector<double> tolerances_;
 };
 
 typedef DifferentiableDGEllipticOperator<DenseLinearOperator, ReactionDiffusionModel> SOp;
-typedef Dune::Fem::NewtonInverseOperator<DenseLinearOperator, DenseLUInverse> Newton;
+// NewtonInverseOperator keeps its linear inverse operator protected; this
+// derived class only reads the tolerances it recorded.
+class Newton : public Dune::Fem::NewtonInverseOperator<DenseLinearOperator, DenseLUInverse> {
+ public:
+  using Dune::Fem::NewtonInverseOperator<DenseLinearOperator, DenseLUInverse>::NewtonInverseOperator;
+  const std::vector<double>& linearTolerances() const { return jInv_.tolerances(); }
+};
+inline const std::vector<double>& newton_linear_tolerances(const Newton& n) { return n.linearTolerances(); }
 
 struct Case {
   const char* name;
@@ -138,6 +151,7 @@ struct Case {
   double rhs_scale;     // f[i] = rhs_scale * ((i * 7919 + 13) % 2003 - 1001) / 1000
   double w0_constant;   // initial guess: this constant (the first Legendre mode of every cell)
   const char* line_search;
+  const char* forcing;
   double tolerance;
 };
 
@@ -163,6 +177,7 @@ void run(const Case& k, bool last) {
   Dune::Fem::ParameterReader params;
   params.set("penalty", k.penalty);
   params.set("fem.solver.nonlinear.linesearch", std::string(k.line_search));
+  params.set("fem.solver.nonlinear.forcing", std::string(k.forcing));
   SOp op(space, model, params);
 
   DGFunction r0(space);
@@ -183,13 +198,16 @@ void run(const Case& k, bool last) {
   std::printf("  {\"name\": \"%s\", \"cells\": [%d, %d, %d], \"periodic\": [%d, %d, %d], \"order\": %d, "
               "\"quad_points\": %d, \"kappa_field\": %s, \"diffusion\": %.17g, \"penalty\": %.17g, "
               "\"reaction\": [%.17g, %.17g, %.17g], \"rhs_scale\": %.17g, \"w0_constant\": %.17g, "
-              "\"line_search\": \"%s\", \"tolerance\": %.17g,\n   \"converged\": %s, \"iterations\": %d, "
+              "\"line_search\": \"%s\", \"forcing\": \"%s\", \"tolerance\": %.17g,\n   \"converged\": %s, \"iterations\": %d, "
               "\"linear_iterations\": %d, \"initial_residual\": %.17g, \"residuals\": [",
               k.name, k.cells[0], k.cells[1], k.cells[2], k.periodic[0], k.periodic[1], k.periodic[2], k.order,
               Dune::Fem::gauss_points_for_order(2 * k.order), k.kappa_field ? "true" : "false", k.diffusion,
-              k.penalty, k.c1, k.c3, k.ce, k.rhs_scale, k.w0_constant, k.line_search, k.tolerance,
+              k.penalty, k.c1, k.c3, k.ce, k.rhs_scale, k.w0_constant, k.line_search, k.forcing, k.tolerance,
               newton.converged() ? "true" : "false", newton.iterations(), newton.linearIterations(), delta0);
   for (std::size_t i = 0; i < residuals.size(); ++i) std::printf("%s%.17g", i ? ", " : "", residuals[i]);
+  std::printf("],\n   \"linear_tolerances\": [");
+  const std::vector<double>& tols = newton_linear_tolerances(newton);
+  for (std::size_t i = 0; i < tols.size(); ++i) std::printf("%s%.17g", i ? ", " : "", tols[i]);
   std::printf("],\n   \"w\": [");
   for (std::size_t i = 0; i < w.dofs().size(); ++i) std::printf("%s%.17g", i ? ", " : "", w.dofs()[i]);
   std::printf("]}%s\n", last ? "" : ",");
@@ -200,11 +218,15 @@ void run(const Case& k, bool last) {
 int main() {
   using refnt::Case;
   const Case cases[] = {
-      {"cubic_periodic_kappa", {3, 2, 2}, {1, 1, 1}, 2, true, 1.0, 90.0, 0.5, 2.0, 0.0, 10.0, 0.0, "none", 1e-10},
-      {"exp_periodic", {3, 3, 3}, {1, 1, 1}, 1, false, 1.0, 40.0, 1.0, 0.0, 0.3, 0.5, 0.0, "none", 1e-10},
-      {"allen_cahn_plain", {2, 2, 2}, {0, 0, 0}, 1, false, 1e-3, 40.0, -1.0, 1.0, 0.0, 0.0, 0.58, "none", 1e-10},
-      {"allen_cahn_line_search", {2, 2, 2}, {0, 0, 0}, 1, false, 1e-3, 40.0, -1.0, 1.0, 0.0, 0.0, 0.58, "simple",
+      {"cubic_periodic_kappa", {3, 2, 2}, {1, 1, 1}, 2, true, 1.0, 90.0, 0.5, 2.0, 0.0, 10.0, 0.0, "none", "none",
        1e-10},
+      {"cubic_periodic_kappa_eisenstat_walker", {3, 2, 2}, {1, 1, 1}, 2, true, 1.0, 90.0, 0.5, 2.0, 0.0, 10.0, 0.0,
+       "none", "eisenstatwalker", 1e-10},
+      {"exp_periodic", {3, 3, 3}, {1, 1, 1}, 1, false, 1.0, 40.0, 1.0, 0.0, 0.3, 0.5, 0.0, "none", "none", 1e-10},
+      {"allen_cahn_plain", {2, 2, 2}, {0, 0, 0}, 1, false, 1e-3, 40.0, -1.0, 1.0, 0.0, 0.0, 0.58, "none", "none",
+       1e-10},
+      {"allen_cahn_line_search", {2, 2, 2}, {0, 0, 0}, 1, false, 1e-3, 40.0, -1.0, 1.0, 0.0, 0.0, 0.58, "simple",
+       "none", 1e-10},
   };
   const int n = int(sizeof(cases) / sizeof(cases[0]));
   std::printf("{\"source\": \"dune-fem NewtonInverseOperator (dune/fem/solver/newtoninverseoperator.hh) over "

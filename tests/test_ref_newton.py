@@ -7,8 +7,10 @@ S the reference's DGEllipticOperator with the source r(u) = c1 u + c3 u^3 +
 ce exp(u) and its Jacobian from DifferentiableDGEllipticOperator::jacobian,
 each Newton step solved exactly (dense LU).  The golden vectors hold the
 residual norm after every step, the step counts and the solution, for a
-cubic reaction with a kappa field, an exponential one, and an Allen-Cahn
-problem started near its inflection point without and with the line search.
+cubic reaction with a kappa field (also with the Eisenstat-Walker forcing,
+whose linear tolerances the golden vectors record), an exponential one, and
+an Allen-Cahn problem started near its inflection point without and with the
+line search.
 """
 import json
 import os
@@ -48,7 +50,8 @@ def operator_kw(case):
 
 
 def test_golden_cases():
-    assert set(CASES) == {"cubic_periodic_kappa", "exp_periodic", "allen_cahn_plain", "allen_cahn_line_search"}
+    assert set(CASES) == {"cubic_periodic_kappa", "cubic_periodic_kappa_eisenstat_walker", "exp_periodic",
+                          "allen_cahn_plain", "allen_cahn_line_search"}
     assert all(c["converged"] for c in CASES.values())
     # the line search shortens the Allen-Cahn solve
     assert CASES["allen_cahn_line_search"]["iterations"] < CASES["allen_cahn_plain"]["iterations"]
@@ -78,18 +81,32 @@ def test_oracle_newton_equals_reference(orc, name):
             J[z * nl:(z + 1) * nl, z * nl:(z + 1) * nl] += blocks[z]
         return J
 
-    w, info = no.newton(S, lambda w, r, tol: (np.linalg.solve(jacobian(w), r), 1), f, w0,
-                        tolerance=case["tolerance"], line_search=case["line_search"] == "simple")
+    forcing = case["forcing"] == "eisenstatwalker"
+    tolerances = []
+
+    def solve(w, r, tol):
+        tolerances.append(tol)
+        return np.linalg.solve(jacobian(w), r), 1
+
+    w, info = no.newton(S, solve, f, w0, tolerance=case["tolerance"], line_search=case["line_search"] == "simple",
+                        forcing=forcing)
     assert info["converged"]
     assert info["iterations"] == case["iterations"] and info["linear_iterations"] == case["linear_iterations"]
     scale = max(case["initial_residual"], float(np.linalg.norm(f)))
     for got, ref in zip(info["residuals"], case["residuals"]):
         assert abs(got - ref) <= 1e-9 * ref + 1e-13 * scale
     assert relmax(w, case["w"]) < 1e-12
+    if forcing:
+        # the forcing terms follow the residuals; the last ones are taken from
+        # residuals at the rounding floor
+        assert len(tolerances) == len(case["linear_tolerances"])
+        for k, (got, ref) in enumerate(zip(tolerances, case["linear_tolerances"])):
+            if k == 0 or case["residuals"][k - 1] > 1e3 * case["tolerance"]:
+                assert abs(got - ref) <= 1e-9 * ref
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("name", sorted(n for n, c in CASES.items() if c["forcing"] == "none"))
 def test_gpu_newton_equals_reference(gb, name):
     """NewtonInverseOperator over NonlinearDGOperator on the GPU: the same
     number of Newton steps and the same solution as the reference's Newton.
