@@ -329,6 +329,11 @@ class FormOperator(gbfem.Operator):
 
     def __init__(self, form, cells, order, quad_points=0, precision=gbfem.F64, penalty=None, periodic=(0, 0, 0),
                  lower=(0.0, 0.0, 0.0), upper=(1.0, 1.0, 1.0)):
+        if getattr(form, "unit_penalty", False):
+            # a UFL form with FacetSize() reads h_F as 1 / sigma
+            if penalty not in (None, 1.0):
+                raise ValueError("FormOperator: this form uses the facet size; its penalty is fixed at 1")
+            penalty = 1.0
         q = quad_points or order + 2
         self.cubin = form.compile(precision, order, q)
         d = gbfem.DgDesc()

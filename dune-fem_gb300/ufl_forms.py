@@ -22,10 +22,23 @@ grad(u)[m, k], the spatial coordinate x[k], numbers and Constant, + - * /
 and ** (numeric or integer exponents), exp, log, sqrt, sin, cos, tan, tanh,
 sinh, cosh, atan, abs, max_value / min_value, conditional(cond, a, b) with
 lt / gt / le / ge, inner / dot over component lists, and the facet normal
-n[k] in a wave speed.  The form must be
-linear in the test function v, with every term integrated over dx.
-Interior facet (dS) and boundary (ds) measures, jump and avg are not
-supported: the face terms are generated.
+n[k] in a wave speed.  The form must be linear in the test function v.
+
+A form of dx terms alone gets its face terms generated (above).  A form
+with facet integrals gives them itself, as UFL does
+(python/dune/models/integrands/ufl.py lowers the same three integrals):
+  - over interior facets, `* dS`, with restrictions e('+') / e('-') of
+    u, grad u, v, grad v and the normal (n('+') is the outward normal of
+    the '+' cell, n('-') = -n('+')), jump(e) = e('+') - e('-'),
+    jump(e, n) = e('+') n('+') + e('-') n('-') and avg(e);
+  - over boundary facets, `* ds`, with u, grad u, v, grad v and n;
+  - FacetSize(): avg(CellVolume) / FacetArea on interior facets and
+    CellVolume / FacetArea on boundary facets (the cell width normal to the
+    face on these grids).
+A dS integrand must not change when '+' and '-' are exchanged (as on any
+mesh, where the choice is arbitrary): each cell takes the v('+') part with
+itself as '+'.  Such a form is lowered to the raw interior / skeleton /
+boundary bodies of integrands.Form; periodic faces are interior facets.
 """
 import numbers
 
@@ -85,6 +98,22 @@ class Expr:
     def __ge__(self, o):
         return Cond(">=", self, _wrap(o))
 
+    def __call__(self, side):
+        """The restriction e('+') or e('-') to one side of an interior facet."""
+        return self.restrict(_side(side))
+
+    def restrict(self, side):
+        return self
+
+    def leaves(self):
+        return []
+
+
+def _side(side):
+    if side not in ("+", "-"):
+        raise ValueError("ufl: restrict with '+' or '-'")
+    return side
+
 
 class Num(Expr):
     def __init__(self, v):
@@ -109,12 +138,31 @@ class Leaf(Expr):
     def cpp(self):
         return self.text
 
+    def restrict(self, side):
+        t = self.text
+        if t.startswith("u[") or t.startswith("g["):
+            return Leaf(t[0] + ("L" if side == "+" else "R") + t[1:])
+        if t.startswith("uL[") or t.startswith("uR[") or t.startswith("gL[") or t.startswith("gR["):
+            raise ValueError("ufl: %s is restricted already" % t)
+        if t.startswith("n[") and side == "-":
+            return Op("-", (self,))
+        return self  # x[k], the facet size
+
+    def leaves(self):
+        return [self.text]
+
 
 class Op(Expr):
     _FN = {"exp", "log", "sqrt", "sin", "cos", "tan", "tanh", "sinh", "cosh", "atan", "fabs", "pow", "max", "min"}
 
     def __init__(self, op, args):
         self.op, self.args = op, args
+
+    def restrict(self, side):
+        return Op(self.op, tuple(a.restrict(side) for a in self.args))
+
+    def leaves(self):
+        return [t for a in self.args for t in a.leaves()]
 
     def cpp(self):
         a = [x.cpp() for x in self.args]
@@ -135,6 +183,12 @@ class Cond(Expr):
     def __init__(self, op, a, b):
         self.op, self.a, self.b = op, a, b
 
+    def restrict(self, side):
+        return Cond(self.op, self.a.restrict(side), self.b.restrict(side))
+
+    def leaves(self):
+        return self.a.leaves() + self.b.leaves()
+
     def cpp(self):
         return "(%s %s %s)" % (self.a.cpp(), self.op, self.b.cpp())
 
@@ -142,6 +196,12 @@ class Cond(Expr):
 class Conditional(Expr):
     def __init__(self, c, a, b):
         self.c, self.a, self.b = c, a, b
+
+    def restrict(self, side):
+        return Conditional(self.c.restrict(side), self.a.restrict(side), self.b.restrict(side))
+
+    def leaves(self):
+        return self.c.leaves() + self.a.leaves() + self.b.leaves()
 
     def cpp(self):
         return "(%s ? D(%s) : D(%s))" % (self.c.cpp(), self.a.cpp(), self.b.cpp())
@@ -235,6 +295,9 @@ class Vector:
     def __neg__(self):
         return Vector([-a for a in self.items])
 
+    def __call__(self, side):
+        return Vector([e(side) for e in self.items])
+
 
 def as_vector(items):
     return Vector([_wrap(e) if not isinstance(e, VLinear) else e for e in items])
@@ -264,6 +327,8 @@ class VLinear:
         return self._scale(1.0 / _wrap(s) if not isinstance(s, numbers.Real) else 1.0 / s)
 
     def __add__(self, o):
+        if isinstance(o, Integrals):
+            return Integrals(dx=self) + o
         if not isinstance(o, VLinear):
             raise ValueError("ufl: a sum of terms linear and not linear in the test function")
         t = dict(self.terms)
@@ -272,10 +337,24 @@ class VLinear:
         return VLinear(t)
 
     def __sub__(self, o):
+        if isinstance(o, Integrals):
+            return Integrals(dx=self) - o
         return self + (-1.0) * o
 
     def __neg__(self):
         return self._scale(-1.0)
+
+    def __call__(self, side):
+        side = _side(side)
+        out = {}
+        for key, c in self.terms.items():
+            if len(key[0]) > 1:
+                raise ValueError("ufl: the test function is restricted already")
+            out[(key[0] + side,) + key[1:]] = c.restrict(side)
+        return VLinear(out)
+
+    def restricted(self):
+        return any(len(k[0]) > 1 for k in self.terms)
 
 
 class TestFunction:
@@ -344,11 +423,80 @@ class Measure:
         self.name = name
 
     def __rmul__(self, integrand):
-        if self.name != "dx":
-            raise NotImplementedError("ufl: only dx; the face terms are generated (interior penalty)")
         if not isinstance(integrand, VLinear):
             raise ValueError("ufl: the integrand must be linear in the test function")
-        return integrand
+        leaves = [t for c in integrand.terms.values() for t in c.leaves()]
+        restricted = [t for t in leaves if t[:2] in ("uL", "uR", "gL", "gR")]
+        facet = [t for t in leaves if t.startswith("n[") or t == _FACET_SIZE]
+        if self.name == "dx":
+            if integrand.restricted() or restricted or facet:
+                raise ValueError("ufl: restrictions, normals and facet sizes belong to dS / ds terms")
+            return integrand
+        if self.name == "dS":
+            unrestricted = [t for t in leaves if t[:2] in ("u[", "g[")]
+            if unrestricted or not integrand.restricted() or any(len(k[0]) == 1 for k in integrand.terms):
+                raise ValueError("ufl: restrict u, grad u and v with ('+') / ('-') in dS terms")
+            return Integrals(dS=integrand)
+        if integrand.restricted() or restricted:
+            raise ValueError("ufl: no restrictions in ds terms")
+        return Integrals(ds=integrand)
+
+
+class Integrals:
+    """A form with facet integrals: its dx, dS and ds integrands."""
+
+    def __init__(self, dx=None, dS=None, ds=None):
+        self.parts = {"dx": dx or VLinear(), "dS": dS or VLinear(), "ds": ds or VLinear()}
+
+    @staticmethod
+    def of(a):
+        if isinstance(a, Integrals):
+            return a
+        if isinstance(a, VLinear):
+            return Integrals(dx=a)
+        raise ValueError("ufl: add forms (integrands times a measure)")
+
+    def __add__(self, o):
+        o = Integrals.of(o)
+        return Integrals(**{k: self.parts[k] + o.parts[k] for k in self.parts})
+
+    __radd__ = __add__
+
+    def __sub__(self, o):
+        o = Integrals.of(o)
+        return Integrals(**{k: self.parts[k] - o.parts[k] for k in self.parts})
+
+    def __rsub__(self, o):
+        return Integrals.of(o) - self
+
+    def __neg__(self):
+        return Integrals(**{k: -p for k, p in self.parts.items()})
+
+
+_FACET_SIZE = "(1.0 / sigma)"
+
+
+def FacetSize():
+    """avg(CellVolume)/FacetArea on interior facets, CellVolume/FacetArea on
+    boundary facets: the cell width normal to the face.  The form kernels
+    pass sigma = penalty / h_F to the face terms; a form that uses the facet
+    size runs with penalty 1 (FormOperator sets it), so h_F = 1 / sigma."""
+    return Leaf(_FACET_SIZE)
+
+
+def jump(e, n=None):
+    """e('+') - e('-'), or e('+') n('+') + e('-') n('-') with a normal."""
+    if n is None:
+        return e("+") - e("-")
+    if not isinstance(n, FacetNormal):
+        raise TypeError("ufl: jump(e, n) takes the FacetNormal")
+    np_, nm = n("+"), n("-")
+    return Vector([e("+") * np_[k] + e("-") * nm[k] for k in range(3)])
+
+
+def avg(e):
+    """(e('+') + e('-')) / 2."""
+    return 0.5 * (e("+") + e("-"))
 
 
 dx = Measure("dx")
@@ -356,14 +504,46 @@ ds = Measure("ds")
 dS = Measure("dS")
 
 
+def _body(v, side=""):
+    """Statements assigning s[m] and F[m][k] from the coefficients of v_m and
+    dv_m/dx_k (of the restriction `side` of v, if given)."""
+    out = []
+    for key, c in sorted(v.terms.items(), key=lambda kv: repr(kv[0])):
+        kind = key[0]
+        if kind == "g" + side:
+            out.append("F[%d][%d] = F[%d][%d] + D(%s);" % (key[1], key[2], key[1], key[2], c.cpp()))
+        elif kind == "v" + side:
+            out.append("s[%d] = s[%d] + D(%s);" % (key[1], key[1], c.cpp()))
+    return "\n".join(out)
+
+
 def to_form(a, components=1, advection=None, wavespeed=None, dirichlet=None, symmetry=1):
-    """integrands.Form of the dx form `a` (linear in the test function):
-    flux F[m][k] = coefficient of dv_m/dx_k, source s[m] = coefficient of
-    v_m.  advection: per component a list of three expressions (Fa[m][k]),
-    wavespeed: an expression (may use n[k]), dirichlet: one expression of x
-    per component (None: natural boundary)."""
+    """integrands.Form of the form `a` (linear in the test function).
+
+    dx terms alone: flux F[m][k] = coefficient of dv_m/dx_k, source s[m] =
+    coefficient of v_m, with the face terms generated; advection: per
+    component a list of three expressions (Fa[m][k]), wavespeed: an
+    expression (may use n[k]), dirichlet: one expression of x per component
+    (None: natural boundary).
+
+    With dS / ds terms: the raw interior, skeleton and boundary bodies of
+    the three integrals (the skeleton from the v('+') part, the cell itself
+    being '+'); advection, wavespeed and dirichlet are then part of the
+    integrals and not given here."""
+    if isinstance(a, Integrals):
+        if not (a.parts["dS"].terms or a.parts["ds"].terms):
+            a = a.parts["dx"]
+        else:
+            if advection is not None or wavespeed is not None or dirichlet is not None or symmetry != 1:
+                raise ValueError("ufl: with facet integrals give the face terms in the form itself")
+            interior = _body(a.parts["dx"])
+            skeleton = _body(a.parts["dS"], "+")
+            boundary = _body(a.parts["ds"])
+            form = integrands.Form(components=components, interior=interior, skeleton=skeleton, boundary=boundary)
+            form.unit_penalty = _FACET_SIZE in skeleton or _FACET_SIZE in boundary
+            return form
     if not isinstance(a, VLinear):
-        raise ValueError("ufl: a must be a form (an integrand linear in v times dx)")
+        raise ValueError("ufl: a must be a form (an integrand linear in v times a measure)")
     flux, source = [], []
     for key, c in sorted(a.terms.items(), key=lambda kv: repr(kv[0])):
         if key[0] == "g":
@@ -383,7 +563,15 @@ def to_form(a, components=1, advection=None, wavespeed=None, dirichlet=None, sym
 
 
 class FacetNormal:
-    """n[k] of the face, for the wave speed of a convective flux."""
+    """n[k], the outward normal of the face, for the wave speed of a
+    convective flux and in ds terms; n('+') / n('-') as vectors in dS
+    terms."""
 
     def __getitem__(self, k):
         return Leaf("n[%d]" % k)
+
+    def __call__(self, side):
+        return Vector([Leaf("n[%d]" % k).restrict(_side(side)) for k in range(3)])
+
+    def vector(self):
+        return Vector([Leaf("n[%d]" % k) for k in range(3)])

@@ -380,8 +380,8 @@ def test_ufl_front_end_lowers_and_compiles(gb):
     u, v = U.TrialFunction(1), U.TestFunction(1)
     with pytest.raises(ValueError):
         (v[0] * v[0]) * U.dx  # not linear in v
-    with pytest.raises(NotImplementedError):
-        (u[0] * v[0]) * U.ds
+    with pytest.raises(ValueError):
+        (u[0] * v[0]) * U.dS  # facet integrals need restrictions (tests/test_ufl_faces.py)
     with pytest.raises(TypeError):
         U.grad(3.0)
     if shutil.which("nvcc") is None and not __import__("os").path.exists("/usr/local/cuda/bin/nvcc"):

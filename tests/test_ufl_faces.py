@@ -1,0 +1,179 @@
+"""Facet integrals in the UFL-shaped front end (dune-fem_gb300/ufl_forms.py).
+
+The reference's advection-diffusion demo writes its SIPG / upwind form in
+UFL with interior-facet (dS) and boundary (ds) terms
+(pydemo/advectiondiffusion.py:33-55).  The same form written with this
+package's UFL notation -- restrictions, jump, avg, the facet normal and the
+facet size -- is lowered to the raw interior / skeleton / boundary bodies of
+integrands.Form.  On the CPU the lowered integrands, evaluated by a small
+tree walker here, go through the form oracle and must reproduce the DG
+oracle's operator (itself pinned to dune-fem's DGEllipticOperator); on the
+GPU the compiled form must equal DGOperator.
+"""
+import numpy as np
+import pytest
+
+from conftest import relmax
+
+EPS, MASS, VEL = 0.7, 0.4, (1.0, 0.5, 0.25)
+
+
+def demo_form(order, eps=EPS, c=MASS, b=VEL):
+    """SIPG + upwind + mass with weak homogeneous Dirichlet data, in the
+    demo's shape: penalty beta / h with h = avg(CellVolume) / FacetArea."""
+    import ufl_forms as U
+    u, v, x, n = U.TrialFunction(1), U.TestFunction(1), U.SpatialCoordinate(), U.FacetNormal()
+    h = U.FacetSize()
+    beta = 10.0 * (order + 1) ** 2
+    bv = U.as_vector(list(b))
+    gu, gv = U.grad(u)[0, :], U.grad(v)[0, :]
+    bn = U.inner(bv, n.vector())
+    hatb = (bn + abs(bn)) / 2.0
+    a = (eps * U.inner(gu, gv) - u[0] * U.inner(bv, gv) + c * u[0] * v[0]) * U.dx
+    a = a + (eps * beta / h * U.jump(u[0]) * U.jump(v[0])
+             - eps * U.inner(U.avg(gu), n("+")) * U.jump(v[0])
+             - eps * U.jump(u[0]) * U.inner(U.avg(gv), n("+"))) * U.dS
+    a = a + U.jump(hatb * u[0]) * U.jump(v[0]) * U.dS
+    a = a + (eps * beta / h * u[0] * v[0] - eps * U.inner(gu, n.vector()) * v[0]
+             - eps * u[0] * U.inner(gv, n.vector())) * U.ds
+    a = a + hatb * u[0] * v[0] * U.ds
+    return a
+
+
+# ---- a numpy evaluation of the lowered expression trees ------------------------------
+
+def _ev(e, env):
+    import ufl_forms as U
+    if isinstance(e, U.Num):
+        return e.v
+    if isinstance(e, U.Leaf):
+        return env[e.text]
+    if isinstance(e, U.Op):
+        a = [_ev(t, env) for t in e.args]
+        if e.op in "+-*/" and len(a) == 2:
+            return {"+": np.add, "-": np.subtract, "*": np.multiply, "/": np.divide}[e.op](a[0], a[1])
+        if e.op == "-":
+            return -a[0]
+        if e.op.startswith("ipow"):
+            return a[0] ** int(e.op[4:])
+        return {"fabs": np.abs, "max": np.maximum, "min": np.minimum, "pow": np.power}.get(
+            e.op, getattr(np, e.op, None))(*a)
+    if isinstance(e, U.Cond):
+        return {"<": np.less, ">": np.greater, "<=": np.less_equal, ">=": np.greater_equal}[e.op](
+            _ev(e.a, env), _ev(e.b, env))
+    if isinstance(e, U.Conditional):
+        return np.where(_ev(e.c, env), _ev(e.a, env), _ev(e.b, env))
+    raise TypeError(e)
+
+
+def _integrand(part, side, M, env_of):
+    def f(*args):
+        env, P = env_of(*args)
+        s, F = np.zeros((P, M)), np.zeros((P, M, 3))
+        for key, c in part.terms.items():
+            val = np.broadcast_to(_ev(c, env), (P,))
+            if key[0] == "v" + side:
+                s[:, key[1]] += val
+            elif key[0] == "g" + side:
+                F[:, key[1], key[2]] += val
+        return s, F
+    return f
+
+
+def _fields(prefix, u, g):
+    env = {}
+    for m in range(u.shape[1]):
+        env["%s[%d]" % (prefix, m)] = u[:, m]
+        for k in range(3):
+            env["%s[%d][%d]" % ("g" + prefix[1:], m, k)] = g[:, m, k]
+    return env
+
+
+def oracle_callables(a, M=1):
+    def interior_env(x, u, g):
+        env = {"x[%d]" % k: x[:, k] for k in range(3)}
+        env.update(_fields("u", u, g))
+        return env, x.shape[0]
+
+    def skeleton_env(x, n, sigma, uL, gL, uR, gR):
+        env = {"x[%d]" % k: x[:, k] for k in range(3)}
+        env.update({"n[%d]" % k: n[k] for k in range(3)})
+        env["(1.0 / sigma)"] = 1.0 / sigma
+        env.update(_fields("uL", uL, gL))
+        env.update(_fields("uR", uR, gR))
+        return env, x.shape[0]
+
+    def boundary_env(x, n, sigma, u, g):
+        env = {"x[%d]" % k: x[:, k] for k in range(3)}
+        env.update({"n[%d]" % k: n[k] for k in range(3)})
+        env["(1.0 / sigma)"] = 1.0 / sigma
+        env.update(_fields("u", u, g))
+        return env, x.shape[0]
+
+    p = a.parts
+    return (_integrand(p["dx"], "", M, interior_env), _integrand(p["dS"], "+", M, skeleton_env),
+            _integrand(p["ds"], "", M, boundary_env))
+
+
+# ---- CPU ----------------------------------------------------------------------------------
+
+
+@pytest.mark.parametrize("order,periodic", [(1, (0, 0, 0)), (2, (1, 0, 1)), (3, (0, 1, 0))])
+def test_demo_form_in_ufl_equals_the_dg_oracle(orc, order, periodic):
+    import form_oracle as fo
+    cells = (3, 2, 2)
+    lo, up = (0.1, -0.5, 0.0), (1.3, 0.5, 0.8)
+    a = demo_form(order)
+    I, S, B = oracle_callables(a)
+    spec = fo.FormSpec(cells, order, 1, I, S, B, penalty=1.0, periodic=periodic, lower=lo, upper=up)
+    prob = orc.DGProblem(cells, order, diffusion=EPS, mass=MASS, velocity=VEL, weak_dirichlet=True,
+                         periodic=periodic, lower=lo, upper=up)
+    u = np.random.default_rng(order).uniform(-1, 1, prob.ndofs)
+    assert relmax(fo.residual(spec, u), prob.apply(u)) < 1e-13
+
+
+def test_lowering_and_errors(gb, tmp_path):
+    import integrands
+    import ufl_forms as U
+    form = U.to_form(demo_form(2))
+    assert form.raw and form.unit_penalty
+    assert "uR[0]" in form.pieces["skeleton"] and "(1.0 / sigma)" in form.pieces["boundary"]
+    assert "uL" not in form.pieces["interior"]
+    assert form.compile(gb.F64, 2, cache_dir=str(tmp_path)).endswith(".cubin")
+    u, v, n = U.TrialFunction(1), U.TestFunction(1), U.FacetNormal()
+    with pytest.raises(ValueError):
+        (u[0] * v[0]) * U.dS  # unrestricted in dS
+    with pytest.raises(ValueError):
+        (u[0]("+") * v[0]) * U.dS  # unrestricted test function in dS
+    with pytest.raises(ValueError):
+        (u[0]("+") * v[0]) * U.ds  # restriction in ds
+    with pytest.raises(ValueError):
+        (u[0] * v[0] * n[0]) * U.dx  # normal in dx
+    with pytest.raises(ValueError):
+        u[0]("+")("-")
+    with pytest.raises(ValueError):
+        U.to_form(demo_form(1), dirichlet=[0.0])  # face terms are in the form
+    with pytest.raises(ValueError):
+        integrands.FormOperator(form, (2, 2, 2), 2, penalty=90.0)
+
+
+# ---- GPU ----------------------------------------------------------------------------------
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order,periodic", [(1, (0, 0, 0)), (2, (1, 0, 1)), (3, (0, 1, 0))])
+def test_demo_form_in_ufl_equals_dg_operator_on_gpu(gb, order, periodic):
+    """The demo's form written in UFL notation, compiled at run time, is
+    DGOperator's SIPG / upwind / mass operator."""
+    import integrands
+    import ufl_forms as U
+    cells = (3, 2, 4)
+    lo, up = (0.1, -0.5, 0.0), (1.3, 0.5, 0.8)
+    op = integrands.FormOperator(U.to_form(demo_form(order)), cells, order, periodic=periodic, lower=lo, upper=up)
+    ref = gb.DGOperator(cells, order, diffusion=EPS, mass=MASS, velocity=VEL, weak_dirichlet=True,
+                        periodic=periodic, lower=lo, upper=up)
+    u = gb.DeviceArray.from_numpy(np.random.default_rng(order).uniform(-1, 1, op.size))
+    w1, w2 = gb.DeviceArray(op.size), gb.DeviceArray(op.size)
+    op(u, w1)
+    ref(u, w2)
+    assert relmax(w1.numpy(), w2.numpy()) < 1e-12
