@@ -356,6 +356,11 @@ class VLinear:
     def restricted(self):
         return any(len(k[0]) > 1 for k in self.terms)
 
+    def __eq__(self, rhs):
+        return Equation(self, rhs)
+
+    __hash__ = None
+
 
 class TestFunction:
     """v of the DG space with `components` components: v[m]."""
@@ -472,6 +477,11 @@ class Integrals:
     def __neg__(self):
         return Integrals(**{k: -p for k, p in self.parts.items()})
 
+    def __eq__(self, rhs):
+        return Equation(self, rhs)
+
+    __hash__ = None
+
 
 _FACET_SIZE = "(1.0 / sigma)"
 
@@ -575,3 +585,91 @@ class FacetNormal:
 
     def vector(self):
         return Vector([Leaf("n[%d]" % k) for k in range(3)])
+
+
+# ---- spaces, boundary conditions and schemes in dune.fem's shape -------------------
+
+class Equation:
+    """a == b: the form a(u, v) - b(v), set to zero by a scheme."""
+
+    def __init__(self, lhs, rhs):
+        self.lhs, self.rhs = lhs, rhs
+
+    def residual(self):
+        if isinstance(self.rhs, numbers.Real) and self.rhs == 0:
+            return self.lhs
+        return self.lhs - self.rhs
+
+
+class DGSpace:
+    """A discontinuous Legendre space of order `order` with `dimRange`
+    components on a structured grid of `cells` (the counterpart of
+    dune.fem.space.dglegendre over a YaspGrid; the dofs are laid out as
+    dune-fem lays out a non-hierarchical Legendre DG space)."""
+
+    def __init__(self, cells, order, dimRange=1, lower=(0.0, 0.0, 0.0), upper=(1.0, 1.0, 1.0),
+                 periodic=(0, 0, 0), precision=None):
+        import gbfem
+        self.cells, self.order, self.dimRange = tuple(int(c) for c in cells), int(order), int(dimRange)
+        self.lower, self.upper, self.periodic = tuple(lower), tuple(upper), tuple(periodic)
+        self.precision = gbfem.F64 if precision is None else precision
+        self.size = self.dimRange * (self.order + 1) ** 3 * self.cells[0] * self.cells[1] * self.cells[2]
+
+    @property
+    def zero(self):
+        import gbfem
+        z = gbfem.DeviceArray(self.size, self.precision)
+        z.clear()
+        return z
+
+
+def dglegendre(cells, order, dimRange=1, **kwargs):
+    """DGSpace(cells, order, dimRange, lower=, upper=, periodic=, precision=)."""
+    return DGSpace(cells, order, dimRange, **kwargs)
+
+
+class DirichletBC:
+    """Dirichlet data g on the non-periodic boundary: one expression of x per
+    component (or one expression for a scalar space).  DG spaces take it
+    weakly, through the interior-penalty boundary terms (the form's
+    dirichlet); the counterpart of dune.ufl.DirichletBC in a DG scheme."""
+
+    def __init__(self, space, value):
+        self.space = space
+        self.value = list(value) if isinstance(value, (list, tuple, Vector)) else [value]
+
+
+def galerkin(integrands, space=None, solver=None, parameters=None, quad_points=0, penalty=None):
+    """A scheme for `integrands`: an Equation (a == b, a == 0), or a list of
+    one Equation and at most one DirichletBC, as dune.fem.scheme.galerkin
+    takes them (python/dune/fem/scheme/__init__.py).  The form is compiled
+    at run time (integrands.FormOperator) on `space` (or the DirichletBC's);
+    solver: the linear method ("cg", "gmres", "bicgstab", ...), stored as
+    "linear.method" in the fem.solver parameters.  Returns a gbfem.Scheme:
+    scheme(u, w), scheme.solve(target=, rightHandSide=)."""
+    import gbfem
+    import integrands as _integrands
+    items = list(integrands) if isinstance(integrands, (list, tuple)) else [integrands]
+    eqs = [e for e in items if isinstance(e, Equation)]
+    bcs = [e for e in items if isinstance(e, DirichletBC)]
+    if len(eqs) != 1 or len(bcs) > 1 or len(eqs) + len(bcs) != len(items):
+        raise ValueError("galerkin: one equation (a == b) and at most one DirichletBC")
+    space = space if space is not None else (bcs[0].space if bcs else None)
+    if not isinstance(space, DGSpace):
+        raise ValueError("galerkin: a DGSpace (dglegendre) is needed")
+    residual = eqs[0].residual()
+    has_faces = isinstance(residual, Integrals) and (residual.parts["dS"].terms or residual.parts["ds"].terms)
+    if bcs and has_faces:
+        raise ValueError("galerkin: a form with its own facet integrals gives its boundary terms itself")
+    if bcs and len(bcs[0].value) != space.dimRange:
+        raise ValueError("galerkin: one Dirichlet expression per component")
+    form = to_form(residual, components=space.dimRange, dirichlet=bcs[0].value if bcs else None)
+    op = _integrands.FormOperator(form, space.cells, space.order, quad_points=quad_points,
+                                  precision=space.precision, penalty=penalty, periodic=space.periodic,
+                                  lower=space.lower, upper=space.upper)
+    prm = dict(parameters or {})
+    if solver is not None:
+        prm["linear.method"] = solver
+    scheme = gbfem.Scheme(op, prm)
+    scheme.form = form
+    return scheme
