@@ -132,6 +132,38 @@ def test_demo_form_in_ufl_equals_the_dg_oracle(orc, order, periodic):
     assert relmax(fo.residual(spec, u), prob.apply(u)) < 1e-13
 
 
+def test_two_component_facet_form_is_two_sipg_operators(orc, gb, tmp_path):
+    """Components 0 and 1 with their own diffusion, written with dS / ds
+    terms on both: the residual of the interleaved dofs (cell M n^3 + i M + m)
+    is the DG oracle's operator on each component."""
+    import form_oracle as fo
+    import ufl_forms as U
+    cells, order, eps = (3, 2, 2), 2, (0.7, 1.9)
+    u, v, n, h = U.TrialFunction(2), U.TestFunction(2), U.FacetNormal(), U.FacetSize()
+    beta = 10.0 * (order + 1) ** 2
+    a = None
+    for m in range(2):
+        gu, gv = U.grad(u)[m, :], U.grad(v)[m, :]
+        t = eps[m] * U.inner(gu, gv) * U.dx
+        t = t + (eps[m] * beta / h * U.jump(u[m]) * U.jump(v[m]) - eps[m] * U.inner(U.avg(gu), n("+")) * U.jump(v[m])
+                 - eps[m] * U.jump(u[m]) * U.inner(U.avg(gv), n("+"))) * U.dS
+        t = t + (eps[m] * beta / h * u[m] * v[m] - eps[m] * U.inner(gu, n.vector()) * v[m]
+                 - eps[m] * u[m] * U.inner(gv, n.vector())) * U.ds
+        a = t if a is None else a + t
+    I, S, B = oracle_callables(a, M=2)
+    spec = fo.FormSpec(cells, order, 2, I, S, B, penalty=1.0)
+    nl = (order + 1) ** 3
+    ncell = int(np.prod(cells))
+    w = np.random.default_rng(5).uniform(-1, 1, (ncell, nl, 2))
+    res = fo.residual(spec, w.reshape(-1)).reshape(ncell, nl, 2)
+    for m in range(2):
+        prob = orc.DGProblem(cells, order, diffusion=eps[m], weak_dirichlet=True)
+        assert relmax(res[:, :, m].ravel(), prob.apply(np.ascontiguousarray(w[:, :, m]).ravel())) < 1e-13
+    form = U.to_form(a, components=2)
+    assert "s[1]" in form.pieces["skeleton"] and "uR[1]" in form.pieces["skeleton"]
+    assert form.compile(gb.F64, order, cache_dir=str(tmp_path)).endswith(".cubin")
+
+
 def test_lowering_and_errors(gb, tmp_path):
     import integrands
     import ufl_forms as U
