@@ -6,13 +6,15 @@
 # Jacobian (dgelliptic.hh over legendre.hh) with oracle/ref_dgelliptic.cpp,
 # its explicit time loop
 # (timeprovider.hh, rungekutta/explicit.hh, butchertable.cc) over that
-# operator with oracle/ref_timeloop.cpp, and its Newton solver
-# (newtoninverseoperator.hh) with oracle/ref_newton.cpp, all against the grid
-# shim in oracle/shim_dg; runs them, and writes the golden vectors
+# operator with oracle/ref_timeloop.cpp, its Newton solver
+# (newtoninverseoperator.hh) with oracle/ref_newton.cpp, and its
+# stationary-iteration preconditioners (fempreconditioning.hh over
+# spmatrix.hh) with oracle/ref_precond.cpp, all against the grid shim in
+# oracle/shim_dg; runs them, and writes the golden vectors
 # tests/golden/ref_tables.json, ref_krylov.json, ref_krylov_sipg.json,
 # ref_dgelliptic.json, ref_dgelliptic_jacobian.json, ref_legendre_order.json
-# (the hierarchical shape-function order), ref_timeloop.json and
-# ref_newton.json.
+# (the hierarchical shape-function order), ref_timeloop.json,
+# ref_newton.json and ref_precond.json.
 # Needs the dune-fem source tree (located by ref_src.sh); without it this
 # recipe does nothing (the committed golden vectors stay as they are).  With
 # --compile-only it builds the drivers and writes nothing.  The reference's
@@ -28,7 +30,7 @@ GOLD="$HERE/../tests/golden"
 mkdir -p "$OUT" "$GOLD"
 CXX=${CXX:-g++}
 LEG="$REF/dune/fem/space/shapefunctionset/legendrepolynomials.cc"
-# the four drivers compile in parallel; each failure is reported
+# the drivers compile in parallel; each failure is reported
 $CXX -O2 -std=c++17 -pthread -I"$HERE/shim" -I"$REF" \
   "$HERE/ref_driver.cpp" "$HERE/oracle.cpp" "$LEG" -o "$OUT/ref_driver" &
 P1=$!
@@ -41,8 +43,11 @@ P3=$!
 $CXX -O2 -std=c++17 -I"$HERE/shim_dg" -I"$HERE/shim" -I"$REF" \
   "$HERE/ref_newton.cpp" "$LEG" -o "$OUT/ref_newton" &
 P4=$!
+$CXX -O2 -std=c++17 -I"$HERE/shim_dg" -I"$HERE/shim" -I"$REF" \
+  "$HERE/ref_precond.cpp" "$LEG" -o "$OUT/ref_precond" &
+P5=$!
 FAIL=0
-for P in $P1 $P2 $P3 $P4; do
+for P in $P1 $P2 $P3 $P4 $P5; do
   wait "$P" || FAIL=1
 done
 if [ "$FAIL" != 0 ]; then
@@ -50,7 +55,7 @@ if [ "$FAIL" != 0 ]; then
   exit 1
 fi
 if [ "$1" = "--compile-only" ]; then
-  echo "built $OUT/ref_driver $OUT/ref_dgelliptic $OUT/ref_timeloop $OUT/ref_newton"
+  echo "built $OUT/ref_driver $OUT/ref_dgelliptic $OUT/ref_timeloop $OUT/ref_newton $OUT/ref_precond"
   exit 0
 fi
 "$OUT/ref_driver" tables > "$GOLD/ref_tables.json"
@@ -61,6 +66,7 @@ fi
 "$OUT/ref_dgelliptic" hierarchical > "$GOLD/ref_legendre_order.json"
 "$OUT/ref_timeloop" > "$GOLD/ref_timeloop.json"
 "$OUT/ref_newton" > "$GOLD/ref_newton.json"
+"$OUT/ref_precond" > "$GOLD/ref_precond.json"
 echo "wrote $GOLD/ref_tables.json $GOLD/ref_krylov.json $GOLD/ref_krylov_sipg.json $GOLD/ref_dgelliptic.json" \
   "$GOLD/ref_dgelliptic_jacobian.json $GOLD/ref_legendre_order.json $GOLD/ref_timeloop.json" \
-  "$GOLD/ref_newton.json"
+  "$GOLD/ref_newton.json $GOLD/ref_precond.json"

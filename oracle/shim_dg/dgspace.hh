@@ -101,11 +101,25 @@ struct LocalFunctionTraits {
   static const int dimRange = 1;
 };
 
+// The dof vector as the reference's block vectors present it (blocks of
+// one dof): find(i) gives an iterator at dof i, [i][0] the dof.
+class DofBlockView {
+ public:
+  explicit DofBlockView(double* d) : d_(d) {}
+  double* find(std::size_t i) const { return d_ + i; }
+  double* operator[](std::size_t i) const { return d_ + i; }
+
+ private:
+  double* d_;
+};
+
 class DGFunction {
  public:
   typedef LegendreDGSpace DiscreteFunctionSpaceType;
   typedef LocalFunctionTraits LocalFunctionType;
   typedef double DofType;
+  typedef double* DofIteratorType;
+  typedef const double* ConstDofIteratorType;
   explicit DGFunction(const LegendreDGSpace& s) : space_(&s), dofs_(s.size(), 0.0) {}
   DGFunction(const std::string&, const LegendreDGSpace& s) : DGFunction(s) {}
   const LegendreDGSpace& space() const { return *space_; }
@@ -124,6 +138,11 @@ class DGFunction {
     for (std::size_t i = 0; i < dofs_.size(); ++i) dofs_[i] += a * x.dofs_[i];
   }
   void communicate() {}
+  DofIteratorType dbegin() { return dofs_.data(); }
+  DofIteratorType dend() { return dofs_.data() + dofs_.size(); }
+  ConstDofIteratorType dbegin() const { return dofs_.data(); }
+  ConstDofIteratorType dend() const { return dofs_.data() + dofs_.size(); }
+  DofBlockView dofVector() const { return DofBlockView(const_cast<double*>(dofs_.data())); }
   std::vector<double>& dofs() { return dofs_; }
   const std::vector<double>& dofs() const { return dofs_; }
 

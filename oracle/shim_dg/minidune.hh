@@ -47,6 +47,7 @@
 #include <type_traits>
 #include <vector>
 
+#include <dune/common/ftraits.hh>
 #include <dune/fem/quadrature/gausspoints.hh>
 
 // exceptions (dune/common/exceptions.hh)
@@ -252,6 +253,13 @@ struct SerialCommunication {
 struct MPIManager {
   typedef SerialCommunication Communication;
   static const Communication& comm() { static Communication c; return c; }
+  static int thread() { return 0; }
+  static int numThreads() { return 1; }
+  template <class F>
+  static void run(F&& f) { f(); }
+};
+struct SingleThreadModeError : Exception {
+  using Exception::Exception;
 };
 
 // checkpointing hooks (dune/fem/io/file/persistencemanager.hh): no-ops here
@@ -300,6 +308,26 @@ struct DifferentiableOperator
                               typename JacobianOperator::RangeFunctionType> {
   virtual void jacobian(const typename JacobianOperator::DomainFunctionType& u, JacobianOperator& jOp) const = 0;
 };
+
+// an operator that holds an assembled matrix (operator/common/operator.hh)
+template <class DomainFunction, class RangeFunction = DomainFunction>
+struct AssembledOperator : public virtual Operator<DomainFunction, RangeFunction> {};
+
+// declared so that the reference's matrix header parses; not instantiated
+template <class Factory>
+class ObjectStack;
+template <class BlockMapper, int blockSize>
+class NonBlockMapper;
+template <class Stack>
+class LocalMatrixWrapper;
+template <class Object>
+class ColumnObject;
+template <class Traits>
+class LocalMatrix;
+template <class Traits>
+class LocalMatrixDefault;
+template <class DomainSpace, class RangeSpace, class Set>
+struct StencilWrapper;
 
 // defined in dgspace.hh
 template <class DomainSpace, class RangeSpace>
