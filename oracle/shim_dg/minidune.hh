@@ -1,8 +1,11 @@
 // A minimal grid / discrete-function-space layer of our own, just large
 // enough to compile dune-fem's DGEllipticOperator (dune/fem/schemes/
 // dgelliptic.hh), LegendreShapeFunctionSet (dune/fem/space/shapefunctionset/
-// legendre.hh), TimeProvider (solver/timeprovider.hh) and
-// ExplicitRungeKuttaSolver (solver/rungekutta/explicit.hh) unmodified,
+// legendre.hh), TimeProvider (solver/timeprovider.hh),
+// ExplicitRungeKuttaSolver (solver/rungekutta/explicit.hh),
+// NewtonInverseOperator (solver/newtoninverseoperator.hh),
+// FemPreconditioning (solver/fempreconditioning.hh) and SparseRowMatrix
+// (operator/matrix/spmatrix.hh) unmodified,
 // standing in for dune-common, dune-geometry and dune-grid and the parts of
 // dune-fem those headers pull in, which are absent here.  Test
 // infrastructure only: built by oracle/make_ref_golden.sh into oracle/_ref/,
@@ -11,7 +14,9 @@
 // What it provides, and the reference behaviour each piece restates:
 //  - DUNE_THROW and the exception types; DynamicVector / DynamicMatrix;
 //    a serial MPIManager; no-op persistence hooks; a ParameterReader over
-//    string values with getEnum, and LocalParameter;
+//    string values with getEnum, and LocalParameter; declarations of the
+//    matrix-object templates spmatrix.hh names but these drivers never
+//    instantiate;
 //    the SpaceOperatorInterface the Runge-Kutta solver calls (operator(),
 //    space(), setTime(), timeStepEstimate());
 //  - FieldVector / FieldMatrix with the dense operations the two headers call
