@@ -18,7 +18,10 @@ numbers).  A convective flux with its wave speed and Dirichlet data are
 given as expressions too.
 
 What is supported: the trial function u (components u[m]), its gradient
-grad(u)[m, k], the spatial coordinate x[k], numbers and Constant, + - * /
+grad(u)[m, k], the spatial coordinate x[k], grad(e) and div(E) of
+coefficient expressions in x and u (symbolic, by the chain rule; e.g. a
+manufactured right-hand side -div(eps grad(exact) - b exact)), numbers and
+Constant, + - * /
 and ** (numeric or integer exponents), exp, log, sqrt, sin, cos, tan, tanh,
 sinh, cosh, atan, abs, max_value / min_value, conditional(cond, a, b) with
 lt / gt / le / ge, inner / dot over component lists, and the facet normal
@@ -402,11 +405,130 @@ class _Grad:
         return Leaf("g[%d][%d]" % (m, k))
 
 
-def grad(f):
-    """grad(u)[m, k] = du_m/dx_k (grad(u)[m, :] is the row as a vector)."""
-    if not isinstance(f, (TestFunction, TrialFunction)):
-        raise TypeError("ufl: grad of a test or trial function only")
-    return _Grad(f)
+# ---- derivatives of coefficient expressions ---------------------------------------
+
+def _zero(e):
+    return isinstance(e, Num) and not isinstance(e, Constant) and e.v == 0.0
+
+
+def _sum(a, b):
+    if _zero(a):
+        return b
+    if _zero(b):
+        return a
+    return Op("+", (a, b))
+
+
+def _prod(a, b):
+    if _zero(a) or _zero(b):
+        return Num(0.0)
+    return _bin("*", a, b)
+
+
+def _diff(e, var):
+    """d e / d var for var "x[k]" or "u[m]", by the chain rule over the tree.
+    Gradients of u inside e would need second derivatives: refused."""
+    if isinstance(e, Num):
+        return Num(0.0)
+    if isinstance(e, Leaf):
+        t = e.text
+        if t == var:
+            return Num(1.0)
+        if t.startswith("g") or t[:2] in ("uL", "uR"):
+            raise ValueError("ufl: grad of an expression needs it in x and u only (not grad u, not restricted)")
+        return Num(0.0)
+    if isinstance(e, (Cond,)):
+        return Num(0.0)
+    if isinstance(e, Conditional):  # almost everywhere
+        return Conditional(e.c, _diff(e.a, var), _diff(e.b, var))
+    if not isinstance(e, Op):
+        raise TypeError("ufl: cannot differentiate %r" % (e,))
+    a = e.args
+    da = [_diff(x, var) for x in a]
+    op = e.op
+    if op == "+" and len(a) == 2:
+        return _sum(da[0], da[1])
+    if op == "-" and len(a) == 2:
+        return _sum(da[0], _prod(Num(-1.0), da[1])) if not _zero(da[1]) else da[0]
+    if op == "-":
+        return Num(0.0) if _zero(da[0]) else Op("-", (da[0],))
+    if op == "*":
+        return _sum(_prod(da[0], a[1]), _prod(a[0], da[1]))
+    if op == "/":
+        num = _sum(_prod(da[0], a[1]), _prod(Num(-1.0), _prod(a[0], da[1])))
+        return Num(0.0) if _zero(num) else Op("/", (num, Op("*", (a[1], a[1]))))
+    if all(_zero(d) for d in da):
+        return Num(0.0)
+    x, dx = a[0], da[0]
+    if op == "exp":
+        return _prod(Op("exp", (x,)), dx)
+    if op == "log":
+        return Op("/", (dx, x))
+    if op == "sqrt":
+        return Op("/", (dx, Op("*", (Num(2.0), Op("sqrt", (x,))))))
+    if op == "sin":
+        return _prod(Op("cos", (x,)), dx)
+    if op == "cos":
+        return _prod(Op("-", (Op("sin", (x,)),)), dx)
+    if op == "tan":
+        return _prod(Op("+", (Num(1.0), Op("ipow2", (Op("tan", (x,)),)))), dx)
+    if op == "tanh":
+        return _prod(Op("-", (Num(1.0), Op("ipow2", (Op("tanh", (x,)),)))), dx)
+    if op == "sinh":
+        return _prod(Op("cosh", (x,)), dx)
+    if op == "cosh":
+        return _prod(Op("sinh", (x,)), dx)
+    if op == "atan":
+        return Op("/", (dx, Op("+", (Num(1.0), Op("ipow2", (x,))))))
+    if op == "fabs":
+        return Conditional(Cond(">=", x, Num(0.0)), dx, Op("-", (dx,)))
+    if op.startswith("ipow"):
+        n = int(op[4:])
+        base = Num(float(n)) if n == 1 else _prod(Num(float(n)), Op("ipow%d" % (n - 1), (x,)) if n > 2 else x)
+        return _prod(base, dx)
+    if op == "pow":
+        if not isinstance(a[1], Num) or not _zero(da[1]):
+            raise ValueError("ufl: grad of pow needs a constant exponent")
+        return _prod(_prod(a[1], Op("pow", (x, Num(a[1].v - 1.0)))), dx)
+    if op in ("max", "min"):
+        pick = Cond(">=" if op == "max" else "<=", a[0], a[1])
+        return Conditional(pick, da[0], da[1])
+    raise ValueError("ufl: cannot differentiate %s" % op)
+
+
+def _total_grad(e, components):
+    """d e / d x_k along the solution: the partial in x_k plus
+    sum_m d e / d u_m * g[m][k]."""
+    e = _wrap(e)
+    out = []
+    for k in range(3):
+        d = _diff(e, "x[%d]" % k)
+        for m in range(components):
+            du = _diff(e, "u[%d]" % m)
+            d = _sum(d, _prod(du, Leaf("g[%d][%d]" % (m, k))))
+        out.append(d)
+    return Vector(out)
+
+
+def grad(f, components=4):
+    """grad(u)[m, k] = du_m/dx_k (grad(u)[m, :] is the row as a vector); of a
+    coefficient expression e(x, u) the vector of its total derivatives
+    d e / d x_k (e may depend on u[m], m < components, but not on grad u)."""
+    if isinstance(f, (TestFunction, TrialFunction)):
+        return _Grad(f)
+    if isinstance(f, Expr):
+        return _total_grad(f, components)
+    raise TypeError("ufl: grad of a test or trial function or of an expression")
+
+
+def div(f, components=4):
+    """sum_k d f_k / d x_k of a vector of expressions."""
+    if not isinstance(f, Vector) or len(f) != 3:
+        raise TypeError("ufl: div of a vector of three expressions")
+    out = Num(0.0)
+    for k in range(3):
+        out = _sum(out, _total_grad(f[k], components)[k])
+    return out
 
 
 def inner(a, b):
