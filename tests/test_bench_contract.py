@@ -27,3 +27,19 @@ def test_reference_arm_prints_one_contract_line():
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_roofline_traffic_covers_the_whole_apply():
+    """The headline roofline's traffic is the DRAM bytes of one apply, both
+    kernels (as its achieved bandwidth is), from the committed ncu summary;
+    the main kernel's own bytes and launch share are reported beside it."""
+    sys.path.insert(0, ROOT)
+    import bench
+    step, main, share = bench.profiled_traffic(os.path.join(ROOT, "profiles", "dg_trace_const_q3_64cube_f64.json"))
+    with open(os.path.join(ROOT, "profiles", "dg_trace_const_q3_64cube_f64.json")) as f:
+        d = json.load(f)
+    t = d["trace_kernel"]
+    assert main == d["dram_read"] + d["dram_write"]
+    assert step == main + t["dram_read"] + t["dram_write"]
+    assert 0.5 < share < 1.0
+    assert bench.profiled_traffic(os.path.join(ROOT, "profiles", "missing.json")) == (None, None, None)
