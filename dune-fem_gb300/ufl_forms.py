@@ -37,7 +37,7 @@ with facet integrals gives them itself, as UFL does
   - over boundary facets, `* ds`, with u, grad u, v, grad v and n;
   - FacetSize(): avg(CellVolume) / FacetArea on interior facets and
     CellVolume / FacetArea on boundary facets (the cell width normal to the
-    face on these grids).
+    face on these grids); those two ratios may also be written as in UFL.
 A dS integrand must not change when '+' and '-' are exchanged (as on any
 mesh, where the choice is arbitrary): each cell takes the v('+') part with
 itself as '+'.  Such a form is lowered to the raw interior / skeleton /
@@ -616,6 +616,33 @@ def FacetSize():
     return Leaf(_FACET_SIZE)
 
 
+class _MeshQuantity:
+    """CellVolume / FacetArea of the uniform structured grid: only their
+    ratio, the facet size, is an expression here (UFL's
+    avg(CellVolume(space)) / FacetArea(space) and CellVolume(space) /
+    FacetArea(space), which are the same on these grids)."""
+
+    def __init__(self, kind):
+        self.kind = kind
+
+    def __call__(self, side):
+        _side(side)
+        return self  # the cells of a uniform grid all have the same volume
+
+    def __truediv__(self, o):
+        if self.kind == "volume" and isinstance(o, _MeshQuantity) and o.kind == "area":
+            return FacetSize()
+        raise ValueError("ufl: CellVolume and FacetArea are supported as CellVolume / FacetArea only")
+
+
+def CellVolume(space=None):
+    return _MeshQuantity("volume")
+
+
+def FacetArea(space=None):
+    return _MeshQuantity("area")
+
+
 def jump(e, n=None):
     """e('+') - e('-'), or e('+') n('+') + e('-') n('-') with a normal."""
     if n is None:
@@ -628,6 +655,8 @@ def jump(e, n=None):
 
 def avg(e):
     """(e('+') + e('-')) / 2."""
+    if isinstance(e, _MeshQuantity):
+        return e
     return 0.5 * (e("+") + e("-"))
 
 

@@ -164,6 +164,26 @@ def test_two_component_facet_form_is_two_sipg_operators(orc, gb, tmp_path):
     assert form.compile(gb.F64, order, cache_dir=str(tmp_path)).endswith(".cubin")
 
 
+def test_demo_mesh_quantities_are_the_facet_size():
+    """The demo's he = avg(CellVolume)/FacetArea and hbnd = CellVolume/FacetArea
+    lower to the facet size: the same form source as with FacetSize()."""
+    import ufl_forms as U
+    space = U.dglegendre((3, 2, 2), 2)
+    u, v, n = U.TrialFunction(1), U.TestFunction(1), U.FacetNormal()
+    he = U.avg(U.CellVolume(space)) / U.FacetArea(space)
+    hbnd = U.CellVolume(space) / U.FacetArea(space)
+    h = U.FacetSize()
+
+    def form(hi, hb):
+        a = U.inner(U.grad(u)[0, :], U.grad(v)[0, :]) * U.dx
+        a = a + 90.0 / hi * U.jump(u[0]) * U.jump(v[0]) * U.dS + 90.0 / hb * u[0] * v[0] * U.ds
+        return U.to_form(a)
+
+    assert form(he, hbnd).source_code(0, 2) == form(h, h).source_code(0, 2)
+    with pytest.raises(ValueError):
+        U.FacetArea(space) / U.CellVolume(space)
+
+
 def test_lowering_and_errors(gb, tmp_path):
     import integrands
     import ufl_forms as U
